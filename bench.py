@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark: Msamples/s of the plain one-image-per-launch GPU path.
+
+Workload (single larger scene): 1.0M FP32 triangles from 64 seeded UV-spheres and
+displaced grids, 40% Lambert / 40% GGX / 20% glass, a 2048x1024 procedural
+equirect sky, 1920x1080, 64 spp, max 16 bounces, MIS next-event estimation
+(PathTracing semantics). Synthetic, seeded. A step = one full render of that
+image (132.7M samples) with the scene resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs independent replicas, one per GPU (each renders its own image with
+its own seed; no data exchange): "scaling": "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+WORKLOAD = "spheres_grids_1M_1080p_64spp_pt16"
+METRIC = "render_msamples_per_s"
+UNIT = "Msamples/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="reduced workload for quick checks")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU time of the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def make_scene(small: bool):
+    from petrichor_gb300 import synth
+    if small:
+        return synth.spheres_grids(tri_budget=100_000, width=480, height=270, spp=16, max_bounces=16,
+                                   env_width=512, env_height=256)
+    return synth.spheres_grids()  # 1.0M tris, 1920x1080, 64 spp, 16 bounces, 2048x1024 env
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(scene, seconds: float, threads: int = 0):
+    """The CPU oracle (a restatement of the reference renderer) on the host cores, on a
+    bounded sample of the same workload: tiles spread evenly over the image at full spp."""
+    import numpy as np
+    import oracle
+    o = oracle.OracleScene(scene)
+    t0 = time.perf_counter()
+    o.build_bvh()
+    bvh_s = time.perf_counter() - t0
+    n_tiles = o.num_tiles()
+    ncores = threads or os.cpu_count() or 1
+    # probe with one tile per core, then size the sample to the time target
+    order = np.random.default_rng(0).permutation(n_tiles)
+    probe = order[:ncores]
+    _, secs, px = o.render_tiles(probe, threads)
+    per_tile = secs / max(1, len(probe)) * ncores
+    n = int(min(n_tiles, max(len(probe), seconds / max(per_tile, 1e-6) * ncores)))
+    tiles = order[:n]
+    _, secs, px = o.render_tiles(tiles, threads)
+    samples = px * scene.settings.spp
+    return {"value": samples / secs / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"{len(tiles)} of {n_tiles} 16x16 tiles (random spread) at the full "
+                      f"{scene.settings.spp} spp: {samples} samples in {secs:.2f} s; BVH build "
+                      f"{bvh_s:.2f} s not included",
+            "bvh_build_s": bvh_s}
+
+
+def run_reference_arm(args):
+    rank, world, local = dist_setup()
+    if rank != 0:
+        return
+    scene = make_scene(args.small)
+    import numpy as np
+    import oracle
+    o = oracle.OracleScene(scene)
+    o.build_bvh()
+    n_tiles = o.num_tiles()
+    ncores = os.cpu_count() or 1
+    order = np.random.default_rng(0).permutation(n_tiles)
+    _, secs, _ = o.render_tiles(order[:ncores])
+    per_tile = secs
+    n = int(min(n_tiles, max(ncores, 20.0 / max(per_tile, 1e-6) * ncores)))
+    tiles = order[:n]
+    for _ in range(args.warmup):
+        o.render_tiles(tiles[:ncores])
+    times = []
+    px = 0
+    for _ in range(args.steps):
+        _, secs, px = o.render_tiles(tiles)
+        times.append(secs)
+    samples = px * scene.settings.spp
+    ms = statistics.mean(times) * 1e3
+    v = samples / (ms / 1e3) / 1e6
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "integrator": "PathTracing (MIS NEE)",
+                   "sample_per_step": f"{len(tiles)} of {n_tiles} tiles at full spp"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
+                         "sample": f"{len(tiles)} random 16x16 tiles x {scene.settings.spp} spp "
+                                   f"per step ({samples} samples)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    import numpy as np
+    import torch
+    from petrichor_gb300 import capi
+
+    rank, world, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    t0 = time.perf_counter()
+    scene = make_scene(args.small)
+    gen_s = time.perf_counter() - t0
+    st = scene.settings
+    ctx = capi.Context(local)
+    t0 = time.perf_counter()
+    sid = ctx.upload(scene)
+    upload_s = time.perf_counter() - t0
+    info = ctx.scene_info(sid)
+    cam = capi.camera_from_scene(scene)
+    sets = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=1 + rank)
+    npx = st.width * st.height
+    samples_per_step = npx * st.spp
+    film = torch.empty(npx * 3, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        ctx.render_device(sid, cam, sets, film.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.stats().kernel_launches
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks.stop()
+    barrier()
+    secs = e0.elapsed_time(e1) / 1e3
+    launches = ctx.stats().kernel_launches - launches0
+    if dist is not None:
+        t = torch.tensor([secs], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    value = world * samples_per_step * args.steps / secs / 1e6
+
+    # ---- end to end through the C ABI with a host film (pinned): per step the
+    # camera + settings go in (kernel arguments) and the film comes back.
+    host = torch.empty(npx * 3, dtype=torch.float32, pin_memory=True)
+    host_np = host.numpy().reshape(st.height, st.width, 3)
+    ctx.render(sid, cam, sets, out=host_np)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.render(sid, cam, sets, out=host_np)
+        _ = float(host_np[0, 0, 0])
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * samples_per_step * args.steps / e2e_s / 1e6
+    img_mean = float(host_np.mean())
+
+    # ---- roofline of the dominant kernel (CUDA events around every stage launch)
+    prof = ctx.render_profile(sid, cam, sets, film.data_ptr(), count_reference=True).as_dict()
+    prof2 = ctx.render_profile(sid, cam, sets, film.data_ptr(), count_reference=False).as_dict()
+    stages = {k: prof2[k] for k in ("raygen_ms", "extend_ms", "shade_ms", "shadow_ms", "accumulate_ms")}
+    dominant = max(stages, key=stages.get)
+    # algorithmic bytes of a traced ray (reference traversal order): 32 B per node
+    # popped and slab-tested, 48 B per triangle test, 32 B ray in, 16 B hit out
+    rays = max(1, prof["ref_rays"])
+    bytes_per_ray = (32.0 * prof["ref_node_tests"] + 48.0 * prof["ref_tri_tests"]) / rays + 48.0
+    ext_launches = max(1, prof2["extend_launches"])
+    bytes_per_launch = bytes_per_ray * prof2["extend_rays"] / ext_launches
+    avg_launch_s = prof2["extend_ms"] / 1e3 / ext_launches
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            peak, peak_src = float(json.load(fh)["hbm_gbs"]), "measured"
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "extend_kernel_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as fh:
+            t = json.load(fh)
+        traffic = t["dram_bytes_per_ray"] * prof2["extend_rays"] / ext_launches
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD if not args.small else WORKLOAD + "_SMALL",
+                   "triangles": info.num_triangles, "bvh_nodes": info.num_nodes,
+                   "resolution": [st.width, st.height], "spp": st.spp, "max_bounces": st.max_bounces,
+                   "env": list(scene.env.texture.shape[:2][::-1]), "mode": "wavefront",
+                   "parallelism": f"replicas{world}",
+                   "l2": "working set > L2 (scene ~%.0f MB resident + wave state)" % (
+                       info.device_bytes / 1e6),
+                   "scene_gen_s": round(gen_s, 2), "scene_upload_s": round(upload_s, 2),
+                   "bvh_build_s": round(info.build_seconds, 2)},
+        "e2e": {"value": e2e, "unit": UNIT,
+                "h2d_bytes_per_step": 64 + 48, "d2h_bytes_per_step": npx * 12},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "roofline": {"bound": "hbm", "kernel": "ExtendKernel (closest-hit traversal)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "bytes_per_ray": bytes_per_ray,
+                     "ref_nodes_per_ray": prof["ref_node_tests"] / rays,
+                     "ref_tris_per_ray": prof["ref_tri_tests"] / rays,
+                     "dominant_stage": dominant, "stage_ms": stages,
+                     "rays_extended": prof2["extend_rays"], "shadow_rays": prof2["shadow_rays"],
+                     "mrays_per_s": (prof2["extend_rays"] + prof2["shadow_rays"]) /
+                                    (sum(stages.values()) / 1e3) / 1e6},
+        "image_mean": img_mean,
+    }
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+    ctx.release(sid)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

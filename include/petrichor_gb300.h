@@ -1,0 +1,206 @@
+/*
+ * petrichor_gb300.h - C ABI of the GB300 path-tracing core.
+ *
+ * Plain pointers, sizes and status codes; no C++ or torch types. Every call
+ * returns PT_OK (0) or a negative PT_ERR_* code; pt_last_error() gives the
+ * message of the last failing call on a context. A context is safe to use from
+ * several host threads (calls are serialised per context).
+ *
+ * Reference interfaces replaced (paths relative to the Petrichor project):
+ *   pt_render            Petrichor::Core::Petrichor::Render(const Scene&)
+ *                        (LibPetrichor/Core/Petrichor.h:30-31, Petrichor.cpp:103-333)
+ *   pt_scene_upload      what Render reads from Scene: GetGeometries/GetLights/
+ *                        GetEnvironment/GetMaterial (LibPetrichor/Core/Scene.h:95-173)
+ *                        plus BinnedSAHBVH::Build (Core/Accel/BinnedSAHBVH.cpp:15-225)
+ *   pt_camera_init       Camera(pos, dir), SetFOV, SetFocalLength, FocusTo,
+ *                        SetApeture (LibPetrichor/Core/Camera.h:19-83)
+ *   pt_settings          RenderSetting (LibPetrichor/Core/RenderSetting.h:10-21)
+ *   pt_trace_closest     AccelBase::Intersect(ray, scene, distMin, distMax)
+ *                        (LibPetrichor/Core/Accel/AccelBase.h:36-55)
+ *   pt_get_progress      Petrichor::GetNumRenderedTiles / GetNumTiles
+ *                        (LibPetrichor/Core/Petrichor.h:41-51)
+ *   pt_render_profile    SCOPE_LOGGER timers around the render passes
+ *                        (LibPetrichor/Core/Logger.h:63-94, used at Petrichor.cpp:106,124)
+ *   pt_bvh_build         BinnedSAHBVH::Build alone, on the host, returning the tree
+ *                        (LibPetrichor/Core/Accel/BinnedSAHBVH.cpp:15-225)
+ */
+#ifndef PETRICHOR_GB300_H_
+#define PETRICHOR_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_ABI_VERSION 1
+
+/* status codes */
+#define PT_OK 0
+#define PT_ERR_INVALID_ARG (-1)
+#define PT_ERR_OUT_OF_MEMORY (-2)
+#define PT_ERR_OVER_BUDGET (-3)
+#define PT_ERR_TIMEOUT (-4)
+#define PT_ERR_CUDA (-5)
+#define PT_ERR_NOT_FOUND (-6)
+#define PT_ERR_UNSUPPORTED (-7)
+#define PT_ERR_BUSY (-8)
+#define PT_ERR_CANCELLED (-9)
+#define PT_ERR_NO_DEVICE (-10)
+#define PT_ERR_DEVICE_FAULT (-11)
+
+/* material kinds: MaterialTypes order (LibPetrichor/Core/Material/MaterialBase.h:15-22) */
+#define PT_MAT_LAMBERT 0
+#define PT_MAT_GLASS 1
+#define PT_MAT_EMISSION 2
+#define PT_MAT_GLOSSY 3 /* GGX */
+#define PT_MAT_MIX 4
+
+/* shading types (LibPetrichor/Core/Geometry/Triangle.h:15-19) */
+#define PT_SHADING_FLAT 0
+#define PT_SHADING_SMOOTH 1
+
+/* integrators */
+#define PT_INTEGRATOR_SIMPLE 0 /* SimplePathTracing: what Petrichor::Render runs */
+#define PT_INTEGRATOR_PT 1     /* PathTracing: MIS next-event estimation */
+
+/* render modes */
+#define PT_MODE_REPLAY 0    /* reproduces the reference's per-tile random stream: same film bits */
+#define PT_MODE_WAVEFRONT 1 /* throughput path: per-(pixel, sample) stream, same estimator */
+
+typedef struct pt_context pt_context;
+typedef int32_t pt_scene_id;
+
+/* One material (Lambert(kd) / GGX(f0, roughness) / Glass(color, ior) /
+ * Emission(color) / MixMaterial(mat0, mat1, mix)). */
+typedef struct pt_material {
+  int32_t kind;
+  float color[3];  /* Lambert kd, GGX reflectance ("f0" argument), Glass color, Emission radiance */
+  float roughness; /* GGX */
+  float ior;       /* Glass */
+  float mix;       /* Mix */
+  int32_t mat0;    /* Mix: index of the material picked when mix <= r */
+  int32_t mat1;    /* Mix: the other one */
+} pt_material;
+
+/* Scene geometry, materials, lights and environment (host memory; copied). */
+typedef struct pt_scene_desc {
+  uint32_t num_vertices;
+  const float* positions; /* num_vertices * 3 */
+  const float* normals;   /* num_vertices * 3 (smooth shading) */
+  const float* uvs;       /* num_vertices * 3, may be NULL */
+  uint32_t num_triangles;
+  const int32_t* indices;      /* num_triangles * 3 */
+  const int32_t* tri_material; /* num_triangles */
+  const uint8_t* tri_shading;  /* num_triangles, PT_SHADING_*; NULL = flat */
+  uint32_t num_materials;
+  const pt_material* materials;
+  uint32_t num_lights;
+  const int32_t* lights; /* triangle indices registered with Scene::AppendLight */
+  float env_base_color[3];
+  float env_z_rotation;
+  int32_t env_width, env_height; /* 0 = no texture (base colour only) */
+  const float* env_rgb;          /* env_height rows of env_width RGB texels */
+} pt_scene_desc;
+
+/* Derived camera state (the private members of Petrichor's Camera). Fill it with
+ * pt_camera_init to get the reference's exact arithmetic. */
+typedef struct pt_camera {
+  float pos[3], right[3], up[3], forward[3];
+  float h_perf;     /* sensor height / focal length */
+  float focus_dist; /* FocusTo distance */
+  float aperture;   /* lens diameter */
+  float reserved;
+} pt_camera;
+
+typedef struct pt_settings {
+  int32_t width, height;  /* RenderSetting::outputWidth/outputHeight */
+  int32_t spp;            /* numSamplesPerPixel */
+  int32_t max_bounces;    /* numMaxBounces */
+  int32_t tile_width, tile_height;
+  int32_t integrator;     /* PT_INTEGRATOR_* */
+  int32_t mode;           /* PT_MODE_* */
+  uint32_t seed;          /* wavefront stream seed */
+  int32_t reserved[3];
+} pt_settings;
+
+typedef struct pt_scene_info {
+  uint32_t num_triangles, num_nodes, tree_height, num_lights;
+  uint64_t device_bytes;
+  double build_seconds; /* host binned-SAH build */
+} pt_scene_info;
+
+typedef struct pt_stats {
+  double last_render_ms;      /* device time of the last render (CUDA events) */
+  uint64_t kernel_launches;   /* kernels launched by this context so far */
+  uint64_t device_bytes_in_use;
+  uint64_t memory_budget;
+  uint64_t renders;
+  int32_t last_device_status; /* error bits reported by kernels (0 = none) */
+  int32_t reserved;
+} pt_stats;
+
+int pt_abi_version(void);
+const char* pt_status_string(int status);
+
+/* Context on one CUDA device. memory_budget_bytes = 0: no limit. */
+int pt_context_create(int device, uint64_t memory_budget_bytes, pt_context** out);
+int pt_context_destroy(pt_context* ctx);
+const char* pt_last_error(const pt_context* ctx);
+
+/* Camera(pos, dir); SetFOV(fov) if fov > 0 else SetFocalLength(focal_length);
+ * FocusTo(*focus_target) if not NULL; SetApeture(aperture). */
+int pt_camera_init(const float pos[3], const float view_dir[3], float fov, float focal_length,
+                   const float* focus_target, float aperture, pt_camera* out);
+
+/* Copies the scene to the device and builds its binned-SAH BVH (kept resident). */
+int pt_scene_upload(pt_context* ctx, const pt_scene_desc* desc, pt_scene_id* out);
+int pt_scene_release(pt_context* ctx, pt_scene_id scene);
+int pt_scene_info_get(pt_context* ctx, pt_scene_id scene, pt_scene_info* info);
+
+/* Renders into a host film of width*height*3 floats (row-major RGB, the layout
+ * of Texture2D::GetRawDataPtr). Blocks until the film is written. */
+int pt_render(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+              const pt_settings* settings, float* film_rgb);
+
+/* Same, into a device film, enqueued on `stream` (cudaStream_t; NULL = the
+ * context's stream). Returns once the work is enqueued. */
+int pt_render_device(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+                     const pt_settings* settings, float* film_rgb_device, void* stream);
+
+/* Closest hits for n device rays (o.xyz, dir.xyz) within [dist_min, dist_max]:
+ * original triangle index (or -1) and distance (or -1). Enqueued on `stream`. */
+int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float* rays_device,
+                     float dist_min, float dist_max, int32_t* tri_device, float* dist_device,
+                     void* stream);
+
+/* Host-only binned-SAH build of the triangles (no device needed). Call with
+ * NULL outputs to get *num_nodes; then with bounds (num_nodes*6 floats: lo.xyz,
+ * hi.xyz), node_ints (num_nodes*5: child0, child1, begin, end, is_leaf) and
+ * prim_ids (num_triangles) to fill them. threads <= 0: all host threads. */
+int pt_bvh_build(const float* positions, uint32_t num_vertices, const int32_t* indices,
+                 uint32_t num_triangles, int32_t threads, uint32_t* num_nodes,
+                 uint32_t* tree_height, float* bounds, int32_t* node_ints, int32_t* prim_ids);
+
+/* Per-stage device times (CUDA events around every stage launch) and work tallies
+ * of one wavefront render. With count_reference != 0 every extended ray is also
+ * walked in the reference's traversal order to count its node and triangle
+ * tests (the algorithmic work per ray). Synchronous. */
+typedef struct pt_profile {
+  double raygen_ms, extend_ms, shade_ms, shadow_ms, accumulate_ms;
+  uint64_t extend_rays, shadow_rays, extend_launches, shadow_launches;
+  uint64_t ref_node_tests, ref_tri_tests, ref_rays;
+} pt_profile;
+int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+                      const pt_settings* settings, float* film_rgb_device, int32_t count_reference,
+                      pt_profile* out);
+
+int pt_get_stats(pt_context* ctx, pt_stats* out);
+/* Tiles finished / total of the last replay render (reference tile grid). */
+int pt_get_progress(pt_context* ctx, uint32_t* rendered_tiles, uint32_t* num_tiles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PETRICHOR_GB300_H_ */

@@ -60,6 +60,8 @@ def lib():
         L.oracle_render.restype = ctypes.c_double
         L.oracle_render.argtypes = [vp, f32p, i32, i32, i32]
         L.oracle_num_tiles.argtypes = [vp]
+        L.oracle_render_tiles.restype = ctypes.c_double
+        L.oracle_render_tiles.argtypes = [vp, f32p, i32, i32p, i32]
         L.oracle_hits.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, f32p, i32p]
         L.oracle_trace.argtypes = [vp, i32, f32p, ctypes.c_float, ctypes.c_float, i32p, f32p]
         L.oracle_env.argtypes = [vp, i32, f32p]
@@ -113,6 +115,21 @@ class OracleScene:
         film = np.zeros((s.height, s.width, 3), np.float32)
         secs = lib().oracle_render(self._h, _fp(film), threads, tile_begin, tile_end)
         return film, secs
+
+    def render_tiles(self, tiles, threads: int = 0):
+        """Render only the listed tile indices; returns (film, seconds, pixels rendered)."""
+        s = self.scene.settings
+        film = np.zeros((s.height, s.width, 3), np.float32)
+        t = np.ascontiguousarray(tiles, np.int32)
+        secs = lib().oracle_render_tiles(self._h, _fp(film), threads, _ip(t), t.size)
+        nx, ny = s.width // s.tile_width, s.height // s.tile_height
+        px = 0
+        for k in t:
+            i, j = int(k) % (nx + 1), int(k) // (nx + 1)
+            w = s.tile_width if i != nx else s.width - nx * s.tile_width
+            h = s.tile_height if j != ny else s.height - ny * s.tile_height
+            px += w * h
+        return film, secs, px
 
     def hits(self, seed_a: int = 7, seed_b: int = 11):
         s = self.scene.settings

@@ -274,7 +274,9 @@ struct Env {  // Core/Environment.{h,cpp}
         const float u0 = 1.0f - (phi - rot) * 0.5f * kInvPi;
         const float v0 = theta * kInvPi;
         const float y = v0 * pdf2D.H;
-        const int y0 = (int)y;
+        // d.z == -1 gives y == H: an out-of-range read (undefined) in the reference;
+        // clamped to the last row here.
+        const int y0 = std::min((int)y, pdf2D.H - 1);
         const int y1 = std::min(y0 + 1, pdf2D.H - 1);
         const float py = Lerp(pdf1D[y0], pdf1D[y1], y - y0);
         return py * pdf2D.ByUV(u0, v0).x;
@@ -1078,6 +1080,38 @@ double oracle_render(void* sp, float* film, int threads, int tileBegin, int tile
             Sampler2D s2(0, 1);
             for (int y = tl.y; y < tl.y + tl.h; y++)
                 for (int x = tl.x; x < tl.x + tl.w; x++) {
+                    if (s.integrator == 0) RenderSimple(s, x, y, film, s1, s2);
+                    else RenderPT(s, x, y, film, s1, s2);
+                }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < threads; i++) pool.emplace_back(work);
+    for (auto& t : pool) t.join();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Render an explicit list of tiles (for bounded, spatially spread CPU samples).
+double oracle_render_tiles(void* sp, float* film, int threads, const int32_t* list, int n) {
+    Scene& s = *(Scene*)sp;
+    if (!s.built) BuildBVH(s);
+    const int nx = s.W / s.tileW, ny = s.H / s.tileH;
+    const int remW = s.W - nx * s.tileW, remH = s.H - ny * s.tileH;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next(0);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= n) break;
+            const int t = list[k], i = t % (nx + 1), j = t / (nx + 1);
+            if (j > ny) continue;
+            const int x0 = i * s.tileW, y0 = j * s.tileH;
+            const int w = i != nx ? s.tileW : remW, h = j != ny ? s.tileH : remH;
+            Sampler1D s1(0);
+            Sampler2D s2(0, 1);
+            for (int y = y0; y < y0 + h; y++)
+                for (int x = x0; x < x0 + w; x++) {
                     if (s.integrator == 0) RenderSimple(s, x, y, film, s1, s2);
                     else RenderPT(s, x, y, film, s1, s2);
                 }

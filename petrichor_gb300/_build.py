@@ -1,0 +1,85 @@
+"""Builds the CUDA library libpetrichor_gb300.so in-tree (sm_103a only).
+
+nvcc compiles the kernels for ``-gencode arch=compute_103a,code=sm_103a``; the
+host C++ is compiled by g++ with ``-ffp-contract=off`` (the reference's x86-64
+rounding for the few host-derived floats). The kernels are compiled with
+``-fmad=false`` so that the replay kernel reproduces the reference's
+unfused float arithmetic and the throughput kernels share its triangle test.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT_DIR = os.path.join(PKG, "_lib")
+OBJ_DIR = os.path.join(OUT_DIR, "obj")
+LIB = os.path.join(OUT_DIR, "libpetrichor_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+CU_SOURCES = ["replay.cu", "wavefront.cu"]
+CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp"]
+
+
+def _nvcc() -> str:
+    p = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found; set CUDA_HOME")
+    return p
+
+
+def _sources():
+    return [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES] + [
+        os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))
+    ] + [os.path.join(ROOT, "include", "petrichor_gb300.h")]
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    return any(os.path.getmtime(s) > t for s in _sources())
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and not _stale():
+        return LIB
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    inc = ["-I", CSRC, "-I", os.path.join(ROOT, "include")]
+    jobs = []
+    for s in CU_SOURCES:
+        o = os.path.join(OBJ_DIR, s + ".o")
+        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
+                     "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", *inc, "-c",
+                     os.path.join(CSRC, s), "-o", o])
+    for s in CPP_SOURCES:
+        o = os.path.join(OBJ_DIR, s + ".o")
+        jobs.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+                     "-pthread", "-Wall", *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c",
+                     os.path.join(CSRC, s), "-o", o])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("compile failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout + r.stderr)
+        return r
+
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(run, jobs))
+    objs = [os.path.join(OBJ_DIR, s + ".o") for s in CU_SOURCES + CPP_SOURCES]
+    tmp = LIB + ".tmp"
+    run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

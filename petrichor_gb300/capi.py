@@ -1,0 +1,332 @@
+"""ctypes binding of the C ABI in ``include/petrichor_gb300.h``.
+
+This is the host-side mirror of the reference's render call for Python users:
+``Context.upload(scene)`` plays the part of filling a ``Petrichor::Core::Scene``
+and ``Context.render(...)`` the part of ``Petrichor::Render(scene)``
+(``LibPetrichor/Core/Petrichor.cpp:103-333``), writing a film with the layout of
+``Texture2D::GetRawDataPtr`` (row-major RGB float32).
+
+The library is built in-tree (``petrichor_gb300/_lib``); there is no fallback:
+if it is missing or no CUDA device is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import _build
+from .scene_io import Scene, INTEGRATOR_SIMPLE, INTEGRATOR_PT
+
+PT_OK = 0
+MODE_REPLAY = 0
+MODE_WAVEFRONT = 1
+
+_f3 = ctypes.c_float * 3
+
+
+class PtMaterial(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("color", _f3), ("roughness", ctypes.c_float),
+                ("ior", ctypes.c_float), ("mix", ctypes.c_float), ("mat0", ctypes.c_int32),
+                ("mat1", ctypes.c_int32)]
+
+
+class PtSceneDesc(ctypes.Structure):
+    _fields_ = [("num_vertices", ctypes.c_uint32), ("positions", ctypes.c_void_p),
+                ("normals", ctypes.c_void_p), ("uvs", ctypes.c_void_p),
+                ("num_triangles", ctypes.c_uint32), ("indices", ctypes.c_void_p),
+                ("tri_material", ctypes.c_void_p), ("tri_shading", ctypes.c_void_p),
+                ("num_materials", ctypes.c_uint32), ("materials", ctypes.POINTER(PtMaterial)),
+                ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
+                ("env_base_color", _f3), ("env_z_rotation", ctypes.c_float),
+                ("env_width", ctypes.c_int32), ("env_height", ctypes.c_int32),
+                ("env_rgb", ctypes.c_void_p)]
+
+
+class PtCamera(ctypes.Structure):
+    _fields_ = [("pos", _f3), ("right", _f3), ("up", _f3), ("forward", _f3),
+                ("h_perf", ctypes.c_float), ("focus_dist", ctypes.c_float),
+                ("aperture", ctypes.c_float), ("reserved", ctypes.c_float)]
+
+
+class PtSettings(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32),
+                ("max_bounces", ctypes.c_int32), ("tile_width", ctypes.c_int32),
+                ("tile_height", ctypes.c_int32), ("integrator", ctypes.c_int32),
+                ("mode", ctypes.c_int32), ("seed", ctypes.c_uint32),
+                ("reserved", ctypes.c_int32 * 3)]
+
+
+class PtSceneInfo(ctypes.Structure):
+    _fields_ = [("num_triangles", ctypes.c_uint32), ("num_nodes", ctypes.c_uint32),
+                ("tree_height", ctypes.c_uint32), ("num_lights", ctypes.c_uint32),
+                ("device_bytes", ctypes.c_uint64), ("build_seconds", ctypes.c_double)]
+
+
+class PtStats(ctypes.Structure):
+    _fields_ = [("last_render_ms", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
+                ("device_bytes_in_use", ctypes.c_uint64), ("memory_budget", ctypes.c_uint64),
+                ("renders", ctypes.c_uint64), ("last_device_status", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class PtProfile(ctypes.Structure):
+    _fields_ = [("raygen_ms", ctypes.c_double), ("extend_ms", ctypes.c_double),
+                ("shade_ms", ctypes.c_double), ("shadow_ms", ctypes.c_double),
+                ("accumulate_ms", ctypes.c_double), ("extend_rays", ctypes.c_uint64),
+                ("shadow_rays", ctypes.c_uint64), ("extend_launches", ctypes.c_uint64),
+                ("shadow_launches", ctypes.c_uint64), ("ref_node_tests", ctypes.c_uint64),
+                ("ref_tri_tests", ctypes.c_uint64), ("ref_rays", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# Every symbol declared in include/petrichor_gb300.h (checked by the CPU tests).
+EXPORTED = [
+    "pt_abi_version", "pt_status_string", "pt_context_create", "pt_context_destroy",
+    "pt_last_error", "pt_camera_init", "pt_scene_upload", "pt_scene_release",
+    "pt_scene_info_get", "pt_render", "pt_render_device", "pt_trace_closest", "pt_get_stats",
+    "pt_get_progress", "pt_bvh_build", "pt_render_profile",
+]
+
+_lib = None
+
+
+class PtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+def load(build: bool = True):
+    """Load (building first if needed) the in-tree CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path}")
+    L = ctypes.CDLL(path)
+    vp, i32, u32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32
+    L.pt_abi_version.restype = ctypes.c_int
+    L.pt_status_string.restype = ctypes.c_char_p
+    L.pt_status_string.argtypes = [ctypes.c_int]
+    L.pt_context_create.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.pt_context_destroy.argtypes = [vp]
+    L.pt_last_error.restype = ctypes.c_char_p
+    L.pt_last_error.argtypes = [vp]
+    L.pt_camera_init.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                 ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_float),
+                                 ctypes.c_float, ctypes.POINTER(PtCamera)]
+    L.pt_scene_upload.argtypes = [vp, ctypes.POINTER(PtSceneDesc), ctypes.POINTER(i32)]
+    L.pt_scene_release.argtypes = [vp, i32]
+    L.pt_scene_info_get.argtypes = [vp, i32, ctypes.POINTER(PtSceneInfo)]
+    L.pt_render.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings), vp]
+    L.pt_render_device.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
+                                   vp, vp]
+    L.pt_trace_closest.argtypes = [vp, i32, i32, vp, ctypes.c_float, ctypes.c_float, vp, vp, vp]
+    L.pt_get_stats.argtypes = [vp, ctypes.POINTER(PtStats)]
+    L.pt_render_profile.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
+                                    vp, i32, ctypes.POINTER(PtProfile)]
+    L.pt_get_progress.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.pt_bvh_build.argtypes = [vp, u32, vp, u32, i32, ctypes.POINTER(u32), ctypes.POINTER(u32),
+                               vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def camera_from_scene(scene: Scene) -> PtCamera:
+    L = load()
+    c = scene.camera
+    pos = np.asarray(c.pos, np.float32)
+    d = np.asarray(c.view_dir, np.float32)
+    ft = None if c.focus_target is None else np.asarray(c.focus_target, np.float32)
+    out = PtCamera()
+    rc = L.pt_camera_init(_fptr(pos), _fptr(d), c.fov, c.focal_length,
+                          _fptr(ft) if ft is not None else None, c.aperture, ctypes.byref(out))
+    if rc != PT_OK:
+        raise PtError(rc, "pt_camera_init failed")
+    return out
+
+
+def settings_from_scene(scene: Scene, mode: int = MODE_REPLAY, seed: int = 1, **over) -> PtSettings:
+    s = scene.settings
+    st = PtSettings()
+    st.width = over.get("width", s.width)
+    st.height = over.get("height", s.height)
+    st.spp = over.get("spp", s.spp)
+    st.max_bounces = over.get("max_bounces", s.max_bounces)
+    st.tile_width = over.get("tile_width", s.tile_width)
+    st.tile_height = over.get("tile_height", s.tile_height)
+    st.integrator = over.get("integrator", s.integrator)
+    st.mode = mode
+    st.seed = seed
+    return st
+
+
+class Context:
+    """One CUDA device context of the path-tracing core."""
+
+    def __init__(self, device: int = 0, memory_budget: int = 0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        rc = self.L.pt_context_create(device, memory_budget, ctypes.byref(h))
+        if rc != PT_OK:
+            raise PtError(rc, "pt_context_create failed: " +
+                          self.L.pt_status_string(rc).decode())
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pt_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc != PT_OK:
+            raise PtError(rc, f"{what}: {self.L.pt_last_error(self.h).decode()}")
+
+    def upload(self, scene: Scene) -> int:
+        pos = np.ascontiguousarray(scene.positions, np.float32)
+        nrm = np.ascontiguousarray(scene.normals, np.float32)
+        idx = np.ascontiguousarray(scene.indices, np.int32)
+        tm = np.ascontiguousarray(scene.tri_material, np.int32)
+        sh = np.ascontiguousarray(scene.tri_shading, np.uint8)
+        lights = np.ascontiguousarray(scene.lights, np.int32)
+        mats = (PtMaterial * max(1, len(scene.materials)))()
+        for k, m in enumerate(scene.materials):
+            mats[k].kind = m.kind
+            mats[k].color = _f3(*m.color)
+            mats[k].roughness = m.roughness
+            mats[k].ior = m.ior
+            mats[k].mix = m.mix
+            mats[k].mat0 = m.mat0
+            mats[k].mat1 = m.mat1
+        d = PtSceneDesc()
+        d.num_vertices = pos.shape[0]
+        d.positions = pos.ctypes.data
+        d.normals = nrm.ctypes.data
+        d.uvs = None
+        d.num_triangles = idx.shape[0]
+        d.indices = idx.ctypes.data
+        d.tri_material = tm.ctypes.data
+        d.tri_shading = sh.ctypes.data
+        d.num_materials = len(scene.materials)
+        d.materials = mats
+        d.num_lights = lights.shape[0]
+        d.lights = lights.ctypes.data if lights.size else None
+        e = scene.env
+        d.env_base_color = _f3(*e.base_color)
+        d.env_z_rotation = e.z_rotation
+        env = None
+        if e.texture is not None:
+            env = np.ascontiguousarray(e.texture, np.float32)
+            d.env_width, d.env_height = env.shape[1], env.shape[0]
+            d.env_rgb = env.ctypes.data
+        sid = ctypes.c_int32()
+        self._check(self.L.pt_scene_upload(self.h, ctypes.byref(d), ctypes.byref(sid)),
+                    "pt_scene_upload")
+        return sid.value
+
+    def release(self, sid: int):
+        self._check(self.L.pt_scene_release(self.h, sid), "pt_scene_release")
+
+    def scene_info(self, sid: int) -> PtSceneInfo:
+        info = PtSceneInfo()
+        self._check(self.L.pt_scene_info_get(self.h, sid, ctypes.byref(info)), "pt_scene_info_get")
+        return info
+
+    def render(self, sid: int, camera: PtCamera, settings: PtSettings,
+               out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((settings.height, settings.width, 3), np.float32)
+        assert out.flags.c_contiguous and out.dtype == np.float32
+        assert out.size == settings.width * settings.height * 3
+        self._check(self.L.pt_render(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
+                                     out.ctypes.data), "pt_render")
+        return out
+
+    def render_device(self, sid: int, camera: PtCamera, settings: PtSettings, film_ptr: int,
+                      stream_ptr: int = 0):
+        self._check(self.L.pt_render_device(self.h, sid, ctypes.byref(camera),
+                                            ctypes.byref(settings), film_ptr, stream_ptr or None),
+                    "pt_render_device")
+
+    def render_profile(self, sid: int, camera: PtCamera, settings: PtSettings, film_ptr: int,
+                       count_reference: bool = True) -> PtProfile:
+        p = PtProfile()
+        self._check(self.L.pt_render_profile(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
+                                             film_ptr, 1 if count_reference else 0, ctypes.byref(p)),
+                    "pt_render_profile")
+        return p
+
+    def trace_closest(self, sid: int, n: int, rays_ptr: int, dist_min: float, dist_max: float,
+                      tri_ptr: int, dist_ptr: int, stream_ptr: int = 0):
+        self._check(self.L.pt_trace_closest(self.h, sid, n, rays_ptr, dist_min, dist_max, tri_ptr,
+                                            dist_ptr, stream_ptr or None), "pt_trace_closest")
+
+    def stats(self) -> PtStats:
+        s = PtStats()
+        self._check(self.L.pt_get_stats(self.h, ctypes.byref(s)), "pt_get_stats")
+        return s
+
+    def progress(self):
+        d, t = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.L.pt_get_progress(self.h, ctypes.byref(d), ctypes.byref(t)), "progress")
+        return d.value, t.value
+
+
+def bvh_build(positions: np.ndarray, indices: np.ndarray, threads: int = 0):
+    """Host binned-SAH build: (bounds (N,6), ints (N,5), prim_ids (T,), height)."""
+    L = load()
+    pos = np.ascontiguousarray(positions, np.float32)
+    idx = np.ascontiguousarray(indices, np.int32)
+    n, h = ctypes.c_uint32(), ctypes.c_uint32()
+    rc = L.pt_bvh_build(pos.ctypes.data, pos.shape[0], idx.ctypes.data, idx.shape[0], threads,
+                        ctypes.byref(n), ctypes.byref(h), None, None, None)
+    if rc != PT_OK:
+        raise PtError(rc, "pt_bvh_build failed")
+    b = np.zeros((n.value, 6), np.float32)
+    q = np.zeros((n.value, 5), np.int32)
+    ids = np.zeros(idx.shape[0], np.int32)
+    rc = L.pt_bvh_build(pos.ctypes.data, pos.shape[0], idx.ctypes.data, idx.shape[0], threads,
+                        ctypes.byref(n), ctypes.byref(h), b.ctypes.data, q.ctypes.data,
+                        ids.ctypes.data)
+    if rc != PT_OK:
+        raise PtError(rc, "pt_bvh_build failed")
+    return b, q, ids, h.value
+
+
+def render_scene(scene: Scene, mode: int = MODE_REPLAY, seed: int = 1, ctx: Optional[Context] = None,
+                 **over) -> np.ndarray:
+    """Upload, render and release in one call (the shape of Petrichor::Render)."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        sid = ctx.upload(scene)
+        try:
+            return ctx.render(sid, camera_from_scene(scene), settings_from_scene(scene, mode, seed, **over))
+        finally:
+            ctx.release(sid)
+    finally:
+        if own:
+            ctx.close()

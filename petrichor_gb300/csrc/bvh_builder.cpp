@@ -1,0 +1,218 @@
+// Host binned-SAH builder; see bvh_builder.h for what it reproduces and how.
+// Built with -ffp-contract=off so every float operation rounds as the
+// reference's x86-64 build does.
+#include "bvh_builder.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <deque>
+#include <future>
+#include <limits>
+#include <mutex>
+#include <thread>
+
+namespace ptg {
+namespace {
+
+constexpr int kBins = 16;           // BinnedSAHBVH.h:174
+constexpr int kMaxLeafPrims = 4;    // BinnedSAHBVH.cpp:62
+constexpr int kParallelCutoff = 32768;
+
+struct Box {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    void Merge(const Box& b) {  // AABB::Merge (AABB.cpp:10-20): std::min/std::max
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], b.lo[a]);
+            hi[a] = std::max(hi[a], b.hi[a]);
+        }
+    }
+    void Merge(const float* p) {
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], p[a]);
+            hi[a] = std::max(hi[a], p[a]);
+        }
+    }
+    float SurfaceArea() const {  // AABB.h:71-76
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    }
+    int WidestAxis() const {  // AABB.cpp:54-71
+        float best = 0.0f;
+        int axis = 0;
+        for (int a = 0; a < 3; a++) {
+            const float w = hi[a] - lo[a];
+            if (w > best) {
+                best = w;
+                axis = a;
+            }
+        }
+        return axis;
+    }
+};
+
+struct Prim {
+    Box box;
+    float c[3];
+};
+
+struct BNode {
+    Box box;
+    int begin, end;
+    BNode* left = nullptr;
+    BNode* right = nullptr;
+};
+
+// Node storage shared by all build tasks (deque keeps addresses stable).
+struct Arena {
+    std::mutex mu;
+    std::deque<BNode> nodes;
+    BNode* New(const Box& b, int begin, int end) {
+        std::lock_guard<std::mutex> g(mu);
+        nodes.push_back(BNode{b, begin, end});
+        return &nodes.back();
+    }
+};
+
+struct Builder {
+    const std::vector<Prim>& prims;
+    std::vector<int32_t>& ids;
+    Arena& arena;
+    std::atomic<int>& budget;  // threads still available for subtree tasks
+
+    // Splits `n` (or leaves it a leaf) exactly as the reference's loop body does.
+    void Split(BNode* n) {
+        const int b = n->begin, e = n->end;
+        if (e - b <= kMaxLeafPrims) return;
+        Box cb;
+        for (int i = b; i < e; i++) cb.Merge(prims[ids[i]].c);
+        const int ax = cb.WidestAxis();
+        std::sort(ids.begin() + b, ids.begin() + e,
+                  [&](int x, int y) { return prims[x].c[ax] < prims[y].c[ax]; });
+        const float len = cb.hi[ax] - cb.lo[ax];
+        Box binBox[kBins];
+        int binCount[kBins] = {0};
+        for (int i = b; i < e; i++) {
+            const Prim& p = prims[ids[i]];
+            const float l = p.c[ax] - cb.lo[ax];
+            const float f = std::nextafter(kBins * l / len, 0.0f);
+            // zero-width centroid range: NaN bin in the reference (an undefined cast);
+            // every candidate split then puts all primitives on one side -> leaf.
+            int bin = std::isnan(f) ? 0 : (int)f;
+            bin = std::min(std::max(bin, 0), kBins - 1);
+            binBox[bin].Merge(p.box);
+            binCount[bin]++;
+        }
+        // GetSAHCost for every candidate split k: left = bins < k, right = bins >= k.
+        Box suffix[kBins + 1];
+        int suffixCount[kBins + 1] = {0};
+        for (int k = kBins - 1; k >= 0; k--) {
+            suffix[k] = suffix[k + 1];
+            suffix[k].Merge(binBox[k]);
+            suffixCount[k] = suffixCount[k + 1] + binCount[k];
+        }
+        Box prefix;
+        int prefixCount = 0;
+        int bestBin = 0, bestLeft = 0;
+        float minCost = std::numeric_limits<float>::max();
+        Box bestL, bestR;
+        for (int k = 0; k < kBins; k++) {
+            if (k > 0) {
+                prefix.Merge(binBox[k - 1]);
+                prefixCount += binCount[k - 1];
+            }
+            const int nl = prefixCount, nr = suffixCount[k];
+            const float sal = nl ? prefix.SurfaceArea() : 0;
+            const float sar = nr ? suffix[k].SurfaceArea() : 0;
+            const float cost = nl * sal + nr * sar;
+            if (cost < minCost) {
+                minCost = cost;
+                bestBin = k;
+                bestLeft = nl;
+                bestL = prefix;
+                bestR = suffix[k];
+            }
+        }
+        if (bestBin == 0) return;
+        n->left = arena.New(bestL, b, b + bestLeft);
+        n->right = arena.New(bestR, b + bestLeft, e);
+    }
+
+    void Build(BNode* n) {
+        Split(n);
+        if (!n->left) return;
+        const bool bigL = n->left->end - n->left->begin > kParallelCutoff;
+        const bool bigR = n->right->end - n->right->begin > kParallelCutoff;
+        if (bigL && bigR && budget.fetch_sub(1) > 0) {
+            auto f = std::async(std::launch::async, [this, n] { Build(n->left); });
+            Build(n->right);
+            f.get();
+            budget.fetch_add(1);
+        } else {
+            if (bigL && bigR) budget.fetch_add(1);
+            Build(n->right);
+            Build(n->left);
+        }
+    }
+};
+
+}  // namespace
+
+BvhResult BuildBinnedSah(const float* P, const int32_t* idx, int T, int threads) {
+    BvhResult out;
+    std::vector<Prim> prims(T);
+    Box root;
+    for (int t = 0; t < T; t++) {
+        Prim& p = prims[t];
+        const float* v[3] = {P + 3 * idx[3 * t], P + 3 * idx[3 * t + 1], P + 3 * idx[3 * t + 2]};
+        for (int k = 0; k < 3; k++) p.box.Merge(v[k]);
+        for (int a = 0; a < 3; a++) p.c[a] = (v[0][a] + v[1][a] + v[2][a]) / 3.0f;  // Triangle::GetCentroid
+        root.Merge(p.box);
+    }
+    out.primIds.resize(T);
+    for (int i = 0; i < T; i++) out.primIds[i] = i;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    Arena arena;
+    std::atomic<int> budget(threads - 1);
+    Builder bld{prims, out.primIds, arena, budget};
+    BNode* r = arena.New(root, 0, T);
+    bld.Build(r);
+
+    // Number nodes in the reference's order: a node's two children get the next two
+    // indices when it is split; the right subtree is then split before the left.
+    out.nodes.reserve(arena.nodes.size());
+    struct Item { BNode* n; int index; int depth; };
+    std::vector<Item> stack;
+    out.nodes.push_back({});
+    stack.push_back({r, 0, 0});
+    while (!stack.empty()) {
+        const Item it = stack.back();
+        stack.pop_back();
+        BvhNodeOut& o = out.nodes[it.index];
+        for (int a = 0; a < 3; a++) {
+            o.lo[a] = it.n->box.lo[a];
+            o.hi[a] = it.n->box.hi[a];
+        }
+        o.begin = it.n->begin;
+        o.end = it.n->end;
+        out.height = std::max(out.height, it.depth);
+        if (!it.n->left) {
+            o.leaf = true;
+            o.child[0] = o.child[1] = (it.index == 0) ? 0 : -1;
+            continue;
+        }
+        o.leaf = false;
+        const int li = (int)out.nodes.size();
+        o.child[0] = li;
+        o.child[1] = li + 1;
+        out.nodes.push_back({});
+        out.nodes.push_back({});
+        stack.push_back({it.n->left, li, it.depth + 1});
+        stack.push_back({it.n->right, li + 1, it.depth + 1});
+    }
+    return out;
+}
+
+}  // namespace ptg

@@ -1,0 +1,34 @@
+// Host binned-SAH BVH builder.
+//
+// Produces the same tree as the reference's BinnedSAHBVH::Build
+// (Core/Accel/BinnedSAHBVH.cpp:15-225): same 16-bin SAH over centroid bins of
+// the widest centroid axis, the same std::sort of each node's primitive range,
+// the same leaf rule (<= 4 primitives, or best split at bin 0) and the same node
+// numbering (children appended in pairs, right subtree numbered before the left).
+// It differs in how it gets there: one binning pass per node instead of 16 cost
+// passes, and independent subtrees built on several threads, with the node
+// numbers assigned in a final depth-first pass.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace ptg {
+
+struct BvhNodeOut {
+    float lo[3], hi[3];
+    int32_t child[2];  // -1 -1 for leaves (children are always consecutive)
+    int32_t begin, end;
+    bool leaf;
+};
+
+struct BvhResult {
+    std::vector<BvhNodeOut> nodes;
+    std::vector<int32_t> primIds;
+    int height = 0;  // longest root-to-leaf edge count
+};
+
+// positions: V x 3 floats; indices: T x 3. threads <= 0: hardware concurrency.
+BvhResult BuildBinnedSah(const float* positions, const int32_t* indices, int numTriangles,
+                         int threads);
+
+}  // namespace ptg

@@ -1,0 +1,716 @@
+// C ABI (include/petrichor_gb300.h): contexts, resident scenes, renders.
+//
+// Host code, built with -ffp-contract=off: the few float quantities derived
+// here (camera basis, light area sum, environment row tables) are computed with
+// the reference's operation order so the replay path stays bit-exact.
+#include "petrichor_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bvh_builder.h"
+#include "pt_kernels.h"
+#include "pt_layout.h"
+
+using namespace ptg;
+
+namespace {
+
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct SceneGpu {
+    DevScene dev{};
+    std::vector<DeviceBuffer> buffers;
+    pt_scene_info info{};
+};
+
+}  // namespace
+
+struct pt_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0;  // 0 = unlimited
+    uint64_t used = 0;
+    std::mutex mu;
+    std::string lastError;
+    std::map<int, std::unique_ptr<SceneGpu>> scenes;
+    int nextId = 1;
+    // wavefront buffers
+    WaveBuffers wb{};
+    std::vector<DeviceBuffer> wbBuffers;
+    int wbCapacity = 0, wbPixels = 0;
+    // scratch for host-film renders and replay stacks
+    DeviceBuffer film, stack, status;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    pt_stats stats{};
+    uint32_t tilesDone = 0, tilesTotal = 0;
+};
+
+namespace {
+
+int Fail(pt_context* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->lastError = msg;
+    return code;
+}
+
+int CudaFail(pt_context* ctx, cudaError_t e, const char* what) {
+    const bool sticky = e == cudaErrorIllegalAddress || e == cudaErrorLaunchFailure ||
+                        e == cudaErrorIllegalInstruction || e == cudaErrorMisalignedAddress ||
+                        e == cudaErrorHardwareStackError;
+    return Fail(ctx, sticky ? PT_ERR_DEVICE_FAULT : PT_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int Alloc(pt_context* ctx, DeviceBuffer& b, size_t bytes) {
+    if (b.bytes >= bytes && b.ptr) return PT_OK;
+    if (ctx->budget && ctx->used - b.bytes + bytes > ctx->budget)
+        return Fail(ctx, PT_ERR_OVER_BUDGET, "allocation of " + std::to_string(bytes) +
+                                                 " bytes exceeds the memory budget");
+    if (b.ptr) {
+        cudaFree(b.ptr);
+        ctx->used -= b.bytes;
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    if (bytes == 0) return PT_OK;
+    const cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        return Fail(ctx, PT_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    ctx->used += bytes;
+    return PT_OK;
+}
+
+void Free(pt_context* ctx, DeviceBuffer& b) {
+    if (b.ptr) {
+        cudaFree(b.ptr);
+        ctx->used -= b.bytes;
+    }
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+template <typename T>
+int Upload(pt_context* ctx, SceneGpu& s, const std::vector<T>& host, const T** devOut) {
+    DeviceBuffer b;
+    const size_t bytes = std::max<size_t>(host.size() * sizeof(T), 16);
+    int rc = Alloc(ctx, b, bytes);
+    if (rc != PT_OK) return rc;
+    s.buffers.push_back(b);
+    if (!host.empty()) {
+        const cudaError_t e =
+          cudaMemcpyAsync(b.ptr, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return CudaFail(ctx, e, "scene upload");
+    }
+    *devOut = (const T*)b.ptr;
+    return PT_OK;
+}
+
+inline float4 F4(float a, float b, float c, float d) {
+    float4 r;
+    r.x = a;
+    r.y = b;
+    r.z = c;
+    r.w = d;
+    return r;
+}
+inline float IntBits(int32_t v) {
+    float f;
+    std::memcpy(&f, &v, 4);
+    return f;
+}
+
+struct HV3 {
+    float x, y, z;
+};
+inline HV3 Sub(HV3 a, HV3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline HV3 Cross(HV3 a, HV3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline float Dot(HV3 a, HV3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float Length(HV3 a) { return (float)std::sqrt((double)Dot(a, a)); }
+inline HV3 Normalized(HV3 a) {
+    const float l = Length(a);
+    return {a.x / l, a.y / l, a.z / l};
+}
+inline HV3 Load(const float* p) { return {p[0], p[1], p[2]}; }
+
+int Validate(pt_context* ctx, const pt_scene_desc* d) {
+    if (!d) return Fail(ctx, PT_ERR_INVALID_ARG, "scene description is NULL");
+    if (d->num_triangles && (!d->indices || !d->tri_material || !d->positions))
+        return Fail(ctx, PT_ERR_INVALID_ARG, "triangles need positions, indices and materials");
+    if (d->num_triangles > (1u << 30)) return Fail(ctx, PT_ERR_INVALID_ARG, "too many triangles");
+    if (d->num_materials == 0 || !d->materials)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "at least one material is required");
+    if (d->num_materials > 65535) return Fail(ctx, PT_ERR_INVALID_ARG, "too many materials");
+    for (uint32_t t = 0; t < d->num_triangles * 3; t++)
+        if (d->indices[t] < 0 || (uint32_t)d->indices[t] >= d->num_vertices)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "triangle vertex index out of range");
+    for (uint32_t t = 0; t < d->num_triangles; t++)
+        if (d->tri_material[t] < 0 || (uint32_t)d->tri_material[t] >= d->num_materials)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "triangle material index out of range");
+    for (uint32_t m = 0; m < d->num_materials; m++) {
+        const pt_material& M = d->materials[m];
+        if (M.kind < PT_MAT_LAMBERT || M.kind > PT_MAT_MIX)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "unknown material kind");
+        if (M.kind == PT_MAT_MIX) {
+            for (int32_t r : {M.mat0, M.mat1})
+                if (r < 0 || (uint32_t)r >= d->num_materials ||
+                    d->materials[r].kind == PT_MAT_MIX)
+                    return Fail(ctx, PT_ERR_INVALID_ARG, "mix material must reference two non-mix materials");
+        }
+    }
+    for (uint32_t i = 0; i < d->num_lights; i++)
+        if (!d->lights || d->lights[i] < 0 || (uint32_t)d->lights[i] >= d->num_triangles)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "light triangle index out of range");
+    if ((d->env_width > 0) != (d->env_height > 0) || d->env_width < 0 || d->env_height < 0)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "environment size is invalid");
+    if (d->env_width > 0 && !d->env_rgb) return Fail(ctx, PT_ERR_INVALID_ARG, "environment texels missing");
+    return PT_OK;
+}
+
+int SetDevice(pt_context* ctx) {
+    const cudaError_t e = cudaSetDevice(ctx->device);
+    return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "cudaSetDevice");
+}
+
+int EnsureWaveBuffers(pt_context* ctx, int capacity, int pixels) {
+    if (ctx->wbCapacity >= capacity && ctx->wbPixels >= pixels) return PT_OK;
+    capacity = std::max(capacity, ctx->wbCapacity);
+    pixels = std::max(pixels, ctx->wbPixels);
+    for (auto& b : ctx->wbBuffers) Free(ctx, b);
+    ctx->wbBuffers.assign(11, DeviceBuffer{});
+    const size_t C = (size_t)capacity;
+    const size_t sizes[11] = {C * 2 * sizeof(float4), C * 2 * sizeof(float4), C * sizeof(float2),
+                              C * sizeof(float4),     C * sizeof(float4),     C * sizeof(float4),
+                              C * sizeof(unsigned long long), C * 4 * sizeof(float4),
+                              16 * sizeof(int),       (size_t)pixels * sizeof(float4), 0};
+    for (int i = 0; i < 10; i++) {
+        const int rc = Alloc(ctx, ctx->wbBuffers[i], sizes[i]);
+        if (rc != PT_OK) return rc;
+    }
+    WaveBuffers& w = ctx->wb;
+    w.capacity = capacity;
+    w.ray[0] = (float4*)ctx->wbBuffers[0].ptr;
+    w.ray[1] = (float4*)ctx->wbBuffers[1].ptr;
+    w.hit = (float2*)ctx->wbBuffers[2].ptr;
+    w.st0 = (float4*)ctx->wbBuffers[3].ptr;
+    w.st1 = (float4*)ctx->wbBuffers[4].ptr;
+    w.st2 = (float4*)ctx->wbBuffers[5].ptr;
+    w.rng = (unsigned long long*)ctx->wbBuffers[6].ptr;
+    w.shadow = (float4*)ctx->wbBuffers[7].ptr;
+    w.counts = (int*)ctx->wbBuffers[8].ptr;
+    w.accum = (float4*)ctx->wbBuffers[9].ptr;
+    if (!w.hostCount) {
+        const cudaError_t e = cudaMallocHost(&w.hostCount, sizeof(int) * 4);
+        if (e != cudaSuccess) return CudaFail(ctx, e, "cudaMallocHost");
+    }
+    ctx->wbCapacity = capacity;
+    ctx->wbPixels = pixels;
+    return PT_OK;
+}
+
+int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
+              SceneGpu** out) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    if (!cam || !st) return Fail(ctx, PT_ERR_INVALID_ARG, "camera and settings are required");
+    if (st->width <= 0 || st->height <= 0 || st->spp <= 0 || st->max_bounces < 0)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "width, height and spp must be positive");
+    if ((int64_t)st->width * st->height > (1ll << 28))
+        return Fail(ctx, PT_ERR_INVALID_ARG, "image too large");
+    if (st->tile_width <= 0 || st->tile_height <= 0)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "tile size must be positive");
+    if (st->integrator != PT_INTEGRATOR_SIMPLE && st->integrator != PT_INTEGRATOR_PT)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "unknown integrator");
+    if (st->mode != PT_MODE_REPLAY && st->mode != PT_MODE_WAVEFRONT)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "unknown mode");
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
+    *out = it->second.get();
+    return PT_OK;
+}
+
+DevCamera ToDev(const pt_camera* c) {
+    DevCamera d{};
+    for (int a = 0; a < 3; a++) {
+        d.pos[a] = c->pos[a];
+        d.right[a] = c->right[a];
+        d.up[a] = c->up[a];
+        d.fwd[a] = c->forward[a];
+    }
+    d.hPerf = c->h_perf;
+    d.focusDist = c->focus_dist;
+    d.aperture = c->aperture;
+    return d;
+}
+
+DevSettings ToDev(const pt_settings* s) {
+    DevSettings d{};
+    d.width = s->width;
+    d.height = s->height;
+    d.spp = s->spp;
+    d.maxBounces = s->max_bounces;
+    d.tileW = s->tile_width;
+    d.tileH = s->tile_height;
+    d.integrator = s->integrator;
+    d.seed = s->seed;
+    return d;
+}
+
+// Enqueue one render into a device film on `stream`.
+int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt_settings* st,
+                   float* dFilm, cudaStream_t stream) {
+    const DevCamera C = ToDev(cam);
+    const DevSettings S = ToDev(st);
+    cudaError_t e;
+    int launches = 0;
+    e = cudaEventRecord(ctx->ev0, stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "cudaEventRecord");
+    if (st->mode == PT_MODE_REPLAY) {
+        const int tiles = NumTiles(S);
+        int rc = Alloc(ctx, ctx->stack, (size_t)tiles * sg.dev.stackDepth * sizeof(int));
+        if (rc != PT_OK) return rc;
+        rc = Alloc(ctx, ctx->status, 16);
+        if (rc != PT_OK) return rc;
+        cudaMemsetAsync(ctx->status.ptr, 0, sizeof(int), stream);
+        ctx->tilesTotal = tiles;
+        ctx->tilesDone = 0;
+        // chunks of tiles so progress can be reported between launches
+        const int chunk = std::max(1, std::min(tiles, 8192));
+        for (int t0 = 0; t0 < tiles; t0 += chunk) {
+            const int t1 = std::min(tiles, t0 + chunk);
+            e = LaunchReplay(sg.dev, C, S, dFilm, (int*)ctx->stack.ptr, (int*)ctx->status.ptr, t0, t1,
+                             stream);
+            launches++;
+            if (e != cudaSuccess) return CudaFail(ctx, e, "replay launch");
+        }
+    } else {
+        const int64_t paths = (int64_t)st->width * st->height * st->spp;
+        const int cap = (int)std::min<int64_t>(paths, 1 << 22);
+        int rc = EnsureWaveBuffers(ctx, std::max(cap, std::min(st->width * st->height, 1 << 22)),
+                                   st->width * st->height);
+        if (rc != PT_OK) return rc;
+        e = RenderWavefront(sg.dev, C, S, ctx->wb, dFilm, stream, &launches, 0);
+        if (e != cudaSuccess) return CudaFail(ctx, e, "wavefront render");
+    }
+    e = cudaEventRecord(ctx->ev1, stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "cudaEventRecord");
+    ctx->stats.kernel_launches += launches;
+    ctx->stats.renders++;
+    return PT_OK;
+}
+
+int FinishStats(pt_context* ctx, cudaStream_t stream) {
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "render");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.last_render_ms = ms;
+    int status = 0;
+    if (ctx->status.ptr) cudaMemcpy(&status, ctx->status.ptr, sizeof(int), cudaMemcpyDeviceToHost);
+    int wstatus = 0;
+    if (ctx->wb.counts) cudaMemcpy(&wstatus, ctx->wb.counts + 3, sizeof(int), cudaMemcpyDeviceToHost);
+    ctx->stats.last_device_status = status | (wstatus << 8);
+    ctx->tilesDone = ctx->tilesTotal;
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_abi_version(void) { return PT_ABI_VERSION; }
+
+const char* pt_status_string(int s) {
+    switch (s) {
+    case PT_OK: return "ok";
+    case PT_ERR_INVALID_ARG: return "invalid argument";
+    case PT_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case PT_ERR_OVER_BUDGET: return "over the memory budget";
+    case PT_ERR_TIMEOUT: return "timed out";
+    case PT_ERR_CUDA: return "CUDA error";
+    case PT_ERR_NOT_FOUND: return "not found";
+    case PT_ERR_UNSUPPORTED: return "unsupported";
+    case PT_ERR_BUSY: return "busy";
+    case PT_ERR_CANCELLED: return "cancelled";
+    case PT_ERR_NO_DEVICE: return "no CUDA device";
+    case PT_ERR_DEVICE_FAULT: return "device fault (context unusable)";
+    default: return "unknown status";
+    }
+}
+
+int pt_context_create(int device, uint64_t budget, pt_context** out) {
+    if (!out) return PT_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return PT_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return PT_ERR_INVALID_ARG;
+    auto ctx = std::make_unique<pt_context>();
+    ctx->device = device;
+    ctx->budget = budget;
+    if (SetDevice(ctx.get()) != PT_OK) return PT_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return PT_ERR_CUDA;
+    if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
+        return PT_ERR_CUDA;
+    ctx->stats.memory_budget = budget;
+    *out = ctx.release();
+    return PT_OK;
+}
+
+int pt_context_destroy(pt_context* ctx) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        for (auto& kv : ctx->scenes)
+            for (auto& b : kv.second->buffers) Free(ctx, b);
+        ctx->scenes.clear();
+        for (auto& b : ctx->wbBuffers) Free(ctx, b);
+        if (ctx->wb.hostCount) cudaFreeHost(ctx->wb.hostCount);
+        Free(ctx, ctx->film);
+        Free(ctx, ctx->stack);
+        Free(ctx, ctx->status);
+        if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+        if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return PT_OK;
+}
+
+const char* pt_last_error(const pt_context* ctx) { return ctx ? ctx->lastError.c_str() : ""; }
+
+int pt_camera_init(const float pos[3], const float dir[3], float fov, float focalLength,
+                   const float* focusTarget, float aperture, pt_camera* out) {
+    if (!pos || !dir || !out) return PT_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    const HV3 p = Load(pos);
+    // Camera::SetViewDir (Camera.cpp:38-44), world up = +Z
+    const HV3 f = Normalized(Load(dir));
+    const HV3 r = Cross(f, HV3{0.0f, 0.0f, 1.0f});
+    const HV3 u = Cross(r, f);
+    const HV3* src[4] = {&p, &r, &u, &f};
+    float* dst[4] = {out->pos, out->right, out->up, out->forward};
+    for (int k = 0; k < 4; k++) {
+        dst[k][0] = src[k]->x;
+        dst[k][1] = src[k]->y;
+        dst[k][2] = src[k]->z;
+    }
+    const float sensor = 24e-3f;
+    if (fov > 0.0f) out->h_perf = (float)(2.0f * std::tan((double)(0.5f * fov)));  // SetFOV
+    else if (focalLength > 0.0f) out->h_perf = sensor / focalLength;             // SetFocalLength
+    else return PT_ERR_INVALID_ARG;
+    out->focus_dist = focusTarget ? Length(Sub(Load(focusTarget), p)) : 1.0f;  // FocusTo
+    out->aperture = aperture;
+    return PT_OK;
+}
+
+int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
+    if (!ctx || !out) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    int rc = Validate(ctx, d);
+    if (rc != PT_OK) return rc;
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    auto sg = std::make_unique<SceneGpu>();
+    const int T = (int)d->num_triangles;
+    const auto t0 = std::chrono::steady_clock::now();
+    BvhResult bvh = BuildBinnedSah(d->positions, d->indices, T, 0);
+    const double buildSec =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    // nodes
+    std::vector<float4> nodes(bvh.nodes.size() * 2);
+    for (size_t i = 0; i < bvh.nodes.size(); i++) {
+        const BvhNodeOut& n = bvh.nodes[i];
+        const int32_t a = n.leaf ? n.begin : n.child[0];
+        const int32_t b = n.leaf ? (n.end - n.begin) : -1;
+        nodes[2 * i] = F4(n.lo[0], n.lo[1], n.lo[2], n.hi[0]);
+        nodes[2 * i + 1] = F4(n.hi[1], n.hi[2], IntBits(a), IntBits(b));
+    }
+    // triangles in leaf order
+    std::vector<float4> tris((size_t)T * 3);
+    for (int k = 0; k < T; k++) {
+        const int t = bvh.primIds[k];
+        const HV3 v0 = Load(d->positions + 3 * d->indices[3 * t]);
+        const HV3 e1 = Sub(Load(d->positions + 3 * d->indices[3 * t + 1]), v0);
+        const HV3 e2 = Sub(Load(d->positions + 3 * d->indices[3 * t + 2]), v0);
+        tris[3 * (size_t)k] = F4(v0.x, v0.y, v0.z, e1.x);
+        tris[3 * (size_t)k + 1] = F4(e1.y, e1.z, e2.x, e2.y);
+        tris[3 * (size_t)k + 2] = F4(e2.z, IntBits(t), 0.0f, 0.0f);
+    }
+    // per-triangle shading records
+    std::vector<float4> shade((size_t)T * 3);
+    for (int t = 0; t < T; t++) {
+        HV3 n[3] = {{0, 0, 1}, {0, 0, 1}, {0, 0, 1}};
+        if (d->normals)
+            for (int k = 0; k < 3; k++) n[k] = Load(d->normals + 3 * d->indices[3 * t + k]);
+        const int smooth = d->tri_shading ? (d->tri_shading[t] ? 1 : 0) : 0;
+        shade[3 * (size_t)t] = F4(n[0].x, n[0].y, n[0].z, IntBits(d->tri_material[t]));
+        shade[3 * (size_t)t + 1] = F4(n[1].x, n[1].y, n[1].z, IntBits(smooth));
+        shade[3 * (size_t)t + 2] = F4(n[2].x, n[2].y, n[2].z, 0.0f);
+    }
+    // materials
+    std::vector<DevMaterial> mats(d->num_materials);
+    for (uint32_t m = 0; m < d->num_materials; m++) {
+        const pt_material& M = d->materials[m];
+        DevMaterial& o = mats[m];
+        o.kind = M.kind;
+        o.cr = M.color[0];
+        o.cg = M.color[1];
+        o.cb = M.color[2];
+        o.alpha = M.roughness * M.roughness;  // GGX::GGX (GGX.cpp:16-20)
+        o.ior = M.ior;
+        o.mix = M.mix;
+        o.mat01 = M.kind == PT_MAT_MIX ? (M.mat0 | (M.mat1 << 16)) : 0;
+    }
+    // lights and 1 / sum(1 / pdfArea_i) (PathTracing.cpp:363-383, Triangle.cpp:155-182)
+    std::vector<float4> lights((size_t)std::max<uint32_t>(d->num_lights, 1) * 3);
+    float sumArea = 0.0f;
+    for (uint32_t i = 0; i < d->num_lights; i++) {
+        const int t = d->lights[i];
+        const HV3 v0 = Load(d->positions + 3 * d->indices[3 * t]);
+        const HV3 e0 = Sub(Load(d->positions + 3 * d->indices[3 * t + 1]), v0);
+        const HV3 e1 = Sub(Load(d->positions + 3 * d->indices[3 * t + 2]), v0);
+        lights[3 * i] = F4(v0.x, v0.y, v0.z, IntBits(t));
+        lights[3 * i + 1] = F4(e0.x, e0.y, e0.z, 0.0f);
+        lights[3 * i + 2] = F4(e1.x, e1.y, e1.z, 0.0f);
+        const float pdfAreaEach = 1.0f / (0.5f * Length(Cross(e0, e1)));
+        sumArea += 1.0f / pdfAreaEach;
+    }
+    // environment texels and the row tables of Environment::PreCalcCumulativeDistTex
+    // (Environment.cpp:56-128). The reference reads its table textures through an
+    // unloaded Texture2D, whose texel reads all return (1, 0, 1): each row's
+    // luminance sum reads as 1, so pdf1D = H / H and cdf1D = (j + 1) / H.
+    const int W = d->env_width, H = d->env_height;
+    std::vector<float4> env((size_t)std::max(W * H, 1));
+    std::vector<float> pdf1D(std::max(H, 1)), cdf1D(std::max(H, 1));
+    if (W > 0) {
+        for (size_t i = 0; i < (size_t)W * H; i++)
+            env[i] = F4(d->env_rgb[3 * i], d->env_rgb[3 * i + 1], d->env_rgb[3 * i + 2], 0.0f);
+        float sum = 0.0f;
+        for (int j = 0; j < H; j++) {
+            const float l = 1.0f;
+            pdf1D[j] = l;
+            sum += l;
+            cdf1D[j] = sum;
+        }
+        for (int j = 0; j < H; j++) {
+            pdf1D[j] *= (H / sum);
+            cdf1D[j] /= sum;
+        }
+    }
+    SceneGpu& s = *sg;
+    DevScene& D = s.dev;
+    if ((rc = Upload(ctx, s, nodes, &D.nodes)) != PT_OK ||
+        (rc = Upload(ctx, s, tris, &D.tris)) != PT_OK ||
+        (rc = Upload(ctx, s, shade, &D.shade)) != PT_OK ||
+        (rc = Upload(ctx, s, mats, &D.mats)) != PT_OK ||
+        (rc = Upload(ctx, s, lights, &D.lights)) != PT_OK ||
+        (rc = Upload(ctx, s, env, &D.env)) != PT_OK ||
+        (rc = Upload(ctx, s, cdf1D, &D.cdf1D)) != PT_OK ||
+        (rc = Upload(ctx, s, pdf1D, &D.pdf1D)) != PT_OK) {
+        for (auto& b : s.buffers) Free(ctx, b);
+        return rc;
+    }
+    D.numNodes = T > 0 ? (int)bvh.nodes.size() : 0;
+    D.numTris = T;
+    D.numMats = (int)d->num_materials;
+    D.numLights = (int)d->num_lights;
+    D.envW = W;
+    D.envH = H;
+    D.envValid = W > 0 ? 1 : 0;
+    D.stackDepth = bvh.height + 2;
+    for (int a = 0; a < 3; a++) D.envBase[a] = d->env_base_color[a];
+    D.envRot = d->env_z_rotation;
+    D.lightPdfArea = 1.0f / sumArea;
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        for (auto& b : s.buffers) Free(ctx, b);
+        return CudaFail(ctx, e, "scene upload");
+    }
+    if (bvh.height + 1 >= kWaveStackDepth) {
+        for (auto& b : s.buffers) Free(ctx, b);
+        return Fail(ctx, PT_ERR_UNSUPPORTED, "BVH height " + std::to_string(bvh.height) +
+                                                 " exceeds the traversal stack");
+    }
+    s.info.num_triangles = T;
+    s.info.num_nodes = (uint32_t)bvh.nodes.size();
+    s.info.tree_height = bvh.height;
+    s.info.num_lights = d->num_lights;
+    s.info.build_seconds = buildSec;
+    for (auto& b : s.buffers) s.info.device_bytes += b.bytes;
+    const int id = ctx->nextId++;
+    ctx->scenes[id] = std::move(sg);
+    *out = id;
+    return PT_OK;
+}
+
+int pt_scene_release(pt_context* ctx, pt_scene_id id) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& b : it->second->buffers) Free(ctx, b);
+    ctx->scenes.erase(it);
+    return PT_OK;
+}
+
+int pt_scene_info_get(pt_context* ctx, pt_scene_id id, pt_scene_info* info) {
+    if (!ctx || !info) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
+    *info = it->second->info;
+    return PT_OK;
+}
+
+int pt_render(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
+              float* film) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!film) return Fail(ctx, PT_ERR_INVALID_ARG, "film is NULL");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    const size_t bytes = (size_t)st->width * st->height * 3 * sizeof(float);
+    if ((rc = Alloc(ctx, ctx->film, bytes)) != PT_OK) return rc;
+    if ((rc = RenderOnStream(ctx, *sg, cam, st, (float*)ctx->film.ptr, ctx->stream)) != PT_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(film, ctx->film.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "film download");
+    return FinishStats(ctx, ctx->stream);
+}
+
+int pt_render_device(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
+                     const pt_settings* st, float* dFilm, void* stream) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!dFilm) return Fail(ctx, PT_ERR_INVALID_ARG, "film is NULL");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return RenderOnStream(ctx, *sg, cam, st, dFilm, s);
+}
+
+int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
+                      const pt_settings* st, float* dFilm, int32_t countReference, pt_profile* out) {
+    if (!ctx || !out) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!dFilm) return Fail(ctx, PT_ERR_INVALID_ARG, "film is NULL");
+    if (st->mode != PT_MODE_WAVEFRONT)
+        return Fail(ctx, PT_ERR_UNSUPPORTED, "profiling covers the wavefront mode");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    const int64_t paths = (int64_t)st->width * st->height * st->spp;
+    const int cap = (int)std::min<int64_t>(paths, 1 << 22);
+    rc = EnsureWaveBuffers(ctx, std::max(cap, std::min(st->width * st->height, 1 << 22)),
+                           st->width * st->height);
+    if (rc != PT_OK) return rc;
+    DeviceBuffer counters;
+    if ((rc = Alloc(ctx, counters, 8 * sizeof(unsigned long long))) != PT_OK) return rc;
+    cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), ctx->stream);
+    WaveProfile prof;
+    prof.countReference = countReference != 0;
+    prof.devCounters = (unsigned long long*)counters.ptr;
+    int launches = 0;
+    const cudaError_t e = RenderWavefront(sg->dev, ToDev(cam), ToDev(st), ctx->wb, dFilm, ctx->stream,
+                                          &launches, 0, &prof);
+    Free(ctx, counters);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "profiled render");
+    ctx->stats.kernel_launches += launches;
+    std::memset(out, 0, sizeof(*out));
+    out->raygen_ms = prof.ms[0];
+    out->extend_ms = prof.ms[1];
+    out->shade_ms = prof.ms[2];
+    out->shadow_ms = prof.ms[3];
+    out->accumulate_ms = prof.ms[4];
+    out->extend_rays = prof.extendRays;
+    out->shadow_rays = prof.shadowRays;
+    out->extend_launches = prof.extendLaunches;
+    out->shadow_launches = prof.shadowLaunches;
+    out->ref_node_tests = prof.refNodeTests;
+    out->ref_tri_tests = prof.refTriTests;
+    out->ref_rays = prof.refRays;
+    return PT_OK;
+}
+
+int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float* rays,
+                     float distMin, float distMax, int32_t* tri, float* dist, void* stream) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
+    if (n < 0 || (n > 0 && (!rays || !tri || !dist)))
+        return Fail(ctx, PT_ERR_INVALID_ARG, "bad ray buffers");
+    int rc = SetDevice(ctx);
+    if (rc != PT_OK) return rc;
+    const cudaError_t e = LaunchTraceClosest(it->second->dev, n, rays, distMin, distMax, tri, dist,
+                                             stream ? (cudaStream_t)stream : ctx->stream);
+    ctx->stats.kernel_launches++;
+    return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "trace");
+}
+
+int pt_bvh_build(const float* positions, uint32_t numVertices, const int32_t* indices,
+                 uint32_t numTriangles, int32_t threads, uint32_t* numNodes, uint32_t* height,
+                 float* bounds, int32_t* nodeInts, int32_t* primIds) {
+    if (!numNodes || (numTriangles && (!positions || !indices))) return PT_ERR_INVALID_ARG;
+    for (uint32_t t = 0; t < numTriangles * 3; t++)
+        if (indices[t] < 0 || (uint32_t)indices[t] >= numVertices) return PT_ERR_INVALID_ARG;
+    const BvhResult r = BuildBinnedSah(positions, indices, (int)numTriangles, threads);
+    *numNodes = (uint32_t)r.nodes.size();
+    if (height) *height = (uint32_t)r.height;
+    if (bounds && nodeInts) {
+        for (size_t i = 0; i < r.nodes.size(); i++) {
+            const BvhNodeOut& n = r.nodes[i];
+            for (int a = 0; a < 3; a++) {
+                bounds[6 * i + a] = n.lo[a];
+                bounds[6 * i + 3 + a] = n.hi[a];
+            }
+            nodeInts[5 * i] = n.child[0];
+            nodeInts[5 * i + 1] = n.child[1];
+            nodeInts[5 * i + 2] = n.begin;
+            nodeInts[5 * i + 3] = n.end;
+            nodeInts[5 * i + 4] = n.leaf ? 1 : 0;
+        }
+    }
+    if (primIds) std::memcpy(primIds, r.primIds.data(), r.primIds.size() * sizeof(int32_t));
+    return PT_OK;
+}
+
+int pt_get_stats(pt_context* ctx, pt_stats* out) {
+    if (!ctx || !out) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->stats.device_bytes_in_use = ctx->used;
+    *out = ctx->stats;
+    return PT_OK;
+}
+
+int pt_get_progress(pt_context* ctx, uint32_t* done, uint32_t* total) {
+    if (!ctx || !done || !total) return PT_ERR_INVALID_ARG;
+    *done = ctx->tilesDone;
+    *total = ctx->tilesTotal;
+    return PT_OK;
+}
+
+}  // extern "C"

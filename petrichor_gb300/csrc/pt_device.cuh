@@ -1,0 +1,630 @@
+// Device-side vector math, samplers and the reference renderer's shading steps.
+//
+// Every function takes a math policy M:
+//   ExactMath    - the transcendental calls of the reference resolve to the
+//                  global double overloads (float arguments promoted, result
+//                  narrowed). ExactMath evaluates them the same way, so a kernel
+//                  compiled with -fmad=false reproduces the reference's floats.
+//   FastMath     - single-precision library calls for the throughput path.
+// Operand order inside every expression follows the reference source
+// (component-wise Vector3f operators, Math/Vector3f.h), which is what makes
+// bit-parity possible; the references are given per function.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "pt_layout.h"
+
+namespace ptg {
+
+constexpr float kEps = 1.0e-3f;                    // Core/Constants.h:8
+constexpr float kFltMax = 3.402823466e+38f;
+constexpr float kInfinity = 0.9f * kFltMax;        // Core/Constants.h:10
+constexpr float kPi = 3.14159265358979f;           // Core/Constants.h:15
+constexpr float kInvPi = 1.0f / kPi;               // Core/Constants.h:16
+
+// ---------------------------------------------------------------- V3
+struct V3 {
+    float x, y, z;
+    __device__ V3() : x(0.f), y(0.f), z(0.f) {}
+    __device__ V3(float a, float b, float c) : x(a), y(b), z(c) {}
+    __device__ float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator-(V3 a) { return V3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return V3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float c) { return V3(a.x * c, a.y * c, a.z * c); }
+__device__ __forceinline__ V3 operator*(float c, V3 a) { return a * c; }
+__device__ __forceinline__ V3 operator/(V3 a, V3 b) { return V3(a.x / b.x, a.y / b.y, a.z / b.z); }
+__device__ __forceinline__ V3 operator/(V3 a, float c) { return V3(a.x / c, a.y / c, a.z / c); }
+__device__ __forceinline__ V3 operator/(float c, V3 a) { return V3(c / a.x, c / a.y, c / a.z); }
+__device__ __forceinline__ float Dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 Cross(V3 a, V3 b) {
+    return V3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float SqLen(V3 a) { return Dot(a, a); }
+__device__ __forceinline__ float Length(V3 a) { return sqrtf(Dot(a, a)); }  // = (float)sqrt(double)
+__device__ __forceinline__ V3 Normalized(V3 a) { return a / Length(a); }
+// std::min / std::max argument semantics (NaN handling included)
+__device__ __forceinline__ float SMin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float SMax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float MinElem(V3 a) { return SMin(a.x, SMin(a.y, a.z)); }
+__device__ __forceinline__ V3 Reflected(V3 d, V3 n) { return d - 2.0f * n * Dot(d, n); }
+__device__ __forceinline__ float Mod1(float x) { return x - 1.0f * floorf(x / 1.0f); }
+__device__ __forceinline__ float Lerp(float a, float b, float t) { return (1.0f - t) * a + t * b; }
+__device__ __forceinline__ float Pow5(float x) { const float x2 = x * x; return x * (x2 * x2); }
+__device__ __forceinline__ int IClamp(int v, int lo, int hi) { return v < lo ? lo : (hi < v ? hi : v); }
+__device__ __forceinline__ V3 LoadV3(const float* p) { return V3(p[0], p[1], p[2]); }
+
+// ---------------------------------------------------------------- math policies
+struct ExactMath {
+    static __device__ __forceinline__ float Cos(float x) { return (float)cos((double)x); }
+    static __device__ __forceinline__ float Sin(float x) { return (float)sin((double)x); }
+    static __device__ __forceinline__ float Acos(float x) { return (float)acos((double)x); }
+    static __device__ __forceinline__ float Atan2(float y, float x) {
+        return (float)atan2((double)y, (double)x);
+    }
+    // a * cos(x) / a * sin(x) with the float factor promoted (Lambert.cpp:67-72)
+    static __device__ __forceinline__ float MulCos(float a, float x) {
+        return (float)((double)a * cos((double)x));
+    }
+    static __device__ __forceinline__ float MulSin(float a, float x) {
+        return (float)((double)a * sin((double)x));
+    }
+    static __device__ __forceinline__ float MulSinMul(float a, float x, float b) {
+        return (float)(((double)a * sin((double)x)) * (double)b);
+    }
+    static __device__ __forceinline__ float SinCos(float t, float p) {
+        return (float)(sin((double)t) * cos((double)p));
+    }
+    static __device__ __forceinline__ float SinSin(float t, float p) {
+        return (float)(sin((double)t) * sin((double)p));
+    }
+    // -0.5f + 0.5f * sqrt(x) evaluated in double (GGX.cpp:148)
+    static __device__ __forceinline__ float SmithLambda(float x) {
+        return (float)((double)-0.5f + (double)0.5f * sqrt((double)x));
+    }
+    // -dn + sqrt(disc) evaluated in double (Vector3f.h:231-232)
+    static __device__ __forceinline__ float RefractScale(float ndn, float disc) {
+        return (float)((double)ndn + sqrt((double)disc));
+    }
+};
+struct FastMath {
+    static __device__ __forceinline__ float Cos(float x) { return cosf(x); }
+    static __device__ __forceinline__ float Sin(float x) { return sinf(x); }
+    static __device__ __forceinline__ float Acos(float x) { return acosf(x); }
+    static __device__ __forceinline__ float Atan2(float y, float x) { return atan2f(y, x); }
+    static __device__ __forceinline__ float MulCos(float a, float x) { return a * cosf(x); }
+    static __device__ __forceinline__ float MulSin(float a, float x) { return a * sinf(x); }
+    static __device__ __forceinline__ float MulSinMul(float a, float x, float b) {
+        return a * sinf(x) * b;
+    }
+    static __device__ __forceinline__ float SinCos(float t, float p) { return sinf(t) * cosf(p); }
+    static __device__ __forceinline__ float SinSin(float t, float p) { return sinf(t) * sinf(p); }
+    static __device__ __forceinline__ float SmithLambda(float x) { return -0.5f + 0.5f * sqrtf(x); }
+    static __device__ __forceinline__ float RefractScale(float ndn, float disc) {
+        return ndn + sqrtf(disc);
+    }
+};
+
+// ---------------------------------------------------------------- samplers
+// Marsaglia xor128 (Random/XorShift.h:12-59); next() = u32 / float(UINT_MAX)
+struct XorShift128 {
+    uint32_t x, y, z, w;
+    __device__ explicit XorShift128(uint32_t seed)
+        : x(123456789u), y(362436069u), z(521288629u), w(seed) {}
+    __device__ __forceinline__ float Next() {
+        const uint32_t t = x ^ (x << 11);
+        x = y;
+        y = z;
+        z = w;
+        w = (w ^ (w >> 19)) ^ (t ^ (t >> 8));
+        return __uint2float_rn(w) / 4294967296.0f;
+    }
+};
+// RandomSampler1D(seed) / RandomSampler2D(seed0, seed1) (Core/Sampler/*)
+struct RefSampler1D {
+    XorShift128 g;
+    __device__ explicit RefSampler1D(uint32_t s) : g(s) {}
+    __device__ __forceinline__ float Next() { return g.Next(); }
+};
+struct RefSampler2D {
+    XorShift128 g0, g1;
+    __device__ RefSampler2D(uint32_t s0, uint32_t s1) : g0(s0), g1(s1) {}
+    __device__ __forceinline__ void Next(float& a, float& b) {
+        a = g0.Next();
+        b = g1.Next();
+    }
+};
+
+// Counter-based per-path stream for the throughput path: SplitMix64 over a
+// 64-bit state keyed by (seed, pixel, sample); any draw depends only on the
+// path's identity, never on scheduling or batching.
+__device__ __forceinline__ uint64_t Mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint64_t PathKey(uint32_t seed, uint32_t pixel, uint32_t sample) {
+    return Mix64(Mix64(((uint64_t)seed << 32) ^ 0x5851F42D4C957F2Dull) ^
+                 (((uint64_t)pixel << 32) | sample));
+}
+struct PathRng {
+    uint64_t s;
+    __device__ explicit PathRng(uint64_t state) : s(state) {}
+    __device__ __forceinline__ float Next() {
+        s += 0x9E3779B97F4A7C15ull;
+        return (float)(uint32_t)(Mix64(s) >> 40) * (1.0f / 16777216.0f);
+    }
+    __device__ __forceinline__ void Next(float& a, float& b) {
+        a = Next();
+        b = Next();
+    }
+};
+
+// ---------------------------------------------------------------- geometry
+struct Ray {  // Core/Ray.h:42-48
+    V3 o, d, T;
+    int bounce;
+    float prob, ior;
+    __device__ Ray() : T(1.f, 1.f, 1.f), bounce(0), prob(1.0f), ior(1.0f) {}
+};
+struct Shading {  // Core/HitInfo.h:20-27 (tangent/uv unused without textures)
+    V3 n, pos;
+    int mat;
+};
+
+__device__ __forceinline__ void LoadTri(const float4* __restrict__ tris, int k, V3& v0, V3& e1, V3& e2) {
+    const float4 a = __ldg(tris + 3 * k), b = __ldg(tris + 3 * k + 1), c = __ldg(tris + 3 * k + 2);
+    v0 = V3(a.x, a.y, a.z);
+    e1 = V3(a.w, b.x, b.y);
+    e2 = V3(b.z, b.w, c.x);
+}
+__device__ __forceinline__ int TriId(const float4* __restrict__ tris, int k) {
+    return __float_as_int(__ldg(&tris[3 * k + 2].y));
+}
+
+// Triangle::Intersect (Core/Geometry/Triangle.cpp:51-88)
+__device__ __forceinline__ bool TriIntersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& dist) {
+    const V3 ce = Cross(e1, e2);
+    const float invDet = 1.0f / Dot(-d, ce);
+    const V3 vec = o - v0;
+    const float w1 = Dot(vec, Cross(d, e2)) * invDet;
+    const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+    if (w1 < 0.0f || w1 >= 1.0f) return false;
+    if (w2 < 0.0f || w2 >= 1.0f) return false;
+    if (w1 + w2 >= 1.0f) return false;
+    const float t = Dot(vec, ce) * invDet;
+    if (t < 0.0f) return false;
+    dist = t;
+    return true;
+}
+
+// GeometryBase::GetMaterial (GeometryBase.h:59-69) with MixMaterial::GetSingleMaterial
+__device__ __forceinline__ int ResolveMaterial(const DevMaterial* __restrict__ mats, int m, float r) {
+    if (m >= 0 && mats[m].kind == kMix) {
+        const int packed = mats[m].mat01;
+        return mats[m].mix <= r ? (packed & 0xFFFF) : (packed >> 16);
+    }
+    return m;
+}
+
+// Triangle::Interpolate (Triangle.cpp:90-153); k = primitive slot
+__device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V3 d, float dist) {
+    Shading si;
+    si.pos = o + d * dist;
+    V3 v0, e1, e2;
+    LoadTri(S.tris, k, v0, e1, e2);
+    const int tri = TriId(S.tris, k);
+    const float4 s0 = __ldg(S.shade + 3 * tri);
+    const float4 s1 = __ldg(S.shade + 3 * tri + 1);
+    const V3 ce = Cross(e1, e2);
+    if (__float_as_int(s1.w) == 0) {
+        si.n = Normalized(ce);
+    } else {
+        const float4 s2 = __ldg(S.shade + 3 * tri + 2);
+        const float invDet = 1.0f / Dot(-d, ce);
+        const V3 vec = o - v0;
+        const float w1 = Dot(vec, Cross(d, e2)) * invDet;
+        const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+        const V3 n0(s0.x, s0.y, s0.z), n1(s1.x, s1.y, s1.z), n2(s2.x, s2.y, s2.z);
+        si.n = Normalized(w1 * (n1 - n0) + w2 * (n2 - n0) + n0);
+    }
+    si.mat = ResolveMaterial(S.mats, __float_as_int(s0.w), 0.0f);
+    return si;
+}
+
+// Triangle::SampleSurface (Triangle.cpp:155-182) for light i; pdfArea not returned
+// (the per-light sum is precomputed in DevScene::lightPdfArea).
+template <class M>
+__device__ __forceinline__ V3 SampleLightPoint(const DevScene& S, int i, float u0, float u1) {
+    const float4 a = __ldg(S.lights + 3 * i), b = __ldg(S.lights + 3 * i + 1),
+                 c = __ldg(S.lights + 3 * i + 2);
+    const V3 v0(a.x, a.y, a.z), e0(b.x, b.y, b.z), e1(c.x, c.y, c.z);
+    const float su = sqrtf(u0);
+    return v0 + (1.0f - su) * e0 + su * u1 * e1;
+}
+
+// ---------------------------------------------------------------- ONB
+struct ONB {  // Math/OrthonormalBasis.cpp:10-62
+    V3 u, v, w;
+    __device__ __forceinline__ void Build(V3 n) {
+        w = Normalized(n);
+        const float sign = copysignf(1.0f, w.z);
+        const float a = -1.0f / (sign + w.z);
+        const float b = w.x * w.y * a;
+        u = V3(1.0f + sign * w.x * w.x * a, sign * b, -sign * w.x);
+        v = V3(b, sign + w.y * w.y * a, -w.y);
+    }
+    __device__ __forceinline__ void Build(V3 ww, V3 uu) {
+        w = Normalized(ww);
+        u = Normalized(uu);
+        v = Cross(w, u);
+    }
+    __device__ __forceinline__ V3 WorldToLocal(V3 a) const { return V3(Dot(a, u), Dot(a, v), Dot(a, w)); }
+    __device__ __forceinline__ V3 LocalToWorld(V3 a) const { return u * a.x + v * a.y + w * a.z; }
+};
+
+// ---------------------------------------------------------------- camera
+// Camera::GenerateRay (Core/Camera.cpp:52-91); (r0,r1) sensor, (r2,r3) lens
+template <class M>
+__device__ __forceinline__ Ray GenerateRay(const DevCamera& c, int i, int j, int W, int H, float r0,
+                                           float r1, float r2, float r3) {
+    const V3 pos = LoadV3(c.pos), right = LoadV3(c.right), up = LoadV3(c.up), fwd = LoadV3(c.fwd);
+    const float aspect = (float)W / H;
+    const float u = (i + r0) / W - 0.5f;
+    const float v = (j + r1) / H - 0.5f;
+    const V3 onSensor = pos + right * u * c.hPerf * c.focusDist * aspect +
+                        -up * v * c.hPerf * c.focusDist + fwd * c.focusDist;
+    const float r = sqrtf(r2);
+    const float theta = 2.0f * kPi * r3;
+    const V3 onLens = pos + right * 0.5f * c.aperture * r * M::Cos(theta) +
+                      -up * 0.5f * c.aperture * r * M::Sin(theta);
+    Ray ray;
+    ray.o = onLens;
+    ray.d = Normalized(onSensor - onLens);
+    const float dd = Dot(ray.d, fwd);
+    ray.T = V3(1.f, 1.f, 1.f) * dd * dd * c.focusDist * c.focusDist / SqLen(onSensor - onLens);
+    return ray;
+}
+
+// ---------------------------------------------------------------- environment
+// Texture2D::GetPixel(int,int) + bilinear GetPixel(float,float) (Texture2D.cpp:260-317)
+__device__ __forceinline__ V3 EnvTexel(const DevScene& S, int i, int j) {
+    const float4 t = __ldg(S.env + (size_t)S.envW * j + i);
+    return V3(t.x, t.y, t.z);
+}
+__device__ __forceinline__ V3 EnvBilinear(const DevScene& S, float x, float y) {
+    int ix0 = (int)x, ix1 = (int)(x + 1.0f), iy0 = (int)y, iy1 = (int)(y + 1.0f);
+    const float wx0 = x - ix0, wy0 = y - iy0, wx1 = ix1 - x, wy1 = iy1 - y;
+    ix0 = IClamp(ix0, 0, S.envW - 1);
+    ix1 = IClamp(ix1, 0, S.envW - 1);
+    iy0 = IClamp(iy0, 0, S.envH - 1);
+    iy1 = IClamp(iy1, 0, S.envH - 1);
+    const V3 c00 = EnvTexel(S, ix0, iy0), c10 = EnvTexel(S, ix1, iy0);
+    const V3 c01 = EnvTexel(S, ix0, iy1), c11 = EnvTexel(S, ix1, iy1);
+    const V3 cm0 = wx1 * c00 + wx0 * c10;
+    const V3 cm1 = wx1 * c01 + wx0 * c11;
+    return wy1 * cm0 + wy0 * cm1;
+}
+// The reference's importance-sampling tables are Texture2Ds that are sized but
+// never marked loaded, so every texel read returns the invalid-texture colour
+// (1, 0, 1) (Texture2D.cpp:263-266, Environment.cpp:56-58). A bilinear read of
+// them is therefore the sum of the bilinear weights; this returns its x.
+__device__ __forceinline__ float UnloadedTableBilinearX(float u, float v, int W, int H) {
+    u = Mod1(u);
+    v = Mod1(v);
+    const float x = u * W, y = v * H;
+    const int ix0 = (int)x, ix1 = (int)(x + 1.0f), iy0 = (int)y, iy1 = (int)(y + 1.0f);
+    const float wx0 = x - ix0, wy0 = y - iy0, wx1 = ix1 - x, wy1 = iy1 - y;
+    const float cm = wx1 * 1.0f + wx0 * 1.0f;
+    return wy1 * cm + wy0 * cm;
+}
+// Environment::GetColor (Environment.cpp:29-48)
+template <class M>
+__device__ __forceinline__ V3 EnvColor(const DevScene& S, V3 d) {
+    const V3 base(S.envBase[0], S.envBase[1], S.envBase[2]);
+    if (!S.envValid) return base;
+    const float theta = M::Acos(d.z);
+    const float phi = M::Atan2(d.y, d.x);
+    float u = 1.0f - (phi - S.envRot) * 0.5f * kInvPi;
+    float v = theta * kInvPi;
+    u = Mod1(u);
+    v = Mod1(v);
+    u = Mod1(u);  // GetPixelByUV wraps again (Texture2D.cpp:332-334)
+    v = Mod1(v);
+    return base * EnvBilinear(S, u * S.envW, v * S.envH);
+}
+// Environment::ImportanceSampling (Environment.cpp:130-220)
+template <class M>
+__device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, float& pdf) {
+    const int W = S.envW, H = S.envH;
+    const float tw = 1.0f / W, th = 1.0f / H;
+    float v0 = 0.0f, v1 = 1.0f;
+    for (int it = 0; it < 64; it++) {
+        const float v = 0.5f * (v0 + v1);
+        const float y = v * H;
+        const int fy = (int)y;
+        const int cy = min(fy + 1, H - 1);
+        const float c = Lerp(__ldg(S.cdf1D + fy), __ldg(S.cdf1D + cy), y - fy);
+        const float diff = c - r0;
+        if (v1 - v0 <= th) { v0 = v1 = v; break; }
+        if (diff > 0) v1 = v;
+        else if (diff < 0) v0 = v;
+        else { v0 = v1 = v; break; }
+    }
+    float u0 = 0.0f, u1 = 1.0f;
+    for (int it = 0; it < 64; it++) {
+        const float u = 0.5f * (u0 + u1);
+        const float c = UnloadedTableBilinearX(u, v0, W, H);
+        const float diff = c - r1;
+        if (u1 - u0 <= tw) { u0 = u1 = u; break; }
+        if (diff >= 0) u1 = u;
+        else u0 = u;
+    }
+    {
+        const float y = v0 * H;
+        const int y0 = (int)y;
+        const int y1 = min(y0 + 1, H - 1);
+        const float py = Lerp(__ldg(S.pdf1D + y0), __ldg(S.pdf1D + y1), y - y0);
+        pdf = py * UnloadedTableBilinearX(u0, v0, W, H);
+    }
+    const float theta = v0 * kPi;
+    const float phi = 2.0f * kPi * (1.0f - u0) + S.envRot;
+    // ONB(UnitZ, UnitX).GetDir(theta, phi): u = X, v = Y, w = Z
+    const float cx = M::SinCos(theta, phi), cy = M::SinSin(theta, phi), cz = M::Cos(theta);
+    return cx * V3(1.f, 0.f, 0.f) + cy * V3(0.f, 1.f, 0.f) + cz * V3(0.f, 0.f, 1.f);
+}
+// Environment::GetImportanceSamplingPDF (Environment.cpp:222-244)
+template <class M>
+__device__ __forceinline__ float EnvPdf(const DevScene& S, V3 d) {
+    const float theta = M::Acos(d.z);
+    const float phi = M::Atan2(d.y, d.x);
+    const float u0 = 1.0f - (phi - S.envRot) * 0.5f * kInvPi;
+    const float v0 = theta * kInvPi;
+    const float y = v0 * S.envH;
+    // d.z == -1 gives y == H, an out-of-range row in the reference (undefined
+    // behaviour there); the row index is clamped to the table here.
+    const int y0 = min((int)y, S.envH - 1);
+    const int y1 = min(y0 + 1, S.envH - 1);
+    const float py = Lerp(__ldg(S.pdf1D + y0), __ldg(S.pdf1D + y1), y - y0);
+    return py * UnloadedTableBilinearX(u0, v0, S.envW, S.envH);
+}
+
+// ---------------------------------------------------------------- materials
+__device__ __forceinline__ V3 MatColor(const DevMaterial& m) { return V3(m.cr, m.cg, m.cb); }
+// GGX::GetF0 with metalness 0 and no map (GGX.h:126-139)
+__device__ __forceinline__ V3 GgxF0(const DevMaterial& m) {
+    const V3 c = MatColor(m);
+    return 0.16f * (c * c) * (1.0f - 0.0f) + V3(1.f, 1.f, 1.f) * 0.0f;
+}
+template <class M>
+__device__ __forceinline__ float GgxLambda(V3 dir, V3 h, float alpha) {  // GGX.cpp:140-152
+    const float a2 = alpha * alpha;
+    const float c = fabsf(Dot(dir, h));
+    const float tan2 = c > 0 ? 1.0f / (c * c) - 1.0f : kInfinity;
+    return M::SmithLambda(1.0f + a2 * tan2);
+}
+// MaterialBase::BxDF for Lambert (Lambert.cpp:27-31, untextured albedo = 1) and GGX
+// (GGX.cpp:22-57); Glass returns zero (Glass.cpp:11-18).
+template <class M>
+__device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) {
+    if (m.kind == kLambert) return MatColor(m) * V3(1.f, 1.f, 1.f) * kInvPi;
+    if (m.kind == kGlossy) {
+        const V3 h = Normalized(-din + dout);
+        const float hn = fabsf(Dot(h, n));
+        const float a = m.alpha, a2 = a * a, hn2 = hn * hn;
+        const float k = (a2 - 1.0f) * hn2 + 1.0f;
+        const float D = a2 / (kPi * k * k);
+        const float li = GgxLambda<M>(dout, h, a), lo = GgxLambda<M>(-din, h, a);
+        const float G = 1.0f / (1.0f + li + lo);
+        const float hl = fabsf(Dot(h, dout));
+        const V3 F = GgxF0(m) + (V3(1.f, 1.f, 1.f) - GgxF0(m)) * Pow5(1.0f - hl);
+        const float ln = fabsf(Dot(dout, n)), vn = fabsf(Dot(-din, n));
+        return D * G * F / (4.0f * ln * vn);
+    }
+    return V3(0.f, 0.f, 0.f);
+}
+// MaterialBase::PDF (Lambert.cpp:33-47, GGX.cpp:59-76, Glass.cpp:20-27)
+__device__ __forceinline__ float BsdfPdf(const DevMaterial& m, V3 din, V3 dout, V3 n) {
+    if (m.kind == kLambert) return fabsf(Dot(dout, n)) * kInvPi;
+    if (m.kind == kGlossy) {
+        const V3 h = Normalized(-din + dout);
+        const float hn = fabsf(Dot(h, n));
+        const float a2 = m.alpha * m.alpha, hn2 = hn * hn;
+        const float tmp = 1.0f - (1.0f - a2) * hn2;
+        return tmp > 0 ? kInvPi * a2 / (tmp * tmp) : kInfinity;
+    }
+    return 0.0f;
+}
+// GGX::SampleGGXVNDF (GGX.cpp:154-208)
+template <class M>
+__device__ __forceinline__ V3 SampleVNDF(const DevMaterial& m, V3 view, V3 n0, float u0, float u1) {
+    const V3 n = n0 * copysignf(1.0f, Dot(view, n0));
+    ONB surf;
+    const V3 t = (fabsf(n.z) < 0.9999f) ? Cross(n, V3(0.f, 0.f, 1.f)) : V3(1.f, 0.f, 0.f);
+    surf.Build(n, t);
+    V3 v = surf.WorldToLocal(view);
+    const float alpha = m.alpha;
+    v = v * V3(alpha, alpha, 1.0f);
+    v = v / Length(v);
+    const V3 t1 = (v.z < 0.9999f) ? Normalized(Cross(v, V3(0.f, 0.f, 1.f))) : V3(1.f, 0.f, 0.f);
+    const V3 t2 = Cross(t1, v);
+    const float a = 1.0f / (1.0f + v.z);
+    const float r = sqrtf(u0);
+    const float phi = (u1 < a) ? u1 / a * kPi : kPi + (u1 - a) / (1.0f - a) * kPi;
+    const float p1 = M::MulCos(r, phi);
+    const float p2 = M::MulSinMul(r, phi, (u1 < a) ? 1.0f : v.z);
+    const float w = sqrtf(SMax(0.0f, 1.0f - p1 * p1 - p2 * p2));
+    V3 h = p1 * t1 + p2 * t2 + w * v;
+    h = V3(alpha * h.x, alpha * h.y, SMax(0.0f, h.z));
+    h = surf.LocalToWorld(h);
+    return h / Length(h);
+}
+// MaterialBase::CreateNextRay for Lambert (Lambert.cpp:49-98), GGX (GGX.cpp:78-138)
+// and Glass (Glass.cpp:29-95). The sampler is drawn exactly where the reference
+// draws (Glass draws only when it refracts).
+template <class M, class S2>
+__device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, const Shading& si, S2& s2) {
+    Ray out;
+    if (m.kind == kLambert) {
+        const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
+        ONB onb;
+        onb.Build(n);
+        float r0, r1;
+        s2.Next(r0, r1);
+        const float phi = 2.0f * kPi * r1;
+        const float st = sqrtf(r0);
+        const float cu = M::MulCos(st, phi);
+        const float cv = M::MulSin(st, phi);
+        const float cw = sqrtf(1.0f - st * st);
+        out.o = si.pos + kEps * n;
+        out.d = cu * onb.u + cv * onb.v + cw * onb.w;
+        out.T = in.T * V3(1.f, 1.f, 1.f);
+        out.bounce = in.bounce + 1;
+        return out;
+    }
+    if (m.kind == kGlossy) {
+        const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
+        float u0, u1;
+        s2.Next(u0, u1);
+        const V3 h = SampleVNDF<M>(m, -in.d, si.n, u0, u1);
+        const V3 od = Reflected(in.d, h);
+        const float hl = fabsf(Dot(h, od));
+        const V3 f0 = GgxF0(m);
+        const V3 F = f0 + (V3(1.f, 1.f, 1.f) - f0) * Pow5(1.0f - hl);
+        const float li = GgxLambda<M>(od, h, m.alpha), lo = GgxLambda<M>(-in.d, h, m.alpha);
+        const float g2 = 1.0f / (1.0f + li + lo);
+        const float g1 = 1.0f / (1.0f + li);
+        out.o = si.pos;
+        out.d = od;
+        out.T = in.T * (F * g2 / g1);
+        out.bounce = in.bounce + 1;
+        out.o = out.o + kEps * n;
+        return out;
+    }
+    if (m.kind == kGlass) {
+        const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
+        const float eta = m.ior / in.ior;
+        const float dn = Dot(in.d, si.n);
+        const float disc = dn * dn - 1 + eta * eta;
+        if (disc < 0) {  // total internal reflection
+            out.o = si.pos + kEps * n;
+            out.d = Normalized(Reflected(in.d, n));
+            out.T = V3(0.f, 0.f, 0.f);
+            out.bounce = 0 + 1;
+            out.prob = in.prob;
+            out.ior = in.ior;
+            return out;
+        }
+        const V3 rd = (1.0f / eta) * (in.d - si.n * M::RefractScale(-dn, disc));
+        out.d = Normalized(rd);
+        const float nd = Dot(si.n, out.d);
+        const float q = (1.0f - eta) / (1.0f + eta);
+        const float f0 = q * q;
+        const float refl = f0 + (1.0f - f0) * Pow5(1.0f - fabsf(nd));
+        float r0, r1;
+        s2.Next(r0, r1);
+        out.T = in.T;
+        out.bounce = in.bounce + 1;
+        out.prob = in.prob;
+        if (r0 <= refl) {  // reflection keeps the refracted direction (Glass.cpp:59-80)
+            out.o = si.pos + kEps * n;
+            out.ior = in.ior;
+        } else {
+            out.o = si.pos - kEps * n;
+            out.ior = (nd < 0) ? 1.0f * eta : 1.0f / eta;
+        }
+        return out;
+    }
+    return out;  // Emission / Mix never reach CreateNextRay
+}
+
+// ---------------------------------------------------------------- reference traversal
+// Per-ray error bits reported through the status word.
+enum : int { kErrStackOverflow = 1, kErrBounceCap = 2 };
+
+// BinnedSAHBVH::Intersect (Core/Accel/BinnedSAHBVH.cpp:272-374) with the slab test
+// of BinnedSAHBVH.h:95-170: pop order, culling rule and child push order as the
+// reference. Returns the primitive slot of the closest hit, or -1.
+// kCount: also count the nodes popped and slab-tested and the triangle tests
+// (the reference traversal's work per ray, used for algorithmic-byte accounting).
+template <bool kCount = false>
+__device__ int TraverseReference(const DevScene& S, V3 o, V3 d, float distMin, float distMax,
+                                 float& bestD, int* __restrict__ stack, int* status,
+                                 unsigned* nodeTests = nullptr, unsigned* triTests = nullptr) {
+    if (S.numNodes == 0) return -1;
+    const V3 inv = 1.0f / d;
+    const int s0 = inv.x < 0.0f, s1 = inv.y < 0.0f, s2 = inv.z < 0.0f;
+    int sp = 0;
+    stack[sp++] = 0;
+    int best = -1;
+    bestD = kInfinity;
+    while (sp > 0) {
+        const int ni = stack[--sp];
+        if (kCount) (*nodeTests)++;
+        const float4 na = __ldg(S.nodes + 2 * ni), nb = __ldg(S.nodes + 2 * ni + 1);
+        const V3 lo(na.x, na.y, na.z), hi(na.w, nb.x, nb.y);
+        const V3 b0 = s0 ? hi : lo, b1 = s0 ? lo : hi;  // aabb[sign], aabb[1 - sign] for x
+        float tMin = (b0.x - o.x) * inv.x;
+        float tMax = (b1.x - o.x) * inv.x;
+        const float tyMin = ((s1 ? hi : lo).y - o.y) * inv.y;
+        const float tyMax = ((s1 ? lo : hi).y - o.y) * inv.y;
+        if (tyMax < tMin || tMax < tyMin) continue;
+        if (tMin < tyMin) tMin = tyMin;
+        if (tyMax < tMax) tMax = tyMax;
+        const float tzMin = ((s2 ? hi : lo).z - o.z) * inv.z;
+        const float tzMax = ((s2 ? lo : hi).z - o.z) * inv.z;
+        if (tzMax < tMin || tMax < tzMin) continue;
+        if (tMin < tzMin) tMin = tzMin;
+        if (tzMax < tMax) tMax = tzMax;
+        float nd = kFltMax;
+        const bool nearOk = (0.0f <= tMin && tMin < nd);
+        if (nearOk) nd = tMin;
+        const bool farOk = (0.0f <= tMax && tMax < nd);
+        if (farOk) nd = tMax;
+        if (!(nearOk || farOk)) continue;
+        if (best >= 0) {
+            const bool inside = lo.x < o.x && o.x < hi.x && lo.y < o.y && o.y < hi.y &&
+                                lo.z < o.z && o.z < hi.z;  // AABB::Contains
+            if (!inside && bestD < nd) continue;
+        }
+        const int a = __float_as_int(nb.z), cnt = __float_as_int(nb.w);
+        if (cnt >= 0) {
+            for (int k = a; k < a + cnt; k++) {
+                V3 v0, e1, e2;
+                LoadTri(S.tris, k, v0, e1, e2);
+                if (kCount) (*triTests)++;
+                float t;
+                if (TriIntersect(v0, e1, e2, o, d, t)) {
+                    if (t < distMin || t > distMax) continue;
+                    if (best < 0 || t < bestD) {
+                        best = k;
+                        bestD = t;
+                    }
+                }
+            }
+        } else {
+            const float4 la = __ldg(S.nodes + 2 * a), lb = __ldg(S.nodes + 2 * a + 1);
+            const float4 ra = __ldg(S.nodes + 2 * a + 2), rb = __ldg(S.nodes + 2 * a + 3);
+            const float dl = SqLen((V3(la.x, la.y, la.z) + V3(la.w, lb.x, lb.y)) * 0.5f - o);
+            const float dr = SqLen((V3(ra.x, ra.y, ra.z) + V3(ra.w, rb.x, rb.y)) * 0.5f - o);
+            if (sp + 2 > S.stackDepth) {
+                *status |= kErrStackOverflow;
+                return best;
+            }
+            if (dl < dr) {
+                stack[sp++] = a + 1;
+                stack[sp++] = a;
+            } else {
+                stack[sp++] = a;
+                stack[sp++] = a + 1;
+            }
+        }
+    }
+    return best;
+}
+
+}  // namespace ptg

@@ -1,0 +1,78 @@
+// Device-resident scene layout shared by the host uploader and the CUDA kernels.
+//
+// HBM layout (all arrays 16-byte aligned, read with float4 loads):
+//   nodes      2 x float4 per BVH node (32 B):
+//                [0] lo.x lo.y lo.z hi.x   [1] hi.y hi.z a b
+//              inner: a = left child (right = left + 1), b = -1
+//              leaf : a = first primitive slot, b = primitive count
+//              Node order and leaf ranges are the reference binned-SAH tree's
+//              (Core/Accel/BinnedSAHBVH.cpp:15-225), so slot k of a leaf is
+//              m_primitiveIDs[k].
+//   tris       3 x float4 per primitive slot (48 B), in leaf order:
+//                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) 0 0
+//              e1 = v1 - v0, e2 = v2 - v0 exactly as Triangle::Intersect forms
+//              them (Core/Geometry/Triangle.cpp:53-54).
+//   shade      3 x float4 per original triangle (48 B):
+//                [0] n0.xyz material(bits) [1] n1.xyz smooth(bits) [2] n2.xyz 0
+//   lights     3 x float4 per light: [0] v0.xyz tri(bits) [1] e0.xyz 0 [2] e1.xyz 0
+//   env        float4 RGB_ texels, row-major (H x W); cdf1D / pdf1D per row.
+#pragma once
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define PT_HD __host__ __device__ __forceinline__
+#else
+#define PT_HD inline
+#include <vector_types.h>
+#endif
+
+namespace ptg {
+
+enum MaterialKind : int32_t {
+    kLambert = 0,
+    kGlass = 1,
+    kEmission = 2,
+    kGlossy = 3,
+    kMix = 4,
+};
+
+struct DevMaterial {  // 32 B
+    int32_t kind;
+    float cr, cg, cb;  // Lambert kd / GGX reflectance strength / Glass color / Emission radiance
+    float alpha;       // GGX roughness^2 (GGX.cpp:16-20)
+    float ior;         // Glass
+    float mix;         // Mix: mix <= r picks mat0 (MixMaterial.h:45-50)
+    int32_t mat01;     // Mix: mat0 | (mat1 << 16)
+};
+
+struct DevCamera {  // derived Camera state (Core/Camera.h:121-130)
+    float pos[3], right[3], up[3], fwd[3];
+    float hPerf, focusDist, aperture, pad;
+};
+
+struct DevScene {
+    const float4* nodes;
+    const float4* tris;
+    const float4* shade;
+    const DevMaterial* mats;
+    const float4* lights;
+    const float4* env;
+    const float* cdf1D;
+    const float* pdf1D;
+    int32_t numNodes, numTris, numMats, numLights;
+    int32_t envW, envH, envValid, stackDepth;  // stackDepth: max traversal stack entries
+    float envBase[3], envRot;
+    float lightPdfArea;  // 1 / sum(1/pdfArea_i), PathTracing.cpp:363-383 (summed in light order)
+    int32_t pad[3];
+};
+
+// Integrators
+enum Integrator : int32_t { kSimplePathTracing = 0, kPathTracing = 1 };
+
+struct DevSettings {
+    int32_t width, height, spp, maxBounces;
+    int32_t tileW, tileH, integrator;
+    uint32_t seed;
+};
+
+}  // namespace ptg

@@ -1,0 +1,614 @@
+// Wavefront throughput path: raygen -> extend -> shade -> shadow -> accumulate.
+//
+// One wave is a block of paths (pixel range x sample range). Each bounce runs
+// three persistent-grid kernels over compacted queues:
+//   extend : closest hit of every queued ray (binary BVH, 32 B nodes, both
+//            children's boxes fetched as one 64 B pair, ordered short stack)
+//   shade  : miss / emission / surface handling of PathTracing or
+//            SimplePathTracing semantics; next-event rays go to the shadow queue,
+//            continuation rays to the next ray queue (warp-aggregated appends)
+//   shadow : visibility of the next-event rays, adds their radiance
+// A path's radiance lives in its own slot and is added to the pixel's running
+// sum in sample order after the wave, so results do not depend on batching.
+// Random numbers are a counter-based stream per (seed, pixel, sample).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <utility>
+#include <vector>
+
+#include "pt_device.cuh"
+#include "pt_kernels.h"
+
+namespace ptg {
+
+enum : int { kFlagNoSignCheck = 1 };
+enum : int { kShadowEnv = 0, kShadowArea = 1 };
+
+__device__ __forceinline__ void PixelOfIndex(int q, int W, int H, int& x, int& y) {
+    // 8-row bands, column-major inside a band: a warp covers a 4 x 8 pixel block
+    const int band = q / (8 * W);
+    const int y0 = band * 8;
+    const int hb = min(8, H - y0);
+    const int r = q - band * 8 * W;
+    x = r / hb;
+    y = y0 + r % hb;
+}
+
+// Box test against [tmin, tmax]; returns the entry distance.
+__device__ __forceinline__ bool SlabFast(float4 a, float4 b, V3 o, V3 inv, float tmin, float tmax,
+                                         float& tEnter) {
+    const float tx0 = (a.x - o.x) * inv.x, tx1 = (a.w - o.x) * inv.x;
+    const float ty0 = (a.y - o.y) * inv.y, ty1 = (b.x - o.y) * inv.y;
+    const float tz0 = (a.z - o.z) * inv.z, tz1 = (b.y - o.z) * inv.z;
+    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    tEnter = tn;
+    return tn <= tf;
+}
+
+// Closest hit (or any hit) in [tmin, tmax]. Triangle test = Triangle::Intersect,
+// so the closest primitive equals the reference's except on exact distance ties.
+template <bool kAnyHit>
+__device__ int TraceFast(const DevScene& S, V3 o, V3 d, float tmin, float tmax, float& tHit,
+                         int* err) {
+    if (S.numNodes == 0) return -1;
+    const V3 inv = 1.0f / d;
+    int best = -1;
+    float tBest = tmax;
+    float tE;
+    if (!SlabFast(__ldg(S.nodes), __ldg(S.nodes + 1), o, inv, 0.0f, tBest, tE)) return -1;
+    int2 stack[kWaveStackDepth];
+    int sp = 0;
+    float4 meta = __ldg(S.nodes + 1);
+    for (;;) {
+        const int a = __float_as_int(meta.z), cnt = __float_as_int(meta.w);
+        bool pop = true;
+        if (cnt >= 0) {
+            for (int k = a; k < a + cnt; k++) {
+                V3 v0, e1, e2;
+                LoadTri(S.tris, k, v0, e1, e2);
+                float t;
+                if (TriIntersect(v0, e1, e2, o, d, t) && t >= tmin && t <= tmax && t < tBest) {
+                    tBest = t;
+                    best = k;
+                    if (kAnyHit) {
+                        tHit = t;
+                        return k;
+                    }
+                }
+            }
+        } else {
+            const float4 la = __ldg(S.nodes + 2 * a), lb = __ldg(S.nodes + 2 * a + 1);
+            const float4 ra = __ldg(S.nodes + 2 * a + 2), rb = __ldg(S.nodes + 2 * a + 3);
+            float tl, tr;
+            const bool hl = SlabFast(la, lb, o, inv, 0.0f, tBest, tl);
+            const bool hr = SlabFast(ra, rb, o, inv, 0.0f, tBest, tr);
+            if (hl && hr) {
+                if (sp >= kWaveStackDepth) {
+                    *err = 1;
+                    break;
+                }
+                if (tr < tl) {
+                    stack[sp++] = make_int2(a, __float_as_int(tl));
+                    meta = rb;
+                } else {
+                    stack[sp++] = make_int2(a + 1, __float_as_int(tr));
+                    meta = lb;
+                }
+                pop = false;
+            } else if (hl) {
+                meta = lb;
+                pop = false;
+            } else if (hr) {
+                meta = rb;
+                pop = false;
+            }
+        }
+        if (pop) {
+            bool found = false;
+            while (sp > 0) {
+                const int2 e = stack[--sp];
+                if (__int_as_float(e.y) <= tBest) {
+                    meta = __ldg(S.nodes + 2 * e.x + 1);
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) break;
+        }
+    }
+    tHit = tBest;
+    return best;
+}
+
+__device__ __forceinline__ int WarpAppend(int* counter, bool pred) {
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, pred);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(active) - 1;
+    int base = 0;
+    if (lane == leader && mask) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(active, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__global__ void RaygenKernel(DevCamera C, DevSettings st, WaveBuffers wb, int q0, int P, int s0,
+                             int Sw, int cur) {
+    const int n = P * Sw;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int q = q0 + i % P, s = s0 + i / P;
+        int x, y;
+        PixelOfIndex(q, st.width, st.height, x, y);
+        PathRng rng(PathKey(st.seed, (uint32_t)(y * st.width + x), (uint32_t)s));
+        float r0, r1, r2, r3;
+        rng.Next(r0, r1);
+        rng.Next(r2, r3);
+        const Ray ray = GenerateRay<FastMath>(C, x, y, st.width, st.height, r0, r1, r2, r3);
+        wb.ray[cur][2 * i] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float(i));
+        wb.ray[cur][2 * i + 1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
+        wb.st0[i] = make_float4(ray.T.x, ray.T.y, ray.T.z, 1.0f);
+        wb.st1[i] = make_float4(0.f, 0.f, 0.f, 1.0f);
+        wb.st2[i] = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
+        wb.rng[i] = rng.s;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur] = n;
+}
+
+__global__ void __launch_bounds__(128) ExtendKernel(DevScene S, WaveBuffers wb, int cur, float tmin) {
+    const int n = wb.counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        wb.counts[cur ^ 1] = 0;
+        wb.counts[2] = 0;
+    }
+    int err = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = wb.ray[cur][2 * i], b = wb.ray[cur][2 * i + 1];
+        float t = 0.0f;
+        const int k = TraceFast<false>(S, V3(a.x, a.y, a.z), V3(b.x, b.y, b.z), tmin, kFltMax, t, &err);
+        wb.hit[i] = make_float2(t, __int_as_float(k));
+    }
+    if (err) atomicOr(wb.counts + 3, 1);
+}
+
+__global__ void __launch_bounds__(128) ShadeKernel(DevScene S, DevSettings st, WaveBuffers wb, int cur) {
+    const int n = wb.counts[cur];
+    const int nxt = cur ^ 1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
+        const float2 h = wb.hit[i];
+        const int path = __float_as_int(ra.w);
+        const V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
+        float4 s0 = wb.st0[path], s1 = wb.st1[path], s2 = wb.st2[path];
+        PathRng rng(wb.rng[path]);
+        V3 L(s1.x, s1.y, s1.z);
+        Ray in;
+        in.o = o;
+        in.d = d;
+        in.T = V3(s0.x, s0.y, s0.z);
+        in.prob = s0.w;
+        in.ior = s1.w;
+        in.bounce = __float_as_int(s2.z);
+        int flags = __float_as_int(s2.w);
+        const int slot = __float_as_int(h.y);
+        bool cont = false;
+        Ray out;
+        float lastPdf = s2.x, lastSin = s2.y;
+        // next-event entry
+        bool shadow = false;
+        float4 sh0, sh1, sh2, sh3;
+
+        if (st.integrator == kSimplePathTracing) {
+            // SimplePathTracing.cpp:45-126
+            flags |= kFlagNoSignCheck;
+            if (slot < 0) {
+                L = L + in.T * EnvColor<FastMath>(S, d);
+            } else {
+                const int tri = TriId(S.tris, slot);
+                const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), rng.Next());
+                if (S.mats[m].kind == kEmission) {
+                    L = L + in.T * MatColor(S.mats[m]);
+                } else {
+                    const Shading si = Interpolate(S, slot, o, d, h.x);
+                    out = NextRay<FastMath>(S.mats[m], in, si, rng);
+                    cont = true;
+                    if (out.bounce > st.maxBounces) {
+                        out.prob *= 0.9f;
+                        out.prob = SMax(0.1f, out.prob);
+                        if (rng.Next() < out.prob) out.T = out.T / out.prob;
+                        else cont = false;
+                    }
+                    // a path with exactly zero throughput adds nothing more
+                    if (out.T.x == 0.0f && out.T.y == 0.0f && out.T.z == 0.0f) cont = false;
+                }
+            }
+        } else {
+            // PathTracing.cpp:38-196; k = BSDF bounces taken so far
+            const int k = in.bounce;
+            if (slot < 0) {
+                if (k == 0) {
+                    L = L + in.T * EnvColor<FastMath>(S, d);
+                    flags |= kFlagNoSignCheck;
+                } else if (S.envValid) {
+                    float mis;
+                    if (d.x != 0 && d.y != 0 && lastSin > 0) {
+                        const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
+                        mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
+                    } else {
+                        mis = 1.0f;
+                    }
+                    L = L + mis * in.T * EnvColor<FastMath>(S, d);
+                } else {
+                    L = L + in.T * EnvColor<FastMath>(S, d);
+                }
+            } else {
+                const Shading si = Interpolate(S, slot, o, d, h.x);
+                const DevMaterial& M = S.mats[si.mat];
+                if (M.kind == kEmission) {
+                    if (k == 0) {
+                        L = L + in.T * MatColor(M);
+                        flags |= kFlagNoSignCheck;
+                    } else {
+                        const float l2 = SqLen(si.pos - o);
+                        const float cosP = fabsf(Dot(d, si.n));
+                        const float pL = l2 / cosP * S.lightPdfArea;
+                        const float mis = lastPdf * lastPdf / (pL * pL + lastPdf * lastPdf);
+                        L = L + mis * in.T * MatColor(M);
+                    }
+                } else if (k < st.maxBounces) {
+                    // ---- next-event estimation (PathTracing.cpp:202-327)
+                    const float dt = -Dot(d, si.n);
+                    const V3 p = si.pos + kEps * copysignf(1.0f, dt) * si.n;
+                    const int nl = S.numLights;
+                    int index = (int)(rng.Next() * (float)(nl + 1));
+                    index = min(index, nl);
+                    if (index >= nl) {
+                        if (S.envValid && M.kind != kGlass) {
+                            float e0, e1;
+                            rng.Next(e0, e1);
+                            float pdfuv = 0.0f;
+                            const V3 sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
+                            const float c = fabsf(Dot(sd, si.n));
+                            const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
+                            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf(M, d, sd, si.n);
+                            const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
+                            const V3 li = EnvColor<FastMath>(S, sd);
+                            const V3 f = BxDF<FastMath>(M, d, sd, si.n);
+                            const V3 contrib = mis * in.T * (li * f * sn * c * 2.0f * kPi * kPi) / pdfuv;
+                            if (contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f) {
+                                shadow = true;
+                                sh0 = make_float4(p.x, p.y, p.z, kFltMax);
+                                sh1 = make_float4(sd.x, sd.y, sd.z, __int_as_float(path));
+                                sh2 = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
+                                sh3 = make_float4(0.f, 0.f, 0.f, 0.f);
+                            }
+                        }  // glass: BxDF = 0 (Glass.cpp:11-18), nothing to add
+                    } else {
+                        float u0, u1;
+                        rng.Next(u0, u1);
+                        const V3 pl = SampleLightPoint<FastMath>(S, index, u0, u1);
+                        const V3 dl = pl - p;
+                        const float dist = Length(dl);
+                        const V3 ld = dl / dist;
+                        const V3 f = BxDF<FastMath>(M, d, ld, si.n);
+                        if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
+                            const V3 Tf = in.T * f;
+                            shadow = true;
+                            sh0 = make_float4(p.x, p.y, p.z, dist);
+                            sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
+                            sh2 = make_float4(Tf.x, Tf.y, Tf.z, BsdfPdf(M, d, ld, si.n));
+                            sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, fabsf(Dot(ld, si.n)));
+                        }
+                    }
+                    // ---- continuation
+                    out = NextRay<FastMath>(M, in, si, rng);
+                    if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
+                        cont = true;
+                        lastPdf = BsdfPdf(M, d, out.d, si.n);
+                        const float c = fabsf(Dot(si.n, out.d));
+                        lastSin = sqrtf(SMax(0.0f, 1.0f - c * c));
+                        out.bounce = k + 1;
+                    }
+                }
+            }
+        }
+        // ---- write back and append
+        const int rslot = WarpAppend(wb.counts + nxt, cont);
+        const int sslot = WarpAppend(wb.counts + 2, shadow);
+        if (cont) {
+            wb.ray[nxt][2 * rslot] = make_float4(out.o.x, out.o.y, out.o.z, __int_as_float(path));
+            wb.ray[nxt][2 * rslot + 1] = make_float4(out.d.x, out.d.y, out.d.z, 0.0f);
+            wb.st0[path] = make_float4(out.T.x, out.T.y, out.T.z, out.prob);
+            wb.st1[path] = make_float4(L.x, L.y, L.z, out.ior);
+            wb.st2[path] = make_float4(lastPdf, lastSin, __int_as_float(out.bounce), __int_as_float(flags));
+        } else {
+            wb.st1[path] = make_float4(L.x, L.y, L.z, in.ior);
+            wb.st2[path] = make_float4(lastPdf, lastSin, __int_as_float(in.bounce), __int_as_float(flags));
+        }
+        wb.rng[path] = rng.s;
+        if (shadow) {
+            float4* e = wb.shadow + 4 * (size_t)sslot;
+            e[0] = sh0;
+            e[1] = sh1;
+            e[2] = sh2;
+            e[3] = sh3;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) ShadowKernel(DevScene S, WaveBuffers wb) {
+    const int n = wb.counts[2];
+    int err = 0;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const float4 e0 = wb.shadow[4 * j], e1 = wb.shadow[4 * j + 1];
+        const int tag = __float_as_int(e1.w);
+        const int path = tag & 0x7FFFFFFF;
+        const V3 p(e0.x, e0.y, e0.z), ld(e1.x, e1.y, e1.z);
+        if (tag >= 0) {  // environment: unoccluded?
+            float t;
+            if (TraceFast<true>(S, p, ld, 0.0f, kFltMax, t, &err) < 0) {
+                const float4 c = wb.shadow[4 * j + 2];
+                float4 l = wb.st1[path];
+                l.x += c.x;
+                l.y += c.y;
+                l.z += c.z;
+                wb.st1[path] = l;
+            }
+        } else {  // area light: closest hit must be the sampled emitter point
+            const float dist = e0.w;
+            float t;
+            const int slot = TraceFast<false>(S, p, ld, 0.0f, dist + 0.05f, t, &err);
+            if (slot < 0) continue;
+            const int tri = TriId(S.tris, slot);
+            const float r = (float)(uint32_t)(Mix64(wb.rng[path] ^ 0xA5A5A5A5DEADBEEFull) >> 40) *
+                            (1.0f / 16777216.0f);
+            const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), r);
+            if (S.mats[m].kind != kEmission) continue;
+            const Shading sl = Interpolate(S, slot, p, ld, t);
+            const V3 pl = p + ld * dist;
+            if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) continue;
+            const float4 e2 = wb.shadow[4 * j + 2], e3 = wb.shadow[4 * j + 3];
+            const V3 sipos(e3.x, e3.y, e3.z);
+            const float l2 = SqLen(sl.pos - sipos);
+            const float cosP = fabsf(Dot(ld, sl.n));
+            const float pdfArea = S.lightPdfArea;
+            float mis = 0.0f;
+            if (l2 > 0.0f) {
+                const float pB = e2.w * cosP / l2;
+                mis = pdfArea * pdfArea / (pdfArea * pdfArea + pB * pB);
+            }
+            const V3 li = MatColor(S.mats[sl.mat]);
+            const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * e3.w * cosP / (pdfArea * l2));
+            float4 l = wb.st1[path];
+            l.x += c.x;
+            l.y += c.y;
+            l.z += c.z;
+            wb.st1[path] = l;
+        }
+    }
+    if (err) atomicOr(wb.counts + 3, 1);
+}
+
+__global__ void AccumulateKernel(DevSettings st, WaveBuffers wb, int q0, int P, int Sw) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        int x, y;
+        PixelOfIndex(q0 + i, st.width, st.height, x, y);
+        const size_t pixel = (size_t)y * st.width + x;
+        float4 acc = wb.accum[pixel];
+        for (int s = 0; s < Sw; s++) {
+            const int p = s * P + i;
+            const float4 l = wb.st1[p];
+            const int flags = __float_as_int(wb.st2[p].w);
+            // PathTracing.cpp:191-195 drops a sample whose smallest channel is
+            // negative or NaN; primary misses/emitters are added directly (:54,:67).
+            if ((flags & kFlagNoSignCheck) || MinElem(V3(l.x, l.y, l.z)) >= 0.0f) {
+                acc.x += l.x;
+                acc.y += l.y;
+                acc.z += l.z;
+            }
+        }
+        wb.accum[pixel] = acc;
+    }
+}
+
+__global__ void FinalizeKernel(DevSettings st, const float4* __restrict__ accum, float* __restrict__ film) {
+    const int n = st.width * st.height;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = accum[i];
+        const float inv = (float)st.spp;
+        film[3 * i] = a.x / inv;
+        film[3 * i + 1] = a.y / inv;
+        film[3 * i + 2] = a.z / inv;
+    }
+}
+
+__global__ void TraceKernel(DevScene S, int n, const float* __restrict__ rays, float tmin, float tmax,
+                            int* __restrict__ triOut, float* __restrict__ distOut, int* err) {
+    int e = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* r = rays + 6 * (size_t)i;
+        float t = 0.0f;
+        const int k = TraceFast<false>(S, V3(r[0], r[1], r[2]), V3(r[3], r[4], r[5]), tmin, tmax, t, &e);
+        triOut[i] = k >= 0 ? TriId(S.tris, k) : -1;
+        distOut[i] = k >= 0 ? t : -1.0f;
+    }
+    if (e && err) atomicOr(err, 1);
+}
+
+// Profiling helpers: ray tallies and the reference traversal's work per ray.
+__global__ void TallyKernel(const int* counts, int cur, unsigned long long* c) {
+    c[3] += (unsigned long long)counts[cur];
+    c[4] += (unsigned long long)counts[2];
+}
+
+__global__ void __launch_bounds__(128) RefCountKernel(DevScene S, WaveBuffers wb, int cur, float tmin,
+                                                      unsigned long long* c) {
+    const int n = wb.counts[cur];
+    unsigned long long nodes = 0, tris = 0;
+    int stack[kWaveStackDepth];
+    int status = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = wb.ray[cur][2 * i], b = wb.ray[cur][2 * i + 1];
+        unsigned nn = 0, nt = 0;
+        float d;
+        TraverseReference<true>(S, V3(a.x, a.y, a.z), V3(b.x, b.y, b.z), tmin, kFltMax, d, stack,
+                                &status, &nn, &nt);
+        nodes += nn;
+        tris += nt;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        nodes += __shfl_down_sync(0xffffffffu, nodes, off);
+        tris += __shfl_down_sync(0xffffffffu, tris, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(c + 0, nodes);
+        atomicAdd(c + 1, tris);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(c + 2, (unsigned long long)n);
+}
+
+namespace {
+struct StageEvents {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[5];
+    void Begin(int k, cudaStream_t s) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        ev[k].push_back({a, b});
+        cudaEventRecord(a, s);
+    }
+    void End(int k, cudaStream_t s) { cudaEventRecord(ev[k].back().second, s); }
+    void Collect(double* ms) {
+        for (int k = 0; k < 5; k++) {
+            for (auto& p : ev[k]) {
+                float t = 0.0f;
+                cudaEventElapsedTime(&t, p.first, p.second);
+                ms[k] += t;
+                cudaEventDestroy(p.first);
+                cudaEventDestroy(p.second);
+            }
+            ev[k].clear();
+        }
+    }
+};
+}  // namespace
+
+size_t WaveBytesPerPath() {
+    return 2 * 2 * sizeof(float4) + sizeof(float2) + 3 * sizeof(float4) + sizeof(unsigned long long) +
+           4 * sizeof(float4);
+}
+size_t WaveBytesPerPixel() { return sizeof(float4); }
+
+int DefaultStageGrid() {
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int perSm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ExtendKernel, 128, 0);
+        if (perSm < 1) perSm = 1;
+        grid = sms * perSm;
+    }
+    return grid;
+}
+
+cudaError_t RenderWavefront(const DevScene& S, const DevCamera& C, const DevSettings& st,
+                            const WaveBuffers& wb, float* film, cudaStream_t stream, int* launches,
+                            int gridOverride, WaveProfile* prof) {
+    const int P_total = st.width * st.height;
+    if (P_total <= 0 || st.spp <= 0) return cudaErrorInvalidValue;
+    const int grid = gridOverride > 0 ? gridOverride : DefaultStageGrid();
+    const int block = 128;
+    int nl = 0;
+    cudaError_t e = cudaMemsetAsync(wb.accum, 0, sizeof(float4) * (size_t)P_total, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(wb.counts, 0, 4 * sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    const int cap = wb.capacity;
+    const int Pc = std::min(P_total, cap);
+    const int Sw = std::max(1, std::min(st.spp, cap / Pc));
+    const float tmin = st.integrator == kSimplePathTracing ? kEps : 0.0f;
+    int* hostCount = wb.hostCount;
+    StageEvents events;
+    for (int s0 = 0; s0 < st.spp; s0 += Sw) {
+        const int sw = std::min(Sw, st.spp - s0);
+        for (int q0 = 0; q0 < P_total; q0 += Pc) {
+            const int pc = std::min(Pc, P_total - q0);
+            StageEvents* sev = prof ? &events : nullptr;
+            if (sev) sev->Begin(0, stream);
+            RaygenKernel<<<grid, block, 0, stream>>>(C, st, wb, q0, pc, s0, sw, 0);
+            if (sev) sev->End(0, stream);
+            nl++;
+            int cur = 0;
+            // PathTracing traces rays 0..maxBounces; SimplePathTracing runs until
+            // every path has ended (polled every 4 bounces).
+            const int fixedIters = st.integrator == kSimplePathTracing ? -1 : st.maxBounces + 1;
+            for (int it = 0;; it++) {
+                if (fixedIters >= 0 && it >= fixedIters) break;
+                if (fixedIters < 0 && it > 0 && it % 4 == 0) {
+                    cudaMemcpyAsync(hostCount, wb.counts + cur, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                    e = cudaStreamSynchronize(stream);
+                    if (e != cudaSuccess) break;
+                    if (*hostCount == 0) break;
+                    if (it >= kMaxReplayBounces) break;
+                }
+                if (sev) sev->Begin(1, stream);
+                ExtendKernel<<<grid, block, 0, stream>>>(S, wb, cur, tmin);
+                if (sev) {
+                    sev->End(1, stream);
+                    if (prof->countReference)
+                        RefCountKernel<<<grid, block, 0, stream>>>(S, wb, cur, tmin, prof->devCounters);
+                    sev->Begin(2, stream);
+                }
+                ShadeKernel<<<grid, block, 0, stream>>>(S, st, wb, cur);
+                if (sev) {
+                    sev->End(2, stream);
+                    TallyKernel<<<1, 1, 0, stream>>>(wb.counts, cur, prof->devCounters);
+                    sev->Begin(3, stream);
+                }
+                ShadowKernel<<<grid, block, 0, stream>>>(S, wb);
+                if (sev) sev->End(3, stream);
+                nl += 3;
+                if (prof) {
+                    prof->extendLaunches++;
+                    prof->shadowLaunches++;
+                }
+                cur ^= 1;
+            }
+            if (sev) sev->Begin(4, stream);
+            AccumulateKernel<<<grid, block, 0, stream>>>(st, wb, q0, pc, sw);
+            if (sev) sev->End(4, stream);
+            nl++;
+        }
+    }
+    if (prof) events.Begin(4, stream);
+    FinalizeKernel<<<grid, block, 0, stream>>>(st, wb.accum, film);
+    if (prof) events.End(4, stream);
+    nl++;
+    if (launches) *launches += nl;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (prof && e == cudaSuccess) {
+        e = cudaStreamSynchronize(stream);
+        events.Collect(prof->ms);
+        unsigned long long c[8];
+        cudaMemcpy(c, prof->devCounters, sizeof(c), cudaMemcpyDeviceToHost);
+        prof->refNodeTests = c[0];
+        prof->refTriTests = c[1];
+        prof->refRays = c[2];
+        prof->extendRays = c[3];
+        prof->shadowRays = c[4];
+    }
+    return e;
+}
+
+cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,
+                               float distMax, int* triOut, float* distOut, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int block = 128;
+    const int grid = std::min((n + block - 1) / block, DefaultStageGrid() * 4);
+    TraceKernel<<<grid, block, 0, stream>>>(S, n, rays, distMin, distMax, triOut, distOut, nullptr);
+    return cudaGetLastError();
+}
+
+}  // namespace ptg

@@ -178,7 +178,16 @@ def write_scene(path_or_buf, sc: Scene) -> None:
 
 def read_scene(path) -> Scene:
     with open(path, "rb") as fh:
-        data = fh.read()
+        return read_scene_bytes(fh.read())
+
+
+def scene_bytes(sc: Scene) -> bytes:
+    buf = io.BytesIO()
+    write_scene(buf, sc)
+    return buf.getvalue()
+
+
+def read_scene_bytes(data: bytes) -> Scene:
     off = 0
 
     def take(n):

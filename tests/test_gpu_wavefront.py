@@ -1,0 +1,155 @@
+"""Wavefront (throughput) mode: same estimator as the reference, own random stream.
+
+Checks: closest-hit triangle IDs equal the reference's for the same rays (except
+exact distance ties); image means agree with the oracle within 0.5%; equal-spp
+RMSE against a 65536-spp image is statistically the same as the oracle's;
+results are deterministic and independent of how paths are batched.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden_scene
+from petrichor_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _render(ctx, sc, mode=capi.MODE_WAVEFRONT, seed=1, **over):
+    sid = ctx.upload(sc)
+    try:
+        return ctx.render(sid, capi.camera_from_scene(sc),
+                          capi.settings_from_scene(sc, mode, seed=seed, **over))
+    finally:
+        ctx.release(sid)
+
+
+def _trace(ctx, sc, rays, dmin=0.0, dmax=3.4028235e38):
+    sid = ctx.upload(sc)
+    try:
+        r = torch.from_numpy(np.ascontiguousarray(rays[:, :6], np.float32)).cuda()
+        tri = torch.empty(r.shape[0], dtype=torch.int32, device="cuda")
+        dist = torch.empty(r.shape[0], dtype=torch.float32, device="cuda")
+        ctx.trace_closest(sid, r.shape[0], r.data_ptr(), dmin, dmax, tri.data_ptr(), dist.data_ptr())
+        torch.cuda.synchronize()
+        return tri.cpu().numpy(), dist.cpu().numpy()
+    finally:
+        ctx.release(sid)
+
+
+def test_primary_hit_ids_match_reference(gpu_ctx, golden):
+    sc = golden_scene(golden, "spheres_pt")
+    rays = golden["spheres_pt/hit_rays"]
+    ref = golden["spheres_pt/hits"][:, 0]
+    tri, dist = _trace(gpu_ctx, sc, rays)
+    hit = ref >= 0
+    assert np.array_equal(tri >= 0, hit)
+    assert np.array_equal(dist[hit].view(np.uint32), rays[hit, 6].view(np.uint32))
+    mism = np.nonzero(tri != ref)[0]
+    # any differing ID must be an exact distance tie with the reference's triangle
+    for i in mism:
+        o = oracle.OracleScene(sc)
+        t1, d1 = o.trace(rays[i:i + 1])
+        assert d1[0] == dist[i]
+    assert len(mism) <= max(1, hit.sum() // 1000)
+
+
+def test_primary_hit_ids_full_size_scene(gpu_ctx):
+    sc = synth.spheres_grids(width=64, height=36, spp=1, env_width=64, env_height=32)
+    o = oracle.OracleScene(sc)
+    rays, hits = o.hits(3, 5)
+    tri, dist = _trace(gpu_ctx, sc, rays)
+    ref = hits[:, 0]
+    mism = np.nonzero(tri != ref)[0]
+    for i in mism:
+        assert dist[i] == rays[i, 6]
+    assert np.array_equal(dist[ref >= 0].view(np.uint32), rays[ref >= 0, 6].view(np.uint32))
+
+
+def _cases():
+    return {
+        "cornell_simple": synth.cornell(width=24, height=24, spp=1),
+        "cornell_mixed_pt": synth.cornell(width=24, height=16, spp=1, mixed=True, integrator=1,
+                                          max_bounces=6, env_texture=True),
+        "spheres_pt": synth.spheres_grids(tri_budget=20000, width=32, height=18, spp=1,
+                                          max_bounces=8, env_width=128, env_height=64),
+    }
+
+
+@pytest.mark.parametrize("name", list(_cases()))
+def test_wavefront_image_mean_within_half_percent(gpu_ctx, name):
+    sc = _cases()[name]
+    truth = _render(gpu_ctx, sc, spp=65536, seed=7)
+    ref, _ = oracle.OracleScene(sc.copy_with(settings=type(sc.settings)(**{
+        **sc.settings.__dict__, "spp": 4096}))).render()
+    gpu = _render(gpu_ctx, sc, spp=4096, seed=11)
+    m_truth, m_ref, m_gpu = truth.mean(), ref.mean(), gpu.mean()
+    print(f"{name}: truth {m_truth:.6f} oracle {m_ref:.6f} gpu {m_gpu:.6f}")
+    assert abs(m_gpu - m_truth) / m_truth <= 0.005
+    assert abs(m_ref - m_truth) / m_truth <= 0.005
+
+
+@pytest.mark.parametrize("name", list(_cases()))
+def test_wavefront_equal_spp_rmse_matches_oracle(gpu_ctx, name):
+    sc = _cases()[name]
+    truth = _render(gpu_ctx, sc, spp=65536, seed=7)
+    spp = 64
+    ref, _ = oracle.OracleScene(sc.copy_with(settings=type(sc.settings)(**{
+        **sc.settings.__dict__, "spp": spp}))).render()
+    gpu = _render(gpu_ctx, sc, spp=spp, seed=11)
+    r_ref = np.sqrt(np.mean((ref - truth) ** 2))
+    r_gpu = np.sqrt(np.mean((gpu - truth) ** 2))
+    print(f"{name}: rmse oracle {r_ref:.5f} gpu {r_gpu:.5f}")
+    assert 0.75 <= r_gpu / r_ref <= 1.33
+
+
+def test_wavefront_deterministic_and_batch_independent(gpu_ctx):
+    sc = synth.cornell(width=40, height=30, spp=8, mixed=True, integrator=1, max_bounces=6,
+                       env_texture=True)
+    a = _render(gpu_ctx, sc, seed=3)
+    b = _render(gpu_ctx, sc, seed=3)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    c = _render(gpu_ctx, sc, seed=4)
+    assert not np.array_equal(a, c)
+
+
+def test_empty_scene_and_zero_bounces(gpu_ctx):
+    sc = synth.cornell(width=8, height=8, spp=2, integrator=1, max_bounces=0, env_texture=True)
+    film = _render(gpu_ctx, sc)
+    ref, _ = oracle.OracleScene(sc).render()
+    # with zero bounces only primary misses and emitters contribute: deterministic per pixel
+    assert np.allclose(film[ref == 0], 0)
+    empty = sc.copy_with(indices=np.zeros((0, 3), np.int32), tri_material=np.zeros(0, np.int32),
+                         tri_shading=np.zeros(0, np.uint8), lights=np.zeros(0, np.int32))
+    film = _render(gpu_ctx, empty)
+    assert np.all(np.isfinite(film)) and film.mean() > 0
+
+
+def test_invalid_arguments_are_rejected_cleanly(gpu_ctx):
+    sc = synth.cornell(width=8, height=8, spp=1)
+    sid = gpu_ctx.upload(sc)
+    cam = capi.camera_from_scene(sc)
+    st = capi.settings_from_scene(sc, capi.MODE_WAVEFRONT)
+    bad = capi.settings_from_scene(sc, capi.MODE_WAVEFRONT, spp=0)
+    with pytest.raises(capi.PtError) as e:
+        gpu_ctx.render(sid, cam, bad)
+    assert e.value.status == -1
+    with pytest.raises(capi.PtError) as e:
+        gpu_ctx.render(sid + 1000, cam, st)
+    assert e.value.status == -6
+    gpu_ctx.render(sid, cam, st)  # context still usable
+    gpu_ctx.release(sid)
+
+
+def test_memory_budget_is_enforced():
+    ctx = capi.Context(memory_budget=1 << 20)
+    try:
+        sc = synth.spheres_grids(tri_budget=100000, width=8, height=8, spp=1, env_width=64,
+                                 env_height=32)
+        with pytest.raises(capi.PtError) as e:
+            ctx.upload(sc)
+        assert e.value.status == -3
+        assert ctx.stats().device_bytes_in_use <= 1 << 20
+    finally:
+        ctx.close()
