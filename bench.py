@@ -211,7 +211,9 @@ def main():
     npx = st.width * st.height
     samples_per_step = npx * st.spp
     film = torch.empty(npx * 3, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a real stream (not the legacy default stream, whose handle is 0): the
+    # renders and the timing events are enqueued on it
+    stream = torch.cuda.Stream()
 
     def step():
         ctx.render_device(sid, cam, sets, film.data_ptr(), stream.cuda_stream)

@@ -60,6 +60,8 @@ def lib():
         L.oracle_render.restype = ctypes.c_double
         L.oracle_render.argtypes = [vp, f32p, i32, i32, i32]
         L.oracle_num_tiles.argtypes = [vp]
+        L.oracle_render_decorrelated.restype = ctypes.c_double
+        L.oracle_render_decorrelated.argtypes = [vp, f32p, i32, ctypes.c_uint32]
         L.oracle_render_tiles.restype = ctypes.c_double
         L.oracle_render_tiles.argtypes = [vp, f32p, i32, i32p, i32]
         L.oracle_hits.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, f32p, i32p]
@@ -114,6 +116,13 @@ class OracleScene:
         s = self.scene.settings
         film = np.zeros((s.height, s.width, 3), np.float32)
         secs = lib().oracle_render(self._h, _fp(film), threads, tile_begin, tile_end)
+        return film, secs
+
+    def render_decorrelated(self, seed: int, threads: int = 0):
+        """Same integrator and arithmetic with independent per-tile random streams."""
+        s = self.scene.settings
+        film = np.zeros((s.height, s.width, 3), np.float32)
+        secs = lib().oracle_render_decorrelated(self._h, _fp(film), threads, seed)
         return film, secs
 
     def render_tiles(self, tiles, threads: int = 0):

@@ -1123,6 +1123,51 @@ double oracle_render_tiles(void* sp, float* film, int threads, const int32_t* li
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// The same integrators with decorrelated generators: per tile, three XorShift128
+// streams seeded from a hash of (seed, tile, stream) and advanced 64 steps, so the
+// 1D stream and the two 2D streams are independent. Used to separate the
+// reference's sampling correlations from the estimator itself.
+static uint32_t HashU32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+double oracle_render_decorrelated(void* sp, float* film, int threads, uint32_t seed) {
+    Scene& s = *(Scene*)sp;
+    if (!s.built) BuildBVH(s);
+    const int nx = s.W / s.tileW, ny = s.H / s.tileH;
+    const int remW = s.W - nx * s.tileW, remH = s.H - ny * s.tileH;
+    const int n = (nx + 1) * (ny + 1);
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next(0);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        for (;;) {
+            const int t = next.fetch_add(1);
+            if (t >= n) break;
+            const int i = t % (nx + 1), j = t / (nx + 1);
+            const int x0 = i * s.tileW, y0 = j * s.tileH;
+            const int w = i != nx ? s.tileW : remW, h = j != ny ? s.tileH : remH;
+            Sampler1D s1(HashU32(HashU32(seed) ^ (uint32_t)(3 * t)));
+            Sampler2D s2(HashU32(HashU32(seed) ^ (uint32_t)(3 * t + 1)),
+                         HashU32(HashU32(seed) ^ (uint32_t)(3 * t + 2)));
+            for (int k = 0; k < 64; k++) {
+                s1.Next();
+                float a, b;
+                s2.Next(&a, &b);
+            }
+            for (int y = y0; y < y0 + h; y++)
+                for (int x = x0; x < x0 + w; x++) {
+                    if (s.integrator == 0) RenderSimple(s, x, y, film, s1, s2);
+                    else RenderPT(s, x, y, film, s1, s2);
+                }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < threads; i++) pool.emplace_back(work);
+    for (auto& th : pool) th.join();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 // Number of tiles of the film (TileManager.cpp:8-43).
 int oracle_num_tiles(void* sp) {
     Scene& s = *(Scene*)sp;
