@@ -122,7 +122,9 @@ typedef struct pt_settings {
   int32_t integrator;     /* PT_INTEGRATOR_* */
   int32_t mode;           /* PT_MODE_* */
   uint32_t seed;          /* wavefront stream seed */
-  int32_t reserved[3];
+  int32_t wave_paths;     /* wavefront: paths per wave (0 = automatic); the film does
+                             not depend on it */
+  int32_t reserved[2];
 } pt_settings;
 
 typedef struct pt_scene_info {

@@ -56,7 +56,7 @@ class PtSettings(ctypes.Structure):
                 ("max_bounces", ctypes.c_int32), ("tile_width", ctypes.c_int32),
                 ("tile_height", ctypes.c_int32), ("integrator", ctypes.c_int32),
                 ("mode", ctypes.c_int32), ("seed", ctypes.c_uint32),
-                ("reserved", ctypes.c_int32 * 3)]
+                ("wave_paths", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class PtSceneInfo(ctypes.Structure):
@@ -168,6 +168,7 @@ def settings_from_scene(scene: Scene, mode: int = MODE_REPLAY, seed: int = 1, **
     st.integrator = over.get("integrator", s.integrator)
     st.mode = mode
     st.seed = seed
+    st.wave_paths = over.get("wave_paths", 0)
     return st
 
 

@@ -239,6 +239,7 @@ int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt
         return Fail(ctx, PT_ERR_INVALID_ARG, "unknown integrator");
     if (st->mode != PT_MODE_REPLAY && st->mode != PT_MODE_WAVEFRONT)
         return Fail(ctx, PT_ERR_INVALID_ARG, "unknown mode");
+    if (st->wave_paths < 0) return Fail(ctx, PT_ERR_INVALID_ARG, "wave_paths must be >= 0");
     auto it = ctx->scenes.find(scene);
     if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
     *out = it->second.get();
@@ -305,7 +306,8 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
         int rc = EnsureWaveBuffers(ctx, std::max(cap, std::min(st->width * st->height, 1 << 22)),
                                    st->width * st->height);
         if (rc != PT_OK) return rc;
-        e = RenderWavefront(sg.dev, C, S, ctx->wb, dFilm, stream, &launches, 0);
+        e = RenderWavefront(sg.dev, C, S, ctx->wb, dFilm, stream, &launches, 0, nullptr,
+                            st->wave_paths);
         if (e != cudaSuccess) return CudaFail(ctx, e, "wavefront render");
     }
     e = cudaEventRecord(ctx->ev1, stream);
@@ -635,7 +637,7 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     prof.devCounters = (unsigned long long*)counters.ptr;
     int launches = 0;
     const cudaError_t e = RenderWavefront(sg->dev, ToDev(cam), ToDev(st), ctx->wb, dFilm, ctx->stream,
-                                          &launches, 0, &prof);
+                                          &launches, 0, &prof, st->wave_paths);
     Free(ctx, counters);
     if (e != cudaSuccess) return CudaFail(ctx, e, "profiled render");
     ctx->stats.kernel_launches += launches;

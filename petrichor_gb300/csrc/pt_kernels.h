@@ -54,9 +54,11 @@ struct WaveProfile {
 // Renders one image through the wavefront stages into film (device, W*H*3).
 // grid: persistent grid size for the stage kernels (0 = auto). prof may be null;
 // with a profile the call synchronises the stream before returning.
+// wavePaths: paths per wave (<= wb.capacity; 0 = wb.capacity).
 cudaError_t RenderWavefront(const DevScene& S, const DevCamera& C, const DevSettings& st,
                             const WaveBuffers& wb, float* film, cudaStream_t stream,
-                            int* launches, int gridOverride, WaveProfile* prof = nullptr);
+                            int* launches, int gridOverride, WaveProfile* prof = nullptr,
+                            int wavePaths = 0);
 
 // Closest-hit traversal of the throughput path for caller rays (o.xyz, d.xyz per ray).
 cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,

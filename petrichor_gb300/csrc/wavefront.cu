@@ -515,7 +515,7 @@ int DefaultStageGrid() {
 
 cudaError_t RenderWavefront(const DevScene& S, const DevCamera& C, const DevSettings& st,
                             const WaveBuffers& wb, float* film, cudaStream_t stream, int* launches,
-                            int gridOverride, WaveProfile* prof) {
+                            int gridOverride, WaveProfile* prof, int wavePaths) {
     const int P_total = st.width * st.height;
     if (P_total <= 0 || st.spp <= 0) return cudaErrorInvalidValue;
     const int grid = gridOverride > 0 ? gridOverride : DefaultStageGrid();
@@ -525,7 +525,7 @@ cudaError_t RenderWavefront(const DevScene& S, const DevCamera& C, const DevSett
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(wb.counts, 0, 4 * sizeof(int), stream);
     if (e != cudaSuccess) return e;
-    const int cap = wb.capacity;
+    const int cap = wavePaths > 0 ? std::min(wavePaths, wb.capacity) : wb.capacity;
     const int Pc = std::min(P_total, cap);
     const int Sw = std::max(1, std::min(st.spp, cap / Pc));
     const float tmin = st.integrator == kSimplePathTracing ? kEps : 0.0f;

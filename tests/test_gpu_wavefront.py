@@ -5,6 +5,8 @@ exact distance ties); image means agree with the oracle within 0.5%; equal-spp
 RMSE against a 65536-spp image is statistically the same as the oracle's;
 results are deterministic and independent of how paths are batched.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -70,6 +72,8 @@ def test_primary_hit_ids_full_size_scene(gpu_ctx):
 def _cases():
     return {
         "cornell_simple": synth.cornell(width=24, height=24, spp=1),
+        "cornell_mixed_simple": synth.cornell(width=24, height=16, spp=1, mixed=True, env_texture=True),
+        "cornell_lambert_pt": synth.cornell(width=24, height=24, spp=1, integrator=1, max_bounces=5),
         "cornell_mixed_pt": synth.cornell(width=24, height=16, spp=1, mixed=True, integrator=1,
                                           max_bounces=6, env_texture=True),
         "spheres_pt": synth.spheres_grids(tri_budget=20000, width=32, height=18, spp=1,
@@ -77,31 +81,49 @@ def _cases():
     }
 
 
+def _with_spp(sc, spp):
+    return sc.copy_with(settings=dataclasses.replace(sc.settings, spp=spp))
+
+
 @pytest.mark.parametrize("name", list(_cases()))
-def test_wavefront_image_mean_within_half_percent(gpu_ctx, name):
+def test_wavefront_image_mean_matches_reference(gpu_ctx, name):
+    """Image mean of the throughput path vs the reference's own estimator (oracle with
+    the reference's random streams), with standard errors from replicate renders:
+    the relative difference must be within 0.5% (or within 4.5 standard errors when
+    the sample cannot resolve 0.5%, which the printout states)."""
     sc = _cases()[name]
-    truth = _render(gpu_ctx, sc, spp=65536, seed=7)
-    ref, _ = oracle.OracleScene(sc.copy_with(settings=type(sc.settings)(**{
-        **sc.settings.__dict__, "spp": 4096}))).render()
-    gpu = _render(gpu_ctx, sc, spp=4096, seed=11)
-    m_truth, m_ref, m_gpu = truth.mean(), ref.mean(), gpu.mean()
-    print(f"{name}: truth {m_truth:.6f} oracle {m_ref:.6f} gpu {m_gpu:.6f}")
-    assert abs(m_gpu - m_truth) / m_truth <= 0.005
-    assert abs(m_ref - m_truth) / m_truth <= 0.005
+    g = np.array([_render(gpu_ctx, sc, spp=16384, seed=s).mean() for s in range(1, 9)])
+    m_g, se_g = g.mean(), g.std(ddof=1) / np.sqrt(len(g))
+    o = oracle.OracleScene(_with_spp(sc, 16384))
+    m_r = float(o.render()[0].mean())
+    # spread of the reference estimator at this spp, from decorrelated replicates at 1/4 spp
+    od = oracle.OracleScene(_with_spp(sc, 4096))
+    d = np.array([od.render_decorrelated(s)[0].mean() for s in range(1, 5)])
+    se_r = d.std(ddof=1) / 2.0
+    se = float(np.sqrt(se_g ** 2 + se_r ** 2))
+    rel = abs(m_g - m_r) / m_r
+    print(f"{name}: gpu {m_g:.6f}+-{se_g:.6f} reference {m_r:.6f}+-{se_r:.6f} "
+          f"rel diff {rel:.4%} (4.5 sigma = {4.5 * se / m_r:.4%})")
+    assert rel <= max(0.005, 4.5 * se / m_r)
 
 
 @pytest.mark.parametrize("name", list(_cases()))
 def test_wavefront_equal_spp_rmse_matches_oracle(gpu_ctx, name):
+    """Equal-spp error against a 65536-spp image: the throughput path's mean squared
+    error equals that of the reference's estimator with independent streams (16
+    replicates each), and is no worse than the reference's own correlated streams."""
     sc = _cases()[name]
-    truth = _render(gpu_ctx, sc, spp=65536, seed=7)
+    truth = _render(gpu_ctx, sc, spp=65536, seed=1000)
     spp = 64
-    ref, _ = oracle.OracleScene(sc.copy_with(settings=type(sc.settings)(**{
-        **sc.settings.__dict__, "spp": spp}))).render()
-    gpu = _render(gpu_ctx, sc, spp=spp, seed=11)
-    r_ref = np.sqrt(np.mean((ref - truth) ** 2))
-    r_gpu = np.sqrt(np.mean((gpu - truth) ** 2))
-    print(f"{name}: rmse oracle {r_ref:.5f} gpu {r_gpu:.5f}")
-    assert 0.75 <= r_gpu / r_ref <= 1.33
+    mse = lambda a: float(np.mean((a - truth) ** 2))
+    e_g = np.mean([mse(_render(gpu_ctx, sc, spp=spp, seed=s)) for s in range(1, 17)])
+    od = oracle.OracleScene(_with_spp(sc, spp))
+    e_d = np.mean([mse(od.render_decorrelated(s)[0]) for s in range(1, 17)])
+    e_r = mse(od.render()[0])
+    print(f"{name}: rmse gpu {np.sqrt(e_g):.5f} independent-stream oracle {np.sqrt(e_d):.5f} "
+          f"reference streams {np.sqrt(e_r):.5f}")
+    assert 0.8 <= e_g / e_d <= 1.25
+    assert e_g <= 1.25 * e_r
 
 
 def test_wavefront_deterministic_and_batch_independent(gpu_ctx):
@@ -112,18 +134,26 @@ def test_wavefront_deterministic_and_batch_independent(gpu_ctx):
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     c = _render(gpu_ctx, sc, seed=4)
     assert not np.array_equal(a, c)
+    # other wave partitions (pixel chunks and sample blocks) give the same bits
+    for wp in (1000, 1200 * 3, 7777):
+        d = _render(gpu_ctx, sc, seed=3, wave_paths=wp)
+        assert np.array_equal(a.view(np.uint32), d.view(np.uint32)), wp
 
 
 def test_empty_scene_and_zero_bounces(gpu_ctx):
-    sc = synth.cornell(width=8, height=8, spp=2, integrator=1, max_bounces=0, env_texture=True)
-    film = _render(gpu_ctx, sc)
-    ref, _ = oracle.OracleScene(sc).render()
-    # with zero bounces only primary misses and emitters contribute: deterministic per pixel
-    assert np.allclose(film[ref == 0], 0)
+    # zero bounces: only primary misses (environment) and emitters contribute
+    sc = synth.cornell(width=16, height=16, spp=1, integrator=1, max_bounces=0, env_texture=True)
+    film = _render(gpu_ctx, sc, spp=4096)
+    ref, _ = oracle.OracleScene(_with_spp(sc, 1024)).render()
+    assert abs(film.mean() - ref.mean()) / ref.mean() < 0.02
+    # every pixel whose footprint lies inside the box interior stays black
+    assert np.all(film[6:10, 6:10] == 0) and np.all(ref[6:10, 6:10] == 0)
     empty = sc.copy_with(indices=np.zeros((0, 3), np.int32), tri_material=np.zeros(0, np.int32),
                          tri_shading=np.zeros(0, np.uint8), lights=np.zeros(0, np.int32))
     film = _render(gpu_ctx, empty)
+    eref, _ = oracle.OracleScene(empty).render()
     assert np.all(np.isfinite(film)) and film.mean() > 0
+    assert abs(film.mean() - eref.mean()) / eref.mean() < 0.05
 
 
 def test_invalid_arguments_are_rejected_cleanly(gpu_ctx):
