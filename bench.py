@@ -40,15 +40,31 @@ def parse():
     ap.add_argument("--small", action="store_true", help="reduced workload for quick checks")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the CPU-baseline sample")
+    ap.add_argument("--width", type=int, default=0, help="override (profiling runs only)")
+    ap.add_argument("--height", type=int, default=0, help="override (profiling runs only)")
+    ap.add_argument("--spp", type=int, default=0, help="override (profiling runs only)")
     return ap.parse_args()
 
 
-def make_scene(small: bool):
+def make_scene(args):
+    import dataclasses
     from petrichor_gb300 import synth
-    if small:
-        return synth.spheres_grids(tri_budget=100_000, width=480, height=270, spp=16, max_bounces=16,
-                                   env_width=512, env_height=256)
-    return synth.spheres_grids()  # 1.0M tris, 1920x1080, 64 spp, 16 bounces, 2048x1024 env
+    if args.small:
+        sc = synth.spheres_grids(tri_budget=100_000, width=480, height=270, spp=16, max_bounces=16,
+                                 env_width=512, env_height=256)
+    else:
+        sc = synth.spheres_grids()  # 1.0M tris, 1920x1080, 64 spp, 16 bounces, 2048x1024 env
+    over = {k: v for k, v in (("width", args.width), ("height", args.height), ("spp", args.spp)) if v}
+    if over:
+        sc = sc.copy_with(settings=dataclasses.replace(sc.settings, **over))
+    return sc
+
+
+def workload_name(args):
+    name = WORKLOAD + ("_SMALL" if args.small else "")
+    if args.width or args.height or args.spp:
+        name += "_OVERRIDE"
+    return name
 
 
 class ClockSampler:
@@ -142,7 +158,7 @@ def run_reference_arm(args):
     rank, world, local = dist_setup()
     if rank != 0:
         return
-    scene = make_scene(args.small)
+    scene = make_scene(args)
     import numpy as np
     import oracle
     o = oracle.OracleScene(scene)
@@ -168,7 +184,7 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "integrator": "PathTracing (MIS NEE)",
+        "config": {"workload": workload_name(args), "integrator": "PathTracing (MIS NEE)",
                    "sample_per_step": f"{len(tiles)} of {n_tiles} tiles at full spp"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
                          "sample": f"{len(tiles)} random 16x16 tiles x {scene.settings.spp} spp "
@@ -198,7 +214,7 @@ def main():
             dist.barrier()
 
     t0 = time.perf_counter()
-    scene = make_scene(args.small)
+    scene = make_scene(args)
     gen_s = time.perf_counter() - t0
     st = scene.settings
     ctx = capi.Context(local)
@@ -289,7 +305,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD if not args.small else WORKLOAD + "_SMALL",
+        "config": {"workload": workload_name(args),
                    "triangles": info.num_triangles, "bvh_nodes": info.num_nodes,
                    "resolution": [st.width, st.height], "spp": st.spp, "max_bounces": st.max_bounces,
                    "env": list(scene.env.texture.shape[:2][::-1]), "mode": "wavefront",

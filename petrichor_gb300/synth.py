@@ -285,8 +285,12 @@ def _mixed_material(rng: Rng, p_lambert=0.4, p_ggx=0.4,
 
 def spheres_grids(seed: int = 2, tri_budget: int = 1_000_000, n_objects: int = 64,
                   width: int = 1920, height: int = 1080, spp: int = 64, max_bounces: int = 16,
-                  env_width: int = 2048, env_height: int = 1024) -> Scene:
-    """64 seeded UV-spheres and displaced grids totalling ~``tri_budget`` triangles."""
+                  env_width: int = 2048, env_height: int = 1024,
+                  sun_peak_over_median: float = 1.0e4) -> Scene:
+    """64 seeded UV-spheres and displaced grids totalling ~``tri_budget`` triangles.
+
+    ``sun_peak_over_median`` scales the sun lobe (1e4 in the benchmark workload;
+    lower values give low-variance variants for statistical tests)."""
     rng = Rng(seed)
     b = _Builder()
     mats: List[Material] = []
@@ -312,7 +316,9 @@ def spheres_grids(seed: int = 2, tri_budget: int = 1_000_000, n_objects: int = 6
                                       rng.one(0.1, 0.35), rng.one(-0.9, 0.9), rng.one(0, 6.28))
             b.add(P, I, m, SHADING_SMOOTH, nrm=N)
     pos, nrm, uv, idx, tm, sh = b.arrays()
-    env = Environment(base_color=(1.0, 1.0, 1.0), texture=sky_env(rng, env_width, env_height))
+    env = Environment(base_color=(1.0, 1.0, 1.0),
+                      texture=sky_env(rng, env_width, env_height,
+                                      sun_peak_over_median=sun_peak_over_median))
     extent = side * spacing
     cam = Camera(pos=(0.0, -0.95 * extent, 0.5 * extent), view_dir=(0.0, 0.95 * extent, -0.5 * extent + 0.5),
                  fov=math.radians(45.0), focus_target=None, aperture=0.0)

