@@ -198,6 +198,20 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* camer
                       const pt_settings* settings, float* film_rgb_device, int32_t count_reference,
                       pt_profile* out);
 
+/* Replay render that allocates no device memory: for callers that cannot call
+ * cudaMalloc while rendering (another allocator owns the device memory, or the
+ * thread must not take the driver's allocation lock). Inputs are the resident
+ * scene, camera and settings (mode must be PT_MODE_REPLAY); the output is the
+ * caller's device film. Scratch (traversal stacks, status word) is a fixed 4 MiB
+ * __device__ array held by every GPU that loads the library: renders needing more
+ * than (tiles * (BVH height + 2)) = 1048560 stack ints are rejected with
+ * PT_ERR_INVALID_ARG. The first call on a device looks up the array's address;
+ * make it before any stream capture. All calls share the array, so calls that
+ * overlap on the GPU race. Enqueued on `stream` (NULL = the context's stream).
+ * No counterpart in the reference. */
+int pt_render_replay_noalloc(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+                             const pt_settings* settings, float* film_rgb_device, void* stream);
+
 int pt_get_stats(pt_context* ctx, pt_stats* out);
 /* Tiles finished / total of the last replay render (reference tile grid). */
 int pt_get_progress(pt_context* ctx, uint32_t* rendered_tiles, uint32_t* num_tiles);

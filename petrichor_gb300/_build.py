@@ -22,7 +22,7 @@ LIB = os.path.join(OUT_DIR, "libpetrichor_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
-CU_SOURCES = ["replay.cu", "wavefront.cu"]
+CU_SOURCES = ["replay.cu", "wavefront.cu", "noalloc.cu"]
 CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp"]
 
 

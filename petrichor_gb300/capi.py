@@ -89,7 +89,7 @@ EXPORTED = [
     "pt_abi_version", "pt_status_string", "pt_context_create", "pt_context_destroy",
     "pt_last_error", "pt_camera_init", "pt_scene_upload", "pt_scene_release",
     "pt_scene_info_get", "pt_render", "pt_render_device", "pt_trace_closest", "pt_get_stats",
-    "pt_get_progress", "pt_bvh_build", "pt_render_profile",
+    "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc",
 ]
 
 _lib = None
@@ -129,6 +129,8 @@ def load(build: bool = True):
                                    vp, vp]
     L.pt_trace_closest.argtypes = [vp, i32, i32, vp, ctypes.c_float, ctypes.c_float, vp, vp, vp]
     L.pt_get_stats.argtypes = [vp, ctypes.POINTER(PtStats)]
+    L.pt_render_replay_noalloc.argtypes = [vp, i32, ctypes.POINTER(PtCamera),
+                                           ctypes.POINTER(PtSettings), vp, vp]
     L.pt_render_profile.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
                                     vp, i32, ctypes.POINTER(PtProfile)]
     L.pt_get_progress.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]

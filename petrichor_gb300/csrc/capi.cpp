@@ -657,6 +657,37 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     return PT_OK;
 }
 
+int pt_render_replay_noalloc(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
+                             const pt_settings* st, float* dFilm, void* stream) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!dFilm) return Fail(ctx, PT_ERR_INVALID_ARG, "film is NULL");
+    if (st->mode != PT_MODE_REPLAY)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "the no-allocation render runs the replay mode only");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    const DevSettings S = ToDev(st);
+    const int tiles = NumTiles(S);
+    const size_t need = (size_t)tiles * sg->dev.stackDepth;
+    if (need > NoAllocScratchInts())
+        return Fail(ctx, PT_ERR_INVALID_ARG,
+                    "render needs " + std::to_string(need) + " stack ints of scratch; the fixed "
+                    "no-allocation array holds " + std::to_string(NoAllocScratchInts()));
+    int *status = nullptr, *stacks = nullptr;
+    cudaError_t e = NoAllocScratch(&status, &stacks);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "no-allocation scratch lookup");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    e = cudaMemsetAsync(status, 0, sizeof(int), s);  // status word starts at zero
+    if (e != cudaSuccess) return CudaFail(ctx, e, "status clear");
+    e = LaunchReplay(sg->dev, ToDev(cam), S, dFilm, stacks, status, 0, tiles, s);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "replay launch");
+    ctx->stats.kernel_launches++;
+    ctx->stats.renders++;
+    return PT_OK;
+}
+
 int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float* rays,
                      float distMin, float distMax, int32_t* tri, float* dist, void* stream) {
     if (!ctx) return PT_ERR_INVALID_ARG;

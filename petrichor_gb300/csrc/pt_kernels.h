@@ -66,4 +66,9 @@ cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, floa
 
 int DefaultStageGrid();
 
+// Fixed scratch of the no-allocation replay render (noalloc.cu): status word and
+// stack area addresses on the current device; capacity of the stack area in ints.
+cudaError_t NoAllocScratch(int** statusOut, int** stacksOut);
+size_t NoAllocScratchInts();
+
 }  // namespace ptg
