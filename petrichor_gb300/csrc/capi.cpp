@@ -225,6 +225,18 @@ int EnsureWaveBuffers(pt_context* ctx, int capacity, int pixels) {
     return PT_OK;
 }
 
+// Paths per wave: the whole image x spp when it fits in kMaxWavePaths (about 12 GB
+// of wave state), otherwise as many full sample blocks as fit. HBM holds this
+// easily; fewer, larger waves mean fewer sparse late-bounce launches.
+constexpr int64_t kMaxWavePaths = int64_t(1) << 26;
+int WaveCapacity(const pt_settings* st) {
+    const int64_t px = (int64_t)st->width * st->height;
+    int64_t cap = std::min<int64_t>(px * st->spp, kMaxWavePaths);
+    cap = std::max<int64_t>(cap, std::min<int64_t>(px, kMaxWavePaths));
+    if (st->wave_paths > 0) cap = std::min<int64_t>(cap, st->wave_paths);
+    return (int)std::max<int64_t>(cap, 1);
+}
+
 int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
               SceneGpu** out) {
     if (!ctx) return PT_ERR_INVALID_ARG;
@@ -301,10 +313,7 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
             if (e != cudaSuccess) return CudaFail(ctx, e, "replay launch");
         }
     } else {
-        const int64_t paths = (int64_t)st->width * st->height * st->spp;
-        const int cap = (int)std::min<int64_t>(paths, 1 << 22);
-        int rc = EnsureWaveBuffers(ctx, std::max(cap, std::min(st->width * st->height, 1 << 22)),
-                                   st->width * st->height);
+        int rc = EnsureWaveBuffers(ctx, WaveCapacity(st), st->width * st->height);
         if (rc != PT_OK) return rc;
         e = RenderWavefront(sg.dev, C, S, ctx->wb, dFilm, stream, &launches, 0, nullptr,
                             st->wave_paths);
@@ -624,10 +633,7 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     if (st->mode != PT_MODE_WAVEFRONT)
         return Fail(ctx, PT_ERR_UNSUPPORTED, "profiling covers the wavefront mode");
     if ((rc = SetDevice(ctx)) != PT_OK) return rc;
-    const int64_t paths = (int64_t)st->width * st->height * st->spp;
-    const int cap = (int)std::min<int64_t>(paths, 1 << 22);
-    rc = EnsureWaveBuffers(ctx, std::max(cap, std::min(st->width * st->height, 1 << 22)),
-                           st->width * st->height);
+    rc = EnsureWaveBuffers(ctx, WaveCapacity(st), st->width * st->height);
     if (rc != PT_OK) return rc;
     DeviceBuffer counters;
     if ((rc = Alloc(ctx, counters, 8 * sizeof(unsigned long long))) != PT_OK) return rc;

