@@ -43,6 +43,12 @@ def parse():
     ap.add_argument("--width", type=int, default=0, help="override (profiling runs only)")
     ap.add_argument("--height", type=int, default=0, help="override (profiling runs only)")
     ap.add_argument("--spp", type=int, default=0, help="override (profiling runs only)")
+    ap.add_argument("--batch", action="store_true",
+                    help="batched uneven instances: 64 scenes in shared waves vs 64 plain launches")
+    ap.add_argument("--serve", action="store_true",
+                    help="serving loop: Poisson request stream, p50/p99 latency vs the plain path")
+    ap.add_argument("--requests", type=int, default=100, help="requests per arrival rate (--serve)")
+    ap.add_argument("--wave-paths", type=int, default=0, help="serving wave size (0: auto)")
     return ap.parse_args()
 
 
@@ -193,10 +199,164 @@ def run_reference_arm(args):
     }))
 
 
+def run_batch(args):
+    """64 uneven scenes (triangles log-uniform 10k-2M, pixels log-uniform 256^2-1024^2,
+    aspect 0.5-2, spp in {4,16,64,256}, own 1024x512 skies): one pt_batch_render vs
+    64 sequential pt_render_device launches; films checked identical."""
+    import numpy as np
+    import torch
+    from petrichor_gb300 import capi, synth
+    t0 = time.perf_counter()
+    scenes = synth.batch_instances()
+    gen_s = time.perf_counter() - t0
+    ctx = capi.Context(0)
+    t0 = time.perf_counter()
+    sids = [ctx.upload(s) for s in scenes]
+    upload_s = time.perf_counter() - t0
+    jobs = []
+    for k, (sc, sid) in enumerate(zip(scenes, sids)):
+        st = capi.settings_from_scene(sc, capi.MODE_WAVEFRONT, seed=k + 1)
+        film = torch.empty(st.width * st.height * 3, dtype=torch.float32, device="cuda")
+        jobs.append((sid, capi.camera_from_scene(sc), st, film))
+    samples = sum(j[2].width * j[2].height * j[2].spp for j in jobs)
+    tris = sum(s.num_triangles for s in scenes)
+    stream = torch.cuda.Stream()
+    plain = [torch.empty_like(j[3]) for j in jobs]
+
+    def run_plain():
+        for (sid, cam, st, _), f in zip(jobs, plain):
+            ctx.render_device(sid, cam, st, f.data_ptr(), stream.cuda_stream)
+
+    def run_batched():
+        ctx.batch_render([(sid, cam, st, f.data_ptr()) for sid, cam, st, f in jobs], stream.cuda_stream)
+
+    for _ in range(max(1, args.warmup)):
+        run_plain()
+        run_batched()
+    torch.cuda.synchronize()
+    res = {}
+    for name, fn in (("plain", run_plain), ("batched", run_batched)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches0 = ctx.stats().kernel_launches
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        secs = e0.elapsed_time(e1) / 1e3 / args.steps
+        res[name] = {"ms_per_batch": secs * 1e3, "msamples_per_s": samples / secs / 1e6,
+                     "gpu_launches_per_batch": (ctx.stats().kernel_launches - launches0) / args.steps}
+    same = all(torch.equal(a[3], b) for a, b in zip(jobs, plain))
+    print(json.dumps({
+        "metric": "batched_msamples_per_s", "value": res["batched"]["msamples_per_s"], "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": res["batched"]["ms_per_batch"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch_64_uneven_spheres_grids", "scenes": len(scenes),
+                   "triangles_total": tris, "samples_per_batch": samples,
+                   "scene_gen_s": round(gen_s, 1), "upload_s": round(upload_s, 1)},
+        "plain_sequential": res["plain"], "batched": res["batched"],
+        "speedup_vs_plain": res["batched"]["msamples_per_s"] / res["plain"]["msamples_per_s"],
+        "films_identical_to_plain": bool(same),
+    }))
+    ctx.close()
+
+
+def run_serve(args):
+    """8 resident scenes (100k-4M triangles, 8192x4096 skies); Poisson arrivals at
+    20/100/500 requests/s; per request resolution log-uniform 128^2-2048^2 (aspect
+    0.5-2), spp in {1,8,32,128}, depth 4-16. The continuous-batching server vs the
+    plain path serving the same stream one request at a time."""
+    import numpy as np
+    import torch
+    from petrichor_gb300 import capi, synth
+    t0 = time.perf_counter()
+    scenes = synth.serving_scenes()
+    gen_s = time.perf_counter() - t0
+    ctx = capi.Context(0)
+    sids = [ctx.upload(s) for s in scenes]
+    resident = sum(ctx.scene_info(sid).device_bytes for sid in sids)
+    cams = [capi.camera_from_scene(s) for s in scenes]
+    out = {"metric": "serve_msamples_per_s", "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "serve_8_scenes_poisson", "scenes": len(scenes),
+                      "triangles": [s.num_triangles for s in scenes],
+                      "resident_bytes": int(resident), "requests_per_rate": args.requests,
+                      "state_budget_bytes": 150 * 2**30, "scene_gen_s": round(gen_s, 1)},
+           "rates": {}}
+    max_px = 2048 * 2048 * 2
+    pinned = [torch.empty(max_px * 3, dtype=torch.float32, pin_memory=True) for _ in range(4)]
+
+    def settings(w, h, spp, depth, seed):
+        st = capi.settings_from_scene(scenes[0], capi.MODE_WAVEFRONT, seed=seed, width=w, height=h,
+                                      spp=spp, max_bounces=depth)
+        return st
+
+    for rate in (20.0, 100.0, 500.0):
+        stream_ = synth.request_stream(int(rate), rate, args.requests)
+        samples = sum(w * h * spp for _, _, w, h, spp, _ in stream_)
+        res = {}
+        # ---- continuous-batching server
+        ctx.serve_start(wave_paths=args.wave_paths or (1 << 24), max_active=512,
+                        state_budget=150 * 2**30)
+        films = [np.empty((h, w, 3), np.float32) for _, _, w, h, _, _ in stream_]
+        rids = []
+        t_start = time.perf_counter()
+        for k, (t, sc, w, h, spp, depth) in enumerate(stream_):
+            dt = t_start + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            rids.append(ctx.serve_submit(sids[sc], cams[sc], settings(w, h, spp, depth, k + 1),
+                                         film_host=films[k]))
+        sts = [ctx.serve_wait(r, 600) for r in rids]
+        ctx.serve_stop()
+        lat = np.array([s.done_s - s.submit_s for s in sts])
+        first = min(s.submit_s for s in sts)
+        last = max(s.done_s for s in sts)
+        res["batched_serve"] = {"msamples_per_s": samples / (last - first) / 1e6,
+                                "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                                "completed": sum(s.state == capi.REQ_DONE for s in sts)}
+        # ---- plain path: one pt_render per request, in arrival order
+        lat_p = []
+        t_start = time.perf_counter()
+        t_first = None
+        for k, (t, sc, w, h, spp, depth) in enumerate(stream_):
+            now = time.perf_counter()
+            if t_start + t > now:
+                time.sleep(t_start + t - now)
+            arrival = t_start + t
+            t_first = t_first or arrival
+            film = pinned[k % 4][: w * h * 3].numpy().reshape(h, w, 3)
+            ctx.render(sids[sc], cams[sc], settings(w, h, spp, depth, k + 1), out=film)
+            lat_p.append(time.perf_counter() - arrival)
+            if k == 0:
+                same_first = bool(np.array_equal(film.view(np.uint32), films[0].view(np.uint32)))
+        t_end = time.perf_counter()
+        lat_p = np.array(lat_p)
+        res["plain"] = {"msamples_per_s": samples / (t_end - t_first) / 1e6,
+                        "p50_ms": float(np.percentile(lat_p, 50) * 1e3),
+                        "p99_ms": float(np.percentile(lat_p, 99) * 1e3)}
+        res["speedup_vs_plain"] = res["batched_serve"]["msamples_per_s"] / res["plain"]["msamples_per_s"]
+        res["first_film_identical_to_plain"] = same_first
+        res["samples"] = samples
+        out["rates"][str(int(rate))] = res
+    top = out["rates"]["500"]
+    out["value"] = top["batched_serve"]["msamples_per_s"]
+    out["p50_ms"] = top["batched_serve"]["p50_ms"]
+    out["p99_ms"] = top["batched_serve"]["p99_ms"]
+    print(json.dumps(out))
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.batch:
+        return run_batch(args)
+    if args.serve:
+        return run_serve(args)
     import numpy as np
     import torch
     from petrichor_gb300 import capi

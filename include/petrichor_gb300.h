@@ -19,6 +19,10 @@
  *                        (LibPetrichor/Core/Accel/AccelBase.h:36-55)
  *   pt_get_progress      Petrichor::GetNumRenderedTiles / GetNumTiles
  *                        (LibPetrichor/Core/Petrichor.h:41-51)
+ *   pt_batch_render      repeated Petrichor::Render calls, one per scene and image
+ *                        (LibPetrichor/Core/Petrichor.cpp:103-171): many images in shared waves
+ *   pt_serve_*           no reference counterpart: a resident render service (scenes
+ *                        stay in HBM; requests are batched continuously)
  *   pt_render_profile    SCOPE_LOGGER timers around the render passes
  *                        (LibPetrichor/Core/Logger.h:63-94, used at Petrichor.cpp:106,124)
  *   pt_bvh_build         BinnedSAHBVH::Build alone, on the host, returning the tree
@@ -170,6 +174,63 @@ int pt_render(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
  * context's stream). Returns once the work is enqueued. */
 int pt_render_device(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
                      const pt_settings* settings, float* film_rgb_device, void* stream);
+
+/* One image of a batch: a resident scene, its camera and settings (mode must be
+ * PT_MODE_WAVEFRONT) and a device film of width*height*3 floats. */
+typedef struct pt_job {
+  pt_scene_id scene;
+  pt_camera camera;
+  pt_settings settings;
+  float* film_device;
+} pt_job;
+
+/* Renders n images (any sizes, scenes, spp and integrators) in shared persistent
+ * waves. Each film equals what pt_render_device produces for that job alone (per
+ * pixel sums in sample order, random stream keyed by (seed, pixel, sample)).
+ * Enqueued on `stream` (NULL = the context's stream); it waits on the stream only
+ * when a SimplePathTracing job needs its queue polled. */
+int pt_batch_render(pt_context* ctx, int32_t n, const pt_job* jobs, void* stream);
+
+/* ---- serving loop: continuous batching of render requests over resident scenes.
+ * A server thread packs the pending samples of every admitted request into shared
+ * waves; requests that arrive while others run are admitted as slots and memory
+ * free up and join the next wave. A request's film is the same as its
+ * pt_render_device film (same seed), alone or in any mix. */
+#define PT_REQ_QUEUED 0
+#define PT_REQ_RUNNING 1
+#define PT_REQ_DONE 2
+#define PT_REQ_CANCELLED 3
+#define PT_REQ_FAILED 4
+
+typedef struct pt_serve_config {
+  int32_t wave_paths;     /* paths per wave (0: 8M) */
+  int32_t max_active;     /* requests admitted at once (0: 256) */
+  uint64_t state_budget;  /* device bytes for per-request state: sums + film staging (0: 4 GiB) */
+} pt_serve_config;
+
+typedef struct pt_request_status {
+  int32_t state;        /* PT_REQ_* */
+  int32_t status;       /* PT_OK or the error of a failed request */
+  double submit_s;      /* seconds since pt_serve_start */
+  double admit_s;       /* admitted to a slot (-1 while queued) */
+  double done_s;        /* film written (-1 until then) */
+  uint32_t samples_done, samples_total;
+} pt_request_status;
+
+int pt_serve_start(pt_context* ctx, const pt_serve_config* config);
+/* Queues a render (settings.mode must be PT_MODE_WAVEFRONT). The film is written
+ * to job->film_device, or, when film_host is not NULL, copied to film_host
+ * (width*height*3 floats; pinned memory recommended) once finished. Requests
+ * whose state can never fit the state budget fail with PT_ERR_OVER_BUDGET. */
+int pt_serve_submit(pt_context* ctx, const pt_job* job, float* film_host, uint64_t* request_id);
+int pt_serve_poll(pt_context* ctx, uint64_t request_id, pt_request_status* out);
+/* Waits until the request is done, cancelled or failed (PT_ERR_TIMEOUT after timeout_s). */
+int pt_serve_wait(pt_context* ctx, uint64_t request_id, double timeout_s, pt_request_status* out);
+int pt_serve_cancel(pt_context* ctx, uint64_t request_id);
+/* Forgets a finished request (its status can no longer be polled). */
+int pt_serve_release(pt_context* ctx, uint64_t request_id);
+/* Stops the server after the wave in flight; queued and running requests are cancelled. */
+int pt_serve_stop(pt_context* ctx);
 
 /* Closest hits for n device rays (o.xyz, dir.xyz) within [dist_min, dist_max]:
  * original triangle index (or -1) and distance (or -1). Enqueued on `stream`. */

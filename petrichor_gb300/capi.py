@@ -59,6 +59,25 @@ class PtSettings(ctypes.Structure):
                 ("wave_paths", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
+class PtJob(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_int32), ("camera", PtCamera), ("settings", PtSettings),
+                ("film_device", ctypes.c_void_p)]
+
+
+class PtServeConfig(ctypes.Structure):
+    _fields_ = [("wave_paths", ctypes.c_int32), ("max_active", ctypes.c_int32),
+                ("state_budget", ctypes.c_uint64)]
+
+
+class PtRequestStatus(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("submit_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("samples_done", ctypes.c_uint32), ("samples_total", ctypes.c_uint32)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
+
+
 class PtSceneInfo(ctypes.Structure):
     _fields_ = [("num_triangles", ctypes.c_uint32), ("num_nodes", ctypes.c_uint32),
                 ("tree_height", ctypes.c_uint32), ("num_lights", ctypes.c_uint32),
@@ -89,7 +108,9 @@ EXPORTED = [
     "pt_abi_version", "pt_status_string", "pt_context_create", "pt_context_destroy",
     "pt_last_error", "pt_camera_init", "pt_scene_upload", "pt_scene_release",
     "pt_scene_info_get", "pt_render", "pt_render_device", "pt_trace_closest", "pt_get_stats",
-    "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc",
+    "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc", "pt_batch_render",
+    "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
+    "pt_serve_release", "pt_serve_stop",
 ]
 
 _lib = None
@@ -129,6 +150,15 @@ def load(build: bool = True):
                                    vp, vp]
     L.pt_trace_closest.argtypes = [vp, i32, i32, vp, ctypes.c_float, ctypes.c_float, vp, vp, vp]
     L.pt_get_stats.argtypes = [vp, ctypes.POINTER(PtStats)]
+    L.pt_batch_render.argtypes = [vp, i32, ctypes.POINTER(PtJob), vp]
+    u64 = ctypes.c_uint64
+    L.pt_serve_start.argtypes = [vp, ctypes.POINTER(PtServeConfig)]
+    L.pt_serve_submit.argtypes = [vp, ctypes.POINTER(PtJob), vp, ctypes.POINTER(u64)]
+    L.pt_serve_poll.argtypes = [vp, u64, ctypes.POINTER(PtRequestStatus)]
+    L.pt_serve_wait.argtypes = [vp, u64, ctypes.c_double, ctypes.POINTER(PtRequestStatus)]
+    L.pt_serve_cancel.argtypes = [vp, u64]
+    L.pt_serve_release.argtypes = [vp, u64]
+    L.pt_serve_stop.argtypes = [vp]
     L.pt_render_replay_noalloc.argtypes = [vp, i32, ctypes.POINTER(PtCamera),
                                            ctypes.POINTER(PtSettings), vp, vp]
     L.pt_render_profile.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
@@ -273,6 +303,56 @@ class Context:
         self._check(self.L.pt_render_device(self.h, sid, ctypes.byref(camera),
                                             ctypes.byref(settings), film_ptr, stream_ptr or None),
                     "pt_render_device")
+
+    def batch_render(self, jobs, stream_ptr: int = 0):
+        """jobs: list of (scene id, PtCamera, PtSettings, device film pointer)."""
+        arr = (PtJob * len(jobs))()
+        for k, (sid, cam, st, film) in enumerate(jobs):
+            arr[k].scene = sid
+            arr[k].camera = cam
+            arr[k].settings = st
+            arr[k].film_device = film
+        self._check(self.L.pt_batch_render(self.h, len(jobs), arr, stream_ptr or None),
+                    "pt_batch_render")
+
+    # ---- serving loop
+    def serve_start(self, wave_paths: int = 0, max_active: int = 0, state_budget: int = 0):
+        cfg = PtServeConfig(wave_paths, max_active, state_budget)
+        self._check(self.L.pt_serve_start(self.h, ctypes.byref(cfg)), "pt_serve_start")
+
+    def serve_submit(self, sid: int, camera: PtCamera, settings: PtSettings, film_device: int = 0,
+                     film_host: Optional[np.ndarray] = None) -> int:
+        job = PtJob()
+        job.scene = sid
+        job.camera = camera
+        job.settings = settings
+        job.film_device = film_device or None
+        rid = ctypes.c_uint64()
+        host = film_host.ctypes.data if film_host is not None else None
+        self._check(self.L.pt_serve_submit(self.h, ctypes.byref(job), host, ctypes.byref(rid)),
+                    "pt_serve_submit")
+        return rid.value
+
+    def serve_poll(self, rid: int) -> PtRequestStatus:
+        st = PtRequestStatus()
+        self._check(self.L.pt_serve_poll(self.h, rid, ctypes.byref(st)), "pt_serve_poll")
+        return st
+
+    def serve_wait(self, rid: int, timeout: float = 60.0) -> PtRequestStatus:
+        st = PtRequestStatus()
+        rc = self.L.pt_serve_wait(self.h, rid, timeout, ctypes.byref(st))
+        if rc not in (PT_OK, -4):
+            self._check(rc, "pt_serve_wait")
+        return st
+
+    def serve_cancel(self, rid: int):
+        self._check(self.L.pt_serve_cancel(self.h, rid), "pt_serve_cancel")
+
+    def serve_release(self, rid: int):
+        self._check(self.L.pt_serve_release(self.h, rid), "pt_serve_release")
+
+    def serve_stop(self):
+        self._check(self.L.pt_serve_stop(self.h), "pt_serve_stop")
 
     def render_profile(self, sid: int, camera: PtCamera, settings: PtSettings, film_ptr: int,
                        count_reference: bool = True) -> PtProfile:

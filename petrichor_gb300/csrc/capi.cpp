@@ -21,45 +21,12 @@
 #include "bvh_builder.h"
 #include "pt_kernels.h"
 #include "pt_layout.h"
+#include "context.h"
+#include "scheduler.h"
 
 using namespace ptg;
 
-namespace {
-
-struct DeviceBuffer {
-    void* ptr = nullptr;
-    size_t bytes = 0;
-};
-
-struct SceneGpu {
-    DevScene dev{};
-    std::vector<DeviceBuffer> buffers;
-    pt_scene_info info{};
-};
-
-}  // namespace
-
-struct pt_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    uint64_t budget = 0;  // 0 = unlimited
-    uint64_t used = 0;
-    std::mutex mu;
-    std::string lastError;
-    std::map<int, std::unique_ptr<SceneGpu>> scenes;
-    int nextId = 1;
-    // wavefront buffers
-    WaveBuffers wb{};
-    std::vector<DeviceBuffer> wbBuffers;
-    int wbCapacity = 0, wbPixels = 0;
-    // scratch for host-film renders and replay stacks
-    DeviceBuffer film, stack, status;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    pt_stats stats{};
-    uint32_t tilesDone = 0, tilesTotal = 0;
-};
-
-namespace {
+namespace ptg {
 
 int Fail(pt_context* ctx, int code, const std::string& msg) {
     if (ctx) ctx->lastError = msg;
@@ -189,20 +156,34 @@ int SetDevice(pt_context* ctx) {
     return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "cudaSetDevice");
 }
 
-int EnsureWaveBuffers(pt_context* ctx, int capacity, int pixels) {
-    if (ctx->wbCapacity >= capacity && ctx->wbPixels >= pixels) return PT_OK;
-    capacity = std::max(capacity, ctx->wbCapacity);
-    pixels = std::max(pixels, ctx->wbPixels);
+// Paths per wave: the whole image x spp when it fits in kMaxWavePaths (about 13 GB
+// of wave state), otherwise as many full sample blocks as fit. HBM holds this
+// easily; fewer, larger waves mean fewer sparse late-bounce launches.
+int WaveCapacity(const pt_settings* st) {
+    const int64_t px = (int64_t)st->width * st->height;
+    int64_t cap = std::min<int64_t>(px * st->spp, kMaxWavePaths);
+    cap = std::max<int64_t>(cap, std::min<int64_t>(px, kMaxWavePaths));
+    if (st->wave_paths > 0) cap = std::min<int64_t>(cap, std::max<int64_t>(st->wave_paths, px));
+    return (int)std::max<int64_t>(cap, 1);
+}
+
+
+int EnsureWaveBuffers(pt_context* ctx, int capacity) {
+    if (ctx->wbCapacity >= capacity) return PT_OK;
     for (auto& b : ctx->wbBuffers) Free(ctx, b);
-    ctx->wbBuffers.assign(11, DeviceBuffer{});
+    ctx->wbBuffers.assign(10, DeviceBuffer{});
     const size_t C = (size_t)capacity;
-    const size_t sizes[11] = {C * 2 * sizeof(float4), C * 2 * sizeof(float4), C * sizeof(float2),
+    const size_t sizes[10] = {C * 2 * sizeof(float4), C * 2 * sizeof(float4), C * sizeof(float2),
                               C * sizeof(float4),     C * sizeof(float4),     C * sizeof(float4),
-                              C * sizeof(unsigned long long), C * 4 * sizeof(float4),
-                              16 * sizeof(int),       (size_t)pixels * sizeof(float4), 0};
+                              C * sizeof(unsigned long long), C * sizeof(int),
+                              C * 4 * sizeof(float4), 16 * sizeof(int)};
     for (int i = 0; i < 10; i++) {
         const int rc = Alloc(ctx, ctx->wbBuffers[i], sizes[i]);
-        if (rc != PT_OK) return rc;
+        if (rc != PT_OK) {
+            for (auto& b : ctx->wbBuffers) Free(ctx, b);
+            ctx->wbCapacity = 0;
+            return rc;
+        }
     }
     WaveBuffers& w = ctx->wb;
     w.capacity = capacity;
@@ -213,28 +194,34 @@ int EnsureWaveBuffers(pt_context* ctx, int capacity, int pixels) {
     w.st1 = (float4*)ctx->wbBuffers[4].ptr;
     w.st2 = (float4*)ctx->wbBuffers[5].ptr;
     w.rng = (unsigned long long*)ctx->wbBuffers[6].ptr;
-    w.shadow = (float4*)ctx->wbBuffers[7].ptr;
-    w.counts = (int*)ctx->wbBuffers[8].ptr;
-    w.accum = (float4*)ctx->wbBuffers[9].ptr;
+    w.pathJob = (int*)ctx->wbBuffers[7].ptr;
+    w.shadow = (float4*)ctx->wbBuffers[8].ptr;
+    w.counts = (int*)ctx->wbBuffers[9].ptr;
+    cudaMemsetAsync(w.counts, 0, 16 * sizeof(int), ctx->stream);
     if (!w.hostCount) {
         const cudaError_t e = cudaMallocHost(&w.hostCount, sizeof(int) * 4);
         if (e != cudaSuccess) return CudaFail(ctx, e, "cudaMallocHost");
     }
     ctx->wbCapacity = capacity;
-    ctx->wbPixels = pixels;
     return PT_OK;
 }
 
-// Paths per wave: the whole image x spp when it fits in kMaxWavePaths (about 12 GB
-// of wave state), otherwise as many full sample blocks as fit. HBM holds this
-// easily; fewer, larger waves mean fewer sparse late-bounce launches.
-constexpr int64_t kMaxWavePaths = int64_t(1) << 26;
-int WaveCapacity(const pt_settings* st) {
-    const int64_t px = (int64_t)st->width * st->height;
-    int64_t cap = std::min<int64_t>(px * st->spp, kMaxWavePaths);
-    cap = std::max<int64_t>(cap, std::min<int64_t>(px, kMaxWavePaths));
-    if (st->wave_paths > 0) cap = std::min<int64_t>(cap, st->wave_paths);
-    return (int)std::max<int64_t>(cap, 1);
+int EnsureTables(pt_context* ctx, int nJobs, size_t accumPixels) {
+    int rc;
+    if ((rc = Alloc(ctx, ctx->jobTable, sizeof(DevJob) * (size_t)std::max(nJobs, 1))) != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->unitTable, sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->jobList, sizeof(int) * (size_t)std::max(nJobs, 1))) != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->accum, sizeof(float4) * std::max<size_t>(accumPixels, 1))) != PT_OK) return rc;
+    return PT_OK;
+}
+
+WaveTables Tables(pt_context* ctx) {
+    WaveTables t;
+    t.jobs = (DevJob*)ctx->jobTable.ptr;
+    t.units = (WaveUnit*)ctx->unitTable.ptr;
+    t.jobList = (int*)ctx->jobList.ptr;
+    t.maxUnits = kMaxUnitsPerWave;
+    return t;
 }
 
 int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
@@ -313,10 +300,17 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
             if (e != cudaSuccess) return CudaFail(ctx, e, "replay launch");
         }
     } else {
-        int rc = EnsureWaveBuffers(ctx, WaveCapacity(st), st->width * st->height);
+        const int cap = WaveCapacity(st);
+        int rc = EnsureWaveBuffers(ctx, cap);
         if (rc != PT_OK) return rc;
-        e = RenderWavefront(sg.dev, C, S, ctx->wb, dFilm, stream, &launches, 0, nullptr,
-                            st->wave_paths);
+        if ((rc = EnsureTables(ctx, 1, (size_t)st->width * st->height)) != PT_OK) return rc;
+        DevJob job{};
+        job.S = sg.dev;
+        job.C = C;
+        job.st = S;
+        job.accum = (float4*)ctx->accum.ptr;
+        job.film = dFilm;
+        e = RenderJobs({job}, Tables(ctx), ctx->wb, cap, stream, &launches, nullptr);
         if (e != cudaSuccess) return CudaFail(ctx, e, "wavefront render");
     }
     e = cudaEventRecord(ctx->ev1, stream);
@@ -341,7 +335,7 @@ int FinishStats(pt_context* ctx, cudaStream_t stream) {
     return PT_OK;
 }
 
-}  // namespace
+}  // namespace ptg
 
 extern "C" {
 
@@ -385,6 +379,7 @@ int pt_context_create(int device, uint64_t budget, pt_context** out) {
 
 int pt_context_destroy(pt_context* ctx) {
     if (!ctx) return PT_ERR_INVALID_ARG;
+    pt_serve_stop(ctx);  // the server thread takes ctx->mu itself
     {
         std::lock_guard<std::mutex> g(ctx->mu);
         cudaSetDevice(ctx->device);
@@ -397,6 +392,10 @@ int pt_context_destroy(pt_context* ctx) {
         Free(ctx, ctx->film);
         Free(ctx, ctx->stack);
         Free(ctx, ctx->status);
+        Free(ctx, ctx->jobTable);
+        Free(ctx, ctx->unitTable);
+        Free(ctx, ctx->jobList);
+        Free(ctx, ctx->accum);
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
         if (ctx->ev1) cudaEventDestroy(ctx->ev1);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -576,6 +575,8 @@ int pt_scene_release(pt_context* ctx, pt_scene_id id) {
     std::lock_guard<std::mutex> g(ctx->mu);
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
+    if (it->second->refs > 0)
+        return Fail(ctx, PT_ERR_BUSY, "scene is used by queued or running served requests");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (auto& b : it->second->buffers) Free(ctx, b);
@@ -633,8 +634,9 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     if (st->mode != PT_MODE_WAVEFRONT)
         return Fail(ctx, PT_ERR_UNSUPPORTED, "profiling covers the wavefront mode");
     if ((rc = SetDevice(ctx)) != PT_OK) return rc;
-    rc = EnsureWaveBuffers(ctx, WaveCapacity(st), st->width * st->height);
-    if (rc != PT_OK) return rc;
+    const int cap = WaveCapacity(st);
+    if ((rc = EnsureWaveBuffers(ctx, cap)) != PT_OK) return rc;
+    if ((rc = EnsureTables(ctx, 1, (size_t)st->width * st->height)) != PT_OK) return rc;
     DeviceBuffer counters;
     if ((rc = Alloc(ctx, counters, 8 * sizeof(unsigned long long))) != PT_OK) return rc;
     cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), ctx->stream);
@@ -642,8 +644,14 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     prof.countReference = countReference != 0;
     prof.devCounters = (unsigned long long*)counters.ptr;
     int launches = 0;
-    const cudaError_t e = RenderWavefront(sg->dev, ToDev(cam), ToDev(st), ctx->wb, dFilm, ctx->stream,
-                                          &launches, 0, &prof, st->wave_paths);
+    DevJob job{};
+    job.S = sg->dev;
+    job.C = ToDev(cam);
+    job.st = ToDev(st);
+    job.accum = (float4*)ctx->accum.ptr;
+    job.film = dFilm;
+    cudaError_t e = RenderJobs({job}, Tables(ctx), ctx->wb, cap, ctx->stream, &launches, &prof);
+    if (e == cudaSuccess) e = CollectProfile(&prof, ctx->stream);
     Free(ctx, counters);
     if (e != cudaSuccess) return CudaFail(ctx, e, "profiled render");
     ctx->stats.kernel_launches += launches;
@@ -660,6 +668,52 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     out->ref_node_tests = prof.refNodeTests;
     out->ref_tri_tests = prof.refTriTests;
     out->ref_rays = prof.refRays;
+    return PT_OK;
+}
+
+int pt_batch_render(pt_context* ctx, int32_t n, const pt_job* jobs, void* stream) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (n <= 0 || n > kMaxJobsPerCall || !jobs)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "batch size must be 1.." + std::to_string(kMaxJobsPerCall));
+    std::vector<DevJob> dj(n);
+    size_t pixels = 0;
+    int64_t paths = 0;
+    int maxPx = 0;
+    for (int i = 0; i < n; i++) {
+        SceneGpu* sg = nullptr;
+        int rc = CheckArgs(ctx, jobs[i].scene, &jobs[i].camera, &jobs[i].settings, &sg);
+        if (rc != PT_OK) return rc;
+        if (jobs[i].settings.mode != PT_MODE_WAVEFRONT)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "batched renders use the wavefront mode");
+        if (!jobs[i].film_device) return Fail(ctx, PT_ERR_INVALID_ARG, "job film is NULL");
+        dj[i].S = sg->dev;
+        dj[i].C = ToDev(&jobs[i].camera);
+        dj[i].st = ToDev(&jobs[i].settings);
+        dj[i].film = jobs[i].film_device;
+        const int P = jobs[i].settings.width * jobs[i].settings.height;
+        pixels += P;
+        paths += (int64_t)P * jobs[i].settings.spp;
+        maxPx = std::max(maxPx, P);
+    }
+    int rc = SetDevice(ctx);
+    if (rc != PT_OK) return rc;
+    const int cap = (int)std::max<int64_t>(std::min<int64_t>(paths, kMaxWavePaths), maxPx);
+    if ((rc = EnsureWaveBuffers(ctx, cap)) != PT_OK) return rc;
+    if ((rc = EnsureTables(ctx, n, pixels)) != PT_OK) return rc;
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        dj[i].accum = (float4*)ctx->accum.ptr + off;
+        off += (size_t)dj[i].st.width * dj[i].st.height;
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    int launches = 0;
+    cudaError_t e = cudaEventRecord(ctx->ev0, s);
+    if (e == cudaSuccess) e = RenderJobs(dj, Tables(ctx), ctx->wb, cap, s, &launches, nullptr);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, s);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "batched render");
+    ctx->stats.kernel_launches += launches;
+    ctx->stats.renders += n;
     return PT_OK;
 }
 

@@ -25,6 +25,26 @@ cudaError_t LaunchReplay(const DevScene& S, const DevCamera& C, const DevSetting
                          cudaStream_t stream);
 
 // ---- wavefront (throughput) path
+// A job is one image: its resident scene, camera, settings, per-pixel running
+// sums and output film. Any number of jobs share a wave; every path carries its
+// job index, and each job's pixels are summed in sample order, so a job's film
+// does not depend on what else is in the wave.
+struct DevJob {
+    DevScene S;
+    DevCamera C;
+    DevSettings st;
+    float4* accum;  // width*height running sums {rgb, 0}; zeroed before the job's first wave
+    float* film;    // width*height*3 output, written by FinalizeJobs
+    int32_t pad[4];
+};
+
+// One job's samples [s0, s0 + sw) over all its pixels: paths
+// [pathBase, pathBase + W*H*sw) of the wave; pixelBase indexes the accumulate pass.
+struct WaveUnit {
+    int32_t job, s0, sw, pathBase;
+    int32_t pixelBase, pad[3];
+};
+
 struct WaveBuffers {
     int capacity;       // paths per wave
     float4* ray[2];     // 2 float4 per entry: {o.xyz, path}, {d.xyz, 0}
@@ -33,38 +53,41 @@ struct WaveBuffers {
     float4* st1;        // per path {L.xyz, ior}
     float4* st2;        // per path {lastPdf, lastSin, bounce, flags}
     unsigned long long* rng;  // per path
+    int* pathJob;       // per path: job index
     float4* shadow;     // 4 float4 per shadow entry
-    int* counts;        // [0],[1] ray queue sizes; [2] shadow queue size; [3] error bits
-    float4* accum;      // per pixel running sum {rgb, 0}
+    int* counts;        // [0],[1] ray queues; [2] shadow queue; [3] error bits; [4],[5] fetch
     int* hostCount;     // pinned host word for queue-size polls
 };
 size_t WaveBytesPerPath();
-size_t WaveBytesPerPixel();
 
-// Optional per-stage profile of one wavefront render (CUDA events around every
-// stage launch; ray tallies; reference-order traversal work over the extended rays).
+// Optional per-stage profile (CUDA events around every stage launch; ray tallies;
+// reference-order traversal work over the extended rays).
 struct WaveProfile {
     double ms[5] = {0, 0, 0, 0, 0};  // raygen, extend, shade, shadow, accumulate+finalize
     unsigned long long extendRays = 0, shadowRays = 0, extendLaunches = 0, shadowLaunches = 0;
     unsigned long long refNodeTests = 0, refTriTests = 0, refRays = 0;
     bool countReference = false;
     unsigned long long* devCounters = nullptr;  // 8 device words, zeroed by the caller
+    void* events = nullptr;                     // internal
 };
 
-// Renders one image through the wavefront stages into film (device, W*H*3).
-// grid: persistent grid size for the stage kernels (0 = auto). prof may be null;
-// with a profile the call synchronises the stream before returning.
-// wavePaths: paths per wave (<= wb.capacity; 0 = wb.capacity).
-cudaError_t RenderWavefront(const DevScene& S, const DevCamera& C, const DevSettings& st,
-                            const WaveBuffers& wb, float* film, cudaStream_t stream,
-                            int* launches, int gridOverride, WaveProfile* prof = nullptr,
-                            int wavePaths = 0);
+// One wave: raygen over `units` (device), the bounce loop, and accumulation into
+// each job's sums. iters >= 0 runs that many bounce iterations; iters < 0 runs
+// until the ray queue drains (polled every 4 iterations).
+cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
+                    int nPixelUnits, int iters, const WaveBuffers& wb, cudaStream_t stream,
+                    int* launches, WaveProfile* prof, int gridOverride = 0);
+// film = accum / spp for the listed jobs (device list of job indices).
+cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int maxPixels,
+                         cudaStream_t stream, int* launches, WaveProfile* prof);
+// Collects the profile's events and counters (synchronises the stream).
+cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream);
+
+int DefaultStageGrid();
 
 // Closest-hit traversal of the throughput path for caller rays (o.xyz, d.xyz per ray).
 cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,
                                float distMax, int* triOut, float* distOut, cudaStream_t stream);
-
-int DefaultStageGrid();
 
 // Fixed scratch of the no-allocation replay render (noalloc.cu): status word and
 // stack area addresses on the current device; capacity of the stack area in ints.

@@ -1,0 +1,36 @@
+// Host-side wave scheduling for the wavefront kernels: splits each job into
+// sample blocks (work units over all of its pixels), packs units into waves of at
+// most `waveCapacity` paths, runs the waves in order and finalizes each job after
+// its last wave. A job's sample blocks are visited in increasing sample order, so
+// its per-pixel sums (and its film) are the same in any packing.
+#pragma once
+#include <vector>
+
+#include "pt_kernels.h"
+
+namespace ptg {
+
+struct WaveTables {      // device buffers owned by the caller
+    DevJob* jobs;        // >= number of jobs
+    WaveUnit* units;     // >= maxUnits
+    int* jobList;        // >= number of jobs
+    int maxUnits;
+};
+
+// Plans the waves for `jobs` (spp, width, height taken from each job's settings).
+// Returns false when one sample of some job does not fit in a wave.
+bool PlanWaves(const std::vector<DevJob>& jobs, int waveCapacity, int maxUnits,
+               std::vector<std::vector<WaveUnit>>* waves);
+
+// Renders the jobs: uploads the job table, zeroes each job's sums, runs every
+// wave and finalizes jobs as they complete. Enqueued on `stream` (synchronises
+// only for SimplePathTracing queue polls).
+cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& tables,
+                       const WaveBuffers& wb, int waveCapacity, cudaStream_t stream, int* launches,
+                       WaveProfile* prof);
+
+// Bounce iterations a wave needs: maxBounces + 1 for PathTracing jobs; -1 (run
+// until the queue drains) when a SimplePathTracing job is present.
+int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
+
+}  // namespace ptg

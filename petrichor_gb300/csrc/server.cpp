@@ -1,0 +1,501 @@
+// Serving loop: continuous batching of render requests over resident scenes.
+//
+// A server thread owns a stream, its own wave buffers, a device job table with
+// one slot per admitted request and an arena for per-request state (per-pixel
+// sums, and film staging for host films). Each iteration it
+//   1. admits queued requests while slots and arena space are free,
+//   2. packs the next sample blocks of every admitted request into one wave
+//      (at most its share of the wave per request, so small requests that
+//      arrive behind a large one still get samples in the next wave),
+//   3. runs the wave and finalizes the requests whose last samples it held.
+// Requests that arrive while a wave runs join the next one. A request's film
+// does not depend on the mix: paths draw from a stream keyed by (seed, pixel,
+// sample) and each pixel sums its samples in sample order.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <thread>
+
+#include "context.h"
+
+namespace ptg {
+
+namespace {
+using Clock = std::chrono::steady_clock;
+
+// First-fit allocator over offsets of one device buffer (256-byte granules).
+class ArenaAllocator {
+public:
+    void Reset(size_t bytes) {
+        free_.clear();
+        if (bytes) free_[0] = bytes;
+    }
+    bool Alloc(size_t bytes, size_t* off) {
+        bytes = (bytes + 255) & ~size_t(255);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                *off = it->first;
+                const size_t rest = it->second - bytes, start = it->first + bytes;
+                free_.erase(it);
+                if (rest) free_[start] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void Release(size_t off, size_t bytes) {
+        bytes = (bytes + 255) & ~size_t(255);
+        auto it = free_.emplace(off, bytes).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+
+private:
+    std::map<size_t, size_t> free_;
+};
+
+struct Request {
+    uint64_t id = 0;
+    pt_job job{};
+    float* filmHost = nullptr;
+    SceneGpu* scene = nullptr;
+    int state = PT_REQ_QUEUED;
+    int status = PT_OK;
+    double submit = 0, admit = -1, done = -1;
+    int pixels = 0, spp = 0;
+    int scheduled = 0, finished = 0;  // samples put in waves / completed
+    int slot = -1;
+    size_t accumOff = 0, accumBytes = 0, filmOff = 0, filmBytes = 0;
+    bool cancel = false;
+};
+}  // namespace
+
+class Server {
+public:
+    Server(pt_context* ctx, const pt_serve_config& cfg) : ctx_(ctx), cfg_(cfg) {
+        if (cfg_.wave_paths <= 0) cfg_.wave_paths = 1 << 23;
+        if (cfg_.max_active <= 0) cfg_.max_active = 256;
+        cfg_.max_active = std::min(cfg_.max_active, kMaxJobsPerCall);
+        if (cfg_.state_budget == 0) cfg_.state_budget = uint64_t(4) << 30;
+    }
+    ~Server() { Stop(); }
+
+    int Start() {  // ctx->mu held by the caller
+        cudaError_t e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return CudaFail(ctx_, e, "server stream");
+        int rc;
+        if ((rc = Alloc(ctx_, arena_, cfg_.state_budget)) != PT_OK ||
+            (rc = Alloc(ctx_, jobTable_, sizeof(DevJob) * cfg_.max_active)) != PT_OK ||
+            (rc = Alloc(ctx_, units_, sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK ||
+            (rc = Alloc(ctx_, jobList_, sizeof(int) * cfg_.max_active)) != PT_OK ||
+            (rc = AllocWave()) != PT_OK) {
+            FreeAll();
+            return rc;
+        }
+        alloc_.Reset(cfg_.state_budget);
+        slotJobs_.assign(cfg_.max_active, DevJob{});
+        for (int s = cfg_.max_active - 1; s >= 0; s--) freeSlots_.push_back(s);
+        t0_ = Clock::now();
+        thread_ = std::thread([this] { Loop(); });
+        return PT_OK;
+    }
+
+    int Submit(const pt_job* job, float* filmHost, uint64_t* id) {
+        const double submitted = Now();
+        SceneGpu* sg = nullptr;
+        {
+            std::lock_guard<std::mutex> g(ctx_->mu);
+            const int rc = CheckArgs(ctx_, job->scene, &job->camera, &job->settings, &sg);
+            if (rc != PT_OK) return rc;
+            if (job->settings.mode != PT_MODE_WAVEFRONT)
+                return Fail(ctx_, PT_ERR_INVALID_ARG, "served renders use the wavefront mode");
+            if (!filmHost && !job->film_device)
+                return Fail(ctx_, PT_ERR_INVALID_ARG, "a device or host film is required");
+            sg->refs++;
+        }
+        auto r = std::make_unique<Request>();
+        r->job = *job;
+        r->filmHost = filmHost;
+        r->scene = sg;
+        r->pixels = job->settings.width * job->settings.height;
+        r->spp = job->settings.spp;
+        r->accumBytes = sizeof(float4) * (size_t)r->pixels;
+        r->filmBytes = filmHost ? sizeof(float) * 3 * (size_t)r->pixels : 0;
+        if (r->pixels > cfg_.wave_paths ||
+            ((r->accumBytes + 255) & ~size_t(255)) + ((r->filmBytes + 255) & ~size_t(255)) >
+              cfg_.state_budget) {
+            sg->refs--;
+            return Fail(ctx_, PT_ERR_OVER_BUDGET, "request exceeds the wave or the state budget");
+        }
+        std::lock_guard<std::mutex> g(mu_);
+        if (stopping_) {
+            sg->refs--;
+            return Fail(ctx_, PT_ERR_BUSY, "server is stopping");
+        }
+        r->id = nextId_++;
+        r->submit = submitted;
+        *id = r->id;
+        queue_.push_back(r->id);
+        reqs_[r->id] = std::move(r);
+        cv_.notify_all();
+        return PT_OK;
+    }
+
+    int Poll(uint64_t id, pt_request_status* out) {
+        std::lock_guard<std::mutex> g(mu_);
+        return Fill(id, out);
+    }
+
+    int Wait(uint64_t id, double timeout, pt_request_status* out) {
+        std::unique_lock<std::mutex> lk(mu_);
+        auto it = reqs_.find(id);
+        if (it == reqs_.end()) return PT_ERR_NOT_FOUND;
+        const bool ok = doneCv_.wait_for(lk, std::chrono::duration<double>(timeout), [&] {
+            const int s = it->second->state;
+            return s == PT_REQ_DONE || s == PT_REQ_CANCELLED || s == PT_REQ_FAILED;
+        });
+        Fill(id, out);
+        return ok ? PT_OK : PT_ERR_TIMEOUT;
+    }
+
+    int Cancel(uint64_t id) {
+        std::lock_guard<std::mutex> g(mu_);
+        auto it = reqs_.find(id);
+        if (it == reqs_.end()) return PT_ERR_NOT_FOUND;
+        it->second->cancel = true;
+        cv_.notify_all();
+        return PT_OK;
+    }
+
+    int Release(uint64_t id) {
+        std::lock_guard<std::mutex> g(mu_);
+        auto it = reqs_.find(id);
+        if (it == reqs_.end()) return PT_ERR_NOT_FOUND;
+        const int s = it->second->state;
+        if (s == PT_REQ_QUEUED || s == PT_REQ_RUNNING) return PT_ERR_BUSY;
+        reqs_.erase(it);
+        return PT_OK;
+    }
+
+    void Stop() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stopping_ = true;
+            cv_.notify_all();
+        }
+        if (thread_.joinable()) thread_.join();
+        std::lock_guard<std::mutex> g(mu_);
+        for (auto& kv : reqs_) {
+            Request& r = *kv.second;
+            if (r.state == PT_REQ_QUEUED || r.state == PT_REQ_RUNNING) Finish(r, PT_REQ_CANCELLED, PT_OK);
+        }
+        doneCv_.notify_all();
+        if (stream_) {
+            std::lock_guard<std::mutex> cg(ctx_->mu);
+            cudaStreamSynchronize(stream_);
+            cudaStreamDestroy(stream_);
+            stream_ = nullptr;
+            FreeAll();
+        }
+    }
+
+private:
+    double Now() const { return std::chrono::duration<double>(Clock::now() - t0_).count(); }
+
+    int Fill(uint64_t id, pt_request_status* out) {
+        auto it = reqs_.find(id);
+        if (it == reqs_.end()) return PT_ERR_NOT_FOUND;
+        const Request& r = *it->second;
+        out->state = r.state;
+        out->status = r.status;
+        out->submit_s = r.submit;
+        out->admit_s = r.admit;
+        out->done_s = r.done;
+        out->samples_done = (uint32_t)r.finished;
+        out->samples_total = (uint32_t)r.spp;
+        return PT_OK;
+    }
+
+    // mu_ held. Releases the request's slot and arena space.
+    void Finish(Request& r, int state, int status) {
+        r.state = state;
+        r.status = status;
+        r.done = Now();
+        if (r.slot >= 0) {
+            alloc_.Release(r.accumOff, r.accumBytes);
+            if (r.filmBytes) alloc_.Release(r.filmOff, r.filmBytes);
+            freeSlots_.push_back(r.slot);
+            r.slot = -1;
+        }
+        active_.erase(std::remove(active_.begin(), active_.end(), r.id), active_.end());
+        if (r.scene) {
+            r.scene->refs--;
+            r.scene = nullptr;
+        }
+    }
+
+    int AllocWave() {
+        wbBufs_.assign(10, DeviceBuffer{});
+        const size_t C = (size_t)cfg_.wave_paths;
+        const size_t sizes[10] = {C * 2 * sizeof(float4), C * 2 * sizeof(float4), C * sizeof(float2),
+                                  C * sizeof(float4), C * sizeof(float4), C * sizeof(float4),
+                                  C * sizeof(unsigned long long), C * sizeof(int),
+                                  C * 4 * sizeof(float4), 16 * sizeof(int)};
+        for (int i = 0; i < 10; i++) {
+            const int rc = Alloc(ctx_, wbBufs_[i], sizes[i]);
+            if (rc != PT_OK) return rc;
+        }
+        wb_.capacity = cfg_.wave_paths;
+        wb_.ray[0] = (float4*)wbBufs_[0].ptr;
+        wb_.ray[1] = (float4*)wbBufs_[1].ptr;
+        wb_.hit = (float2*)wbBufs_[2].ptr;
+        wb_.st0 = (float4*)wbBufs_[3].ptr;
+        wb_.st1 = (float4*)wbBufs_[4].ptr;
+        wb_.st2 = (float4*)wbBufs_[5].ptr;
+        wb_.rng = (unsigned long long*)wbBufs_[6].ptr;
+        wb_.pathJob = (int*)wbBufs_[7].ptr;
+        wb_.shadow = (float4*)wbBufs_[8].ptr;
+        wb_.counts = (int*)wbBufs_[9].ptr;
+        cudaMemset(wb_.counts, 0, 16 * sizeof(int));
+        const cudaError_t e = cudaMallocHost(&wb_.hostCount, sizeof(int) * 4);
+        return e == cudaSuccess ? PT_OK : CudaFail(ctx_, e, "cudaMallocHost");
+    }
+
+    void FreeAll() {  // ctx->mu held
+        for (auto& b : wbBufs_) Free(ctx_, b);
+        wbBufs_.clear();
+        if (wb_.hostCount) cudaFreeHost(wb_.hostCount);
+        wb_.hostCount = nullptr;
+        Free(ctx_, arena_);
+        Free(ctx_, jobTable_);
+        Free(ctx_, units_);
+        Free(ctx_, jobList_);
+    }
+
+    void Loop() {
+        cudaSetDevice(ctx_->device);
+        for (;;) {
+            std::vector<Request*> admitted, finishing;
+            std::vector<WaveUnit> units;
+            std::vector<std::pair<Request*, int>> scheduled;
+            int paths = 0, pixels = 0;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait_for(lk, std::chrono::milliseconds(20),
+                             [&] { return stopping_ || !queue_.empty() || !active_.empty(); });
+                if (stopping_) return;
+                // cancelled requests leave between waves
+                for (uint64_t id : std::vector<uint64_t>(active_)) {
+                    Request& r = *reqs_[id];
+                    if (r.cancel) Finish(r, PT_REQ_CANCELLED, PT_OK);
+                }
+                for (auto it = queue_.begin(); it != queue_.end();) {
+                    Request& r = *reqs_[*it];
+                    if (r.cancel) {
+                        Finish(r, PT_REQ_CANCELLED, PT_OK);
+                        it = queue_.erase(it);
+                    } else {
+                        ++it;
+                    }
+                }
+                doneCv_.notify_all();
+                // admission: in arrival order while a slot and arena space are free
+                while (!queue_.empty() && !freeSlots_.empty()) {
+                    Request& r = *reqs_[queue_.front()];
+                    size_t off = 0, foff = 0;
+                    if (!alloc_.Alloc(r.accumBytes, &off)) break;
+                    if (r.filmBytes && !alloc_.Alloc(r.filmBytes, &foff)) {
+                        alloc_.Release(off, r.accumBytes);
+                        break;
+                    }
+                    r.accumOff = off;
+                    r.filmOff = foff;
+                    r.slot = freeSlots_.back();
+                    freeSlots_.pop_back();
+                    r.state = PT_REQ_RUNNING;
+                    r.admit = Now();
+                    active_.push_back(r.id);
+                    queue_.pop_front();
+                    admitted.push_back(&r);
+                }
+                // wave: each active request's next sample blocks, up to its share
+                const int cap = cfg_.wave_paths;
+                const int share = std::max(1, cap / std::max<int>(1, (int)active_.size()));
+                for (uint64_t id : active_) {
+                    Request& r = *reqs_[id];
+                    const int remaining = r.spp - r.scheduled;
+                    if (remaining <= 0) continue;
+                    const int room = (cap - paths) / r.pixels;
+                    if (room < 1 || (int)units.size() >= kMaxUnitsPerWave) continue;
+                    const int sw = std::min({remaining, room, std::max(1, share / r.pixels)});
+                    WaveUnit u{};
+                    u.job = r.slot;
+                    u.s0 = r.scheduled;
+                    u.sw = sw;
+                    u.pathBase = paths;
+                    u.pixelBase = pixels;
+                    units.push_back(u);
+                    paths += r.pixels * sw;
+                    pixels += r.pixels;
+                    r.scheduled += sw;
+                    scheduled.push_back({&r, sw});
+                    if (r.scheduled == r.spp) finishing.push_back(&r);
+                }
+            }
+            if (units.empty()) continue;
+            cudaError_t e = cudaSuccess;
+            {
+                std::lock_guard<std::mutex> cg(ctx_->mu);
+                for (Request* r : admitted) {
+                    DevJob& J = slotJobs_[r->slot];
+                    J = DevJob{};
+                    J.S = r->scene->dev;
+                    J.C = ToDev(&r->job.camera);
+                    J.st = ToDev(&r->job.settings);
+                    J.accum = (float4*)((char*)arena_.ptr + r->accumOff);
+                    J.film = r->filmHost ? (float*)((char*)arena_.ptr + r->filmOff) : r->job.film_device;
+                    if (e == cudaSuccess)
+                        e = cudaMemcpyAsync((DevJob*)jobTable_.ptr + r->slot, &J, sizeof(DevJob),
+                                            cudaMemcpyHostToDevice, stream_);
+                    if (e == cudaSuccess) e = cudaMemsetAsync(J.accum, 0, r->accumBytes, stream_);
+                }
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(units_.ptr, units.data(), units.size() * sizeof(WaveUnit),
+                                        cudaMemcpyHostToDevice, stream_);
+                int launches = 0;
+                if (e == cudaSuccess)
+                    e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, (int)units.size(), paths,
+                                pixels, WaveIterations(slotJobs_, units), wb_, stream_, &launches,
+                                nullptr);
+                if (e == cudaSuccess && !finishing.empty()) {
+                    std::vector<int> slots;
+                    int maxPx = 0;
+                    for (Request* r : finishing) {
+                        slots.push_back(r->slot);
+                        maxPx = std::max(maxPx, r->pixels);
+                    }
+                    e = cudaMemcpyAsync(jobList_.ptr, slots.data(), slots.size() * sizeof(int),
+                                        cudaMemcpyHostToDevice, stream_);
+                    if (e == cudaSuccess)
+                        e = FinalizeJobs((DevJob*)jobTable_.ptr, (int*)jobList_.ptr, (int)slots.size(),
+                                         maxPx, stream_, &launches, nullptr);
+                    for (Request* r : finishing)
+                        if (e == cudaSuccess && r->filmHost)
+                            e = cudaMemcpyAsync(r->filmHost, (char*)arena_.ptr + r->filmOff, r->filmBytes,
+                                                cudaMemcpyDeviceToHost, stream_);
+                }
+                ctx_->stats.kernel_launches += launches;
+            }
+            // the wave runs on the server's own stream and buffers: other calls on
+            // the context proceed while it executes
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+            std::lock_guard<std::mutex> g(mu_);
+            for (auto& [r, sw] : scheduled) r->finished += sw;
+            if (e != cudaSuccess) {
+                const int code = CudaFail(ctx_, e, "served wave");
+                for (uint64_t id : std::vector<uint64_t>(active_)) Finish(*reqs_[id], PT_REQ_FAILED, code);
+            } else {
+                for (Request* r : finishing) {
+                    Finish(*r, PT_REQ_DONE, PT_OK);
+                    ctx_->stats.renders++;
+                }
+            }
+            doneCv_.notify_all();
+        }
+    }
+
+    pt_context* ctx_;
+    pt_serve_config cfg_;
+    std::thread thread_;
+    std::mutex mu_;
+    std::condition_variable cv_, doneCv_;
+    bool stopping_ = false;
+    std::map<uint64_t, std::unique_ptr<Request>> reqs_;
+    std::deque<uint64_t> queue_;
+    std::vector<uint64_t> active_;
+    std::vector<int> freeSlots_;
+    uint64_t nextId_ = 1;
+    ArenaAllocator alloc_;
+    DeviceBuffer arena_, jobTable_, units_, jobList_;
+    std::vector<DeviceBuffer> wbBufs_;
+    WaveBuffers wb_{};
+    std::vector<DevJob> slotJobs_;
+    cudaStream_t stream_ = nullptr;
+    Clock::time_point t0_;
+};
+
+}  // namespace ptg
+
+using namespace ptg;
+
+pt_context::pt_context() = default;
+pt_context::~pt_context() = default;
+
+extern "C" {
+
+int pt_serve_start(pt_context* ctx, const pt_serve_config* config) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    pt_serve_config cfg{};
+    if (config) cfg = *config;
+    if (cfg.wave_paths < 0 || cfg.max_active < 0) return Fail(ctx, PT_ERR_INVALID_ARG, "bad serve config");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (ctx->server) return Fail(ctx, PT_ERR_BUSY, "server already running");
+    int rc = SetDevice(ctx);
+    if (rc != PT_OK) return rc;
+    auto s = std::make_unique<Server>(ctx, cfg);
+    if ((rc = s->Start()) != PT_OK) return rc;
+    ctx->server = std::move(s);
+    return PT_OK;
+}
+
+int pt_serve_submit(pt_context* ctx, const pt_job* job, float* filmHost, uint64_t* id) {
+    if (!ctx || !job || !id) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return Fail(ctx, PT_ERR_NOT_FOUND, "server not running");
+    return ctx->server->Submit(job, filmHost, id);
+}
+
+int pt_serve_poll(pt_context* ctx, uint64_t id, pt_request_status* out) {
+    if (!ctx || !out) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return PT_ERR_NOT_FOUND;
+    return ctx->server->Poll(id, out);
+}
+
+int pt_serve_wait(pt_context* ctx, uint64_t id, double timeout, pt_request_status* out) {
+    if (!ctx || !out) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return PT_ERR_NOT_FOUND;
+    return ctx->server->Wait(id, timeout, out);
+}
+
+int pt_serve_cancel(pt_context* ctx, uint64_t id) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return PT_ERR_NOT_FOUND;
+    return ctx->server->Cancel(id);
+}
+
+int pt_serve_release(pt_context* ctx, uint64_t id) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return PT_ERR_NOT_FOUND;
+    return ctx->server->Release(id);
+}
+
+int pt_serve_stop(pt_context* ctx) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return PT_ERR_NOT_FOUND;
+    ctx->server->Stop();
+    ctx->server.reset();
+    return PT_OK;
+}
+
+}  // extern "C"

@@ -1,7 +1,9 @@
 // Wavefront throughput path: raygen -> extend -> shade -> shadow -> accumulate.
 //
-// One wave is a block of paths (pixel range x sample range). Each bounce runs
-// three persistent-grid kernels over compacted queues:
+// One wave is a set of work units (a job's sample block over all its pixels),
+// from one image or many (batched renders and the serving loop share the same
+// kernels: every path carries its job index). Each bounce runs three
+// persistent-grid kernels over compacted queues:
 //   extend : closest hit of every queued ray (binary BVH, 32 B nodes, both
 //            children's boxes fetched as one 64 B pair, ordered short stack)
 //   shade  : miss / emission / surface handling of PathTracing or
@@ -146,16 +148,18 @@ struct LaneRay {
     float tmin, tmax, tBest;
     int best;
     bool anyHit;
+    const float4* nodes;  // the lane's scene (rays of different jobs share a warp)
+    const float4* tris;
 };
 
 // Visits the node in `meta`; returns true when the ray is finished.
-__device__ __forceinline__ bool TraverseStep(const DevScene& S, LaneRay& r, int2* stack, int& sp,
-                                             float4& meta, int& err) {
+__device__ __forceinline__ bool TraverseStep(LaneRay& r, int2* stack, int& sp, float4& meta,
+                                             int& err) {
     const int a = __float_as_int(meta.z), cnt = __float_as_int(meta.w);
     if (cnt >= 0) {
         for (int k = a; k < a + cnt; k++) {
             V3 v0, e1, e2;
-            LoadTri(S.tris, k, v0, e1, e2);
+            LoadTri(r.tris, k, v0, e1, e2);
             float t;
             if (TriIntersect(v0, e1, e2, r.o, r.d, t) && t >= r.tmin && t <= r.tmax && t < r.tBest) {
                 r.tBest = t;
@@ -164,8 +168,8 @@ __device__ __forceinline__ bool TraverseStep(const DevScene& S, LaneRay& r, int2
             }
         }
     } else {
-        const float4 la = __ldg(S.nodes + 2 * a), lb = __ldg(S.nodes + 2 * a + 1);
-        const float4 ra = __ldg(S.nodes + 2 * a + 2), rb = __ldg(S.nodes + 2 * a + 3);
+        const float4 la = __ldg(r.nodes + 2 * a), lb = __ldg(r.nodes + 2 * a + 1);
+        const float4 ra = __ldg(r.nodes + 2 * a + 2), rb = __ldg(r.nodes + 2 * a + 3);
         float tl, tr;
         const bool hl = SlabFast(la, lb, r.o, r.inv, 0.0f, r.tBest, tl);
         const bool hr = SlabFast(ra, rb, r.o, r.inv, 0.0f, r.tBest, tr);
@@ -195,17 +199,18 @@ __device__ __forceinline__ bool TraverseStep(const DevScene& S, LaneRay& r, int2
     while (sp > 0) {
         const int2 e = stack[--sp];
         if (__int_as_float(e.y) <= r.tBest) {
-            meta = __ldg(S.nodes + 2 * e.x + 1);
+            meta = __ldg(r.nodes + 2 * e.x + 1);
             return false;
         }
     }
     return true;
 }
 
-// Q provides: void Load(int i, LaneRay&) and void Finish(int i, const LaneRay&).
+// Q provides: void Load(int i, LaneRay&) (ray, range, and the scene: nodes = nullptr
+// for an empty scene) and void Finish(int i, const LaneRay&).
 // Must be called by every lane of the warp (blockDim a multiple of 32).
 template <class Q>
-__device__ void TraceQueue(const DevScene& S, Q& q, int n, int* fetch, int& err) {
+__device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
     const int lane = threadIdx.x & 31;
     const unsigned lowerLanes = (1u << lane) - 1u;
     LaneRay r;
@@ -233,9 +238,9 @@ __device__ void TraceQueue(const DevScene& S, Q& q, int n, int* fetch, int& err)
                     r.best = -1;
                     sp = 0;
                     float tE;
-                    if (S.numNodes > 0 &&
-                        SlabFast(__ldg(S.nodes), __ldg(S.nodes + 1), r.o, r.inv, 0.0f, r.tBest, tE)) {
-                        meta = __ldg(S.nodes + 1);
+                    if (r.nodes &&
+                        SlabFast(__ldg(r.nodes), __ldg(r.nodes + 1), r.o, r.inv, 0.0f, r.tBest, tE)) {
+                        meta = __ldg(r.nodes + 1);
                         active = true;
                     } else {
                         q.Finish(i, r);
@@ -247,31 +252,46 @@ __device__ void TraceQueue(const DevScene& S, Q& q, int n, int* fetch, int& err)
             if (exhausted) break;
             continue;
         }
-        if (active && TraverseStep(S, r, stack, sp, meta, err)) {
+        if (active && TraverseStep(r, stack, sp, meta, err)) {
             q.Finish(idx, r);
             active = false;
         }
     }
 }
 
-__global__ void RaygenKernel(DevCamera C, DevSettings st, WaveBuffers wb, int q0, int P, int s0,
-                             int Sw, int cur) {
-    const int n = P * Sw;
+__device__ __forceinline__ int FindUnit(const WaveUnit* __restrict__ units, int n, int key, bool byPixel) {
+    int lo = 0, hi = n - 1;  // last unit whose base <= key
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int base = byPixel ? units[mid].pixelBase : units[mid].pathBase;
+        if (base <= key) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
+                             int nUnits, int n, WaveBuffers wb, int cur) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int q = q0 + i % P, s = s0 + i / P;
+        const WaveUnit u = units[FindUnit(units, nUnits, i, false)];
+        const DevJob& J = jobs[u.job];
+        const int W = J.st.width, H = J.st.height, P = W * H;
+        const int local = i - u.pathBase;
+        const int q = local % P, s = u.s0 + local / P;
         int x, y;
-        PixelOfIndex(q, st.width, st.height, x, y);
-        PathRng rng(PathKey(st.seed, (uint32_t)(y * st.width + x), (uint32_t)s));
+        PixelOfIndex(q, W, H, x, y);
+        PathRng rng(PathKey(J.st.seed, (uint32_t)(y * W + x), (uint32_t)s));
         float r0, r1, r2, r3;
         rng.Next(r0, r1);
         rng.Next(r2, r3);
-        const Ray ray = GenerateRay<FastMath>(C, x, y, st.width, st.height, r0, r1, r2, r3);
+        const Ray ray = GenerateRay<FastMath>(J.C, x, y, W, H, r0, r1, r2, r3);
         wb.ray[cur][2 * i] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float(i));
         wb.ray[cur][2 * i + 1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
         wb.st0[i] = make_float4(ray.T.x, ray.T.y, ray.T.z, 1.0f);
         wb.st1[i] = make_float4(0.f, 0.f, 0.f, 1.0f);
         wb.st2[i] = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
         wb.rng[i] = rng.s;
+        wb.pathJob[i] = u.job;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wb.counts[cur] = n;
@@ -280,16 +300,22 @@ __global__ void RaygenKernel(DevCamera C, DevSettings st, WaveBuffers wb, int q0
 }
 
 struct ExtendQueue {
+    const DevJob* jobs;
+    const int* pathJob;
     const float4* rays;
     float2* hit;
-    float tmin;
     __device__ void Load(int i, LaneRay& r) const {
         const float4 a = rays[2 * i], b = rays[2 * i + 1];
+        const DevJob& J = jobs[pathJob[__float_as_int(a.w)]];
         r.o = V3(a.x, a.y, a.z);
         r.d = V3(b.x, b.y, b.z);
-        r.tmin = tmin;
+        // SimplePathTracing intersects with distMin = kEps, PathTracing with 0
+        // (SimplePathTracing.cpp:81, PathTracing.cpp:50, AccelBase.h:44-55)
+        r.tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
         r.tmax = kFltMax;
         r.anyHit = false;
+        r.nodes = J.S.numNodes > 0 ? J.S.nodes : nullptr;
+        r.tris = J.S.tris;
     }
     __device__ void Finish(int i, const LaneRay& r) const {
         hit[i] = make_float2(r.tBest, __int_as_float(r.best));
@@ -298,7 +324,8 @@ struct ExtendQueue {
 
 // counts: [0],[1] ray queues, [2] shadow queue, [3] error bits,
 //         [4] extend fetch counter, [5] shadow fetch counter
-__global__ void __launch_bounds__(128) ExtendKernel(DevScene S, WaveBuffers wb, int cur, float tmin) {
+__global__ void __launch_bounds__(128) ExtendKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+                                                    int cur) {
     const int n = wb.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wb.counts[cur ^ 1] = 0;
@@ -306,18 +333,22 @@ __global__ void __launch_bounds__(128) ExtendKernel(DevScene S, WaveBuffers wb, 
         wb.counts[5] = 0;  // the shadow kernel that follows fetches from zero
     }
     int err = 0;
-    ExtendQueue q{wb.ray[cur], wb.hit, tmin};
-    TraceQueue(S, q, n, wb.counts + 4, err);
+    ExtendQueue q{jobs, wb.pathJob, wb.ray[cur], wb.hit};
+    TraceQueue(q, n, wb.counts + 4, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
 
-__global__ void __launch_bounds__(128) ShadeKernel(DevScene S, DevSettings st, WaveBuffers wb, int cur) {
+__global__ void __launch_bounds__(128) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+                                                   int cur) {
     const int n = wb.counts[cur];
     const int nxt = cur ^ 1;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
         const float2 h = wb.hit[i];
         const int path = __float_as_int(ra.w);
+        const DevJob& J = jobs[wb.pathJob[path]];
+        const DevScene& S = J.S;
+        const DevSettings& st = J.st;
         const V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
         float4 s0 = wb.st0[path], s1 = wb.st1[path], s2 = wb.st2[path];
         PathRng rng(wb.rng[path]);
@@ -477,12 +508,16 @@ __global__ void __launch_bounds__(128) ShadeKernel(DevScene S, DevSettings st, W
 }
 
 struct ShadowQueue {
-    DevScene S;
+    const DevJob* jobs;
+    const int* pathJob;
     const float4* entries;
     float4* st1;
     const unsigned long long* rng;
     __device__ void Load(int j, LaneRay& r) const {
         const float4 e0 = entries[4 * j], e1 = entries[4 * j + 1];
+        const DevScene& S = jobs[pathJob[__float_as_int(e1.w) & 0x7FFFFFFF]].S;
+        r.nodes = S.numNodes > 0 ? S.nodes : nullptr;
+        r.tris = S.tris;
         r.o = V3(e0.x, e0.y, e0.z);
         r.d = V3(e1.x, e1.y, e1.z);
         r.tmin = 0.0f;
@@ -506,6 +541,7 @@ struct ShadowQueue {
         }
         // area light: the closest hit must be an emitter at the sampled point
         if (r.best < 0) return;
+        const DevScene& S = jobs[pathJob[path]].S;
         const float4 e0 = entries[4 * j];
         const int tri = TriId(S.tris, r.best);
         const float u = (float)(uint32_t)(Mix64(rng[path] ^ 0xA5A5A5A5DEADBEEFull) >> 40) *
@@ -535,23 +571,28 @@ struct ShadowQueue {
     }
 };
 
-__global__ void __launch_bounds__(128) ShadowKernel(DevScene S, WaveBuffers wb) {
+__global__ void __launch_bounds__(128) ShadowKernel(const DevJob* __restrict__ jobs, WaveBuffers wb) {
     const int n = wb.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // next extend fetches from zero
     int err = 0;
-    ShadowQueue q{S, wb.shadow, wb.st1, wb.rng};
-    TraceQueue(S, q, n, wb.counts + 5, err);
+    ShadowQueue q{jobs, wb.pathJob, wb.shadow, wb.st1, wb.rng};
+    TraceQueue(q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
 
-__global__ void AccumulateKernel(DevSettings st, WaveBuffers wb, int q0, int P, int Sw) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+__global__ void AccumulateKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
+                                 int nUnits, int n, WaveBuffers wb) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const WaveUnit u = units[FindUnit(units, nUnits, i, true)];
+        const DevJob& J = jobs[u.job];
+        const int W = J.st.width, H = J.st.height, P = W * H;
+        const int q = i - u.pixelBase;
         int x, y;
-        PixelOfIndex(q0 + i, st.width, st.height, x, y);
-        const size_t pixel = (size_t)y * st.width + x;
-        float4 acc = wb.accum[pixel];
-        for (int s = 0; s < Sw; s++) {
-            const int p = s * P + i;
+        PixelOfIndex(q, W, H, x, y);
+        const size_t pixel = (size_t)y * W + x;
+        float4 acc = J.accum[pixel];
+        for (int s = 0; s < u.sw; s++) {
+            const int p = u.pathBase + s * P + q;
             const float4 l = wb.st1[p];
             const int flags = __float_as_int(wb.st2[p].w);
             // PathTracing.cpp:191-195 drops a sample whose smallest channel is
@@ -562,18 +603,21 @@ __global__ void AccumulateKernel(DevSettings st, WaveBuffers wb, int q0, int P, 
                 acc.z += l.z;
             }
         }
-        wb.accum[pixel] = acc;
+        J.accum[pixel] = acc;
     }
 }
 
-__global__ void FinalizeKernel(DevSettings st, const float4* __restrict__ accum, float* __restrict__ film) {
-    const int n = st.width * st.height;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 a = accum[i];
-        const float inv = (float)st.spp;
-        film[3 * i] = a.x / inv;
-        film[3 * i + 1] = a.y / inv;
-        film[3 * i + 2] = a.z / inv;
+__global__ void FinalizeKernel(const DevJob* __restrict__ jobs, const int* __restrict__ jobList,
+                               int maxPixels) {
+    const DevJob& J = jobs[jobList[blockIdx.y]];
+    const int n = J.st.width * J.st.height;
+    const float inv = (float)J.st.spp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n && i < maxPixels;
+         i += gridDim.x * blockDim.x) {
+        const float4 a = J.accum[i];
+        J.film[3 * i] = a.x / inv;
+        J.film[3 * i + 1] = a.y / inv;
+        J.film[3 * i + 2] = a.z / inv;
     }
 }
 
@@ -596,17 +640,19 @@ __global__ void TallyKernel(const int* counts, int cur, unsigned long long* c) {
     c[4] += (unsigned long long)counts[2];
 }
 
-__global__ void __launch_bounds__(128) RefCountKernel(DevScene S, WaveBuffers wb, int cur, float tmin,
-                                                      unsigned long long* c) {
+__global__ void __launch_bounds__(128) RefCountKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+                                                      int cur, unsigned long long* c) {
     const int n = wb.counts[cur];
     unsigned long long nodes = 0, tris = 0;
     int stack[kWaveStackDepth];
     int status = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = wb.ray[cur][2 * i], b = wb.ray[cur][2 * i + 1];
+        const DevJob& J = jobs[wb.pathJob[__float_as_int(a.w)]];
+        const float tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
         unsigned nn = 0, nt = 0;
         float d;
-        TraverseReference<true>(S, V3(a.x, a.y, a.z), V3(b.x, b.y, b.z), tmin, kFltMax, d, stack,
+        TraverseReference<true>(J.S, V3(a.x, a.y, a.z), V3(b.x, b.y, b.z), tmin, kFltMax, d, stack,
                                 &status, &nn, &nt);
         nodes += nn;
         tris += nt;
@@ -650,9 +696,8 @@ struct StageEvents {
 
 size_t WaveBytesPerPath() {
     return 2 * 2 * sizeof(float4) + sizeof(float2) + 3 * sizeof(float4) + sizeof(unsigned long long) +
-           4 * sizeof(float4);
+           sizeof(int) + 4 * sizeof(float4);
 }
-size_t WaveBytesPerPixel() { return sizeof(float4); }
 
 int DefaultStageGrid() {
     static int grid = 0;
@@ -668,94 +713,94 @@ int DefaultStageGrid() {
     return grid;
 }
 
-cudaError_t RenderWavefront(const DevScene& S, const DevCamera& C, const DevSettings& st,
-                            const WaveBuffers& wb, float* film, cudaStream_t stream, int* launches,
-                            int gridOverride, WaveProfile* prof, int wavePaths) {
-    const int P_total = st.width * st.height;
-    if (P_total <= 0 || st.spp <= 0) return cudaErrorInvalidValue;
+cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
+                    int nPixelUnits, int iters, const WaveBuffers& wb, cudaStream_t stream,
+                    int* launches, WaveProfile* prof, int gridOverride) {
+    if (nPaths <= 0) return cudaSuccess;
+    if (nPaths > wb.capacity) return cudaErrorInvalidValue;
     const int grid = gridOverride > 0 ? gridOverride : DefaultStageGrid();
     const int block = 128;
+    StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     int nl = 0;
-    cudaError_t e = cudaMemsetAsync(wb.accum, 0, sizeof(float4) * (size_t)P_total, stream);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(wb.counts, 0, 4 * sizeof(int), stream);
-    if (e != cudaSuccess) return e;
-    const int cap = wavePaths > 0 ? std::min(wavePaths, wb.capacity) : wb.capacity;
-    const int Pc = std::min(P_total, cap);
-    const int Sw = std::max(1, std::min(st.spp, cap / Pc));
-    const float tmin = st.integrator == kSimplePathTracing ? kEps : 0.0f;
-    int* hostCount = wb.hostCount;
-    StageEvents events;
-    for (int s0 = 0; s0 < st.spp; s0 += Sw) {
-        const int sw = std::min(Sw, st.spp - s0);
-        for (int q0 = 0; q0 < P_total; q0 += Pc) {
-            const int pc = std::min(Pc, P_total - q0);
-            StageEvents* sev = prof ? &events : nullptr;
-            if (sev) sev->Begin(0, stream);
-            RaygenKernel<<<grid, block, 0, stream>>>(C, st, wb, q0, pc, s0, sw, 0);
-            if (sev) sev->End(0, stream);
-            nl++;
-            int cur = 0;
-            // PathTracing traces rays 0..maxBounces; SimplePathTracing runs until
-            // every path has ended (polled every 4 bounces).
-            const int fixedIters = st.integrator == kSimplePathTracing ? -1 : st.maxBounces + 1;
-            for (int it = 0;; it++) {
-                if (fixedIters >= 0 && it >= fixedIters) break;
-                if (fixedIters < 0 && it > 0 && it % 4 == 0) {
-                    cudaMemcpyAsync(hostCount, wb.counts + cur, sizeof(int), cudaMemcpyDeviceToHost, stream);
-                    e = cudaStreamSynchronize(stream);
-                    if (e != cudaSuccess) break;
-                    if (*hostCount == 0) break;
-                    if (it >= kMaxReplayBounces) break;
-                }
-                if (sev) sev->Begin(1, stream);
-                ExtendKernel<<<grid, block, 0, stream>>>(S, wb, cur, tmin);
-                if (sev) {
-                    sev->End(1, stream);
-                    if (prof->countReference)
-                        RefCountKernel<<<grid, block, 0, stream>>>(S, wb, cur, tmin, prof->devCounters);
-                    sev->Begin(2, stream);
-                }
-                ShadeKernel<<<grid, block, 0, stream>>>(S, st, wb, cur);
-                if (sev) {
-                    sev->End(2, stream);
-                    TallyKernel<<<1, 1, 0, stream>>>(wb.counts, cur, prof->devCounters);
-                    sev->Begin(3, stream);
-                }
-                ShadowKernel<<<grid, block, 0, stream>>>(S, wb);
-                if (sev) sev->End(3, stream);
-                nl += 3;
-                if (prof) {
-                    prof->extendLaunches++;
-                    prof->shadowLaunches++;
-                }
-                cur ^= 1;
-            }
-            if (sev) sev->Begin(4, stream);
-            AccumulateKernel<<<grid, block, 0, stream>>>(st, wb, q0, pc, sw);
-            if (sev) sev->End(4, stream);
-            nl++;
+    cudaError_t e = cudaSuccess;
+    if (ev) ev->Begin(0, stream);
+    RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, nUnits, nPaths, wb, 0);
+    if (ev) ev->End(0, stream);
+    nl++;
+    int cur = 0;
+    for (int it = 0;; it++) {
+        if (iters >= 0 && it >= iters) break;
+        if (iters < 0 && it > 0 && it % 4 == 0) {
+            cudaMemcpyAsync(wb.hostCount, wb.counts + cur, sizeof(int), cudaMemcpyDeviceToHost, stream);
+            e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) break;
+            if (*wb.hostCount == 0 || it >= kMaxReplayBounces) break;
         }
+        if (ev) ev->Begin(1, stream);
+        ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+        if (ev) {
+            ev->End(1, stream);
+            if (prof->countReference)
+                RefCountKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, prof->devCounters);
+            ev->Begin(2, stream);
+        }
+        ShadeKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+        if (ev) {
+            ev->End(2, stream);
+            TallyKernel<<<1, 1, 0, stream>>>(wb.counts, cur, prof->devCounters);
+            ev->Begin(3, stream);
+        }
+        ShadowKernel<<<grid, block, 0, stream>>>(jobs, wb);
+        if (ev) ev->End(3, stream);
+        nl += 3;
+        if (prof) {
+            prof->extendLaunches++;
+            prof->shadowLaunches++;
+        }
+        cur ^= 1;
     }
-    if (prof) events.Begin(4, stream);
-    FinalizeKernel<<<grid, block, 0, stream>>>(st, wb.accum, film);
-    if (prof) events.End(4, stream);
+    if (ev) ev->Begin(4, stream);
+    AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, nUnits, nPixelUnits, wb);
+    if (ev) ev->End(4, stream);
     nl++;
     if (launches) *launches += nl;
     if (e == cudaSuccess) e = cudaGetLastError();
-    if (prof && e == cudaSuccess) {
-        e = cudaStreamSynchronize(stream);
-        events.Collect(prof->ms);
-        unsigned long long c[8];
-        cudaMemcpy(c, prof->devCounters, sizeof(c), cudaMemcpyDeviceToHost);
-        prof->refNodeTests = c[0];
-        prof->refTriTests = c[1];
-        prof->refRays = c[2];
-        prof->extendRays = c[3];
-        prof->shadowRays = c[4];
-    }
     return e;
 }
+
+cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int maxPixels,
+                         cudaStream_t stream, int* launches, WaveProfile* prof) {
+    if (nJobs <= 0) return cudaSuccess;
+    StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
+    const int block = 256;
+    const int gx = std::max(1, std::min(DefaultStageGrid(), (maxPixels + block - 1) / block));
+    if (ev) ev->Begin(4, stream);
+    FinalizeKernel<<<dim3(gx, nJobs), block, 0, stream>>>(jobs, jobList, maxPixels);
+    if (ev) ev->End(4, stream);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream) {
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return e;
+    StageEvents* ev = (StageEvents*)prof->events;
+    if (ev) {
+        ev->Collect(prof->ms);
+        delete ev;
+        prof->events = nullptr;
+    }
+    unsigned long long c[8];
+    e = cudaMemcpy(c, prof->devCounters, sizeof(c), cudaMemcpyDeviceToHost);
+    prof->refNodeTests = c[0];
+    prof->refTriTests = c[1];
+    prof->refRays = c[2];
+    prof->extendRays = c[3];
+    prof->shadowRays = c[4];
+    return e;
+}
+
+void* NewStageEvents() { return new StageEvents(); }
 
 cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,
                                float distMax, int* triOut, float* distOut, cudaStream_t stream) {

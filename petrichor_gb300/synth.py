@@ -286,7 +286,7 @@ def _mixed_material(rng: Rng, p_lambert=0.4, p_ggx=0.4,
 def spheres_grids(seed: int = 2, tri_budget: int = 1_000_000, n_objects: int = 64,
                   width: int = 1920, height: int = 1080, spp: int = 64, max_bounces: int = 16,
                   env_width: int = 2048, env_height: int = 1024,
-                  sun_peak_over_median: float = 1.0e4) -> Scene:
+                  sun_peak_over_median: float = 1.0e4, env_texture=None) -> Scene:
     """64 seeded UV-spheres and displaced grids totalling ~``tri_budget`` triangles.
 
     ``sun_peak_over_median`` scales the sun lobe (1e4 in the benchmark workload;
@@ -316,9 +316,9 @@ def spheres_grids(seed: int = 2, tri_budget: int = 1_000_000, n_objects: int = 6
                                       rng.one(0.1, 0.35), rng.one(-0.9, 0.9), rng.one(0, 6.28))
             b.add(P, I, m, SHADING_SMOOTH, nrm=N)
     pos, nrm, uv, idx, tm, sh = b.arrays()
-    env = Environment(base_color=(1.0, 1.0, 1.0),
-                      texture=sky_env(rng, env_width, env_height,
-                                      sun_peak_over_median=sun_peak_over_median))
+    if env_texture is None:
+        env_texture = sky_env(rng, env_width, env_height, sun_peak_over_median=sun_peak_over_median)
+    env = Environment(base_color=(1.0, 1.0, 1.0), texture=env_texture)
     extent = side * spacing
     cam = Camera(pos=(0.0, -0.95 * extent, 0.5 * extent), view_dir=(0.0, 0.95 * extent, -0.5 * extent + 0.5),
                  fov=math.radians(45.0), focus_target=None, aperture=0.0)
@@ -363,3 +363,58 @@ def terrain_rocks(seed: int = 5, terrain_n: int = 3000, n_rocks: int = 4000, roc
     st = Settings(width=width, height=height, spp=spp, max_bounces=max_bounces,
                   integrator=INTEGRATOR_PT)
     return Scene(pos, nrm, uv, idx, tm, sh, np.zeros(0, np.int32), mats, cam, env, st)
+
+
+def batch_instances(seed: int = 3, n: int = 64, tri_lo: float = 1e4, tri_hi: float = 2e6,
+                    px_lo: float = 256 ** 2, px_hi: float = 1024 ** 2, spps=(4, 16, 64, 256),
+                    env_width: int = 1024, env_height: int = 512, max_bounces: int = 16):
+    """``n`` independent spheres-and-grids scenes of uneven size: triangle counts and
+    pixel counts log-uniform, aspect uniform in [0.5, 2], spp drawn from ``spps``."""
+    rng = Rng(seed)
+    out = []
+    for k in range(n):
+        tris = int(math.exp(rng.one(math.log(tri_lo), math.log(tri_hi))))
+        px = math.exp(rng.one(math.log(px_lo), math.log(px_hi)))
+        aspect = rng.one(0.5, 2.0)
+        w = max(8, int(round(math.sqrt(px * aspect))))
+        h = max(8, int(round(px / w)))
+        spp = spps[int(rng.one() * len(spps)) % len(spps)]
+        out.append(spheres_grids(seed=1000 + k, tri_budget=tris, width=w, height=h, spp=spp,
+                                 max_bounces=max_bounces, env_width=env_width,
+                                 env_height=env_height))
+    return out
+
+
+def serving_scenes(seed: int = 4, n: int = 8, tri_lo: float = 1e5, tri_hi: float = 4e6,
+                   env_width: int = 8192, env_height: int = 4096):
+    """``n`` resident scenes for the serving workload, triangle counts spread
+    log-uniformly over [tri_lo, tri_hi] (first and last at the ends)."""
+    # one procedural sky, uploaded as each scene's own texture
+    sky = sky_env(Rng(seed), env_width, env_height)
+    out = []
+    for k in range(n):
+        f = k / max(1, n - 1)
+        tris = int(math.exp(math.log(tri_lo) + f * (math.log(tri_hi) - math.log(tri_lo))))
+        out.append(spheres_grids(seed=2000 + k + seed, tri_budget=tris, width=64, height=64,
+                                 spp=1, env_texture=sky))
+    return out
+
+
+def request_stream(seed: int, rate: float, count: int, n_scenes: int = 8,
+                   px_lo: float = 128 ** 2, px_hi: float = 2048 ** 2, spps=(1, 8, 32, 128),
+                   depth_lo: int = 4, depth_hi: int = 16):
+    """Poisson arrivals: list of (arrival_s, scene index, width, height, spp, max_bounces)."""
+    rng = Rng(seed)
+    t = 0.0
+    out = []
+    for _ in range(count):
+        t += -math.log1p(-rng.one()) / rate
+        sc = int(rng.one() * n_scenes) % n_scenes
+        px = math.exp(rng.one(math.log(px_lo), math.log(px_hi)))
+        aspect = rng.one(0.5, 2.0)
+        w = max(8, int(round(math.sqrt(px * aspect))))
+        h = max(8, int(round(px / w)))
+        spp = spps[int(rng.one() * len(spps)) % len(spps)]
+        depth = depth_lo + int(rng.one() * (depth_hi - depth_lo + 1))
+        out.append((t, sc, w, h, spp, min(depth, depth_hi)))
+    return out
