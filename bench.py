@@ -297,9 +297,10 @@ def run_serve(args):
         samples = sum(w * h * spp for _, _, w, h, spp, _ in stream_)
         res = {}
         # ---- continuous-batching server
-        ctx.serve_start(wave_paths=args.wave_paths or (1 << 24), max_active=512,
-                        state_budget=150 * 2**30)
-        films = [np.empty((h, w, 3), np.float32) for _, _, w, h, _, _ in stream_]
+        ctx.serve_start(wave_paths=args.wave_paths, max_active=512, state_budget=150 * 2**30)
+        # pinned host films, as for the plain path
+        films = [torch.empty(h * w * 3, dtype=torch.float32, pin_memory=True).numpy().reshape(h, w, 3)
+                 for _, _, w, h, _, _ in stream_]
         rids = []
         t_start = time.perf_counter()
         for k, (t, sc, w, h, spp, depth) in enumerate(stream_):

@@ -4,10 +4,12 @@
 // one slot per admitted request and an arena for per-request state (per-pixel
 // sums, and film staging for host films). Each iteration it
 //   1. admits queued requests while slots and arena space are free,
-//   2. packs the next sample blocks of every admitted request into one wave
-//      (at most its share of the wave per request, so small requests that
-//      arrive behind a large one still get samples in the next wave),
-//   3. runs the wave and finalizes the requests whose last samples it held.
+//   2. packs the next sample blocks of the admitted requests into one wave,
+//      least remaining work first (a short request that arrives behind a long
+//      one finishes in the next wave; the long one takes what is left),
+//   3. enqueues the wave and the finalization of the requests it completes,
+//      then retires the previous wave (two waves in flight keep the GPU busy
+//      while the host plans).
 // Requests that arrive while a wave runs join the next one. A request's film
 // does not depend on the mix: paths draw from a stream keyed by (seed, pixel,
 // sample) and each pixel sums its samples in sample order.
@@ -78,6 +80,7 @@ struct Request {
     int scheduled = 0, finished = 0;  // samples put in waves / completed
     int slot = -1;
     size_t accumOff = 0, accumBytes = 0, filmOff = 0, filmBytes = 0;
+    int inFlight = 0;  // waves holding this request's samples
     bool cancel = false;
 };
 }  // namespace
@@ -85,7 +88,7 @@ struct Request {
 class Server {
 public:
     Server(pt_context* ctx, const pt_serve_config& cfg) : ctx_(ctx), cfg_(cfg) {
-        if (cfg_.wave_paths <= 0) cfg_.wave_paths = 1 << 23;
+        if (cfg_.wave_paths <= 0) cfg_.wave_paths = 1 << 25;
         if (cfg_.max_active <= 0) cfg_.max_active = 256;
         cfg_.max_active = std::min(cfg_.max_active, kMaxJobsPerCall);
         if (cfg_.state_budget == 0) cfg_.state_budget = uint64_t(4) << 30;
@@ -284,136 +287,189 @@ private:
         Free(ctx_, jobList_);
     }
 
+    // One planned and enqueued wave: what it did, to retire once its event fires.
+    struct InFlight {
+        cudaEvent_t done = nullptr;
+        std::vector<std::pair<Request*, int>> scheduled;  // request, samples in this wave
+        std::vector<Request*> finishing;
+        cudaError_t error = cudaSuccess;
+    };
+
+    // mu_ held. Admits queued requests in arrival order while a slot and arena
+    // space are free; returns the admitted ones (their job entries go to the device
+    // with the next wave).
+    std::vector<Request*> Admit() {
+        std::vector<Request*> admitted;
+        for (uint64_t id : std::vector<uint64_t>(active_)) {
+            Request& r = *reqs_[id];
+            if (r.cancel && r.inFlight == 0) Finish(r, PT_REQ_CANCELLED, PT_OK);
+        }
+        for (auto it = queue_.begin(); it != queue_.end();) {
+            Request& r = *reqs_[*it];
+            if (r.cancel) {
+                Finish(r, PT_REQ_CANCELLED, PT_OK);
+                it = queue_.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        while (!queue_.empty() && !freeSlots_.empty()) {
+            Request& r = *reqs_[queue_.front()];
+            size_t off = 0, foff = 0;
+            if (!alloc_.Alloc(r.accumBytes, &off)) break;
+            if (r.filmBytes && !alloc_.Alloc(r.filmBytes, &foff)) {
+                alloc_.Release(off, r.accumBytes);
+                break;
+            }
+            r.accumOff = off;
+            r.filmOff = foff;
+            r.slot = freeSlots_.back();
+            freeSlots_.pop_back();
+            r.state = PT_REQ_RUNNING;
+            r.admit = Now();
+            active_.push_back(r.id);
+            queue_.pop_front();
+            admitted.push_back(&r);
+        }
+        return admitted;
+    }
+
+    // mu_ held. Packs the next sample blocks into a wave, least remaining work
+    // first (short requests finish in the next wave; long ones take what is left).
+    void Plan(std::vector<WaveUnit>* units, InFlight* w, int* paths, int* pixels) {
+        std::vector<Request*> order;
+        for (uint64_t id : active_) {
+            Request& r = *reqs_[id];
+            if (!r.cancel && r.scheduled < r.spp) order.push_back(&r);
+        }
+        std::stable_sort(order.begin(), order.end(), [](const Request* a, const Request* b) {
+            return (int64_t)(a->spp - a->scheduled) * a->pixels <
+                   (int64_t)(b->spp - b->scheduled) * b->pixels;
+        });
+        const int cap = cfg_.wave_paths;
+        for (Request* r : order) {
+            const int room = (cap - *paths) / r->pixels;
+            if (room < 1 || (int)units->size() >= kMaxUnitsPerWave) continue;
+            const int sw = std::min(r->spp - r->scheduled, room);
+            WaveUnit u{};
+            u.job = r->slot;
+            u.s0 = r->scheduled;
+            u.sw = sw;
+            u.pathBase = *paths;
+            u.pixelBase = *pixels;
+            units->push_back(u);
+            *paths += r->pixels * sw;
+            *pixels += r->pixels;
+            r->scheduled += sw;
+            r->inFlight++;
+            w->scheduled.push_back({r, sw});
+            if (r->scheduled == r->spp) w->finishing.push_back(r);
+        }
+    }
+
+    // ctx->mu held. Enqueues the admitted requests' job entries, the wave and the
+    // finalization of the requests whose last samples it holds.
+    cudaError_t Enqueue(const std::vector<Request*>& admitted, const std::vector<WaveUnit>& units,
+                        int paths, int pixels, InFlight* w, int* launches) {
+        cudaError_t e = cudaSuccess;
+        for (Request* r : admitted) {
+            DevJob& J = slotJobs_[r->slot];
+            J = DevJob{};
+            J.S = r->scene->dev;
+            J.C = ToDev(&r->job.camera);
+            J.st = ToDev(&r->job.settings);
+            J.accum = (float4*)((char*)arena_.ptr + r->accumOff);
+            J.film = r->filmHost ? (float*)((char*)arena_.ptr + r->filmOff) : r->job.film_device;
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync((DevJob*)jobTable_.ptr + r->slot, &J, sizeof(DevJob),
+                                    cudaMemcpyHostToDevice, stream_);
+            if (e == cudaSuccess) e = cudaMemsetAsync(J.accum, 0, r->accumBytes, stream_);
+        }
+        if (units.empty()) return e;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(units_.ptr, units.data(), units.size() * sizeof(WaveUnit),
+                                cudaMemcpyHostToDevice, stream_);
+        if (e == cudaSuccess)
+            e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, (int)units.size(), paths, pixels,
+                        WaveIterations(slotJobs_, units), wb_, stream_, launches, nullptr);
+        if (e == cudaSuccess && !w->finishing.empty()) {
+            std::vector<int> slots;
+            int maxPx = 0;
+            for (Request* r : w->finishing) {
+                slots.push_back(r->slot);
+                maxPx = std::max(maxPx, r->pixels);
+            }
+            e = cudaMemcpyAsync(jobList_.ptr, slots.data(), slots.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, stream_);
+            if (e == cudaSuccess)
+                e = FinalizeJobs((DevJob*)jobTable_.ptr, (int*)jobList_.ptr, (int)slots.size(), maxPx,
+                                 stream_, launches, nullptr);
+            for (Request* r : w->finishing)
+                if (e == cudaSuccess && r->filmHost)
+                    e = cudaMemcpyAsync(r->filmHost, (char*)arena_.ptr + r->filmOff, r->filmBytes,
+                                        cudaMemcpyDeviceToHost, stream_);
+        }
+        return e;
+    }
+
+    // Waits for the oldest wave in flight and retires it.
+    void Retire(std::deque<InFlight>& flight) {
+        InFlight w = std::move(flight.front());
+        flight.pop_front();
+        cudaError_t e = w.error;
+        if (e == cudaSuccess) e = cudaEventSynchronize(w.done);
+        cudaEventDestroy(w.done);
+        std::lock_guard<std::mutex> g(mu_);
+        for (auto& [r, sw] : w.scheduled) {
+            r->finished += sw;
+            r->inFlight--;
+        }
+        if (e != cudaSuccess) {
+            const int code = CudaFail(ctx_, e, "served wave");
+            for (uint64_t id : std::vector<uint64_t>(active_)) Finish(*reqs_[id], PT_REQ_FAILED, code);
+        } else {
+            for (Request* r : w.finishing) {
+                if (r->state == PT_REQ_RUNNING) Finish(*r, PT_REQ_DONE, PT_OK);
+                ctx_->stats.renders++;
+            }
+        }
+        doneCv_.notify_all();
+    }
+
+    // Two waves in flight: while the GPU runs one, the next is planned and enqueued
+    // behind it on the same stream, so the GPU does not wait for the host.
     void Loop() {
         cudaSetDevice(ctx_->device);
+        std::deque<InFlight> flight;
         for (;;) {
-            std::vector<Request*> admitted, finishing;
+            std::vector<Request*> admitted;
             std::vector<WaveUnit> units;
-            std::vector<std::pair<Request*, int>> scheduled;
+            InFlight w;
             int paths = 0, pixels = 0;
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait_for(lk, std::chrono::milliseconds(20),
-                             [&] { return stopping_ || !queue_.empty() || !active_.empty(); });
-                if (stopping_) return;
-                // cancelled requests leave between waves
-                for (uint64_t id : std::vector<uint64_t>(active_)) {
-                    Request& r = *reqs_[id];
-                    if (r.cancel) Finish(r, PT_REQ_CANCELLED, PT_OK);
-                }
-                for (auto it = queue_.begin(); it != queue_.end();) {
-                    Request& r = *reqs_[*it];
-                    if (r.cancel) {
-                        Finish(r, PT_REQ_CANCELLED, PT_OK);
-                        it = queue_.erase(it);
-                    } else {
-                        ++it;
-                    }
-                }
+                if (flight.empty())
+                    cv_.wait_for(lk, std::chrono::milliseconds(20),
+                                 [&] { return stopping_ || !queue_.empty() || !active_.empty(); });
+                if (stopping_) break;
+                admitted = Admit();
+                Plan(&units, &w, &paths, &pixels);
                 doneCv_.notify_all();
-                // admission: in arrival order while a slot and arena space are free
-                while (!queue_.empty() && !freeSlots_.empty()) {
-                    Request& r = *reqs_[queue_.front()];
-                    size_t off = 0, foff = 0;
-                    if (!alloc_.Alloc(r.accumBytes, &off)) break;
-                    if (r.filmBytes && !alloc_.Alloc(r.filmBytes, &foff)) {
-                        alloc_.Release(off, r.accumBytes);
-                        break;
-                    }
-                    r.accumOff = off;
-                    r.filmOff = foff;
-                    r.slot = freeSlots_.back();
-                    freeSlots_.pop_back();
-                    r.state = PT_REQ_RUNNING;
-                    r.admit = Now();
-                    active_.push_back(r.id);
-                    queue_.pop_front();
-                    admitted.push_back(&r);
-                }
-                // wave: each active request's next sample blocks, up to its share
-                const int cap = cfg_.wave_paths;
-                const int share = std::max(1, cap / std::max<int>(1, (int)active_.size()));
-                for (uint64_t id : active_) {
-                    Request& r = *reqs_[id];
-                    const int remaining = r.spp - r.scheduled;
-                    if (remaining <= 0) continue;
-                    const int room = (cap - paths) / r.pixels;
-                    if (room < 1 || (int)units.size() >= kMaxUnitsPerWave) continue;
-                    const int sw = std::min({remaining, room, std::max(1, share / r.pixels)});
-                    WaveUnit u{};
-                    u.job = r.slot;
-                    u.s0 = r.scheduled;
-                    u.sw = sw;
-                    u.pathBase = paths;
-                    u.pixelBase = pixels;
-                    units.push_back(u);
-                    paths += r.pixels * sw;
-                    pixels += r.pixels;
-                    r.scheduled += sw;
-                    scheduled.push_back({&r, sw});
-                    if (r.scheduled == r.spp) finishing.push_back(&r);
-                }
             }
-            if (units.empty()) continue;
-            cudaError_t e = cudaSuccess;
-            {
-                std::lock_guard<std::mutex> cg(ctx_->mu);
-                for (Request* r : admitted) {
-                    DevJob& J = slotJobs_[r->slot];
-                    J = DevJob{};
-                    J.S = r->scene->dev;
-                    J.C = ToDev(&r->job.camera);
-                    J.st = ToDev(&r->job.settings);
-                    J.accum = (float4*)((char*)arena_.ptr + r->accumOff);
-                    J.film = r->filmHost ? (float*)((char*)arena_.ptr + r->filmOff) : r->job.film_device;
-                    if (e == cudaSuccess)
-                        e = cudaMemcpyAsync((DevJob*)jobTable_.ptr + r->slot, &J, sizeof(DevJob),
-                                            cudaMemcpyHostToDevice, stream_);
-                    if (e == cudaSuccess) e = cudaMemsetAsync(J.accum, 0, r->accumBytes, stream_);
-                }
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync(units_.ptr, units.data(), units.size() * sizeof(WaveUnit),
-                                        cudaMemcpyHostToDevice, stream_);
+            if (!units.empty() || !admitted.empty()) {
                 int launches = 0;
-                if (e == cudaSuccess)
-                    e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, (int)units.size(), paths,
-                                pixels, WaveIterations(slotJobs_, units), wb_, stream_, &launches,
-                                nullptr);
-                if (e == cudaSuccess && !finishing.empty()) {
-                    std::vector<int> slots;
-                    int maxPx = 0;
-                    for (Request* r : finishing) {
-                        slots.push_back(r->slot);
-                        maxPx = std::max(maxPx, r->pixels);
-                    }
-                    e = cudaMemcpyAsync(jobList_.ptr, slots.data(), slots.size() * sizeof(int),
-                                        cudaMemcpyHostToDevice, stream_);
-                    if (e == cudaSuccess)
-                        e = FinalizeJobs((DevJob*)jobTable_.ptr, (int*)jobList_.ptr, (int)slots.size(),
-                                         maxPx, stream_, &launches, nullptr);
-                    for (Request* r : finishing)
-                        if (e == cudaSuccess && r->filmHost)
-                            e = cudaMemcpyAsync(r->filmHost, (char*)arena_.ptr + r->filmOff, r->filmBytes,
-                                                cudaMemcpyDeviceToHost, stream_);
+                {
+                    std::lock_guard<std::mutex> cg(ctx_->mu);
+                    w.error = Enqueue(admitted, units, paths, pixels, &w, &launches);
+                    ctx_->stats.kernel_launches += launches;
                 }
-                ctx_->stats.kernel_launches += launches;
+                if (w.error == cudaSuccess) w.error = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
+                if (w.error == cudaSuccess) w.error = cudaEventRecord(w.done, stream_);
+                flight.push_back(std::move(w));
             }
-            // the wave runs on the server's own stream and buffers: other calls on
-            // the context proceed while it executes
-            if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
-            std::lock_guard<std::mutex> g(mu_);
-            for (auto& [r, sw] : scheduled) r->finished += sw;
-            if (e != cudaSuccess) {
-                const int code = CudaFail(ctx_, e, "served wave");
-                for (uint64_t id : std::vector<uint64_t>(active_)) Finish(*reqs_[id], PT_REQ_FAILED, code);
-            } else {
-                for (Request* r : finishing) {
-                    Finish(*r, PT_REQ_DONE, PT_OK);
-                    ctx_->stats.renders++;
-                }
-            }
-            doneCv_.notify_all();
+            if (flight.size() >= 2 || (units.empty() && !flight.empty())) Retire(flight);
         }
+        while (!flight.empty()) Retire(flight);
     }
 
     pt_context* ctx_;
