@@ -6,7 +6,9 @@
 #include <algorithm>
 #include <atomic>
 #include <cfloat>
+#include <climits>
 #include <cmath>
+#include <cstring>
 #include <deque>
 #include <future>
 #include <limits>
@@ -213,6 +215,102 @@ BvhResult BuildBinnedSah(const float* P, const int32_t* idx, int T, int threads)
         stack.push_back({it.n->right, li + 1, it.depth + 1});
     }
     return out;
+}
+
+namespace {
+
+struct WideCollapser {
+    const BvhResult& b;
+    std::vector<float>& out;  // 32 floats per wide node
+    bool ok = true;
+
+    static float Area(const BvhNodeOut& n) {
+        const float dx = n.hi[0] - n.lo[0], dy = n.hi[1] - n.lo[1], dz = n.hi[2] - n.lo[2];
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    }
+    int NewNode() {
+        const int w = (int)(out.size() / 32);
+        out.resize(out.size() + 32, 0.0f);
+        int32_t* codes = reinterpret_cast<int32_t*>(&out[(size_t)w * 32 + 24]);
+        for (int i = 0; i < 4; i++) codes[i] = INT32_MIN;
+        return w;
+    }
+    void SetChild(int w, int i, const float* lo, const float* hi, int32_t code) {
+        float* f = &out[(size_t)w * 32];
+        for (int a = 0; a < 3; a++) {
+            f[4 * a + i] = lo[a];
+            f[12 + 4 * a + i] = hi[a];
+        }
+        std::memcpy(&f[24 + i], &code, 4);
+    }
+    int32_t LeafCode(int first, int count) {
+        if (first >= (1 << 25)) ok = false;
+        return -((first << 6) | count) - 1;
+    }
+    // A leaf range as a child code: one chunk, or a chain of leaf-list nodes.
+    int32_t Leaf(const BvhNodeOut& n) {
+        const int count = n.end - n.begin;
+        if (count <= kWideLeafMax) return LeafCode(n.begin, count);
+        const int w = NewNode();
+        int first = n.begin, left = count;
+        for (int i = 0; i < 4 && left > 0; i++) {
+            if (i == 3 && left > kWideLeafMax) {
+                BvhNodeOut rest = n;
+                rest.begin = first;
+                rest.end = n.end;
+                SetChild(w, i, n.lo, n.hi, Leaf(rest));
+                left = 0;
+                break;
+            }
+            const int c = std::min(left, kWideLeafMax);
+            SetChild(w, i, n.lo, n.hi, LeafCode(first, c));
+            first += c;
+            left -= c;
+        }
+        return w;
+    }
+    int32_t Node(int bi) {
+        const BvhNodeOut& n = b.nodes[bi];
+        if (n.leaf) return Leaf(n);
+        int cand[4] = {n.child[0], n.child[1], -1, -1};
+        int k = 2;
+        while (k < 4) {
+            int best = -1;
+            float bestA = -1.0f;
+            for (int i = 0; i < k; i++)
+                if (!b.nodes[cand[i]].leaf && Area(b.nodes[cand[i]]) > bestA) {
+                    bestA = Area(b.nodes[cand[i]]);
+                    best = i;
+                }
+            if (best < 0) break;
+            const int open = cand[best];
+            cand[best] = b.nodes[open].child[0];
+            cand[k++] = b.nodes[open].child[1];
+        }
+        const int w = NewNode();
+        for (int i = 0; i < k; i++) {
+            const BvhNodeOut& c = b.nodes[cand[i]];
+            const int32_t code = c.leaf ? Leaf(c) : Node(cand[i]);
+            SetChild(w, i, c.lo, c.hi, code);
+        }
+        return w;
+    }
+};
+
+}  // namespace
+
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide) {
+    wide->clear();
+    if (bvh.primIds.empty()) return true;
+    WideCollapser c{bvh, *wide};
+    const BvhNodeOut& root = bvh.nodes[0];
+    if (root.leaf) {  // the root itself is a leaf: a wide root with that one leaf child
+        const int w = c.NewNode();
+        c.SetChild(w, 0, root.lo, root.hi, c.Leaf(root));
+    } else {
+        c.Node(0);
+    }
+    return c.ok;
 }
 
 }  // namespace ptg

@@ -27,6 +27,14 @@ struct BvhResult {
     int height = 0;  // longest root-to-leaf edge count
 };
 
+// Collapses the binary tree into 4-wide nodes (8 float4 each; layout in
+// pt_layout.h): each wide node takes a binary node's children and repeatedly
+// opens the largest-area inner child until it has four. Leaves of more than 63
+// primitives become chains of leaf chunks. Returns false if a leaf starts beyond
+// the 2^25 slots the child code can hold.
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide);
+constexpr int kWideLeafMax = 63;
+
 // positions: V x 3 floats; indices: T x 3. threads <= 0: hardware concurrency.
 BvhResult BuildBinnedSah(const float* positions, const int32_t* indices, int numTriangles,
                          int threads);

@@ -452,6 +452,12 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         nodes[2 * i] = F4(n.lo[0], n.lo[1], n.lo[2], n.hi[0]);
         nodes[2 * i + 1] = F4(n.hi[1], n.hi[2], IntBits(a), IntBits(b));
     }
+    // 4-wide collapse for the throughput traversal
+    std::vector<float> wideF;
+    if (!CollapseWide(bvh, &wideF))
+        return Fail(ctx, PT_ERR_UNSUPPORTED, "too many triangles for the wide BVH leaf encoding");
+    std::vector<float4> wide(wideF.size() / 4);
+    std::memcpy(wide.data(), wideF.data(), wideF.size() * sizeof(float));
     // triangles in leaf order
     std::vector<float4> tris((size_t)T * 3);
     for (int k = 0; k < T; k++) {
@@ -527,6 +533,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     SceneGpu& s = *sg;
     DevScene& D = s.dev;
     if ((rc = Upload(ctx, s, nodes, &D.nodes)) != PT_OK ||
+        (rc = Upload(ctx, s, wide, &D.wide)) != PT_OK ||
         (rc = Upload(ctx, s, tris, &D.tris)) != PT_OK ||
         (rc = Upload(ctx, s, shade, &D.shade)) != PT_OK ||
         (rc = Upload(ctx, s, mats, &D.mats)) != PT_OK ||
@@ -538,6 +545,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         return rc;
     }
     D.numNodes = T > 0 ? (int)bvh.nodes.size() : 0;
+    D.numWide = (int)(wide.size() / 8);
     D.numTris = T;
     D.numMats = (int)d->num_materials;
     D.numLights = (int)d->num_lights;
@@ -758,7 +766,9 @@ int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float*
         return Fail(ctx, PT_ERR_INVALID_ARG, "bad ray buffers");
     int rc = SetDevice(ctx);
     if (rc != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->status, 16)) != PT_OK) return rc;
     const cudaError_t e = LaunchTraceClosest(it->second->dev, n, rays, distMin, distMax, tri, dist,
+                                             (int*)ctx->status.ptr + 1,
                                              stream ? (cudaStream_t)stream : ctx->stream);
     ctx->stats.kernel_launches++;
     return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "trace");

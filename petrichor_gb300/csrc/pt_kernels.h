@@ -86,8 +86,10 @@ cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream);
 int DefaultStageGrid();
 
 // Closest-hit traversal of the throughput path for caller rays (o.xyz, d.xyz per ray).
+// fetchCounter: one device int of scratch for the persistent fetch.
 cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,
-                               float distMax, int* triOut, float* distOut, cudaStream_t stream);
+                               float distMax, int* triOut, float* distOut, int* fetchCounter,
+                               cudaStream_t stream);
 
 // Fixed scratch of the no-allocation replay render (noalloc.cu): status word and
 // stack area addresses on the current device; capacity of the stack area in ints.

@@ -8,6 +8,12 @@
 //              Node order and leaf ranges are the reference binned-SAH tree's
 //              (Core/Accel/BinnedSAHBVH.cpp:15-225), so slot k of a leaf is
 //              m_primitiveIDs[k].
+//   wide       8 x float4 per 4-wide node (128 B, one L2 line), the binary tree
+//              collapsed for the throughput traversal:
+//                [0..5] lo.x lo.y lo.z hi.x hi.y hi.z of the four children (SoA)
+//                [6]    child codes: >= 0 wide node; < 0 leaf, -(first*64+count)-1;
+//                       INT_MIN empty slot
+//                [7]    unused
 //   tris       3 x float4 per primitive slot (48 B), in leaf order:
 //                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) 0 0
 //              e1 = v1 - v0, e2 = v2 - v0 exactly as Triangle::Intersect forms
@@ -52,6 +58,7 @@ struct DevCamera {  // derived Camera state (Core/Camera.h:121-130)
 
 struct DevScene {
     const float4* nodes;
+    const float4* wide;  // 4-wide collapse of the same tree (throughput traversal)
     const float4* tris;
     const float4* shade;
     const DevMaterial* mats;
@@ -63,7 +70,8 @@ struct DevScene {
     int32_t envW, envH, envValid, stackDepth;  // stackDepth: max traversal stack entries
     float envBase[3], envRot;
     float lightPdfArea;  // 1 / sum(1/pdfArea_i), PathTracing.cpp:363-383 (summed in light order)
-    int32_t pad[3];
+    int32_t numWide;
+    int32_t pad[2];
 };
 
 // Integrators

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <utility>
 #include <vector>
 
@@ -49,81 +50,6 @@ __device__ __forceinline__ bool SlabFast(float4 a, float4 b, V3 o, V3 inv, float
     return tn <= tf;
 }
 
-// Closest hit (or any hit) in [tmin, tmax]. Triangle test = Triangle::Intersect,
-// so the closest primitive equals the reference's except on exact distance ties.
-template <bool kAnyHit>
-__device__ int TraceFast(const DevScene& S, V3 o, V3 d, float tmin, float tmax, float& tHit,
-                         int* err) {
-    if (S.numNodes == 0) return -1;
-    const V3 inv = 1.0f / d;
-    int best = -1;
-    float tBest = tmax;
-    float tE;
-    if (!SlabFast(__ldg(S.nodes), __ldg(S.nodes + 1), o, inv, 0.0f, tBest, tE)) return -1;
-    int2 stack[kWaveStackDepth];
-    int sp = 0;
-    float4 meta = __ldg(S.nodes + 1);
-    for (;;) {
-        const int a = __float_as_int(meta.z), cnt = __float_as_int(meta.w);
-        bool pop = true;
-        if (cnt >= 0) {
-            for (int k = a; k < a + cnt; k++) {
-                V3 v0, e1, e2;
-                LoadTri(S.tris, k, v0, e1, e2);
-                float t;
-                if (TriIntersect(v0, e1, e2, o, d, t) && t >= tmin && t <= tmax && t < tBest) {
-                    tBest = t;
-                    best = k;
-                    if (kAnyHit) {
-                        tHit = t;
-                        return k;
-                    }
-                }
-            }
-        } else {
-            const float4 la = __ldg(S.nodes + 2 * a), lb = __ldg(S.nodes + 2 * a + 1);
-            const float4 ra = __ldg(S.nodes + 2 * a + 2), rb = __ldg(S.nodes + 2 * a + 3);
-            float tl, tr;
-            const bool hl = SlabFast(la, lb, o, inv, 0.0f, tBest, tl);
-            const bool hr = SlabFast(ra, rb, o, inv, 0.0f, tBest, tr);
-            if (hl && hr) {
-                if (sp >= kWaveStackDepth) {
-                    *err = 1;
-                    break;
-                }
-                if (tr < tl) {
-                    stack[sp++] = make_int2(a, __float_as_int(tl));
-                    meta = rb;
-                } else {
-                    stack[sp++] = make_int2(a + 1, __float_as_int(tr));
-                    meta = lb;
-                }
-                pop = false;
-            } else if (hl) {
-                meta = lb;
-                pop = false;
-            } else if (hr) {
-                meta = rb;
-                pop = false;
-            }
-        }
-        if (pop) {
-            bool found = false;
-            while (sp > 0) {
-                const int2 e = stack[--sp];
-                if (__int_as_float(e.y) <= tBest) {
-                    meta = __ldg(S.nodes + 2 * e.x + 1);
-                    found = true;
-                    break;
-                }
-            }
-            if (!found) break;
-        }
-    }
-    tHit = tBest;
-    return best;
-}
-
 __device__ __forceinline__ int WarpAppend(int* counter, bool pred) {
     const unsigned active = __activemask();
     const unsigned mask = __ballot_sync(active, pred);
@@ -148,16 +74,29 @@ struct LaneRay {
     float tmin, tmax, tBest;
     int best;
     bool anyHit;
-    const float4* nodes;  // the lane's scene (rays of different jobs share a warp)
+    const float4* nodes;  // the lane's 4-wide tree (rays of different jobs share a warp)
     const float4* tris;
 };
 
-// Visits the node in `meta`; returns true when the ray is finished.
-__device__ __forceinline__ bool TraverseStep(LaneRay& r, int2* stack, int& sp, float4& meta,
-                                             int& err) {
-    const int a = __float_as_int(meta.z), cnt = __float_as_int(meta.w);
-    if (cnt >= 0) {
-        for (int k = a; k < a + cnt; k++) {
+__device__ __forceinline__ void SortPair(float& ta, int& ca, float& tb, int& cb) {
+    if (tb < ta) {
+        const float t = ta;
+        ta = tb;
+        tb = t;
+        const int c = ca;
+        ca = cb;
+        cb = c;
+    }
+}
+
+// Visits the item `cur` of the 4-wide tree (a wide node, or a leaf range);
+// returns true when the ray is finished. Hit children are visited nearest first;
+// the others wait on the stack with their entry distance.
+__device__ __forceinline__ bool TraverseStep(LaneRay& r, int2* stack, int& sp, int& cur, int& err) {
+    if (cur < 0) {
+        const int v = -cur - 1;
+        const int first = v >> 6, cnt = v & 63;
+        for (int k = first; k < first + cnt; k++) {
             V3 v0, e1, e2;
             LoadTri(r.tris, k, v0, e1, e2);
             float t;
@@ -168,38 +107,45 @@ __device__ __forceinline__ bool TraverseStep(LaneRay& r, int2* stack, int& sp, f
             }
         }
     } else {
-        const float4 la = __ldg(r.nodes + 2 * a), lb = __ldg(r.nodes + 2 * a + 1);
-        const float4 ra = __ldg(r.nodes + 2 * a + 2), rb = __ldg(r.nodes + 2 * a + 3);
-        float tl, tr;
-        const bool hl = SlabFast(la, lb, r.o, r.inv, 0.0f, r.tBest, tl);
-        const bool hr = SlabFast(ra, rb, r.o, r.inv, 0.0f, r.tBest, tr);
-        if (hl && hr) {
-            if (sp >= kWaveStackDepth) {
+        const float4* n = r.nodes + 8 * (size_t)cur;
+        const float4 lx = __ldg(n), ly = __ldg(n + 1), lz = __ldg(n + 2);
+        const float4 hx = __ldg(n + 3), hy = __ldg(n + 4), hz = __ldg(n + 5);
+        const int4 code = __ldg(reinterpret_cast<const int4*>(n + 6));
+        const float inf = __int_as_float(0x7f800000);
+        float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
+        int c0 = code.x, c1 = code.y, c2 = code.z, c3 = code.w;
+        float te;
+        if (c0 != INT_MIN && SlabFast(make_float4(lx.x, ly.x, lz.x, hx.x), make_float4(hy.x, hz.x, 0.f, 0.f),
+                                      r.o, r.inv, 0.0f, r.tBest, te)) t0 = te;
+        if (c1 != INT_MIN && SlabFast(make_float4(lx.y, ly.y, lz.y, hx.y), make_float4(hy.y, hz.y, 0.f, 0.f),
+                                      r.o, r.inv, 0.0f, r.tBest, te)) t1 = te;
+        if (c2 != INT_MIN && SlabFast(make_float4(lx.z, ly.z, lz.z, hx.z), make_float4(hy.z, hz.z, 0.f, 0.f),
+                                      r.o, r.inv, 0.0f, r.tBest, te)) t2 = te;
+        if (c3 != INT_MIN && SlabFast(make_float4(lx.w, ly.w, lz.w, hx.w), make_float4(hy.w, hz.w, 0.f, 0.f),
+                                      r.o, r.inv, 0.0f, r.tBest, te)) t3 = te;
+        // sorting network, nearest first
+        SortPair(t0, c0, t1, c1);
+        SortPair(t2, c2, t3, c3);
+        SortPair(t0, c0, t2, c2);
+        SortPair(t1, c1, t3, c3);
+        SortPair(t1, c1, t2, c2);
+        if (t0 != inf) {
+            const int pushes = (t1 != inf) + (t2 != inf) + (t3 != inf);
+            if (sp + pushes > kWaveStackDepth) {
                 err = 1;
                 return true;
             }
-            if (tr < tl) {
-                stack[sp++] = make_int2(a, __float_as_int(tl));
-                meta = rb;
-            } else {
-                stack[sp++] = make_int2(a + 1, __float_as_int(tr));
-                meta = lb;
-            }
-            return false;
-        }
-        if (hl) {
-            meta = lb;
-            return false;
-        }
-        if (hr) {
-            meta = rb;
+            if (t3 != inf) stack[sp++] = make_int2(c3, __float_as_int(t3));
+            if (t2 != inf) stack[sp++] = make_int2(c2, __float_as_int(t2));
+            if (t1 != inf) stack[sp++] = make_int2(c1, __float_as_int(t1));
+            cur = c0;
             return false;
         }
     }
     while (sp > 0) {
         const int2 e = stack[--sp];
         if (__int_as_float(e.y) <= r.tBest) {
-            meta = __ldg(r.nodes + 2 * e.x + 1);
+            cur = e.x;
             return false;
         }
     }
@@ -218,7 +164,7 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
     bool active = false;
     int2 stack[kWaveStackDepth];
     int sp = 0;
-    float4 meta = make_float4(0.f, 0.f, 0.f, 0.f);
+    int cur = 0;
     bool exhausted = false;  // warp-uniform
     for (;;) {
         const unsigned idle = __ballot_sync(kFullMask, !active);
@@ -237,10 +183,8 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
                     r.tBest = r.tmax;
                     r.best = -1;
                     sp = 0;
-                    float tE;
-                    if (r.nodes &&
-                        SlabFast(__ldg(r.nodes), __ldg(r.nodes + 1), r.o, r.inv, 0.0f, r.tBest, tE)) {
-                        meta = __ldg(r.nodes + 1);
+                    if (r.nodes) {
+                        cur = 0;  // wide root
                         active = true;
                     } else {
                         q.Finish(i, r);
@@ -252,7 +196,7 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
             if (exhausted) break;
             continue;
         }
-        if (active && TraverseStep(r, stack, sp, meta, err)) {
+        if (active && TraverseStep(r, stack, sp, cur, err)) {
             q.Finish(idx, r);
             active = false;
         }
@@ -314,7 +258,7 @@ struct ExtendQueue {
         r.tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
         r.tmax = kFltMax;
         r.anyHit = false;
-        r.nodes = J.S.numNodes > 0 ? J.S.nodes : nullptr;
+        r.nodes = J.S.numWide > 0 ? J.S.wide : nullptr;
         r.tris = J.S.tris;
     }
     __device__ void Finish(int i, const LaneRay& r) const {
@@ -516,7 +460,7 @@ struct ShadowQueue {
     __device__ void Load(int j, LaneRay& r) const {
         const float4 e0 = entries[4 * j], e1 = entries[4 * j + 1];
         const DevScene& S = jobs[pathJob[__float_as_int(e1.w) & 0x7FFFFFFF]].S;
-        r.nodes = S.numNodes > 0 ? S.nodes : nullptr;
+        r.nodes = S.numWide > 0 ? S.wide : nullptr;
         r.tris = S.tris;
         r.o = V3(e0.x, e0.y, e0.z);
         r.d = V3(e1.x, e1.y, e1.z);
@@ -621,17 +565,35 @@ __global__ void FinalizeKernel(const DevJob* __restrict__ jobs, const int* __res
     }
 }
 
-__global__ void TraceKernel(DevScene S, int n, const float* __restrict__ rays, float tmin, float tmax,
-                            int* __restrict__ triOut, float* __restrict__ distOut, int* err) {
-    int e = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float* r = rays + 6 * (size_t)i;
-        float t = 0.0f;
-        const int k = TraceFast<false>(S, V3(r[0], r[1], r[2]), V3(r[3], r[4], r[5]), tmin, tmax, t, &e);
-        triOut[i] = k >= 0 ? TriId(S.tris, k) : -1;
-        distOut[i] = k >= 0 ? t : -1.0f;
+struct RayBatchQueue {
+    const float4* nodes;
+    const float4* tris;
+    const float* rays;
+    float tmin, tmax;
+    int* triOut;
+    float* distOut;
+    __device__ void Load(int i, LaneRay& r) const {
+        const float* p = rays + 6 * (size_t)i;
+        r.o = V3(p[0], p[1], p[2]);
+        r.d = V3(p[3], p[4], p[5]);
+        r.tmin = tmin;
+        r.tmax = tmax;
+        r.anyHit = false;
+        r.nodes = nodes;
+        r.tris = tris;
     }
-    if (e && err) atomicOr(err, 1);
+    __device__ void Finish(int i, const LaneRay& r) const {
+        triOut[i] = r.best >= 0 ? TriId(tris, r.best) : -1;
+        distOut[i] = r.best >= 0 ? r.tBest : -1.0f;
+    }
+};
+
+__global__ void __launch_bounds__(128) TraceKernel(DevScene S, int n, const float* __restrict__ rays,
+                                                   float tmin, float tmax, int* __restrict__ triOut,
+                                                   float* __restrict__ distOut, int* fetch) {
+    RayBatchQueue q{S.numWide > 0 ? S.wide : nullptr, S.tris, rays, tmin, tmax, triOut, distOut};
+    int err = 0;
+    TraceQueue(q, n, fetch, err);
 }
 
 // Profiling helpers: ray tallies and the reference traversal's work per ray.
@@ -803,11 +765,13 @@ cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream) {
 void* NewStageEvents() { return new StageEvents(); }
 
 cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,
-                               float distMax, int* triOut, float* distOut, cudaStream_t stream) {
+                               float distMax, int* triOut, float* distOut, int* fetchCounter,
+                               cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    const int block = 128;
-    const int grid = std::min((n + block - 1) / block, DefaultStageGrid() * 4);
-    TraceKernel<<<grid, block, 0, stream>>>(S, n, rays, distMin, distMax, triOut, distOut, nullptr);
+    cudaError_t e = cudaMemsetAsync(fetchCounter, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    TraceKernel<<<DefaultStageGrid(), 128, 0, stream>>>(S, n, rays, distMin, distMax, triOut, distOut,
+                                                        fetchCounter);
     return cudaGetLastError();
 }
 
