@@ -46,7 +46,7 @@ def _stale() -> bool:
     return any(os.path.getmtime(s) > t for s in _sources())
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, defines=()) -> str:
     if not force and not _stale():
         return LIB
     os.makedirs(OBJ_DIR, exist_ok=True)
@@ -56,6 +56,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for s in CU_SOURCES:
         o = os.path.join(OBJ_DIR, s + ".o")
         jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
+                     *[f"-D{d}" for d in defines],
                      "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", *inc, "-c",
                      os.path.join(CSRC, s), "-o", o])
     for s in CPP_SOURCES:

@@ -171,35 +171,16 @@ int WaveCapacity(const pt_settings* st) {
 int EnsureWaveBuffers(pt_context* ctx, int capacity) {
     if (ctx->wbCapacity >= capacity) return PT_OK;
     for (auto& b : ctx->wbBuffers) Free(ctx, b);
-    ctx->wbBuffers.assign(10, DeviceBuffer{});
-    const size_t C = (size_t)capacity;
-    const size_t sizes[10] = {C * 2 * sizeof(float4), C * 2 * sizeof(float4), C * sizeof(float2),
-                              C * sizeof(float4),     C * sizeof(float4),     C * sizeof(float4),
-                              C * sizeof(unsigned long long), C * sizeof(int),
-                              C * 4 * sizeof(float4), 16 * sizeof(int)};
-    for (int i = 0; i < 10; i++) {
-        const int rc = Alloc(ctx, ctx->wbBuffers[i], sizes[i]);
-        if (rc != PT_OK) {
-            for (auto& b : ctx->wbBuffers) Free(ctx, b);
-            ctx->wbCapacity = 0;
-            return rc;
-        }
-    }
-    WaveBuffers& w = ctx->wb;
-    w.capacity = capacity;
-    w.ray[0] = (float4*)ctx->wbBuffers[0].ptr;
-    w.ray[1] = (float4*)ctx->wbBuffers[1].ptr;
-    w.hit = (float2*)ctx->wbBuffers[2].ptr;
-    w.st0 = (float4*)ctx->wbBuffers[3].ptr;
-    w.st1 = (float4*)ctx->wbBuffers[4].ptr;
-    w.st2 = (float4*)ctx->wbBuffers[5].ptr;
-    w.rng = (unsigned long long*)ctx->wbBuffers[6].ptr;
-    w.pathJob = (int*)ctx->wbBuffers[7].ptr;
-    w.shadow = (float4*)ctx->wbBuffers[8].ptr;
-    w.counts = (int*)ctx->wbBuffers[9].ptr;
-    cudaMemsetAsync(w.counts, 0, 16 * sizeof(int), ctx->stream);
-    if (!w.hostCount) {
-        const cudaError_t e = cudaMallocHost(&w.hostCount, sizeof(int) * 4);
+    ctx->wbBuffers.assign(1, DeviceBuffer{});
+    ctx->wbCapacity = 0;
+    const int rc = Alloc(ctx, ctx->wbBuffers[0], WaveBuffersBytes(capacity));
+    if (rc != PT_OK) return rc;
+    int* hostCount = ctx->wb.hostCount;
+    ctx->wb = CarveWaveBuffers(ctx->wbBuffers[0].ptr, capacity);
+    ctx->wb.hostCount = hostCount;
+    cudaMemsetAsync(ctx->wb.counts, 0, 16 * sizeof(int), ctx->stream);
+    if (!ctx->wb.hostCount) {
+        const cudaError_t e = cudaMallocHost(&ctx->wb.hostCount, sizeof(int) * 4);
         if (e != cudaSuccess) return CudaFail(ctx, e, "cudaMallocHost");
     }
     ctx->wbCapacity = capacity;

@@ -45,20 +45,27 @@ struct WaveUnit {
     int32_t pixelBase, pad[3];
 };
 
+// Path state travels with its ray through the compacted queues (so the shade
+// stage reads and writes it in queue order); only the radiance sum stays per
+// path (written at termination and by next-event rays).
 struct WaveBuffers {
-    int capacity;       // paths per wave
-    float4* ray[2];     // 2 float4 per entry: {o.xyz, path}, {d.xyz, 0}
-    float2* hit;        // {t, slot} per ray entry (slot < 0: miss)
-    float4* st0;        // per path {T.xyz, prob}
-    float4* st1;        // per path {L.xyz, ior}
-    float4* st2;        // per path {lastPdf, lastSin, bounce, flags}
-    unsigned long long* rng;  // per path
-    int* pathJob;       // per path: job index
-    float4* shadow;     // 4 float4 per shadow entry
-    int* counts;        // [0],[1] ray queues; [2] shadow queue; [3] error bits; [4],[5] fetch
-    int* hostCount;     // pinned host word for queue-size polls
+    int capacity;                  // paths per wave
+    float4* ray[2];                // per entry: {o.xyz, path}, {d.xyz, ior}
+    float4* qs0[2];                // per entry: {T.xyz, prob}
+    float4* qs1[2];                // per entry: {lastPdf, lastSin, bounce, flags}
+    unsigned long long* qrng[2];   // per entry: random stream state
+    float2* hit;                   // per entry of the current queue: {t, slot} (slot < 0: miss)
+    float4* pathL;                 // per path: {L.xyz, flags}
+    int* pathJob;                  // per path: job index
+    float4* shadow;                // 4 float4 per next-event entry
+    int* counts;                   // [0],[1] ray queues; [2] shadow queue; [3] error bits; [4],[5] fetch
+    int* hostCount;                // pinned host word for queue-size polls
 };
-size_t WaveBytesPerPath();
+// Device bytes of the wave buffers for `capacity` paths, and their carving out of
+// one 256-byte-aligned allocation (hostCount is left for the caller).
+size_t WaveBuffersBytes(int capacity);
+WaveBuffers CarveWaveBuffers(void* base, int capacity);
+
 
 // Optional per-stage profile (CUDA events around every stage launch; ray tallies;
 // reference-order traversal work over the extended rays).

@@ -250,27 +250,10 @@ private:
     }
 
     int AllocWave() {
-        wbBufs_.assign(10, DeviceBuffer{});
-        const size_t C = (size_t)cfg_.wave_paths;
-        const size_t sizes[10] = {C * 2 * sizeof(float4), C * 2 * sizeof(float4), C * sizeof(float2),
-                                  C * sizeof(float4), C * sizeof(float4), C * sizeof(float4),
-                                  C * sizeof(unsigned long long), C * sizeof(int),
-                                  C * 4 * sizeof(float4), 16 * sizeof(int)};
-        for (int i = 0; i < 10; i++) {
-            const int rc = Alloc(ctx_, wbBufs_[i], sizes[i]);
-            if (rc != PT_OK) return rc;
-        }
-        wb_.capacity = cfg_.wave_paths;
-        wb_.ray[0] = (float4*)wbBufs_[0].ptr;
-        wb_.ray[1] = (float4*)wbBufs_[1].ptr;
-        wb_.hit = (float2*)wbBufs_[2].ptr;
-        wb_.st0 = (float4*)wbBufs_[3].ptr;
-        wb_.st1 = (float4*)wbBufs_[4].ptr;
-        wb_.st2 = (float4*)wbBufs_[5].ptr;
-        wb_.rng = (unsigned long long*)wbBufs_[6].ptr;
-        wb_.pathJob = (int*)wbBufs_[7].ptr;
-        wb_.shadow = (float4*)wbBufs_[8].ptr;
-        wb_.counts = (int*)wbBufs_[9].ptr;
+        wbBufs_.assign(1, DeviceBuffer{});
+        const int rc = Alloc(ctx_, wbBufs_[0], WaveBuffersBytes(cfg_.wave_paths));
+        if (rc != PT_OK) return rc;
+        wb_ = CarveWaveBuffers(wbBufs_[0].ptr, cfg_.wave_paths);
         cudaMemset(wb_.counts, 0, 16 * sizeof(int));
         const cudaError_t e = cudaMallocHost(&wb_.hostCount, sizeof(int) * 4);
         return e == cudaSuccess ? PT_OK : CudaFail(ctx_, e, "cudaMallocHost");

@@ -25,6 +25,15 @@
 
 namespace ptg {
 
+// Minimum resident blocks per SM requested from the register allocator for the
+// trace (extend/shadow) and shade stages; 1 leaves the choice to the compiler.
+#ifndef PT_TRACE_MIN_BLOCKS
+#define PT_TRACE_MIN_BLOCKS 1
+#endif
+#ifndef PT_SHADE_MIN_BLOCKS
+#define PT_SHADE_MIN_BLOCKS 1
+#endif
+
 enum : int { kFlagNoSignCheck = 1 };
 enum : int { kShadowEnv = 0, kShadowArea = 1 };
 
@@ -230,11 +239,11 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         rng.Next(r2, r3);
         const Ray ray = GenerateRay<FastMath>(J.C, x, y, W, H, r0, r1, r2, r3);
         wb.ray[cur][2 * i] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float(i));
-        wb.ray[cur][2 * i + 1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
-        wb.st0[i] = make_float4(ray.T.x, ray.T.y, ray.T.z, 1.0f);
-        wb.st1[i] = make_float4(0.f, 0.f, 0.f, 1.0f);
-        wb.st2[i] = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
-        wb.rng[i] = rng.s;
+        wb.ray[cur][2 * i + 1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 1.0f);
+        wb.qs0[cur][i] = make_float4(ray.T.x, ray.T.y, ray.T.z, 1.0f);
+        wb.qs1[cur][i] = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
+        wb.qrng[cur][i] = rng.s;
+        wb.pathL[i] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
         wb.pathJob[i] = u.job;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -268,7 +277,7 @@ struct ExtendQueue {
 
 // counts: [0],[1] ray queues, [2] shadow queue, [3] error bits,
 //         [4] extend fetch counter, [5] shadow fetch counter
-__global__ void __launch_bounds__(128) ExtendKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+__global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                     int cur) {
     const int n = wb.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -282,7 +291,7 @@ __global__ void __launch_bounds__(128) ExtendKernel(const DevJob* __restrict__ j
     if (err) atomicOr(wb.counts + 3, 1);
 }
 
-__global__ void __launch_bounds__(128) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+__global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                    int cur) {
     const int n = wb.counts[cur];
     const int nxt = cur ^ 1;
@@ -294,15 +303,15 @@ __global__ void __launch_bounds__(128) ShadeKernel(const DevJob* __restrict__ jo
         const DevScene& S = J.S;
         const DevSettings& st = J.st;
         const V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
-        float4 s0 = wb.st0[path], s1 = wb.st1[path], s2 = wb.st2[path];
-        PathRng rng(wb.rng[path]);
-        V3 L(s1.x, s1.y, s1.z);
+        const float4 s0 = wb.qs0[cur][i], s2 = wb.qs1[cur][i];
+        PathRng rng(wb.qrng[cur][i]);
+        V3 L;  // radiance this shade adds (terminations); next-event adds come later
         Ray in;
         in.o = o;
         in.d = d;
         in.T = V3(s0.x, s0.y, s0.z);
         in.prob = s0.w;
-        in.ior = s1.w;
+        in.ior = rb.w;
         in.bounce = __float_as_int(s2.z);
         int flags = __float_as_int(s2.w);
         const int slot = __float_as_int(h.y);
@@ -406,13 +415,15 @@ __global__ void __launch_bounds__(128) ShadeKernel(const DevJob* __restrict__ jo
                         const float dist = Length(dl);
                         const V3 ld = dl / dist;
                         const V3 f = BxDF<FastMath>(M, d, ld, si.n);
+                        // emitter material pick for the visibility test (GetMaterial with a draw)
+                        const float pick = rng.Next();
                         if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
-                            const V3 Tf = in.T * f;
+                            const V3 Tfc = in.T * f * fabsf(Dot(ld, si.n));
                             shadow = true;
                             sh0 = make_float4(p.x, p.y, p.z, dist);
                             sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
-                            sh2 = make_float4(Tf.x, Tf.y, Tf.z, BsdfPdf(M, d, ld, si.n));
-                            sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, fabsf(Dot(ld, si.n)));
+                            sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf(M, d, ld, si.n));
+                            sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, pick);
                         }
                     }
                     // ---- continuation
@@ -432,15 +443,15 @@ __global__ void __launch_bounds__(128) ShadeKernel(const DevJob* __restrict__ jo
         const int sslot = WarpAppend(wb.counts + 2, shadow);
         if (cont) {
             wb.ray[nxt][2 * rslot] = make_float4(out.o.x, out.o.y, out.o.z, __int_as_float(path));
-            wb.ray[nxt][2 * rslot + 1] = make_float4(out.d.x, out.d.y, out.d.z, 0.0f);
-            wb.st0[path] = make_float4(out.T.x, out.T.y, out.T.z, out.prob);
-            wb.st1[path] = make_float4(L.x, L.y, L.z, out.ior);
-            wb.st2[path] = make_float4(lastPdf, lastSin, __int_as_float(out.bounce), __int_as_float(flags));
+            wb.ray[nxt][2 * rslot + 1] = make_float4(out.d.x, out.d.y, out.d.z, out.ior);
+            wb.qs0[nxt][rslot] = make_float4(out.T.x, out.T.y, out.T.z, out.prob);
+            wb.qs1[nxt][rslot] = make_float4(lastPdf, lastSin, __int_as_float(out.bounce),
+                                             __int_as_float(flags));
+            wb.qrng[nxt][rslot] = rng.s;
         } else {
-            wb.st1[path] = make_float4(L.x, L.y, L.z, in.ior);
-            wb.st2[path] = make_float4(lastPdf, lastSin, __int_as_float(in.bounce), __int_as_float(flags));
+            float4 l = wb.pathL[path];  // next-event radiance added so far
+            wb.pathL[path] = make_float4(l.x + L.x, l.y + L.y, l.z + L.z, __int_as_float(flags));
         }
-        wb.rng[path] = rng.s;
         if (shadow) {
             float4* e = wb.shadow + 4 * (size_t)sslot;
             e[0] = sh0;
@@ -455,8 +466,7 @@ struct ShadowQueue {
     const DevJob* jobs;
     const int* pathJob;
     const float4* entries;
-    float4* st1;
-    const unsigned long long* rng;
+    float4* pathL;
     __device__ void Load(int j, LaneRay& r) const {
         const float4 e0 = entries[4 * j], e1 = entries[4 * j + 1];
         const DevScene& S = jobs[pathJob[__float_as_int(e1.w) & 0x7FFFFFFF]].S;
@@ -476,11 +486,11 @@ struct ShadowQueue {
         if (tag >= 0) {  // environment: adds when unoccluded
             if (r.best >= 0) return;
             const float4 c = entries[4 * j + 2];
-            float4 l = st1[path];
+            float4 l = pathL[path];
             l.x += c.x;
             l.y += c.y;
             l.z += c.z;
-            st1[path] = l;
+            pathL[path] = l;
             return;
         }
         // area light: the closest hit must be an emitter at the sampled point
@@ -488,14 +498,12 @@ struct ShadowQueue {
         const DevScene& S = jobs[pathJob[path]].S;
         const float4 e0 = entries[4 * j];
         const int tri = TriId(S.tris, r.best);
-        const float u = (float)(uint32_t)(Mix64(rng[path] ^ 0xA5A5A5A5DEADBEEFull) >> 40) *
-                        (1.0f / 16777216.0f);
-        const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), u);
+        const float4 e2 = entries[4 * j + 2], e3 = entries[4 * j + 3];
+        const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), e3.w);
         if (S.mats[m].kind != kEmission) return;
         const Shading sl = Interpolate(S, r.best, r.o, r.d, r.tBest);
         const V3 pl = r.o + r.d * e0.w;
         if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
-        const float4 e2 = entries[4 * j + 2], e3 = entries[4 * j + 3];
         const V3 sipos(e3.x, e3.y, e3.z);
         const float l2 = SqLen(sl.pos - sipos);
         const float cosP = fabsf(Dot(r.d, sl.n));
@@ -506,20 +514,20 @@ struct ShadowQueue {
             mis = pdfArea * pdfArea / (pdfArea * pdfArea + pB * pB);
         }
         const V3 li = MatColor(S.mats[sl.mat]);
-        const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * e3.w * cosP / (pdfArea * l2));
-        float4 l = st1[path];
+        const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * cosP / (pdfArea * l2));
+        float4 l = pathL[path];
         l.x += c.x;
         l.y += c.y;
         l.z += c.z;
-        st1[path] = l;
+        pathL[path] = l;
     }
 };
 
-__global__ void __launch_bounds__(128) ShadowKernel(const DevJob* __restrict__ jobs, WaveBuffers wb) {
+__global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ShadowKernel(const DevJob* __restrict__ jobs, WaveBuffers wb) {
     const int n = wb.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // next extend fetches from zero
     int err = 0;
-    ShadowQueue q{jobs, wb.pathJob, wb.shadow, wb.st1, wb.rng};
+    ShadowQueue q{jobs, wb.pathJob, wb.shadow, wb.pathL};
     TraceQueue(q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
@@ -537,8 +545,8 @@ __global__ void AccumulateKernel(const DevJob* __restrict__ jobs, const WaveUnit
         float4 acc = J.accum[pixel];
         for (int s = 0; s < u.sw; s++) {
             const int p = u.pathBase + s * P + q;
-            const float4 l = wb.st1[p];
-            const int flags = __float_as_int(wb.st2[p].w);
+            const float4 l = wb.pathL[p];
+            const int flags = __float_as_int(l.w);
             // PathTracing.cpp:191-195 drops a sample whose smallest channel is
             // negative or NaN; primary misses/emitters are added directly (:54,:67).
             if ((flags & kFlagNoSignCheck) || MinElem(V3(l.x, l.y, l.z)) >= 0.0f) {
@@ -656,9 +664,39 @@ struct StageEvents {
 };
 }  // namespace
 
-size_t WaveBytesPerPath() {
-    return 2 * 2 * sizeof(float4) + sizeof(float2) + 3 * sizeof(float4) + sizeof(unsigned long long) +
-           sizeof(int) + 4 * sizeof(float4);
+namespace {
+// Buffers carved out of one allocation: {element bytes per path, count multiplier}.
+constexpr size_t kAlign = 256;
+size_t Up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
+}  // namespace
+
+size_t WaveBuffersBytes(int capacity) {
+    const size_t C = (size_t)capacity;
+    return 2 * Up(C * 2 * sizeof(float4)) + 2 * Up(C * sizeof(float4)) + 2 * Up(C * sizeof(float4)) +
+           2 * Up(C * sizeof(unsigned long long)) + Up(C * sizeof(float2)) + Up(C * sizeof(float4)) +
+           Up(C * sizeof(int)) + Up(C * 4 * sizeof(float4)) + Up(16 * sizeof(int));
+}
+
+WaveBuffers CarveWaveBuffers(void* base, int capacity) {
+    const size_t C = (size_t)capacity;
+    char* p = static_cast<char*>(base);
+    auto take = [&](size_t bytes) {
+        char* q = p;
+        p += Up(bytes);
+        return q;
+    };
+    WaveBuffers w{};
+    w.capacity = capacity;
+    for (int k = 0; k < 2; k++) w.ray[k] = (float4*)take(C * 2 * sizeof(float4));
+    for (int k = 0; k < 2; k++) w.qs0[k] = (float4*)take(C * sizeof(float4));
+    for (int k = 0; k < 2; k++) w.qs1[k] = (float4*)take(C * sizeof(float4));
+    for (int k = 0; k < 2; k++) w.qrng[k] = (unsigned long long*)take(C * sizeof(unsigned long long));
+    w.hit = (float2*)take(C * sizeof(float2));
+    w.pathL = (float4*)take(C * sizeof(float4));
+    w.pathJob = (int*)take(C * sizeof(int));
+    w.shadow = (float4*)take(C * 4 * sizeof(float4));
+    w.counts = (int*)take(16 * sizeof(int));
+    return w;
 }
 
 int DefaultStageGrid() {
