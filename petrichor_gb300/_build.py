@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 CU_SOURCES = ["replay.cu", "wavefront.cu", "noalloc.cu"]
-CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp", "scheduler.cpp", "server.cpp"]
+CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp", "scheduler.cpp", "server.cpp", "cpp_api.cpp"]
 
 
 def _nvcc() -> str:
@@ -36,7 +36,8 @@ def _nvcc() -> str:
 def _sources():
     return [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES] + [
         os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))
-    ] + [os.path.join(ROOT, "include", "petrichor_gb300.h")]
+    ] + [os.path.join(ROOT, "include", "petrichor_gb300.h"),
+          os.path.join(ROOT, "include", "petrichor_gb300", "Petrichor.hpp")]
 
 
 def _stale() -> bool:

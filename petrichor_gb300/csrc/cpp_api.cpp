@@ -1,0 +1,387 @@
+// The C++ scene/renderer API (include/petrichor_gb300/Petrichor.hpp) over the C ABI.
+//
+// Camera arithmetic restates the reference's (Core/Camera.cpp:23-44), so the
+// derived state handed to the kernels is the same float by float; built with
+// -ffp-contract=off like the rest of the host code.
+#include "petrichor_gb300/Petrichor.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+
+#include "petrichor_gb300.h"
+
+namespace Petrichor {
+namespace Math {
+
+float Vector3f::Length() const { return (float)std::sqrt((double)Dot(*this, *this)); }
+Vector3f Vector3f::Normalized() const { return *this / Length(); }
+
+}  // namespace Math
+
+namespace Core {
+
+namespace {
+constexpr float kPi = 3.14159265358979f;
+
+std::string Slurp(const std::filesystem::path& path, bool* ok) {
+    std::ifstream f(path, std::ios::in | std::ios::binary);
+    *ok = !f.fail();
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ss.str();
+}
+
+// "key": <int> pairs of a flat JSON object.
+std::map<std::string, long> JsonInts(const std::string& s) {
+    std::map<std::string, long> out;
+    size_t i = 0;
+    while ((i = s.find('"', i)) != std::string::npos) {
+        const size_t j = s.find('"', i + 1);
+        if (j == std::string::npos) break;
+        const std::string key = s.substr(i + 1, j - i - 1);
+        size_t k = j + 1;
+        while (k < s.size() && std::isspace((unsigned char)s[k])) k++;
+        if (k < s.size() && s[k] == ':') {
+            k++;
+            while (k < s.size() && std::isspace((unsigned char)s[k])) k++;
+            size_t e = k;
+            if (e < s.size() && (s[e] == '-' || s[e] == '+')) e++;
+            while (e < s.size() && std::isdigit((unsigned char)s[e])) e++;
+            if (e > k) out[key] = std::stol(s.substr(k, e - k));
+            i = e;
+        } else {
+            i = j + 1;
+        }
+    }
+    return out;
+}
+
+// "[table]" headers and "key = <int>" lines, reported as "table.key".
+std::map<std::string, long> TomlInts(const std::string& s) {
+    std::map<std::string, long> out;
+    std::istringstream in(s);
+    std::string line, table;
+    while (std::getline(in, line)) {
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line = line.substr(0, hash);
+        const size_t a = line.find_first_not_of(" \t\r");
+        if (a == std::string::npos) continue;
+        line = line.substr(a);
+        if (line[0] == '[') {
+            const size_t b = line.find(']');
+            table = line.substr(1, b == std::string::npos ? std::string::npos : b - 1);
+            continue;
+        }
+        const size_t eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        std::string key = line.substr(0, eq);
+        key = key.substr(0, key.find_last_not_of(" \t") + 1);
+        const std::string val = line.substr(eq + 1);
+        const size_t v0 = val.find_first_not_of(" \t");
+        if (v0 == std::string::npos) continue;
+        try {
+            out[table.empty() ? key : table + "." + key] = std::stol(val.substr(v0));
+        } catch (...) {
+        }
+    }
+    return out;
+}
+
+void Read(int* dst, const std::map<std::string, long>& kv, const char* key) {
+    const auto it = kv.find(key);
+    if (it != kv.end()) *dst = (int)it->second;
+    else std::cerr << "RenderSetting: key is not found. [" << key << "]\n";
+}
+}  // namespace
+
+// ---------------------------------------------------------------- Texture2D
+Texture2D::Texture2D(int width, int height) : m_width(width), m_height(height) { Clear(); }
+
+void Texture2D::Clear(const Color3f& c) {
+    m_pixels.assign((size_t)std::max(m_width, 0) * std::max(m_height, 0) * 3, 0.0f);
+    for (size_t i = 0; i < m_pixels.size(); i += 3) {
+        m_pixels[i] = c.x;
+        m_pixels[i + 1] = c.y;
+        m_pixels[i + 2] = c.z;
+    }
+}
+
+bool Texture2D::Load(const std::filesystem::path& path) {
+    std::ifstream f(path, std::ios::binary);
+    char magic[8];
+    uint32_t dims[2];
+    if (!f || !f.read(magic, 8) || std::memcmp(magic, "PTRAWF32", 8) != 0 ||
+        !f.read((char*)dims, 8)) {
+        std::cerr << "Could not read texture. [" << path.string() << "]\n";
+        return false;
+    }
+    std::vector<float> px((size_t)dims[0] * dims[1] * 3);
+    if (!f.read((char*)px.data(), (std::streamsize)(px.size() * 4))) return false;
+    m_width = (int)dims[0];
+    m_height = (int)dims[1];
+    m_pixels = std::move(px);
+    m_isLoaded = true;
+    return true;
+}
+
+Color3f Texture2D::GetPixel(int i, int j) const {  // Texture2D.cpp:260-271
+    if (!IsValid()) return Color3f(1.0f, 0.0f, 1.0f);
+    const float* p = &m_pixels[((size_t)m_width * j + i) * 3];
+    return Color3f(p[0], p[1], p[2]);
+}
+
+void Texture2D::SetPixel(int i, int j, const Color3f& c) {
+    float* p = &m_pixels[((size_t)m_width * j + i) * 3];
+    p[0] = c.x;
+    p[1] = c.y;
+    p[2] = c.z;
+}
+
+// ---------------------------------------------------------------- Environment
+void Environment::Load(const std::filesystem::path& path) {
+    auto t = std::make_shared<Texture2D>();
+    if (t->Load(path)) m_tex = t;
+}
+
+void Environment::SetTexture(const Texture2D& texture) {
+    m_tex = std::make_shared<Texture2D>(texture);
+    m_tex->SetLoaded(true);
+}
+
+// ---------------------------------------------------------------- Camera (Camera.cpp:23-44)
+Camera::Camera(const Math::Vector3f& pos, const Math::Vector3f& dir) : m_pos(pos) { SetViewDir(dir); }
+void Camera::SetFocalLength(float focalLength) { m_hPerf = m_sensorHeight / focalLength; }
+void Camera::FocusTo(const Math::Vector3f& target) { m_focusDist = (target - m_pos).Length(); }
+void Camera::SetFOV(float fov) { m_hPerf = (float)(2.0f * std::tan((double)(0.5f * fov))); }
+void Camera::SetViewDir(const Math::Vector3f& dir) {
+    m_forward = dir.Normalized();
+    m_right = Math::Cross(m_forward, Math::Vector3f::UnitZ());
+    m_up = Math::Cross(m_right, m_forward);
+}
+void Camera::LookAt(const Math::Vector3f& target) { SetViewDir(target - m_pos); }
+float Camera::GetFOV() const { return (float)(2.0f * std::atan((double)(0.5f * m_sensorHeight / m_focusDist))); }
+float Camera::GetLensArea() const { return kPi * (0.5f * m_apeture) * (0.5f * m_apeture); }
+
+// ---------------------------------------------------------------- Scene
+void Scene::LoadRenderSetting(const std::filesystem::path& path) {
+    bool ok = false;
+    const std::string text = Slurp(path, &ok);
+    if (!ok) {
+        std::cerr << "Failed to read the render setting file. [" << path.string() << "]\n";
+        return;
+    }
+    RenderSetting rs;
+    if (path.extension() == ".toml") {  // RenderSettingLoader.cpp:105-124
+        const auto kv = TomlInts(text);
+        Read(&rs.outputWidth, kv, "settings.render_width");
+        Read(&rs.outputHeight, kv, "settings.render_height");
+        Read(&rs.numSamplesPerPixel, kv, "settings.spp");
+        Read(&rs.numMaxBounces, kv, "settings.maxBounces");
+        Read(&rs.tileWidth, kv, "settings.tile_width");
+        Read(&rs.tileHeight, kv, "settings.tile_height");
+        Read(&rs.numThreads, kv, "settings.num_threads");
+    } else {  // RenderSettingLoader.cpp:49-64
+        const auto kv = JsonInts(text);
+        Read(&rs.outputWidth, kv, "outputWidth");
+        Read(&rs.outputHeight, kv, "outputHeight");
+        Read(&rs.numSamplesPerPixel, kv, "spp");
+        Read(&rs.numSppForDenoising, kv, "denoising_spp");
+        Read(&rs.numMaxBounces, kv, "maxBounces");
+        Read(&rs.tileWidth, kv, "tileWidth");
+        Read(&rs.tileHeight, kv, "tileHeight");
+        Read(&rs.numThreads, kv, "numThreads");
+    }
+    m_renderSetting = rs;
+}
+
+// ---------------------------------------------------------------- Petrichor::Render
+Petrichor::Petrichor() = default;
+Petrichor::~Petrichor() {
+    if (m_ctx) pt_context_destroy(m_ctx);
+}
+
+uint32_t Petrichor::GetNumRenderedTiles() const {
+    uint32_t d = 0, t = 0;
+    if (m_ctx) pt_get_progress(m_ctx, &d, &t);
+    return d;
+}
+
+uint32_t Petrichor::GetNumTiles() const {
+    uint32_t d = 0, t = 0;
+    if (m_ctx) pt_get_progress(m_ctx, &d, &t);
+    return t;
+}
+
+void Petrichor::Render(const Scene& scene) {
+    const auto t0 = std::chrono::steady_clock::now();
+    auto fail = [&](int status, const std::string& msg) {
+        m_lastStatus = status;
+        m_lastError = msg;
+        std::cerr << "[Error] " << msg << "\n";
+    };
+    m_lastStatus = PT_OK;
+    m_lastError.clear();
+    Texture2D* target = scene.GetTargetTexture(Scene::AOVType::Rendered);
+    if (!target) return fail(PT_ERR_INVALID_ARG, "Target texture has not been set.");
+    const Camera* cam = scene.GetMainCamera();
+    if (!cam) return fail(PT_ERR_INVALID_ARG, "Main camera is not found.");
+    for (int a = Scene::AOVType::UV; a < Scene::AOVType::NumAOVTypes; a++)
+        if (scene.GetTargetTexture((Scene::AOVType::Value)a))
+            std::cerr << "[petrichor_gb300] AOV target " << a << " is not rendered\n";
+    if (!m_ctx) {
+        const int rc = pt_context_create(0, 0, &m_ctx);
+        if (rc != PT_OK) return fail(rc, std::string("no GPU context: ") + pt_status_string(rc));
+    }
+
+    // flatten what the render reads (Scene.h:95-173)
+    std::vector<float> pos, nrm, uv;
+    std::vector<int32_t> idx, triMat, lights;
+    std::vector<uint8_t> shading;
+    std::vector<pt_material> mats;
+    std::unordered_map<const Vertex*, int32_t> vertexIndex;
+    std::unordered_map<const MaterialBase*, int32_t> matIndex;
+    std::unordered_map<const GeometryBase*, int32_t> triIndex;
+    std::function<int32_t(const MaterialBase*)> addMaterial = [&](const MaterialBase* m) -> int32_t {
+        auto it = matIndex.find(m);
+        if (it != matIndex.end()) return it->second;
+        pt_material pm{};
+        switch (m->GetMaterialType()) {
+        case MaterialTypes::Lambert: {
+            const auto* l = static_cast<const Lambert*>(m);
+            pm.kind = PT_MAT_LAMBERT;
+            pm.color[0] = l->GetKd().x, pm.color[1] = l->GetKd().y, pm.color[2] = l->GetKd().z;
+            break;
+        }
+        case MaterialTypes::Glossy: {
+            const auto* g = static_cast<const GGX*>(m);
+            pm.kind = PT_MAT_GLOSSY;
+            const Color3f& c = g->GetReflectance();
+            pm.color[0] = c.x, pm.color[1] = c.y, pm.color[2] = c.z;
+            pm.roughness = g->GetRoughness();
+            break;
+        }
+        case MaterialTypes::Glass: {
+            const auto* g = static_cast<const Glass*>(m);
+            pm.kind = PT_MAT_GLASS;
+            const Color3f& c = g->GetColor();
+            pm.color[0] = c.x, pm.color[1] = c.y, pm.color[2] = c.z;
+            pm.ior = g->GetIOR();
+            break;
+        }
+        case MaterialTypes::Emission: {
+            const Color3f& c = static_cast<const Emission*>(m)->GetLightColor();
+            pm.kind = PT_MAT_EMISSION;
+            pm.color[0] = c.x, pm.color[1] = c.y, pm.color[2] = c.z;
+            break;
+        }
+        case MaterialTypes::Mix: {
+            const auto* x = static_cast<const MixMaterial*>(m);
+            pm.kind = PT_MAT_MIX;
+            pm.mat0 = addMaterial(x->GetMat0());
+            pm.mat1 = addMaterial(x->GetMat1());
+            pm.mix = x->GetMix();
+            break;
+        }
+        }
+        mats.push_back(pm);
+        return matIndex[m] = (int32_t)mats.size() - 1;
+    };
+    auto addVertex = [&](const Vertex* v) -> int32_t {
+        auto it = vertexIndex.find(v);
+        if (it != vertexIndex.end()) return it->second;
+        const int32_t k = (int32_t)(pos.size() / 3);
+        for (float f : {v->pos.x, v->pos.y, v->pos.z}) pos.push_back(f);
+        for (float f : {v->normal.x, v->normal.y, v->normal.z}) nrm.push_back(f);
+        for (float f : {v->uv.x, v->uv.y, v->uv.z}) uv.push_back(f);
+        return vertexIndex[v] = k;
+    };
+    for (const GeometryBase* g : scene.GetGeometries()) {
+        const auto* t = dynamic_cast<const Triangle*>(g);
+        if (!t) return fail(PT_ERR_UNSUPPORTED, "only triangle geometry is supported");
+        if (!t->GetMaterialPointer()) return fail(PT_ERR_INVALID_ARG, "geometry without material");
+        triIndex[g] = (int32_t)triMat.size();
+        for (const Vertex* v : t->GetVertices()) idx.push_back(addVertex(v));
+        triMat.push_back(addMaterial(t->GetMaterialPointer()));
+        shading.push_back(t->GetShadingType() == ShadingTypes::Smooth ? 1 : 0);
+    }
+    for (const GeometryBase* l : scene.GetLights()) {
+        auto it = triIndex.find(l);
+        if (it == triIndex.end()) return fail(PT_ERR_INVALID_ARG, "light is not a scene geometry");
+        lights.push_back(it->second);
+    }
+    if (mats.empty()) mats.push_back(pt_material{});  // an empty scene still needs one
+
+    pt_scene_desc d{};
+    d.num_vertices = (uint32_t)(pos.size() / 3);
+    d.positions = pos.data();
+    d.normals = nrm.data();
+    d.uvs = uv.data();
+    d.num_triangles = (uint32_t)triMat.size();
+    d.indices = idx.data();
+    d.tri_material = triMat.data();
+    d.tri_shading = shading.data();
+    d.num_materials = (uint32_t)mats.size();
+    d.materials = mats.data();
+    d.num_lights = (uint32_t)lights.size();
+    d.lights = lights.data();
+    const Environment& env = scene.GetEnvironment();
+    d.env_base_color[0] = env.GetBaseColor().x;
+    d.env_base_color[1] = env.GetBaseColor().y;
+    d.env_base_color[2] = env.GetBaseColor().z;
+    d.env_z_rotation = env.GetZAxisRotation();
+    if (env.GetTexture() && env.GetTexture()->IsValid()) {
+        d.env_width = env.GetTexture()->GetWidth();
+        d.env_height = env.GetTexture()->GetHeight();
+        d.env_rgb = env.GetTexture()->GetRawDataPtr();
+    }
+    pt_scene_id sid = 0;
+    int rc = pt_scene_upload(m_ctx, &d, &sid);
+    if (rc != PT_OK) return fail(rc, pt_last_error(m_ctx));
+
+    pt_camera pc{};
+    const Math::Vector3f* src[4] = {&cam->Position(), nullptr, nullptr, nullptr};
+    const Math::Vector3f right = cam->Right(), up = cam->Up(), fwd = cam->Forward();
+    src[1] = &right;
+    src[2] = &up;
+    src[3] = &fwd;
+    float* dst[4] = {pc.pos, pc.right, pc.up, pc.forward};
+    for (int k = 0; k < 4; k++) {
+        dst[k][0] = src[k]->x;
+        dst[k][1] = src[k]->y;
+        dst[k][2] = src[k]->z;
+    }
+    pc.h_perf = cam->GetHPerf();
+    pc.focus_dist = cam->GetFocusDist();
+    pc.aperture = cam->GetApeture();
+
+    const RenderSetting& rs = scene.GetRenderSetting();
+    pt_settings st{};
+    st.width = target->GetWidth();
+    st.height = target->GetHeight();
+    st.spp = rs.numSamplesPerPixel;
+    st.max_bounces = rs.numMaxBounces;
+    st.tile_width = rs.tileWidth;
+    st.tile_height = rs.tileHeight;
+    st.integrator = m_integrator;
+    st.mode = m_mode;
+    st.seed = m_seed;
+    rc = pt_render(m_ctx, sid, &pc, &st, target->GetRawDataPtr());
+    if (rc != PT_OK) fail(rc, pt_last_error(m_ctx));
+    pt_scene_release(m_ctx, sid);
+    if (m_callback) {
+        RenderingResult r;
+        r.totalSec = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
+        m_callback(r);
+    }
+}
+
+}  // namespace Core
+}  // namespace Petrichor

@@ -1,0 +1,206 @@
+// Client program for the C++ drop-in API (include/petrichor_gb300/Petrichor.hpp).
+//
+// Builds a scene from a .ptscene file with the calls a Petrichor application
+// makes (Vertex, Triangle, Lambert/GGX/Glass/Emission/MixMaterial,
+// Scene::RegisterMaterial/AppendGeometry/AppendLight/SetMainCamera/
+// SetEnvironment/SetTargetTexture/LoadRenderSetting, Environment::Load,
+// Camera(pos, dir)/SetFOV/SetFocalLength/FocusTo/SetApeture), renders it with
+// Petrichor::Render and writes the Rendered texture as raw float32 RGB rows.
+//
+//   drop_in_render <scene.ptscene> <film.bin> [wavefront]
+//
+// Without "wavefront" the renderer keeps its defaults (replay mode with
+// SimplePathTracing: the reference's own Render output). Exit status: 0 on
+// success, 3 when Render reported an error (its status code is printed).
+#include <petrichor_gb300/Petrichor.hpp>
+#include <petrichor_gb300.h>
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iterator>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace Petrichor;
+using namespace Petrichor::Core;
+
+namespace {
+
+class Bytes {
+public:
+    explicit Bytes(const std::string& path) {
+        std::ifstream f(path, std::ios::binary);
+        if (!f) throw std::runtime_error("cannot open " + path);
+        m_buf.assign(std::istreambuf_iterator<char>(f), {});
+    }
+    void Take(void* dst, size_t n) {
+        if (m_off + n > m_buf.size()) throw std::runtime_error("truncated scene file");
+        std::memcpy(dst, m_buf.data() + m_off, n);
+        m_off += n;
+    }
+    template <typename T>
+    T Get() {
+        T v;
+        Take(&v, sizeof(T));
+        return v;
+    }
+
+private:
+    std::vector<char> m_buf;
+    size_t m_off = 0;
+};
+
+Math::Vector3f V(const float* p) { return Math::Vector3f(p[0], p[1], p[2]); }
+
+// Everything the scene points at lives here for the lifetime of the render.
+struct App {
+    Scene scene;
+    std::vector<Vertex> vertices;
+    std::vector<Triangle> triangles;
+    std::unique_ptr<Texture2D> film;
+    int integrator = 0;
+};
+
+void BuildScene(const std::string& path, const std::string& scratch, App& app) {
+    Bytes r(path);
+    char magic[8];
+    r.Take(magic, 8);
+    if (std::memcmp(magic, "PTSCENE1", 8) != 0) throw std::runtime_error("not a .ptscene file");
+    int32_t s[8];
+    r.Take(s, sizeof(s));
+    app.integrator = s[7];
+    {  // render settings go through the JSON loader, as an application's would
+        const std::string json = scratch + ".settings.json";
+        std::ofstream f(json);
+        f << "{\n  \"outputWidth\": " << s[0] << ",\n  \"outputHeight\": " << s[1]
+          << ",\n  \"spp\": " << s[2] << ",\n  \"denoising_spp\": 1,\n  \"maxBounces\": " << s[3]
+          << ",\n  \"tileWidth\": " << s[4] << ",\n  \"tileHeight\": " << s[5]
+          << ",\n  \"numThreads\": " << s[6] << "\n}\n";
+        f.close();
+        app.scene.LoadRenderSetting(json);
+    }
+    float cam[12];
+    r.Take(cam, sizeof(cam));
+    const uint32_t hasFocus = r.Get<uint32_t>();
+    auto camera = std::make_unique<Camera>(V(cam), V(cam + 3));
+    if (cam[6] > 0.0f) camera->SetFOV(cam[6]);
+    else camera->SetFocalLength(cam[7]);
+    if (hasFocus) camera->FocusTo(V(cam + 8));
+    camera->SetApeture(cam[11]);
+    app.scene.SetMainCamera(std::move(camera));
+
+    float envf[4];
+    r.Take(envf, sizeof(envf));
+    const int32_t ew = r.Get<int32_t>(), eh = r.Get<int32_t>();
+    (void)r.Get<uint32_t>();
+    Environment env;
+    env.SetBaseColor(V(envf));
+    env.SetZAxisRotation(envf[3]);
+    if (ew > 0 && eh > 0) {  // the texture goes through Environment::Load of an image file
+        std::vector<float> px((size_t)ew * eh * 3);
+        r.Take(px.data(), px.size() * 4);
+        const std::string hdr = scratch + ".env.hdr";
+        std::ofstream f(hdr, std::ios::binary);
+        const uint32_t dims[2] = {(uint32_t)ew, (uint32_t)eh};
+        f.write("PTRAWF32", 8);
+        f.write(reinterpret_cast<const char*>(dims), 8);
+        f.write(reinterpret_cast<const char*>(px.data()), (std::streamsize)(px.size() * 4));
+        f.close();
+        env.Load(hdr);
+    }
+    app.scene.SetEnvironment(env);
+
+    const uint32_t M = r.Get<uint32_t>();
+    std::vector<float> mf((size_t)M * 8);
+    std::vector<int32_t> mi((size_t)M * 4);
+    r.Take(mf.data(), mf.size() * 4);
+    r.Take(mi.data(), mi.size() * 4);
+    std::vector<const MaterialBase*> mats(M, nullptr);
+    auto name = [](uint32_t k) { return "material" + std::to_string(k); };
+    for (uint32_t k = 0; k < M; k++) {  // plain materials, then mixes of them
+        const float* f = &mf[(size_t)k * 8];
+        std::unique_ptr<const MaterialBase> m;
+        switch (mi[(size_t)k * 4]) {
+        case 0: m = std::make_unique<Lambert>(V(f)); break;
+        case 1: m = std::make_unique<Glass>(V(f), f[4]); break;
+        case 2: m = std::make_unique<Emission>(V(f)); break;
+        case 3: m = std::make_unique<GGX>(V(f), f[3]); break;
+        default: continue;
+        }
+        app.scene.RegisterMaterial(name(k), std::move(m));
+        mats[k] = app.scene.GetMaterial(name(k));
+    }
+    for (uint32_t k = 0; k < M; k++) {
+        const int32_t* q = &mi[(size_t)k * 4];
+        if (q[0] != 4) continue;
+        if (!mats.at(q[1]) || !mats.at(q[2])) throw std::runtime_error("mix of a mix");
+        app.scene.RegisterMaterial(name(k),
+                                   std::make_unique<MixMaterial>(mats[q[1]], mats[q[2]], mf[(size_t)k * 8 + 5]));
+        mats[k] = app.scene.GetMaterial(name(k));
+    }
+
+    const uint32_t NV = r.Get<uint32_t>();
+    std::vector<float> pos((size_t)NV * 3), nrm((size_t)NV * 3), uv((size_t)NV * 3);
+    r.Take(pos.data(), pos.size() * 4);
+    r.Take(nrm.data(), nrm.size() * 4);
+    r.Take(uv.data(), uv.size() * 4);
+    app.vertices.reserve(NV);
+    for (uint32_t i = 0; i < NV; i++)
+        app.vertices.emplace_back(V(&pos[i * 3]), V(&nrm[i * 3]), V(&uv[i * 3]));
+    const uint32_t T = r.Get<uint32_t>();
+    std::vector<int32_t> idx((size_t)T * 3), tm(T);
+    std::vector<uint8_t> sh(T + (4 - T % 4) % 4);
+    r.Take(idx.data(), idx.size() * 4);
+    r.Take(tm.data(), tm.size() * 4);
+    r.Take(sh.data(), sh.size());
+    app.triangles.reserve(T);
+    for (uint32_t t = 0; t < T; t++) {
+        app.triangles.emplace_back(&app.vertices.at(idx[t * 3]), &app.vertices.at(idx[t * 3 + 1]),
+                                   &app.vertices.at(idx[t * 3 + 2]),
+                                   sh[t] ? ShadingTypes::Smooth : ShadingTypes::Flat);
+        app.triangles.back().SetMaterial(mats.at(tm[t]));
+    }
+    for (const Triangle& t : app.triangles) app.scene.AppendGeometry(&t);
+    const uint32_t NL = r.Get<uint32_t>();
+    for (uint32_t i = 0; i < NL; i++) app.scene.AppendLight(&app.triangles.at(r.Get<int32_t>()));
+
+    app.film = std::make_unique<Texture2D>(s[0], s[1]);
+    app.scene.SetTargetTexture(Scene::AOVType::Rendered, app.film.get());
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 3) {
+        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront]\n", argv[0]);
+        return 2;
+    }
+    try {
+        App app;
+        BuildScene(argv[1], argv[2], app);
+        Core::Petrichor renderer;
+        if (argc > 3 && std::string(argv[3]) == "wavefront") renderer.SetMode(PT_MODE_WAVEFRONT);
+        renderer.SetIntegrator(app.integrator);
+        float seconds = -1.0f;
+        renderer.SetRenderCallback([&](const RenderingResult& r) { seconds = r.totalSec; });
+        renderer.Render(app.scene);
+        std::printf("{\"status\": %d, \"tiles\": [%u, %u], \"seconds\": %.6f}\n",
+                    renderer.GetLastStatus(), renderer.GetNumRenderedTiles(),
+                    renderer.GetNumTiles(), seconds);
+        if (renderer.GetLastStatus() != PT_OK) {
+            std::fprintf(stderr, "render failed: %s\n", renderer.GetLastError().c_str());
+            return 3;
+        }
+        const Texture2D& film = *app.film;
+        std::ofstream f(argv[2], std::ios::binary);
+        f.write(reinterpret_cast<const char*>(film.GetRawDataPtr()),
+                (std::streamsize)((size_t)film.GetWidth() * film.GetHeight() * 3 * 4));
+        return f ? 0 : 1;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+}
