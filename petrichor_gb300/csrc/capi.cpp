@@ -489,27 +489,13 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         const float pdfAreaEach = 1.0f / (0.5f * Length(Cross(e0, e1)));
         sumArea += 1.0f / pdfAreaEach;
     }
-    // environment texels and the row tables of Environment::PreCalcCumulativeDistTex
-    // (Environment.cpp:56-128). The reference reads its table textures through an
-    // unloaded Texture2D, whose texel reads all return (1, 0, 1): each row's
-    // luminance sum reads as 1, so pdf1D = H / H and cdf1D = (j + 1) / H.
+    // environment texels (the importance-sampling row tables of
+    // Environment::PreCalcCumulativeDistTex depend on H alone; the kernels evaluate them)
     const int W = d->env_width, H = d->env_height;
     std::vector<float4> env((size_t)std::max(W * H, 1));
-    std::vector<float> pdf1D(std::max(H, 1)), cdf1D(std::max(H, 1));
     if (W > 0) {
         for (size_t i = 0; i < (size_t)W * H; i++)
             env[i] = F4(d->env_rgb[3 * i], d->env_rgb[3 * i + 1], d->env_rgb[3 * i + 2], 0.0f);
-        float sum = 0.0f;
-        for (int j = 0; j < H; j++) {
-            const float l = 1.0f;
-            pdf1D[j] = l;
-            sum += l;
-            cdf1D[j] = sum;
-        }
-        for (int j = 0; j < H; j++) {
-            pdf1D[j] *= (H / sum);
-            cdf1D[j] /= sum;
-        }
     }
     SceneGpu& s = *sg;
     DevScene& D = s.dev;
@@ -519,9 +505,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         (rc = Upload(ctx, s, shade, &D.shade)) != PT_OK ||
         (rc = Upload(ctx, s, mats, &D.mats)) != PT_OK ||
         (rc = Upload(ctx, s, lights, &D.lights)) != PT_OK ||
-        (rc = Upload(ctx, s, env, &D.env)) != PT_OK ||
-        (rc = Upload(ctx, s, cdf1D, &D.cdf1D)) != PT_OK ||
-        (rc = Upload(ctx, s, pdf1D, &D.pdf1D)) != PT_OK) {
+        (rc = Upload(ctx, s, env, &D.env)) != PT_OK) {
         for (auto& b : s.buffers) Free(ctx, b);
         return rc;
     }

@@ -322,6 +322,12 @@ __device__ __forceinline__ float UnloadedTableBilinearX(float u, float v, int W,
     const float cm = wx1 * 1.0f + wx0 * 1.0f;
     return wy1 * cm + wy0 * cm;
 }
+// The row tables of Environment::PreCalcCumulativeDistTex (Environment.cpp:56-128)
+// sum those unloaded reads: every row's luminance is 1, so the running sum is the
+// exact integer j + 1 and the tables are cdf1D[j] = (j + 1) / H (one rounded
+// division) and pdf1D[j] = 1 * (H / H) = 1. They are evaluated here instead of read.
+__device__ __forceinline__ float EnvRowCdf(int j, int H) { return __fdiv_rn((float)(j + 1), (float)H); }
+constexpr float kEnvRowPdf = 1.0f;
 // Environment::GetColor (Environment.cpp:29-48)
 template <class M>
 __device__ __forceinline__ V3 EnvColor(const DevScene& S, V3 d) {
@@ -348,7 +354,7 @@ __device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, f
         const float y = v * H;
         const int fy = (int)y;
         const int cy = min(fy + 1, H - 1);
-        const float c = Lerp(__ldg(S.cdf1D + fy), __ldg(S.cdf1D + cy), y - fy);
+        const float c = Lerp(EnvRowCdf(fy, H), EnvRowCdf(cy, H), y - fy);
         const float diff = c - r0;
         if (v1 - v0 <= th) { v0 = v1 = v; break; }
         if (diff > 0) v1 = v;
@@ -368,7 +374,7 @@ __device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, f
         const float y = v0 * H;
         const int y0 = (int)y;
         const int y1 = min(y0 + 1, H - 1);
-        const float py = Lerp(__ldg(S.pdf1D + y0), __ldg(S.pdf1D + y1), y - y0);
+        const float py = Lerp(kEnvRowPdf, kEnvRowPdf, y - y0);
         pdf = py * UnloadedTableBilinearX(u0, v0, W, H);
     }
     const float theta = v0 * kPi;
@@ -389,7 +395,7 @@ __device__ __forceinline__ float EnvPdf(const DevScene& S, V3 d) {
     // behaviour there); the row index is clamped to the table here.
     const int y0 = min((int)y, S.envH - 1);
     const int y1 = min(y0 + 1, S.envH - 1);
-    const float py = Lerp(__ldg(S.pdf1D + y0), __ldg(S.pdf1D + y1), y - y0);
+    const float py = Lerp(kEnvRowPdf, kEnvRowPdf, y - y0);
     return py * UnloadedTableBilinearX(u0, v0, S.envW, S.envH);
 }
 

@@ -80,10 +80,11 @@ struct WaveProfile {
 
 // One wave: raygen over `units` (device), the bounce loop, and accumulation into
 // each job's sums. iters >= 0 runs that many bounce iterations; iters < 0 runs
-// until the ray queue drains (polled every 4 iterations).
+// until the ray queue drains (polled every 4 iterations). integrator: the one
+// integrator of all the wave's jobs, or -1 when they differ.
 cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
-                    int nPixelUnits, int iters, const WaveBuffers& wb, cudaStream_t stream,
-                    int* launches, WaveProfile* prof, int gridOverride = 0);
+                    int nPixelUnits, int iters, int integrator, const WaveBuffers& wb,
+                    cudaStream_t stream, int* launches, WaveProfile* prof, int gridOverride = 0);
 // film = accum / spp for the listed jobs (device list of job indices).
 cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int maxPixels,
                          cudaStream_t stream, int* launches, WaveProfile* prof);

@@ -21,7 +21,8 @@
 //   shade      3 x float4 per original triangle (48 B):
 //                [0] n0.xyz material(bits) [1] n1.xyz smooth(bits) [2] n2.xyz 0
 //   lights     3 x float4 per light: [0] v0.xyz tri(bits) [1] e0.xyz 0 [2] e1.xyz 0
-//   env        float4 RGB_ texels, row-major (H x W); cdf1D / pdf1D per row.
+//   env        float4 RGB_ texels, row-major (H x W). The importance-sampling row
+//              tables are a function of H alone and are evaluated in the kernels.
 #pragma once
 #include <stdint.h>
 
@@ -64,8 +65,6 @@ struct DevScene {
     const DevMaterial* mats;
     const float4* lights;
     const float4* env;
-    const float* cdf1D;
-    const float* pdf1D;
     int32_t numNodes, numTris, numMats, numLights;
     int32_t envW, envH, envValid, stackDepth;  // stackDepth: max traversal stack entries
     float envBase[3], envRot;

@@ -54,6 +54,16 @@ int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
     return iters;
 }
 
+int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units) {
+    int integ = -2;
+    for (const WaveUnit& u : units) {
+        const int k = jobs[u.job].st.integrator;
+        if (integ == -2) integ = k;
+        else if (integ != k) return -1;
+    }
+    return integ < 0 ? -1 : integ;
+}
+
 cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, const WaveBuffers& wb,
                        int cap, cudaStream_t stream, int* launches, WaveProfile* prof) {
     std::vector<std::vector<WaveUnit>> waves;
@@ -84,7 +94,7 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
             pixels += P;
         }
         e = RunWave(T.jobs, T.units, (int)units.size(), paths, pixels, WaveIterations(jobs, units),
-                    wb, stream, launches, prof);
+                    WaveIntegrator(jobs, units), wb, stream, launches, prof);
         if (e != cudaSuccess) return e;
         std::vector<int> done;
         int maxPx = 0;

@@ -32,5 +32,7 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& tables
 // Bounce iterations a wave needs: maxBounces + 1 for PathTracing jobs; -1 (run
 // until the queue drains) when a SimplePathTracing job is present.
 int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
+// The integrator shared by all of a wave's jobs, or -1 when they differ.
+int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
 
 }  // namespace ptg

@@ -28,7 +28,7 @@ namespace ptg {
 // Minimum resident blocks per SM requested from the register allocator for the
 // trace (extend/shadow) and shade stages; 1 leaves the choice to the compiler.
 #ifndef PT_TRACE_MIN_BLOCKS
-#define PT_TRACE_MIN_BLOCKS 1
+#define PT_TRACE_MIN_BLOCKS 8
 #endif
 #ifndef PT_SHADE_MIN_BLOCKS
 #define PT_SHADE_MIN_BLOCKS 1
@@ -76,7 +76,10 @@ __device__ __forceinline__ int WarpAppend(int* counter, bool pred) {
 // finished, so long rays do not hold a warp of finished lanes (the load
 // imbalance of incoherent secondary rays). One node visit per loop iteration.
 constexpr unsigned kFullMask = 0xffffffffu;
-constexpr int kRefillLanes = 8;
+#ifndef PT_REFILL_LANES
+#define PT_REFILL_LANES 8
+#endif
+constexpr int kRefillLanes = PT_REFILL_LANES;
 
 struct LaneRay {
     V3 o, d, inv;
@@ -98,82 +101,133 @@ __device__ __forceinline__ void SortPair(float& ta, int& ca, float& tb, int& cb)
     }
 }
 
-// Visits the item `cur` of the 4-wide tree (a wide node, or a leaf range);
-// returns true when the ray is finished. Hit children are visited nearest first;
-// the others wait on the stack with their entry distance.
-__device__ __forceinline__ bool TraverseStep(LaneRay& r, int2* stack, int& sp, int& cur, int& err) {
-    if (cur < 0) {
-        const int v = -cur - 1;
-        const int first = v >> 6, cnt = v & 63;
-        for (int k = first; k < first + cnt; k++) {
-            V3 v0, e1, e2;
-            LoadTri(r.tris, k, v0, e1, e2);
+// Entries of the traversal stack kept in shared memory per thread; deeper ones go
+// to local memory. Shared entries are entry-major with one column per thread of
+// the 128-thread block, so a warp's accesses always fall in 32 distinct banks.
+#ifndef PT_SMEM_STACK
+#define PT_SMEM_STACK 16
+#endif
+// 1: a warp steps every lane through inner nodes until it reaches a leaf, then
+// intersects the lanes' leaves together; 0: one node or leaf per lane per step.
+// Both visit the same nodes and leaves in the same order for every ray.
+#ifndef PT_WHILE_WHILE
+#define PT_WHILE_WHILE 1
+#endif
+constexpr int kTraceBlock = 128;
+constexpr int kSmemStack = PT_SMEM_STACK;
+constexpr int kDone = INT_MIN;  // no further item (never a child code of a visited slot)
+
+struct TravStack {
+    int* code;   // shared, kSmemStack x kTraceBlock
+    float* dist;
+    int2 deep[kWaveStackDepth - kSmemStack > 0 ? kWaveStackDepth - kSmemStack : 1];
+    int sp;
+    __device__ __forceinline__ void Push(int c, float t) {
+        if (sp < kSmemStack) {
+            code[sp * kTraceBlock + threadIdx.x] = c;
+            dist[sp * kTraceBlock + threadIdx.x] = t;
+        } else {
+            deep[sp - kSmemStack] = make_int2(c, __float_as_int(t));
+        }
+        sp++;
+    }
+    // Next entry whose box starts no farther than tBest, or kDone.
+    __device__ __forceinline__ int Pop(float tBest) {
+        while (sp > 0) {
+            --sp;
+            int c;
             float t;
-            if (TriIntersect(v0, e1, e2, r.o, r.d, t) && t >= r.tmin && t <= r.tmax && t < r.tBest) {
-                r.tBest = t;
-                r.best = k;
-                if (r.anyHit) return true;
+            if (sp < kSmemStack) {
+                c = code[sp * kTraceBlock + threadIdx.x];
+                t = dist[sp * kTraceBlock + threadIdx.x];
+            } else {
+                const int2 e = deep[sp - kSmemStack];
+                c = e.x;
+                t = __int_as_float(e.y);
             }
+            if (t <= tBest) return c;
         }
-    } else {
-        const float4* n = r.nodes + 8 * (size_t)cur;
-        const float4 lx = __ldg(n), ly = __ldg(n + 1), lz = __ldg(n + 2);
-        const float4 hx = __ldg(n + 3), hy = __ldg(n + 4), hz = __ldg(n + 5);
-        const int4 code = __ldg(reinterpret_cast<const int4*>(n + 6));
-        const float inf = __int_as_float(0x7f800000);
-        float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
-        int c0 = code.x, c1 = code.y, c2 = code.z, c3 = code.w;
-        float te;
-        if (c0 != INT_MIN && SlabFast(make_float4(lx.x, ly.x, lz.x, hx.x), make_float4(hy.x, hz.x, 0.f, 0.f),
-                                      r.o, r.inv, 0.0f, r.tBest, te)) t0 = te;
-        if (c1 != INT_MIN && SlabFast(make_float4(lx.y, ly.y, lz.y, hx.y), make_float4(hy.y, hz.y, 0.f, 0.f),
-                                      r.o, r.inv, 0.0f, r.tBest, te)) t1 = te;
-        if (c2 != INT_MIN && SlabFast(make_float4(lx.z, ly.z, lz.z, hx.z), make_float4(hy.z, hz.z, 0.f, 0.f),
-                                      r.o, r.inv, 0.0f, r.tBest, te)) t2 = te;
-        if (c3 != INT_MIN && SlabFast(make_float4(lx.w, ly.w, lz.w, hx.w), make_float4(hy.w, hz.w, 0.f, 0.f),
-                                      r.o, r.inv, 0.0f, r.tBest, te)) t3 = te;
-        // sorting network, nearest first
-        SortPair(t0, c0, t1, c1);
-        SortPair(t2, c2, t3, c3);
-        SortPair(t0, c0, t2, c2);
-        SortPair(t1, c1, t3, c3);
-        SortPair(t1, c1, t2, c2);
-        if (t0 != inf) {
-            const int pushes = (t1 != inf) + (t2 != inf) + (t3 != inf);
-            if (sp + pushes > kWaveStackDepth) {
-                err = 1;
-                return true;
-            }
-            if (t3 != inf) stack[sp++] = make_int2(c3, __float_as_int(t3));
-            if (t2 != inf) stack[sp++] = make_int2(c2, __float_as_int(t2));
-            if (t1 != inf) stack[sp++] = make_int2(c1, __float_as_int(t1));
-            cur = c0;
-            return false;
+        return kDone;
+    }
+};
+
+// Tests the triangles of leaf `cur`; returns true when an any-hit ray is done.
+// Otherwise `cur` becomes the next item from the stack (or kDone).
+__device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur) {
+    const int v = -cur - 1;
+    const int first = v >> 6, cnt = v & 63;
+    for (int k = first; k < first + cnt; k++) {
+        V3 v0, e1, e2;
+        LoadTri(r.tris, k, v0, e1, e2);
+        float t;
+        if (TriIntersect(v0, e1, e2, r.o, r.d, t) && t >= r.tmin && t <= r.tmax && t < r.tBest) {
+            r.tBest = t;
+            r.best = k;
+            if (r.anyHit) return true;
         }
     }
-    while (sp > 0) {
-        const int2 e = stack[--sp];
-        if (__int_as_float(e.y) <= r.tBest) {
-            cur = e.x;
-            return false;
-        }
+    cur = stk.Pop(r.tBest);
+    return false;
+}
+
+// Tests the four children of wide node `cur`; `cur` becomes the nearest hit child
+// and the other hit children are pushed farthest first (or the next stack item).
+__device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur, int& err) {
+    const float4* n = r.nodes + 8 * (size_t)cur;
+    const float4 lx = __ldg(n), ly = __ldg(n + 1), lz = __ldg(n + 2);
+    const float4 hx = __ldg(n + 3), hy = __ldg(n + 4), hz = __ldg(n + 5);
+    const int4 code = __ldg(reinterpret_cast<const int4*>(n + 6));
+    const float inf = __int_as_float(0x7f800000);
+    float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
+    int c0 = code.x, c1 = code.y, c2 = code.z, c3 = code.w;
+    float te;
+    if (c0 != INT_MIN && SlabFast(make_float4(lx.x, ly.x, lz.x, hx.x), make_float4(hy.x, hz.x, 0.f, 0.f),
+                                  r.o, r.inv, 0.0f, r.tBest, te)) t0 = te;
+    if (c1 != INT_MIN && SlabFast(make_float4(lx.y, ly.y, lz.y, hx.y), make_float4(hy.y, hz.y, 0.f, 0.f),
+                                  r.o, r.inv, 0.0f, r.tBest, te)) t1 = te;
+    if (c2 != INT_MIN && SlabFast(make_float4(lx.z, ly.z, lz.z, hx.z), make_float4(hy.z, hz.z, 0.f, 0.f),
+                                  r.o, r.inv, 0.0f, r.tBest, te)) t2 = te;
+    if (c3 != INT_MIN && SlabFast(make_float4(lx.w, ly.w, lz.w, hx.w), make_float4(hy.w, hz.w, 0.f, 0.f),
+                                  r.o, r.inv, 0.0f, r.tBest, te)) t3 = te;
+    // sorting network, nearest first
+    SortPair(t0, c0, t1, c1);
+    SortPair(t2, c2, t3, c3);
+    SortPair(t0, c0, t2, c2);
+    SortPair(t1, c1, t3, c3);
+    SortPair(t1, c1, t2, c2);
+    if (t0 == inf) {
+        cur = stk.Pop(r.tBest);
+        return;
     }
-    return true;
+    const int pushes = (t1 != inf) + (t2 != inf) + (t3 != inf);
+    if (stk.sp + pushes > kWaveStackDepth) {
+        err = 1;
+        cur = kDone;
+        return;
+    }
+    if (t3 != inf) stk.Push(c3, t3);
+    if (t2 != inf) stk.Push(c2, t2);
+    if (t1 != inf) stk.Push(c1, t1);
+    cur = c0;
 }
 
 // Q provides: void Load(int i, LaneRay&) (ray, range, and the scene: nodes = nullptr
 // for an empty scene) and void Finish(int i, const LaneRay&).
-// Must be called by every lane of the warp (blockDim a multiple of 32).
+// Must be called by every lane of the warp, in blocks of kTraceBlock threads.
 template <class Q>
 __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
+    __shared__ int sCode[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
+    __shared__ float sDist[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
     const int lane = threadIdx.x & 31;
     const unsigned lowerLanes = (1u << lane) - 1u;
     LaneRay r;
     int idx = -1;
     bool active = false;
-    int2 stack[kWaveStackDepth];
-    int sp = 0;
-    int cur = 0;
+    TravStack stk;
+    stk.code = sCode;
+    stk.dist = sDist;
+    stk.sp = 0;
+    int cur = kDone;
     bool exhausted = false;  // warp-uniform
     for (;;) {
         const unsigned idle = __ballot_sync(kFullMask, !active);
@@ -191,7 +245,7 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
                     r.inv = 1.0f / r.d;
                     r.tBest = r.tmax;
                     r.best = -1;
-                    sp = 0;
+                    stk.sp = 0;
                     if (r.nodes) {
                         cur = 0;  // wide root
                         active = true;
@@ -205,9 +259,23 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
             if (exhausted) break;
             continue;
         }
-        if (active && TraverseStep(r, stack, sp, cur, err)) {
-            q.Finish(idx, r);
-            active = false;
+#if PT_WHILE_WHILE
+        const unsigned busy = __ballot_sync(kFullMask, active);
+#endif
+        if (active) {
+            bool done = false;
+#if PT_WHILE_WHILE
+            while (cur >= 0) VisitInner(r, stk, cur, err);
+            __syncwarp(busy);  // the lanes' leaves are intersected together
+            if (cur != kDone) done = VisitLeaf(r, stk, cur);
+#else
+            if (cur >= 0) VisitInner(r, stk, cur, err);
+            else if (cur != kDone) done = VisitLeaf(r, stk, cur);
+#endif
+            if (done || cur == kDone) {
+                q.Finish(idx, r);
+                active = false;
+            }
         }
     }
 }
@@ -291,6 +359,9 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const D
     if (err) atomicOr(wb.counts + 3, 1);
 }
 
+// kInteg: the integrator of every job in the wave, or -1 when the wave mixes them
+// (then read per path). A fixed integrator halves the kernel's code.
+template <int kInteg>
 __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                    int cur) {
     const int n = wb.counts[cur];
@@ -322,7 +393,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
         bool shadow = false;
         float4 sh0, sh1, sh2, sh3;
 
-        if (st.integrator == kSimplePathTracing) {
+        if ((kInteg >= 0 ? kInteg : st.integrator) == kSimplePathTracing) {
             // SimplePathTracing.cpp:45-126
             flags |= kFlagNoSignCheck;
             if (slot < 0) {
@@ -426,6 +497,16 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                             sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, pick);
                         }
                     }
+                    // the next-event entry is queued before the BSDF sample, so its
+                    // registers are free for it
+                    const int sslot = WarpAppend(wb.counts + 2, shadow);
+                    if (shadow) {
+                        float4* e = wb.shadow + 4 * (size_t)sslot;
+                        e[0] = sh0;
+                        e[1] = sh1;
+                        e[2] = sh2;
+                        e[3] = sh3;
+                    }
                     // ---- continuation
                     out = NextRay<FastMath>(M, in, si, rng);
                     if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
@@ -440,7 +521,6 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
         }
         // ---- write back and append
         const int rslot = WarpAppend(wb.counts + nxt, cont);
-        const int sslot = WarpAppend(wb.counts + 2, shadow);
         if (cont) {
             wb.ray[nxt][2 * rslot] = make_float4(out.o.x, out.o.y, out.o.z, __int_as_float(path));
             wb.ray[nxt][2 * rslot + 1] = make_float4(out.d.x, out.d.y, out.d.z, out.ior);
@@ -451,13 +531,6 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
         } else {
             float4 l = wb.pathL[path];  // next-event radiance added so far
             wb.pathL[path] = make_float4(l.x + L.x, l.y + L.y, l.z + L.z, __int_as_float(flags));
-        }
-        if (shadow) {
-            float4* e = wb.shadow + 4 * (size_t)sslot;
-            e[0] = sh0;
-            e[1] = sh1;
-            e[2] = sh2;
-            e[3] = sh3;
         }
     }
 }
@@ -713,9 +786,25 @@ int DefaultStageGrid() {
     return grid;
 }
 
+// Grid of the shade stage: PT_SHADE_BLOCKS_PER_SM blocks per SM (0: the trace grid).
+#ifndef PT_SHADE_BLOCKS_PER_SM
+#define PT_SHADE_BLOCKS_PER_SM 0
+#endif
+static int ShadeGrid(int traceGrid) {
+    if (PT_SHADE_BLOCKS_PER_SM <= 0) return traceGrid;
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = sms * PT_SHADE_BLOCKS_PER_SM;
+    }
+    return grid;
+}
+
 cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
-                    int nPixelUnits, int iters, const WaveBuffers& wb, cudaStream_t stream,
-                    int* launches, WaveProfile* prof, int gridOverride) {
+                    int nPixelUnits, int iters, int integrator, const WaveBuffers& wb,
+                    cudaStream_t stream, int* launches, WaveProfile* prof, int gridOverride) {
     if (nPaths <= 0) return cudaSuccess;
     if (nPaths > wb.capacity) return cudaErrorInvalidValue;
     const int grid = gridOverride > 0 ? gridOverride : DefaultStageGrid();
@@ -744,7 +833,13 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int n
                 RefCountKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, prof->devCounters);
             ev->Begin(2, stream);
         }
-        ShadeKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+        const int sgrid = ShadeGrid(grid);
+        if (integrator == kPathTracing)
+            ShadeKernel<kPathTracing><<<sgrid, block, 0, stream>>>(jobs, wb, cur);
+        else if (integrator == kSimplePathTracing)
+            ShadeKernel<kSimplePathTracing><<<sgrid, block, 0, stream>>>(jobs, wb, cur);
+        else
+            ShadeKernel<-1><<<sgrid, block, 0, stream>>>(jobs, wb, cur);
         if (ev) {
             ev->End(2, stream);
             TallyKernel<<<1, 1, 0, stream>>>(wb.counts, cur, prof->devCounters);
