@@ -450,16 +450,18 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         tris[3 * (size_t)k + 1] = F4(e1.y, e1.z, e2.x, e2.y);
         tris[3 * (size_t)k + 2] = F4(e2.z, IntBits(t), 0.0f, 0.0f);
     }
-    // per-triangle shading records
+    // shading records, also in leaf order: a hit's slot addresses both records
+    // without a dependent read of the triangle id
     std::vector<float4> shade((size_t)T * 3);
-    for (int t = 0; t < T; t++) {
+    for (int k = 0; k < T; k++) {
+        const int t = bvh.primIds[k];
         HV3 n[3] = {{0, 0, 1}, {0, 0, 1}, {0, 0, 1}};
         if (d->normals)
-            for (int k = 0; k < 3; k++) n[k] = Load(d->normals + 3 * d->indices[3 * t + k]);
+            for (int v = 0; v < 3; v++) n[v] = Load(d->normals + 3 * d->indices[3 * t + v]);
         const int smooth = d->tri_shading ? (d->tri_shading[t] ? 1 : 0) : 0;
-        shade[3 * (size_t)t] = F4(n[0].x, n[0].y, n[0].z, IntBits(d->tri_material[t]));
-        shade[3 * (size_t)t + 1] = F4(n[1].x, n[1].y, n[1].z, IntBits(smooth));
-        shade[3 * (size_t)t + 2] = F4(n[2].x, n[2].y, n[2].z, 0.0f);
+        shade[3 * (size_t)k] = F4(n[0].x, n[0].y, n[0].z, IntBits(d->tri_material[t]));
+        shade[3 * (size_t)k + 1] = F4(n[1].x, n[1].y, n[1].z, IntBits(smooth));
+        shade[3 * (size_t)k + 2] = F4(n[2].x, n[2].y, n[2].z, 0.0f);
     }
     // materials
     std::vector<DevMaterial> mats(d->num_materials);

@@ -185,6 +185,10 @@ __device__ __forceinline__ void LoadTri(const float4* __restrict__ tris, int k, 
 __device__ __forceinline__ int TriId(const float4* __restrict__ tris, int k) {
     return __float_as_int(__ldg(&tris[3 * k + 2].y));
 }
+// Material index of the triangle in primitive slot k (before Mix resolution).
+__device__ __forceinline__ int SlotMaterial(const float4* __restrict__ shade, int k) {
+    return __float_as_int(__ldg(&shade[3 * k].w));
+}
 
 // Triangle::Intersect (Core/Geometry/Triangle.cpp:51-88)
 __device__ __forceinline__ bool TriIntersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& dist) {
@@ -217,14 +221,13 @@ __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V
     si.pos = o + d * dist;
     V3 v0, e1, e2;
     LoadTri(S.tris, k, v0, e1, e2);
-    const int tri = TriId(S.tris, k);
-    const float4 s0 = __ldg(S.shade + 3 * tri);
-    const float4 s1 = __ldg(S.shade + 3 * tri + 1);
+    const float4 s0 = __ldg(S.shade + 3 * k);
+    const float4 s1 = __ldg(S.shade + 3 * k + 1);
     const V3 ce = Cross(e1, e2);
     if (__float_as_int(s1.w) == 0) {
         si.n = Normalized(ce);
     } else {
-        const float4 s2 = __ldg(S.shade + 3 * tri + 2);
+        const float4 s2 = __ldg(S.shade + 3 * k + 2);
         const float invDet = 1.0f / Dot(-d, ce);
         const V3 vec = o - v0;
         const float w1 = Dot(vec, Cross(d, e2)) * invDet;

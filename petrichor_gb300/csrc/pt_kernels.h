@@ -57,6 +57,7 @@ struct WaveBuffers {
     float2* hit;                   // per entry of the current queue: {t, slot} (slot < 0: miss)
     float4* pathL;                 // per path: {L.xyz, flags}
     int* pathJob;                  // per path: job index
+    int soleJob;                   // the wave's only job, or -1 (then read pathJob)
     float4* shadow;                // 4 float4 per next-event entry
     int* counts;                   // [0],[1] ray queues; [2] shadow queue; [3] error bits; [4],[5] fetch
     int* hostCount;                // pinned host word for queue-size polls
@@ -81,9 +82,10 @@ struct WaveProfile {
 // One wave: raygen over `units` (device), the bounce loop, and accumulation into
 // each job's sums. iters >= 0 runs that many bounce iterations; iters < 0 runs
 // until the ray queue drains (polled every 4 iterations). integrator: the one
-// integrator of all the wave's jobs, or -1 when they differ.
+// integrator of all the wave's jobs, or -1 when they differ; soleJob: the wave's
+// only job, or -1.
 cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
-                    int nPixelUnits, int iters, int integrator, const WaveBuffers& wb,
+                    int nPixelUnits, int iters, int integrator, int soleJob, const WaveBuffers& wb,
                     cudaStream_t stream, int* launches, WaveProfile* prof, int gridOverride = 0);
 // film = accum / spp for the listed jobs (device list of job indices).
 cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int maxPixels,

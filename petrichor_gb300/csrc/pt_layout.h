@@ -18,7 +18,7 @@
 //                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) 0 0
 //              e1 = v1 - v0, e2 = v2 - v0 exactly as Triangle::Intersect forms
 //              them (Core/Geometry/Triangle.cpp:53-54).
-//   shade      3 x float4 per original triangle (48 B):
+//   shade      3 x float4 per primitive slot (48 B), in leaf order like tris:
 //                [0] n0.xyz material(bits) [1] n1.xyz smooth(bits) [2] n2.xyz 0
 //   lights     3 x float4 per light: [0] v0.xyz tri(bits) [1] e0.xyz 0 [2] e1.xyz 0
 //   env        float4 RGB_ texels, row-major (H x W). The importance-sampling row

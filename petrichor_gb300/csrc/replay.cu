@@ -37,8 +37,7 @@ __device__ void ReplaySimplePixel(const DevScene& S, const DevCamera& C, const D
                 contrib = contrib + ray.T * EnvColor<ExactMath>(S, ray.d);
                 break;
             }
-            const int tri = TriId(S.tris, k);
-            const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), s1.Next());
+            const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, k), s1.Next());
             if (IsEmission(S, m)) {
                 contrib = contrib + ray.T * MatColor(S.mats[m]);
                 break;
@@ -104,9 +103,7 @@ __device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1
         float d;
         const int k = TraverseReference(S, p, ld, 0.0f, kFltMax, d, stack, status);
         if (k >= 0) {
-            const int tri = TriId(S.tris, k);
-            if (IsEmission(S, ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)),
-                                              s1.Next()))) {
+            if (IsEmission(S, ResolveMaterial(S.mats, SlotMaterial(S.shade, k), s1.Next()))) {
                 const Shading sl = Interpolate(S, k, p, ld, d);
                 const float dist = SqLen(pl - sl.pos);
                 if (fabsf(dist - 0.0f) < kEps) {

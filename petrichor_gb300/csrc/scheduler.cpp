@@ -64,6 +64,12 @@ int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
     return integ < 0 ? -1 : integ;
 }
 
+int WaveSoleJob(const std::vector<WaveUnit>& units) {
+    for (const WaveUnit& u : units)
+        if (u.job != units.front().job) return -1;
+    return units.empty() ? -1 : units.front().job;
+}
+
 cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, const WaveBuffers& wb,
                        int cap, cudaStream_t stream, int* launches, WaveProfile* prof) {
     std::vector<std::vector<WaveUnit>> waves;
@@ -94,7 +100,7 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
             pixels += P;
         }
         e = RunWave(T.jobs, T.units, (int)units.size(), paths, pixels, WaveIterations(jobs, units),
-                    WaveIntegrator(jobs, units), wb, stream, launches, prof);
+                    WaveIntegrator(jobs, units), WaveSoleJob(units), wb, stream, launches, prof);
         if (e != cudaSuccess) return e;
         std::vector<int> done;
         int maxPx = 0;

@@ -34,5 +34,7 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& tables
 int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
 // The integrator shared by all of a wave's jobs, or -1 when they differ.
 int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
+// The job of all of a wave's units, or -1 when they belong to several.
+int WaveSoleJob(const std::vector<WaveUnit>& units);
 
 }  // namespace ptg

@@ -374,8 +374,8 @@ private:
                                 cudaMemcpyHostToDevice, stream_);
         if (e == cudaSuccess)
             e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, (int)units.size(), paths, pixels,
-                        WaveIterations(slotJobs_, units), WaveIntegrator(slotJobs_, units), wb_,
-                        stream_, launches, nullptr);
+                        WaveIterations(slotJobs_, units), WaveIntegrator(slotJobs_, units),
+                        WaveSoleJob(units), wb_, stream_, launches, nullptr);
         if (e == cudaSuccess && !w->finishing.empty()) {
             std::vector<int> slots;
             int maxPx = 0;

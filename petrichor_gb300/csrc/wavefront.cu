@@ -320,14 +320,19 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
     }
 }
 
+__device__ __forceinline__ int JobOf(const int* __restrict__ pathJob, int soleJob, int path) {
+    return soleJob >= 0 ? soleJob : pathJob[path];
+}
+
 struct ExtendQueue {
     const DevJob* jobs;
     const int* pathJob;
+    int soleJob;
     const float4* rays;
     float2* hit;
     __device__ void Load(int i, LaneRay& r) const {
         const float4 a = rays[2 * i], b = rays[2 * i + 1];
-        const DevJob& J = jobs[pathJob[__float_as_int(a.w)]];
+        const DevJob& J = jobs[JobOf(pathJob, soleJob, __float_as_int(a.w))];
         r.o = V3(a.x, a.y, a.z);
         r.d = V3(b.x, b.y, b.z);
         // SimplePathTracing intersects with distMin = kEps, PathTracing with 0
@@ -354,7 +359,7 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const D
         wb.counts[5] = 0;  // the shadow kernel that follows fetches from zero
     }
     int err = 0;
-    ExtendQueue q{jobs, wb.pathJob, wb.ray[cur], wb.hit};
+    ExtendQueue q{jobs, wb.pathJob, wb.soleJob, wb.ray[cur], wb.hit};
     TraceQueue(q, n, wb.counts + 4, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
@@ -370,7 +375,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
         const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
         const float2 h = wb.hit[i];
         const int path = __float_as_int(ra.w);
-        const DevJob& J = jobs[wb.pathJob[path]];
+        const DevJob& J = jobs[JobOf(wb.pathJob, wb.soleJob, path)];
         const DevScene& S = J.S;
         const DevSettings& st = J.st;
         const V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
@@ -399,8 +404,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
             if (slot < 0) {
                 L = L + in.T * EnvColor<FastMath>(S, d);
             } else {
-                const int tri = TriId(S.tris, slot);
-                const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), rng.Next());
+                const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, slot), rng.Next());
                 if (S.mats[m].kind == kEmission) {
                     L = L + in.T * MatColor(S.mats[m]);
                 } else {
@@ -538,11 +542,12 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
 struct ShadowQueue {
     const DevJob* jobs;
     const int* pathJob;
+    int soleJob;
     const float4* entries;
     float4* pathL;
     __device__ void Load(int j, LaneRay& r) const {
         const float4 e0 = entries[4 * j], e1 = entries[4 * j + 1];
-        const DevScene& S = jobs[pathJob[__float_as_int(e1.w) & 0x7FFFFFFF]].S;
+        const DevScene& S = jobs[JobOf(pathJob, soleJob, __float_as_int(e1.w) & 0x7FFFFFFF)].S;
         r.nodes = S.numWide > 0 ? S.wide : nullptr;
         r.tris = S.tris;
         r.o = V3(e0.x, e0.y, e0.z);
@@ -568,11 +573,10 @@ struct ShadowQueue {
         }
         // area light: the closest hit must be an emitter at the sampled point
         if (r.best < 0) return;
-        const DevScene& S = jobs[pathJob[path]].S;
+        const DevScene& S = jobs[JobOf(pathJob, soleJob, path)].S;
         const float4 e0 = entries[4 * j];
-        const int tri = TriId(S.tris, r.best);
         const float4 e2 = entries[4 * j + 2], e3 = entries[4 * j + 3];
-        const int m = ResolveMaterial(S.mats, __float_as_int(__ldg(&S.shade[3 * tri].w)), e3.w);
+        const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, r.best), e3.w);
         if (S.mats[m].kind != kEmission) return;
         const Shading sl = Interpolate(S, r.best, r.o, r.d, r.tBest);
         const V3 pl = r.o + r.d * e0.w;
@@ -600,7 +604,7 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ShadowKernel(const D
     const int n = wb.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // next extend fetches from zero
     int err = 0;
-    ShadowQueue q{jobs, wb.pathJob, wb.shadow, wb.pathL};
+    ShadowQueue q{jobs, wb.pathJob, wb.soleJob, wb.shadow, wb.pathL};
     TraceQueue(q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
@@ -767,6 +771,7 @@ WaveBuffers CarveWaveBuffers(void* base, int capacity) {
     w.hit = (float2*)take(C * sizeof(float2));
     w.pathL = (float4*)take(C * sizeof(float4));
     w.pathJob = (int*)take(C * sizeof(int));
+    w.soleJob = -1;
     w.shadow = (float4*)take(C * 4 * sizeof(float4));
     w.counts = (int*)take(16 * sizeof(int));
     return w;
@@ -803,8 +808,11 @@ static int ShadeGrid(int traceGrid) {
 }
 
 cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
-                    int nPixelUnits, int iters, int integrator, const WaveBuffers& wb,
-                    cudaStream_t stream, int* launches, WaveProfile* prof, int gridOverride) {
+                    int nPixelUnits, int iters, int integrator, int soleJob,
+                    const WaveBuffers& wave, cudaStream_t stream, int* launches, WaveProfile* prof,
+                    int gridOverride) {
+    WaveBuffers wb = wave;
+    wb.soleJob = soleJob;
     if (nPaths <= 0) return cudaSuccess;
     if (nPaths > wb.capacity) return cudaErrorInvalidValue;
     const int grid = gridOverride > 0 ? gridOverride : DefaultStageGrid();
