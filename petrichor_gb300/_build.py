@@ -63,7 +63,7 @@ def build(force: bool = False, verbose: bool = False, defines=()) -> str:
     for s in CPP_SOURCES:
         o = os.path.join(OBJ_DIR, s + ".o")
         jobs.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
-                     "-pthread", "-Wall", *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c",
+                     "-pthread", "-Wall", *[f"-D{d}" for d in defines], *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c",
                      os.path.join(CSRC, s), "-o", o])
 
     def run(cmd):

@@ -156,9 +156,9 @@ int SetDevice(pt_context* ctx) {
     return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "cudaSetDevice");
 }
 
-// Paths per wave: the whole image x spp when it fits in kMaxWavePaths (about 13 GB
-// of wave state), otherwise as many full sample blocks as fit. HBM holds this
-// easily; fewer, larger waves mean fewer sparse late-bounce launches.
+// Paths per wave: the whole image x spp when it fits in kMaxWavePaths (236 B of
+// wave state per path), otherwise as many full sample blocks as fit. HBM holds
+// this easily; fewer, larger waves mean fewer sparse late-bounce launches.
 int WaveCapacity(const pt_settings* st) {
     const int64_t px = (int64_t)st->width * st->height;
     int64_t cap = std::min<int64_t>(px * st->spp, kMaxWavePaths);

@@ -31,7 +31,11 @@ struct SceneGpu {
 class Server;  // server.cpp
 
 // Paths per wave: the whole image x spp when it fits, otherwise full sample blocks.
-constexpr int64_t kMaxWavePaths = int64_t(1) << 26;
+// 2^27 paths hold a 1920x1080 frame at 64 spp in one wave (about 32 GB of state).
+#ifndef PT_MAX_WAVE_LOG2
+#define PT_MAX_WAVE_LOG2 27
+#endif
+constexpr int64_t kMaxWavePaths = int64_t(1) << PT_MAX_WAVE_LOG2;
 constexpr int kMaxJobsPerCall = 4096;
 constexpr int kMaxUnitsPerWave = 8192;
 
