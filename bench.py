@@ -456,8 +456,8 @@ def main():
         with open(peaks_path) as fh:
             peak, peak_src = float(json.load(fh)["hbm_gbs"]), "measured"
     traffic = None
-    tp = os.path.join(HERE, "profiles", "extend_kernel_traffic.json")
-    if os.path.exists(tp):
+    tp = os.path.join(HERE, "profiles", "extend_kernel_traffic_spheres_grids_1M_1080p_64spp.json")
+    if os.path.exists(tp) and workload_name(args) == WORKLOAD:  # measured on this workload only
         with open(tp) as fh:
             t = json.load(fh)
         traffic = t["dram_bytes_per_ray"] * prof2["extend_rays"] / ext_launches
