@@ -27,6 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 WORKLOAD = "spheres_grids_1M_1080p_64spp_pt16"
+STRESS_WORKLOAD = "terrain_rocks_20M_2160p_256spp_pt12"
 METRIC = "render_msamples_per_s"
 UNIT = "Msamples/s"
 
@@ -43,6 +44,8 @@ def parse():
     ap.add_argument("--width", type=int, default=0, help="override (profiling runs only)")
     ap.add_argument("--height", type=int, default=0, help="override (profiling runs only)")
     ap.add_argument("--spp", type=int, default=0, help="override (profiling runs only)")
+    ap.add_argument("--stress", action="store_true",
+                    help="memory-bound stress scene: 20M triangles, 3840x2160, 256 spp, 8192x4096 env")
     ap.add_argument("--batch", action="store_true",
                     help="batched uneven instances: 64 scenes in shared waves vs 64 plain launches")
     ap.add_argument("--serve", action="store_true",
@@ -55,7 +58,9 @@ def parse():
 def make_scene(args):
     import dataclasses
     from petrichor_gb300 import synth
-    if args.small:
+    if args.stress:
+        sc = synth.terrain_rocks()  # 20M tris, 3840x2160, 256 spp, 12 bounces, 8192x4096 env
+    elif args.small:
         sc = synth.spheres_grids(tri_budget=100_000, width=480, height=270, spp=16, max_bounces=16,
                                  env_width=512, env_height=256)
     else:
@@ -67,7 +72,10 @@ def make_scene(args):
 
 
 def workload_name(args):
-    name = WORKLOAD + ("_SMALL" if args.small else "")
+    if args.stress:
+        name = STRESS_WORKLOAD
+    else:
+        name = WORKLOAD + ("_SMALL" if args.small else "")
     if args.width or args.height or args.spp:
         name += "_OVERRIDE"
     return name
@@ -230,12 +238,27 @@ def run_batch(args):
     def run_batched():
         ctx.batch_render([(sid, cam, st, f.data_ptr()) for sid, cam, st, f in jobs], stream.cuda_stream)
 
+    # autotuned launch configuration (grid, pixel bands, graph replay), probed on the
+    # job with the most samples; both arms then run with it
+    t0 = time.perf_counter()
+    big = max(jobs, key=lambda j: j[2].width * j[2].height * j[2].spp)
+    tuning = ctx.autotune(big[0], big[1], big[2], probe_spp=4).as_dict()
+    tune_s = time.perf_counter() - t0
+
+    def run_batched_ungraphed():
+        t = ctx.get_tuning()
+        ctx.set_tuning(t.wave_paths, t.blocks_per_sm, t.band_rows, 0)
+        run_batched()
+        torch.cuda.synchronize()
+        ctx.set_tuning(t.wave_paths, t.blocks_per_sm, t.band_rows, t.use_graphs)
+
     for _ in range(max(1, args.warmup)):
         run_plain()
         run_batched()
     torch.cuda.synchronize()
     res = {}
-    for name, fn in (("plain", run_plain), ("batched", run_batched)):
+    for name, fn in (("plain", run_plain), ("batched", run_batched),
+                     ("batched_without_graphs", run_batched_ungraphed)):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         launches0 = ctx.stats().kernel_launches
         e0.record(stream)
@@ -254,8 +277,10 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batch_64_uneven_spheres_grids", "scenes": len(scenes),
                    "triangles_total": tris, "samples_per_batch": samples,
-                   "scene_gen_s": round(gen_s, 1), "upload_s": round(upload_s, 1)},
+                   "scene_gen_s": round(gen_s, 1), "upload_s": round(upload_s, 1),
+                   "autotuned": tuning, "autotune_s": round(tune_s, 2)},
         "plain_sequential": res["plain"], "batched": res["batched"],
+        "batched_without_graphs": res["batched_without_graphs"],
         "speedup_vs_plain": res["batched"]["msamples_per_s"] / res["plain"]["msamples_per_s"],
         "films_identical_to_plain": bool(same),
     }))

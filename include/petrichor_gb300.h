@@ -203,7 +203,7 @@ int pt_batch_render(pt_context* ctx, int32_t n, const pt_job* jobs, void* stream
 #define PT_REQ_FAILED 4
 
 typedef struct pt_serve_config {
-  int32_t wave_paths;     /* paths per wave (0: 8M) */
+  int32_t wave_paths;     /* paths per wave (0: 32M) */
   int32_t max_active;     /* requests admitted at once (0: 256) */
   uint64_t state_budget;  /* device bytes for per-request state: sums + film staging (0: 4 GiB) */
 } pt_serve_config;
@@ -258,6 +258,26 @@ typedef struct pt_profile {
 int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
                       const pt_settings* settings, float* film_rgb_device, int32_t count_reference,
                       pt_profile* out);
+
+/* Launch configuration of the wavefront path: what the batch autotuner picks. Every
+ * configuration gives the same films; only speed differs. Zero fields keep the
+ * defaults. No reference counterpart (the reference's only knobs are tile size and
+ * thread count, RenderSetting.h:10-21). */
+typedef struct pt_tuning {
+  int32_t wave_paths;    /* paths per wave (0: the whole job, up to 2^27) */
+  int32_t blocks_per_sm; /* stage kernel grid, blocks of 128 threads per SM (0: occupancy) */
+  int32_t band_rows;     /* rows per pixel band of the path order (0: 8) */
+  int32_t use_graphs;    /* 1: replay each wave's stage sequence from a captured CUDA graph */
+  double probe_ms;       /* pt_autotune: probe render time of the chosen configuration */
+} pt_tuning;
+/* Times candidate grids, pixel bands and graph replay on probe renders of one job
+ * (its scene, camera and settings in wavefront mode, spp reduced to probe_spp; 0:
+ * min(spp, 4)), then keeps the fastest for the context's later wavefront renders,
+ * batches and servers. Synchronous; writes the choice to *out when not NULL. */
+int pt_autotune(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+                const pt_settings* settings, int32_t probe_spp, pt_tuning* out);
+int pt_set_tuning(pt_context* ctx, const pt_tuning* tuning);
+int pt_get_tuning(pt_context* ctx, pt_tuning* out);
 
 /* Replay render that allocates no device memory: for callers that cannot call
  * cudaMalloc while rendering (another allocator owns the device memory, or the

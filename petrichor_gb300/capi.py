@@ -103,6 +103,15 @@ class PtProfile(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PtTuning(ctypes.Structure):
+    _fields_ = [("wave_paths", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("band_rows", ctypes.c_int32), ("use_graphs", ctypes.c_int32),
+                ("probe_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every symbol declared in include/petrichor_gb300.h (checked by the CPU tests).
 EXPORTED = [
     "pt_abi_version", "pt_status_string", "pt_context_create", "pt_context_destroy",
@@ -110,7 +119,7 @@ EXPORTED = [
     "pt_scene_info_get", "pt_render", "pt_render_device", "pt_trace_closest", "pt_get_stats",
     "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc", "pt_batch_render",
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
-    "pt_serve_release", "pt_serve_stop",
+    "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
 ]
 
 _lib = None
@@ -164,6 +173,10 @@ def load(build: bool = True):
     L.pt_render_profile.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
                                     vp, i32, ctypes.POINTER(PtProfile)]
     L.pt_get_progress.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.pt_autotune.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings), i32,
+                              ctypes.POINTER(PtTuning)]
+    L.pt_set_tuning.argtypes = [vp, ctypes.POINTER(PtTuning)]
+    L.pt_get_tuning.argtypes = [vp, ctypes.POINTER(PtTuning)]
     L.pt_bvh_build.argtypes = [vp, u32, vp, u32, i32, ctypes.POINTER(u32), ctypes.POINTER(u32),
                                vp, vp, vp]
     _lib = L
@@ -361,6 +374,22 @@ class Context:
                                              film_ptr, 1 if count_reference else 0, ctypes.byref(p)),
                     "pt_render_profile")
         return p
+
+    def autotune(self, sid: int, camera: PtCamera, settings: PtSettings, probe_spp: int = 0) -> PtTuning:
+        t = PtTuning()
+        self._check(self.L.pt_autotune(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
+                                       probe_spp, ctypes.byref(t)), "pt_autotune")
+        return t
+
+    def set_tuning(self, wave_paths: int = 0, blocks_per_sm: int = 0, band_rows: int = 0,
+                   use_graphs: int = 1):
+        t = PtTuning(wave_paths, blocks_per_sm, band_rows, use_graphs, 0.0)
+        self._check(self.L.pt_set_tuning(self.h, ctypes.byref(t)), "pt_set_tuning")
+
+    def get_tuning(self) -> PtTuning:
+        t = PtTuning()
+        self._check(self.L.pt_get_tuning(self.h, ctypes.byref(t)), "pt_get_tuning")
+        return t
 
     def trace_closest(self, sid: int, n: int, rays_ptr: int, dist_min: float, dist_max: float,
                       tri_ptr: int, dist_ptr: int, stream_ptr: int = 0):

@@ -159,14 +159,20 @@ int SetDevice(pt_context* ctx) {
 // Paths per wave: the whole image x spp when it fits in kMaxWavePaths (236 B of
 // wave state per path), otherwise as many full sample blocks as fit. HBM holds
 // this easily; fewer, larger waves mean fewer sparse late-bounce launches.
-int WaveCapacity(const pt_settings* st) {
+int WaveCapacity(const pt_context* ctx, const pt_settings* st) {
     const int64_t px = (int64_t)st->width * st->height;
     int64_t cap = std::min<int64_t>(px * st->spp, kMaxWavePaths);
     cap = std::max<int64_t>(cap, std::min<int64_t>(px, kMaxWavePaths));
-    if (st->wave_paths > 0) cap = std::min<int64_t>(cap, std::max<int64_t>(st->wave_paths, px));
+    const int64_t limit = st->wave_paths > 0 ? st->wave_paths : ctx->tunedWavePaths;
+    if (limit > 0) cap = std::min<int64_t>(cap, std::max<int64_t>(limit, px));
     return (int)std::max<int64_t>(cap, 1);
 }
 
+
+WaveGraphCache* Graphs(pt_context* ctx) {
+    if (!ctx->graphs) ctx->graphs = NewWaveGraphCache();
+    return ctx->graphs;
+}
 
 int EnsureWaveBuffers(pt_context* ctx, int capacity) {
     if (ctx->wbCapacity >= capacity) return PT_OK;
@@ -281,7 +287,7 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
             if (e != cudaSuccess) return CudaFail(ctx, e, "replay launch");
         }
     } else {
-        const int cap = WaveCapacity(st);
+        const int cap = WaveCapacity(ctx, st);
         int rc = EnsureWaveBuffers(ctx, cap);
         if (rc != PT_OK) return rc;
         if ((rc = EnsureTables(ctx, 1, (size_t)st->width * st->height)) != PT_OK) return rc;
@@ -291,7 +297,8 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
         job.st = S;
         job.accum = (float4*)ctx->accum.ptr;
         job.film = dFilm;
-        e = RenderJobs({job}, Tables(ctx), ctx->wb, cap, stream, &launches, nullptr);
+        e = RenderJobs({job}, Tables(ctx), ctx->wb, cap, stream, &launches, nullptr, ctx->tuning,
+                       Graphs(ctx));
         if (e != cudaSuccess) return CudaFail(ctx, e, "wavefront render");
     }
     e = cudaEventRecord(ctx->ev1, stream);
@@ -377,6 +384,8 @@ int pt_context_destroy(pt_context* ctx) {
         Free(ctx, ctx->unitTable);
         Free(ctx, ctx->jobList);
         Free(ctx, ctx->accum);
+        FreeWaveGraphCache(ctx->graphs);
+        ctx->graphs = nullptr;
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
         if (ctx->ev1) cudaEventDestroy(ctx->ev1);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -598,6 +607,95 @@ int pt_render_device(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     return RenderOnStream(ctx, *sg, cam, st, dFilm, s);
 }
 
+int pt_set_tuning(pt_context* ctx, const pt_tuning* t) {
+    if (!ctx || !t) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (t->wave_paths < 0 || t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->band_rows < 0 ||
+        t->band_rows > 4096 || (t->use_graphs != 0 && t->use_graphs != 1))
+        return Fail(ctx, PT_ERR_INVALID_ARG, "bad tuning");
+    ctx->tunedWavePaths = t->wave_paths;
+    ctx->tuning.blocksPerSm = t->blocks_per_sm;
+    ctx->tuning.band = t->band_rows;
+    ctx->tuning.graphs = t->use_graphs;
+    return PT_OK;
+}
+
+int pt_get_tuning(pt_context* ctx, pt_tuning* out) {
+    if (!ctx || !out) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    out->wave_paths = ctx->tunedWavePaths;
+    out->blocks_per_sm = ctx->tuning.blocksPerSm;
+    out->band_rows = ctx->tuning.band;
+    out->use_graphs = ctx->tuning.graphs;
+    out->probe_ms = ctx->tunedProbeMs;
+    return PT_OK;
+}
+
+// Coordinate descent over the launch configuration: each knob in turn takes the
+// value with the shortest probe render (best of two timed runs after one warm-up,
+// which also captures the graphs), the others held at their current best.
+int pt_autotune(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
+                int32_t probeSpp, pt_tuning* out) {
+    if (!ctx || probeSpp < 0) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    pt_settings ps = *st;
+    ps.mode = PT_MODE_WAVEFRONT;
+    ps.spp = probeSpp > 0 ? probeSpp : std::min(st->spp, 4);
+    ps.wave_paths = 0;
+    const size_t bytes = (size_t)ps.width * ps.height * 3 * sizeof(float);
+    if ((rc = Alloc(ctx, ctx->film, bytes)) != PT_OK) return rc;
+    auto probe = [&](const WaveTuning& t, double* ms) {
+        ctx->tuning = t;
+        *ms = 1e300;
+        for (int r = 0; r < 3; r++) {
+            int k = RenderOnStream(ctx, *sg, cam, &ps, (float*)ctx->film.ptr, ctx->stream);
+            if (k == PT_OK) k = FinishStats(ctx, ctx->stream);
+            if (k != PT_OK) return k;
+            if (r > 0) *ms = std::min(*ms, ctx->stats.last_render_ms);
+        }
+        return PT_OK;
+    };
+    WaveTuning best = ctx->tuning;
+    double bestMs = 0.0;
+    if ((rc = probe(best, &bestMs)) != PT_OK) return rc;
+    const int grids[] = {0, 4, 12, 16, 24};
+    const int bands[] = {8, 4, 16, 32};
+    const int graphs[] = {1, 0};
+    for (int knob = 0; knob < 3; knob++) {
+        const int* vals = knob == 0 ? grids : knob == 1 ? bands : graphs;
+        const int nv = knob == 0 ? 5 : knob == 1 ? 4 : 2;
+        for (int i = 0; i < nv; i++) {
+            WaveTuning t = best;
+            int& field = knob == 0 ? t.blocksPerSm : knob == 1 ? t.band : t.graphs;
+            if (field == vals[i]) continue;
+            field = vals[i];
+            double ms = 0.0;
+            if ((rc = probe(t, &ms)) != PT_OK) {
+                ctx->tuning = best;
+                return rc;
+            }
+            if (ms < bestMs) {
+                bestMs = ms;
+                best = t;
+            }
+        }
+    }
+    ctx->tuning = best;
+    ctx->tunedProbeMs = bestMs;
+    if (out) {
+        out->wave_paths = ctx->tunedWavePaths;
+        out->blocks_per_sm = best.blocksPerSm;
+        out->band_rows = best.band;
+        out->use_graphs = best.graphs;
+        out->probe_ms = bestMs;
+    }
+    return PT_OK;
+}
+
 int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
                       const pt_settings* st, float* dFilm, int32_t countReference, pt_profile* out) {
     if (!ctx || !out) return PT_ERR_INVALID_ARG;
@@ -609,7 +707,7 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     if (st->mode != PT_MODE_WAVEFRONT)
         return Fail(ctx, PT_ERR_UNSUPPORTED, "profiling covers the wavefront mode");
     if ((rc = SetDevice(ctx)) != PT_OK) return rc;
-    const int cap = WaveCapacity(st);
+    const int cap = WaveCapacity(ctx, st);
     if ((rc = EnsureWaveBuffers(ctx, cap)) != PT_OK) return rc;
     if ((rc = EnsureTables(ctx, 1, (size_t)st->width * st->height)) != PT_OK) return rc;
     DeviceBuffer counters;
@@ -625,7 +723,8 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     job.st = ToDev(st);
     job.accum = (float4*)ctx->accum.ptr;
     job.film = dFilm;
-    cudaError_t e = RenderJobs({job}, Tables(ctx), ctx->wb, cap, ctx->stream, &launches, &prof);
+    cudaError_t e =
+      RenderJobs({job}, Tables(ctx), ctx->wb, cap, ctx->stream, &launches, &prof, ctx->tuning, nullptr);
     if (e == cudaSuccess) e = CollectProfile(&prof, ctx->stream);
     Free(ctx, counters);
     if (e != cudaSuccess) return CudaFail(ctx, e, "profiled render");
@@ -684,7 +783,8 @@ int pt_batch_render(pt_context* ctx, int32_t n, const pt_job* jobs, void* stream
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     int launches = 0;
     cudaError_t e = cudaEventRecord(ctx->ev0, s);
-    if (e == cudaSuccess) e = RenderJobs(dj, Tables(ctx), ctx->wb, cap, s, &launches, nullptr);
+    if (e == cudaSuccess)
+        e = RenderJobs(dj, Tables(ctx), ctx->wb, cap, s, &launches, nullptr, ctx->tuning, Graphs(ctx));
     if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, s);
     if (e != cudaSuccess) return CudaFail(ctx, e, "batched render");
     ctx->stats.kernel_launches += launches;

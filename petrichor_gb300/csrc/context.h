@@ -58,6 +58,11 @@ struct pt_context {
     ptg::DeviceBuffer film, stack, status;
     // wavefront job tables and per-job running sums
     ptg::DeviceBuffer jobTable, unitTable, jobList, accum;
+    // launch configuration (pt_autotune / pt_set_tuning) and captured wave sequences
+    ptg::WaveTuning tuning{};
+    int tunedWavePaths = 0;  // 0: the automatic wave size
+    double tunedProbeMs = 0.0;
+    ptg::WaveGraphCache* graphs = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_stats stats{};
     uint32_t tilesDone = 0, tilesTotal = 0;

@@ -45,6 +45,15 @@ struct WaveUnit {
     int32_t pixelBase, pad[3];
 };
 
+// Scalars of the wave being run, read by the kernels from device memory so that
+// one captured launch sequence serves every wave of the same shape.
+struct WaveDesc {
+    int32_t nUnits, nPaths, nPixelUnits;
+    int32_t soleJob;  // the wave's only job, or -1 (then read pathJob)
+    int32_t band;     // rows per pixel band of the path order
+    int32_t pad[3];
+};
+
 // Path state travels with its ray through the compacted queues (so the shade
 // stage reads and writes it in queue order); only the radiance sum stays per
 // path (written at termination and by next-event rays).
@@ -57,7 +66,7 @@ struct WaveBuffers {
     float2* hit;                   // per entry of the current queue: {t, slot} (slot < 0: miss)
     float4* pathL;                 // per path: {L.xyz, flags}
     int* pathJob;                  // per path: job index
-    int soleJob;                   // the wave's only job, or -1 (then read pathJob)
+    struct WaveDesc* desc;         // the current wave's scalars (device)
     float4* shadow;                // 4 float4 per next-event entry
     int* counts;                   // [0],[1] ray queues; [2] shadow queue; [3] error bits; [4],[5] fetch
     int* hostCount;                // pinned host word for queue-size polls
@@ -79,14 +88,30 @@ struct WaveProfile {
     void* events = nullptr;                     // internal
 };
 
+// What one wave runs. iters >= 0: that many bounce iterations; iters < 0: until
+// the ray queue drains (polled every 4 iterations). integrator: the one integrator
+// of all the wave's jobs, or -1 when they differ; soleJob: the wave's only job, or -1.
+struct WaveShape {
+    int nUnits = 0, nPaths = 0, nPixelUnits = 0;
+    int iters = 0, integrator = -1, soleJob = -1;
+};
+// Launch configuration (all choices give the same films). 0 = default.
+struct WaveTuning {
+    int blocksPerSm = 0;  // stage grid: blocks of 128 threads per SM (0: occupancy of the trace kernels)
+    int band = 0;         // rows per pixel band of the path order (0: 8)
+    int graphs = 1;       // replay each wave's stage sequence from a captured CUDA graph
+};
+// Captured stage sequences, keyed by wave shape and buffers (owned by a context or server).
+struct WaveGraphCache;
+WaveGraphCache* NewWaveGraphCache();
+void FreeWaveGraphCache(WaveGraphCache* cache);
+
 // One wave: raygen over `units` (device), the bounce loop, and accumulation into
-// each job's sums. iters >= 0 runs that many bounce iterations; iters < 0 runs
-// until the ray queue drains (polled every 4 iterations). integrator: the one
-// integrator of all the wave's jobs, or -1 when they differ; soleJob: the wave's
-// only job, or -1.
-cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
-                    int nPixelUnits, int iters, int integrator, int soleJob, const WaveBuffers& wb,
-                    cudaStream_t stream, int* launches, WaveProfile* prof, int gridOverride = 0);
+// each job's sums. With a cache and no profile, the launches of each wave shape
+// are captured once into a CUDA graph and replayed.
+cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& shape,
+                    const WaveBuffers& wb, cudaStream_t stream, int* launches, WaveProfile* prof,
+                    const WaveTuning& tune, WaveGraphCache* graphs);
 // film = accum / spp for the listed jobs (device list of job indices).
 cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int maxPixels,
                          cudaStream_t stream, int* launches, WaveProfile* prof);
@@ -94,6 +119,7 @@ cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int 
 cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream);
 
 int DefaultStageGrid();
+int StageGrid(const WaveTuning& tune);
 
 // Closest-hit traversal of the throughput path for caller rays (o.xyz, d.xyz per ray).
 // fetchCounter: one device int of scratch for the persistent fetch.

@@ -71,7 +71,8 @@ int WaveSoleJob(const std::vector<WaveUnit>& units) {
 }
 
 cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, const WaveBuffers& wb,
-                       int cap, cudaStream_t stream, int* launches, WaveProfile* prof) {
+                       int cap, cudaStream_t stream, int* launches, WaveProfile* prof,
+                       const WaveTuning& tune, WaveGraphCache* graphs) {
     std::vector<std::vector<WaveUnit>> waves;
     if (!PlanWaves(jobs, std::min(cap, wb.capacity), T.maxUnits, &waves))
         return cudaErrorInvalidValue;
@@ -93,14 +94,17 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
         e = cudaMemcpyAsync(T.units, units.data(), units.size() * sizeof(WaveUnit),
                             cudaMemcpyHostToDevice, stream);
         if (e != cudaSuccess) return e;
-        int paths = 0, pixels = 0;
+        WaveShape shape;
         for (const WaveUnit& u : units) {
             const int P = jobs[u.job].st.width * jobs[u.job].st.height;
-            paths += P * u.sw;
-            pixels += P;
+            shape.nPaths += P * u.sw;
+            shape.nPixelUnits += P;
         }
-        e = RunWave(T.jobs, T.units, (int)units.size(), paths, pixels, WaveIterations(jobs, units),
-                    WaveIntegrator(jobs, units), WaveSoleJob(units), wb, stream, launches, prof);
+        shape.nUnits = (int)units.size();
+        shape.iters = WaveIterations(jobs, units);
+        shape.integrator = WaveIntegrator(jobs, units);
+        shape.soleJob = WaveSoleJob(units);
+        e = RunWave(T.jobs, T.units, shape, wb, stream, launches, prof, tune, graphs);
         if (e != cudaSuccess) return e;
         std::vector<int> done;
         int maxPx = 0;

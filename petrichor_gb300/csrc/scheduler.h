@@ -27,7 +27,8 @@ bool PlanWaves(const std::vector<DevJob>& jobs, int waveCapacity, int maxUnits,
 // only for SimplePathTracing queue polls).
 cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& tables,
                        const WaveBuffers& wb, int waveCapacity, cudaStream_t stream, int* launches,
-                       WaveProfile* prof);
+                       WaveProfile* prof, const WaveTuning& tune = WaveTuning{},
+                       WaveGraphCache* graphs = nullptr);
 
 // Bounce iterations a wave needs: maxBounces + 1 for PathTracing jobs; -1 (run
 // until the queue drains) when a SimplePathTracing job is present.

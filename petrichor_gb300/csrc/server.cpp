@@ -108,6 +108,8 @@ public:
             return rc;
         }
         alloc_.Reset(cfg_.state_budget);
+        tune_ = ctx_->tuning;
+        graphs_ = NewWaveGraphCache();
         slotJobs_.assign(cfg_.max_active, DevJob{});
         for (int s = cfg_.max_active - 1; s >= 0; s--) freeSlots_.push_back(s);
         t0_ = Clock::now();
@@ -260,6 +262,8 @@ private:
     }
 
     void FreeAll() {  // ctx->mu held
+        FreeWaveGraphCache(graphs_);
+        graphs_ = nullptr;
         for (auto& b : wbBufs_) Free(ctx_, b);
         wbBufs_.clear();
         if (wb_.hostCount) cudaFreeHost(wb_.hostCount);
@@ -372,10 +376,17 @@ private:
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(units_.ptr, units.data(), units.size() * sizeof(WaveUnit),
                                 cudaMemcpyHostToDevice, stream_);
-        if (e == cudaSuccess)
-            e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, (int)units.size(), paths, pixels,
-                        WaveIterations(slotJobs_, units), WaveIntegrator(slotJobs_, units),
-                        WaveSoleJob(units), wb_, stream_, launches, nullptr);
+        if (e == cudaSuccess) {
+            WaveShape shape;
+            shape.nUnits = (int)units.size();
+            shape.nPaths = paths;
+            shape.nPixelUnits = pixels;
+            shape.iters = WaveIterations(slotJobs_, units);
+            shape.integrator = WaveIntegrator(slotJobs_, units);
+            shape.soleJob = WaveSoleJob(units);
+            e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, shape, wb_, stream_, launches,
+                        nullptr, tune_, graphs_);
+        }
         if (e == cudaSuccess && !w->finishing.empty()) {
             std::vector<int> slots;
             int maxPx = 0;
@@ -471,6 +482,8 @@ private:
     DeviceBuffer arena_, jobTable_, units_, jobList_;
     std::vector<DeviceBuffer> wbBufs_;
     WaveBuffers wb_{};
+    WaveTuning tune_{};
+    WaveGraphCache* graphs_ = nullptr;
     std::vector<DevJob> slotJobs_;
     cudaStream_t stream_ = nullptr;
     Clock::time_point t0_;

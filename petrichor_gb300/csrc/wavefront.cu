@@ -37,12 +37,13 @@ namespace ptg {
 enum : int { kFlagNoSignCheck = 1 };
 enum : int { kShadowEnv = 0, kShadowArea = 1 };
 
-__device__ __forceinline__ void PixelOfIndex(int q, int W, int H, int& x, int& y) {
-    // 8-row bands, column-major inside a band: a warp covers a 4 x 8 pixel block
-    const int band = q / (8 * W);
-    const int y0 = band * 8;
-    const int hb = min(8, H - y0);
-    const int r = q - band * 8 * W;
+__device__ __forceinline__ void PixelOfIndex(int q, int W, int H, int rows, int& x, int& y) {
+    // bands of `rows` rows, column-major inside a band: with 8 rows a warp covers a
+    // 4 x 8 pixel block
+    const int band = q / (rows * W);
+    const int y0 = band * rows;
+    const int hb = min(rows, H - y0);
+    const int r = q - band * rows * W;
     x = r / hb;
     y = y0 + r % hb;
 }
@@ -292,7 +293,9 @@ __device__ __forceinline__ int FindUnit(const WaveUnit* __restrict__ units, int 
 }
 
 __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
-                             int nUnits, int n, WaveBuffers wb, int cur) {
+                             WaveBuffers wb, int cur) {
+    const WaveDesc wd = *wb.desc;
+    const int n = wd.nPaths, nUnits = wd.nUnits;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WaveUnit u = units[FindUnit(units, nUnits, i, false)];
         const DevJob& J = jobs[u.job];
@@ -300,7 +303,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         const int local = i - u.pathBase;
         const int q = local % P, s = u.s0 + local / P;
         int x, y;
-        PixelOfIndex(q, W, H, x, y);
+        PixelOfIndex(q, W, H, wd.band, x, y);
         PathRng rng(PathKey(J.st.seed, (uint32_t)(y * W + x), (uint32_t)s));
         float r0, r1, r2, r3;
         rng.Next(r0, r1);
@@ -359,7 +362,7 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const D
         wb.counts[5] = 0;  // the shadow kernel that follows fetches from zero
     }
     int err = 0;
-    ExtendQueue q{jobs, wb.pathJob, wb.soleJob, wb.ray[cur], wb.hit};
+    ExtendQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.ray[cur], wb.hit};
     TraceQueue(q, n, wb.counts + 4, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
@@ -371,11 +374,12 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                                                    int cur) {
     const int n = wb.counts[cur];
     const int nxt = cur ^ 1;
+    const int sole = wb.desc->soleJob;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
         const float2 h = wb.hit[i];
         const int path = __float_as_int(ra.w);
-        const DevJob& J = jobs[JobOf(wb.pathJob, wb.soleJob, path)];
+        const DevJob& J = jobs[JobOf(wb.pathJob, sole, path)];
         const DevScene& S = J.S;
         const DevSettings& st = J.st;
         const V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
@@ -604,20 +608,22 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ShadowKernel(const D
     const int n = wb.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // next extend fetches from zero
     int err = 0;
-    ShadowQueue q{jobs, wb.pathJob, wb.soleJob, wb.shadow, wb.pathL};
+    ShadowQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.shadow, wb.pathL};
     TraceQueue(q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, 1);
 }
 
 __global__ void AccumulateKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
-                                 int nUnits, int n, WaveBuffers wb) {
+                                 WaveBuffers wb) {
+    const WaveDesc wd = *wb.desc;
+    const int n = wd.nPixelUnits, nUnits = wd.nUnits;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WaveUnit u = units[FindUnit(units, nUnits, i, true)];
         const DevJob& J = jobs[u.job];
         const int W = J.st.width, H = J.st.height, P = W * H;
         const int q = i - u.pixelBase;
         int x, y;
-        PixelOfIndex(q, W, H, x, y);
+        PixelOfIndex(q, W, H, wd.band, x, y);
         const size_t pixel = (size_t)y * W + x;
         float4 acc = J.accum[pixel];
         for (int s = 0; s < u.sw; s++) {
@@ -742,38 +748,42 @@ struct StageEvents {
 }  // namespace
 
 namespace {
-// Buffers carved out of one allocation: {element bytes per path, count multiplier}.
+// Alignment of the buffers carved out of one allocation.
 constexpr size_t kAlign = 256;
 size_t Up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 }  // namespace
 
-size_t WaveBuffersBytes(int capacity) {
+// The one layout of the wave buffers: offsets from `base` (0 to measure the size).
+// Returns the bytes used; fills *w when given.
+static size_t LayOutWaveBuffers(uintptr_t base, int capacity, WaveBuffers* w) {
     const size_t C = (size_t)capacity;
-    return 2 * Up(C * 2 * sizeof(float4)) + 2 * Up(C * sizeof(float4)) + 2 * Up(C * sizeof(float4)) +
-           2 * Up(C * sizeof(unsigned long long)) + Up(C * sizeof(float2)) + Up(C * sizeof(float4)) +
-           Up(C * sizeof(int)) + Up(C * 4 * sizeof(float4)) + Up(16 * sizeof(int));
+    uintptr_t p = base;
+    auto take = [&](size_t bytes) {
+        const uintptr_t q = p;
+        p += Up(bytes);
+        return reinterpret_cast<void*>(q);
+    };
+    WaveBuffers v{};
+    v.capacity = capacity;
+    for (int k = 0; k < 2; k++) v.ray[k] = (float4*)take(C * 2 * sizeof(float4));
+    for (int k = 0; k < 2; k++) v.qs0[k] = (float4*)take(C * sizeof(float4));
+    for (int k = 0; k < 2; k++) v.qs1[k] = (float4*)take(C * sizeof(float4));
+    for (int k = 0; k < 2; k++) v.qrng[k] = (unsigned long long*)take(C * sizeof(unsigned long long));
+    v.hit = (float2*)take(C * sizeof(float2));
+    v.pathL = (float4*)take(C * sizeof(float4));
+    v.pathJob = (int*)take(C * sizeof(int));
+    v.desc = (WaveDesc*)take(sizeof(WaveDesc));
+    v.shadow = (float4*)take(C * 4 * sizeof(float4));
+    v.counts = (int*)take(16 * sizeof(int));
+    if (w) *w = v;
+    return (size_t)(p - base);
 }
 
+size_t WaveBuffersBytes(int capacity) { return LayOutWaveBuffers(0, capacity, nullptr); }
+
 WaveBuffers CarveWaveBuffers(void* base, int capacity) {
-    const size_t C = (size_t)capacity;
-    char* p = static_cast<char*>(base);
-    auto take = [&](size_t bytes) {
-        char* q = p;
-        p += Up(bytes);
-        return q;
-    };
     WaveBuffers w{};
-    w.capacity = capacity;
-    for (int k = 0; k < 2; k++) w.ray[k] = (float4*)take(C * 2 * sizeof(float4));
-    for (int k = 0; k < 2; k++) w.qs0[k] = (float4*)take(C * sizeof(float4));
-    for (int k = 0; k < 2; k++) w.qs1[k] = (float4*)take(C * sizeof(float4));
-    for (int k = 0; k < 2; k++) w.qrng[k] = (unsigned long long*)take(C * sizeof(unsigned long long));
-    w.hit = (float2*)take(C * sizeof(float2));
-    w.pathL = (float4*)take(C * sizeof(float4));
-    w.pathJob = (int*)take(C * sizeof(int));
-    w.soleJob = -1;
-    w.shadow = (float4*)take(C * 4 * sizeof(float4));
-    w.counts = (int*)take(16 * sizeof(int));
+    LayOutWaveBuffers(reinterpret_cast<uintptr_t>(base), capacity, &w);
     return w;
 }
 
@@ -795,44 +805,31 @@ int DefaultStageGrid() {
 #ifndef PT_SHADE_BLOCKS_PER_SM
 #define PT_SHADE_BLOCKS_PER_SM 0
 #endif
-static int ShadeGrid(int traceGrid) {
-    if (PT_SHADE_BLOCKS_PER_SM <= 0) return traceGrid;
-    static int grid = 0;
-    if (grid == 0) {
-        int dev = 0, sms = 0;
+static int SmCount() {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = sms * PT_SHADE_BLOCKS_PER_SM;
     }
-    return grid;
+    return sms;
+}
+static int ShadeGrid(int traceGrid) {
+    return PT_SHADE_BLOCKS_PER_SM > 0 ? SmCount() * PT_SHADE_BLOCKS_PER_SM : traceGrid;
 }
 
-cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int nPaths,
-                    int nPixelUnits, int iters, int integrator, int soleJob,
-                    const WaveBuffers& wave, cudaStream_t stream, int* launches, WaveProfile* prof,
-                    int gridOverride) {
-    WaveBuffers wb = wave;
-    wb.soleJob = soleJob;
-    if (nPaths <= 0) return cudaSuccess;
-    if (nPaths > wb.capacity) return cudaErrorInvalidValue;
-    const int grid = gridOverride > 0 ? gridOverride : DefaultStageGrid();
-    const int block = 128;
+int StageGrid(const WaveTuning& tune) {
+    return tune.blocksPerSm > 0 ? SmCount() * tune.blocksPerSm : DefaultStageGrid();
+}
+
+// The bounce iterations [it0, it0 + count) of a wave (queue parity from it0).
+static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integrator, int grid,
+                          int it0, int count, cudaStream_t stream, WaveProfile* prof, int* nl) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
-    int nl = 0;
-    cudaError_t e = cudaSuccess;
-    if (ev) ev->Begin(0, stream);
-    RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, nUnits, nPaths, wb, 0);
-    if (ev) ev->End(0, stream);
-    nl++;
-    int cur = 0;
-    for (int it = 0;; it++) {
-        if (iters >= 0 && it >= iters) break;
-        if (iters < 0 && it > 0 && it % 4 == 0) {
-            cudaMemcpyAsync(wb.hostCount, wb.counts + cur, sizeof(int), cudaMemcpyDeviceToHost, stream);
-            e = cudaStreamSynchronize(stream);
-            if (e != cudaSuccess) break;
-            if (*wb.hostCount == 0 || it >= kMaxReplayBounces) break;
-        }
+    const int block = kTraceBlock;
+    const int sgrid = ShadeGrid(grid);
+    for (int it = it0; it < it0 + count; it++) {
+        const int cur = it & 1;
         if (ev) ev->Begin(1, stream);
         ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
         if (ev) {
@@ -841,7 +838,6 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int n
                 RefCountKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, prof->devCounters);
             ev->Begin(2, stream);
         }
-        const int sgrid = ShadeGrid(grid);
         if (integrator == kPathTracing)
             ShadeKernel<kPathTracing><<<sgrid, block, 0, stream>>>(jobs, wb, cur);
         else if (integrator == kSimplePathTracing)
@@ -855,17 +851,145 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, int nUnits, int n
         }
         ShadowKernel<<<grid, block, 0, stream>>>(jobs, wb);
         if (ev) ev->End(3, stream);
-        nl += 3;
+        *nl += 3;
         if (prof) {
             prof->extendLaunches++;
             prof->shadowLaunches++;
         }
-        cur ^= 1;
     }
-    if (ev) ev->Begin(4, stream);
-    AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, nUnits, nPixelUnits, wb);
-    if (ev) ev->End(4, stream);
-    nl++;
+}
+
+// A captured sequence: for fixed-depth waves the whole wave (raygen, iters
+// bounces, accumulate); for queue-polled waves a block of kPollEvery bounces.
+constexpr int kPollEvery = 4;
+struct WaveGraphKey {
+    const void* jobs;
+    const void* units;
+    const void* buffers;
+    int capacity, iters, integrator, grid;
+    bool operator==(const WaveGraphKey& o) const {
+        return jobs == o.jobs && units == o.units && buffers == o.buffers && capacity == o.capacity &&
+               iters == o.iters && integrator == o.integrator && grid == o.grid;
+    }
+};
+struct WaveGraph {
+    WaveGraphKey key;
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+};
+struct WaveGraphCache {
+    std::vector<WaveGraph> graphs;  // few shapes per owner; least recently added dropped first
+    static constexpr size_t kMax = 16;
+    ~WaveGraphCache() {
+        for (WaveGraph& g : graphs) cudaGraphExecDestroy(g.exec);
+    }
+};
+WaveGraphCache* NewWaveGraphCache() { return new WaveGraphCache(); }
+void FreeWaveGraphCache(WaveGraphCache* cache) { delete cache; }
+
+template <class F>
+static cudaError_t ReplayCaptured(WaveGraphCache* cache, const WaveGraphKey& key, cudaStream_t stream,
+                                  int* nl, F&& record) {
+    WaveGraph* g = nullptr;
+    for (WaveGraph& c : cache->graphs)
+        if (c.key == key) g = &c;
+    if (!g) {
+        cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        int kernels = 0;
+        record(&kernels);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess) return e;
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return e;
+        if (cache->graphs.size() >= WaveGraphCache::kMax) {
+            cudaGraphExecDestroy(cache->graphs.front().exec);
+            cache->graphs.erase(cache->graphs.begin());
+        }
+        cache->graphs.push_back(WaveGraph{key, exec, kernels});
+        g = &cache->graphs.back();
+    }
+    *nl += g->kernels;
+    return cudaGraphLaunch(g->exec, stream);
+}
+
+cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& shape,
+                    const WaveBuffers& wb, cudaStream_t stream, int* launches, WaveProfile* prof,
+                    const WaveTuning& tune, WaveGraphCache* graphs) {
+    if (shape.nPaths <= 0) return cudaSuccess;
+    if (shape.nPaths > wb.capacity) return cudaErrorInvalidValue;
+    const int grid = StageGrid(tune);
+    const int block = kTraceBlock;
+    StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
+    bool useGraphs = graphs && !prof && tune.graphs && stream != 0 && stream != cudaStreamLegacy;
+    if (useGraphs) {  // a caller capturing this stream records the launches themselves
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+            useGraphs = false;
+    }
+    // the wave's scalars (pageable source: staged before the call returns)
+    WaveDesc d{};
+    d.nUnits = shape.nUnits;
+    d.nPaths = shape.nPaths;
+    d.nPixelUnits = shape.nPixelUnits;
+    d.soleJob = shape.soleJob;
+    d.band = tune.band > 0 ? tune.band : 8;
+    cudaError_t e = cudaMemcpyAsync(wb.desc, &d, sizeof(d), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    int nl = 0;
+    const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid};
+    if (shape.iters >= 0) {
+        auto record = [&](int* n) {
+            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n);
+            AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
+            *n += 2;
+        };
+        if (useGraphs) {
+            e = ReplayCaptured(graphs, key, stream, &nl, record);
+        } else {
+            if (ev) ev->Begin(0, stream);
+            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
+            if (ev) ev->End(0, stream);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl);
+            if (ev) ev->Begin(4, stream);
+            AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
+            if (ev) ev->End(4, stream);
+            nl += 2;
+        }
+    } else {
+        // SimplePathTracing has no depth cap: run blocks of bounces until the queue drains
+        if (ev) ev->Begin(0, stream);
+        RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
+        if (ev) ev->End(0, stream);
+        nl++;
+        for (int it = 0;; it += kPollEvery) {
+            if (it > 0) {
+                e = cudaMemcpyAsync(wb.hostCount, wb.counts, sizeof(int), cudaMemcpyDeviceToHost, stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess || *wb.hostCount == 0 || it >= kMaxReplayBounces) break;
+            }
+            if (useGraphs) {
+                WaveGraphKey k = key;
+                k.iters = -kPollEvery;
+                e = ReplayCaptured(graphs, k, stream, &nl, [&](int* n) {
+                    LaunchBounces(jobs, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n);
+                });
+                if (e != cudaSuccess) break;
+            } else {
+                LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl);
+            }
+        }
+        if (e == cudaSuccess) {
+            if (ev) ev->Begin(4, stream);
+            AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
+            if (ev) ev->End(4, stream);
+            nl++;
+        }
+    }
     if (launches) *launches += nl;
     if (e == cudaSuccess) e = cudaGetLastError();
     return e;

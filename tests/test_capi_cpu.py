@@ -110,3 +110,11 @@ def test_bvh_edge_cases():
     # bad index rejected
     with pytest.raises(capi.PtError):
         capi.bvh_build(P, np.array([[0, 1, 5]], np.int32))
+
+
+def test_tuning_calls_reject_missing_context():
+    lib = capi.load()
+    t = capi.PtTuning()
+    assert lib.pt_set_tuning(None, ctypes.byref(t)) == -1
+    assert lib.pt_get_tuning(None, ctypes.byref(t)) == -1
+    assert lib.pt_autotune(None, 1, None, None, 0, ctypes.byref(t)) == -1

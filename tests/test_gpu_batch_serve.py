@@ -101,7 +101,7 @@ def test_serve_admits_while_others_run(served):
     ctx.serve_start(wave_paths=20000, max_active=4, state_budget=1 << 24)
     try:
         sid, cam, st = jobs[1]
-        big = capi.settings_from_scene(_scenes()[1], capi.MODE_WAVEFRONT, seed=5, spp=512)
+        big = capi.settings_from_scene(_scenes()[1], capi.MODE_WAVEFRONT, seed=5, spp=4096)
         h_big = np.empty((big.height, big.width, 3), np.float32)
         r_big = ctx.serve_submit(sid, cam, big, film_host=h_big)
         time.sleep(0.05)

@@ -1,0 +1,107 @@
+"""Launch configuration of the wavefront path: captured CUDA graphs, grid sizes,
+pixel bands, wave sizes and the autotuner.
+
+None of these may change a film: the random stream is keyed by (seed, pixel,
+sample), every ray visits its nodes in its own fixed order, and each pixel sums
+its samples in sample order.
+"""
+import numpy as np
+import pytest
+
+from petrichor_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+CONFIGS = [
+    dict(),                                                   # defaults (graphs on)
+    dict(use_graphs=0),
+    dict(blocks_per_sm=4, band_rows=16, use_graphs=1),
+    dict(blocks_per_sm=24, band_rows=4, use_graphs=0),
+    dict(blocks_per_sm=12, band_rows=1, use_graphs=1, wave_paths=3000),
+]
+
+
+def _scenes():
+    return {
+        "pt": synth.cornell(width=40, height=30, spp=8, mixed=True, integrator=1, max_bounces=6,
+                            env_texture=True),
+        "simple": synth.cornell(width=33, height=17, spp=5),  # queue-polled bounce blocks
+        "tris": synth.spheres_grids(tri_budget=30000, width=64, height=36, spp=4, max_bounces=8,
+                                    env_width=128, env_height=64),
+    }
+
+
+@pytest.fixture(scope="module")
+def tuned_ctx():
+    ctx = capi.Context()
+    scenes = _scenes()
+    jobs = {}
+    for name, s in scenes.items():
+        jobs[name] = (ctx.upload(s), capi.camera_from_scene(s),
+                      capi.settings_from_scene(s, capi.MODE_WAVEFRONT, seed=7))
+    yield ctx, jobs
+    ctx.close()
+
+
+def _render(ctx, sid, cam, st):
+    film = torch.full((st.width * st.height * 3,), float("nan"), device="cuda")
+    ctx.render_device(sid, cam, st, film.data_ptr(), 0)
+    torch.cuda.synchronize()
+    return film.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["pt", "simple", "tris"])
+def test_films_do_not_depend_on_launch_configuration(tuned_ctx, name):
+    ctx, jobs = tuned_ctx
+    sid, cam, st = jobs[name]
+    ctx.set_tuning()
+    ref = _render(ctx, sid, cam, st)
+    assert np.isfinite(ref).all()
+    for cfg in CONFIGS:
+        ctx.set_tuning(**cfg)
+        for _ in range(2):  # the second render replays the captured graph
+            got = _render(ctx, sid, cam, st)
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), cfg
+    ctx.set_tuning()
+
+
+def test_graph_replay_counts_the_same_kernels(tuned_ctx):
+    ctx, jobs = tuned_ctx
+    sid, cam, st = jobs["tris"]
+    counts = {}
+    for graphs in (0, 1):
+        ctx.set_tuning(use_graphs=graphs)
+        _render(ctx, sid, cam, st)  # capture
+        before = ctx.stats().kernel_launches
+        _render(ctx, sid, cam, st)
+        counts[graphs] = ctx.stats().kernel_launches - before
+    ctx.set_tuning()
+    assert counts[0] == counts[1] > 0
+
+
+def test_autotune_picks_a_valid_configuration(tuned_ctx):
+    ctx, jobs = tuned_ctx
+    sid, cam, st = jobs["tris"]
+    ctx.set_tuning()
+    ref = _render(ctx, sid, cam, st)
+    t = ctx.autotune(sid, cam, st, probe_spp=2)
+    assert t.probe_ms > 0
+    assert t.blocks_per_sm in (0, 4, 12, 16, 24)
+    assert t.band_rows in (0, 4, 8, 16, 32)
+    assert t.use_graphs in (0, 1)
+    got = ctx.get_tuning()
+    assert (got.blocks_per_sm, got.band_rows, got.use_graphs) == (t.blocks_per_sm, t.band_rows,
+                                                                    t.use_graphs)
+    film = _render(ctx, sid, cam, st)
+    assert np.array_equal(film.view(np.uint32), ref.view(np.uint32))
+    ctx.set_tuning()
+
+
+def test_set_tuning_rejects_bad_values(tuned_ctx):
+    ctx, _ = tuned_ctx
+    for bad in (dict(blocks_per_sm=-1), dict(blocks_per_sm=65), dict(band_rows=-2),
+                dict(wave_paths=-5), dict(use_graphs=2)):
+        with pytest.raises(capi.PtError):
+            ctx.set_tuning(**bad)
+    ctx.set_tuning()
