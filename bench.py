@@ -481,8 +481,11 @@ def main():
         with open(peaks_path) as fh:
             peak, peak_src = float(json.load(fh)["hbm_gbs"]), "measured"
     traffic = None
-    tp = os.path.join(HERE, "profiles", "extend_kernel_traffic_spheres_grids_1M_1080p_64spp.json")
-    if os.path.exists(tp) and workload_name(args) == WORKLOAD:  # measured on this workload only
+    # measured DRAM bytes per extension ray (ncu launch list) of the named workloads only
+    traffic_files = {WORKLOAD: "extend_kernel_traffic_spheres_grids_1M_1080p_64spp.json",
+                     STRESS_WORKLOAD: "extend_kernel_traffic_terrain_rocks_20M_2160p_256spp.json"}
+    tp = os.path.join(HERE, "profiles", traffic_files.get(workload_name(args), "-"))
+    if os.path.exists(tp):
         with open(tp) as fh:
             t = json.load(fh)
         traffic = t["dram_bytes_per_ray"] * prof2["extend_rays"] / ext_launches
