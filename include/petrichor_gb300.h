@@ -128,7 +128,9 @@ typedef struct pt_settings {
   uint32_t seed;          /* wavefront stream seed */
   int32_t wave_paths;     /* wavefront: paths per wave (0 = automatic); the film does
                              not depend on it */
-  int32_t reserved[2];
+  int32_t denoising_spp;  /* numSppForDenoising: samples of the denoising AOV passes
+                             (0 = the reference's default, 128) */
+  int32_t reserved;
 } pt_settings;
 
 typedef struct pt_scene_info {
@@ -169,6 +171,21 @@ int pt_scene_info_get(pt_context* ctx, pt_scene_id scene, pt_scene_info* info);
  * of Texture2D::GetRawDataPtr). Blocks until the film is written. */
 int pt_render(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
               const pt_settings* settings, float* film_rgb);
+
+/* AOV passes of Petrichor::Render (Core/Petrichor.cpp:104-261; Core/AOV/AOVUVCoordinate.cpp,
+ * AOVDenoisingAlbedo.cpp, AOVDenoisingNormal.cpp). */
+#define PT_AOV_UV 0               /* AOVUVCoordinate: mean hit uv over settings.spp samples */
+#define PT_AOV_DENOISING_ALBEDO 1 /* AOVDenoisingAlbedo: settings.denoising_spp samples */
+#define PT_AOV_DENOISING_NORMAL 2 /* AOVDenoisingNormal: settings.denoising_spp samples */
+/* Renders one AOV pass into a host film of width*height*3 floats, bit-identical to
+ * the reference's pass: the reference's per-tile random streams (tile k seeded k),
+ * traversal order and arithmetic. settings.mode is ignored. Synchronous. */
+int pt_render_aov(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+                  const pt_settings* settings, int32_t aov, float* film_rgb);
+/* Same, into a device film, enqueued on `stream` (NULL = the context's stream). */
+int pt_render_aov_device(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
+                         const pt_settings* settings, int32_t aov, float* film_rgb_device,
+                         void* stream);
 
 /* Same, into a device film, enqueued on `stream` (cudaStream_t; NULL = the
  * context's stream). Returns once the work is enqueued. */

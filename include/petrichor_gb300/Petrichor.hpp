@@ -9,9 +9,10 @@
 // Differences, all additive: Petrichor::SetMode/SetIntegrator/SetSeed choose the
 // GB300 path (default: replay mode, SimplePathTracing, i.e. the reference's own
 // Render output bit for bit); Scene::SetRenderSetting sets settings without a
-// file; Environment::SetTexture takes a texture from memory. Only the Rendered
-// pass is produced (AOV targets are reported and left untouched), and only
-// triangle geometry is accepted.
+// file; Environment::SetTexture takes a texture from memory. The Rendered pass and
+// the UV / DenoisingAlbedo / DenoisingNormal AOV passes are produced for the
+// targets that are set, each equal to the reference's; only triangle geometry is
+// accepted.
 #pragma once
 
 #include <array>

@@ -67,6 +67,8 @@ def lib():
         L.oracle_hits.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, f32p, i32p]
         L.oracle_trace.argtypes = [vp, i32, f32p, ctypes.c_float, ctypes.c_float, i32p, f32p]
         L.oracle_env.argtypes = [vp, i32, f32p]
+        L.oracle_render_aov.restype = ctypes.c_double
+        L.oracle_render_aov.argtypes = [vp, f32p, i32, i32, i32]
         _lib = L
     return _lib
 
@@ -117,6 +119,13 @@ class OracleScene:
         film = np.zeros((s.height, s.width, 3), np.float32)
         secs = lib().oracle_render(self._h, _fp(film), threads, tile_begin, tile_end)
         return film, secs
+
+    def render_aov(self, aov: int, denoising_spp: int = 1, threads: int = 0):
+        """AOV pass of Petrichor::Render: 0 UV, 1 denoising albedo, 2 denoising normal."""
+        s = self.scene.settings
+        film = np.zeros((s.height, s.width, 3), np.float32)
+        lib().oracle_render_aov(self._h, _fp(film), threads, aov, denoising_spp)
+        return film
 
     def render_decorrelated(self, seed: int, threads: int = 0):
         """Same integrator and arithmetic with independent per-tile random streams."""

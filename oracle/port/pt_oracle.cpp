@@ -771,6 +771,59 @@ static void RenderSimple(const Scene& s, int px, int py, float* film, Sampler1D&
     o[0] = avg.x; o[1] = avg.y; o[2] = avg.z;
 }
 
+// ---------------------------------------------------------------- AOV passes
+// Core/AOV/AOVUVCoordinate.cpp:11-51: numSamplesPerPixel camera rays; hit uv summed.
+static void RenderAovUV(const Scene& s, int px, int py, float* film, Sampler2D& s2) {
+    V3 sum;
+    for (int sp = 0; sp < s.spp; sp++) {
+        const Ray ray = s.cam.Generate(px, py, s.W, s.H, s2);
+        float d;
+        const int t = Intersect(s, ray, kEps, kInfinity, &d);
+        if (t >= 0) sum = sum + Interpolate(s, t, ray, d).uv;
+    }
+    const V3 avg = sum / (float)s.spp;
+    float* o = film + ((size_t)py * s.W + px) * 3;
+    o[0] = avg.x; o[1] = avg.y; o[2] = avg.z;
+}
+// AOVDenoisingAlbedo.cpp:56-133 (normal == false) and AOVDenoisingNormal.cpp:54-128
+// (normal == true): follow specular glass / zero-roughness GGX bounces up to
+// numMaxBounces, then report the first diffuse-like surface (or the environment).
+static V3 AovPath(const Scene& s, Ray ray, bool normal, Sampler1D& s1, Sampler2D& s2) {
+    for (int bounce = 0; bounce < s.maxBounces; bounce++) {
+        float d;
+        const int t = Intersect(s, ray, kEps, kInfinity, &d);
+        if (t < 0) return normal ? ray.T * (-ray.dir) : ray.T * s.env.GetColor(ray.dir);
+        const int m = s.GetMaterial(t, s1.Next());
+        const Shading si = Interpolate(s, t, ray, d);
+        const Material& M = s.mats[m];
+        switch (M.kind) {
+        case kLambert:
+            return normal ? ray.T * si.normal : ray.T * LambertAlbedo(M);
+        case kGlass:  // Glass::GetAlpha is 0: always follows the refracted/reflected ray
+            ray = NextRay(s, m, ray, si, s2);
+            break;
+        case kGlossy:
+            if (M.alpha != 0) return normal ? ray.T * si.normal : ray.T * GgxF0(M);
+            ray = NextRay(s, m, ray, si, s2);
+            break;
+        default:  // Emission: the ASSERT(false) branch returns zero in release builds
+            return V3();
+        }
+    }
+    return V3();
+}
+static void RenderAovDenoise(const Scene& s, bool normal, int dspp, int px, int py, float* film,
+                             Sampler1D& s1, Sampler2D& s2) {
+    V3 sum;
+    for (int sp = 0; sp < dspp; sp++) {
+        const Ray ray = s.cam.Generate(px, py, s.W, s.H, s2);
+        sum = sum + AovPath(s, ray, normal, s1, s2);
+    }
+    const V3 avg = sum / (float)dspp;
+    float* o = film + ((size_t)py * s.W + px) * 3;
+    o[0] = avg.x; o[1] = avg.y; o[2] = avg.z;
+}
+
 // PathTracing.cpp:329-386
 static V3 SampleLight(const Scene& s, V3 o, float rv, Sampler2D& s2, float* pdfArea,
                       bool* sampleEnv) {
@@ -1087,6 +1140,40 @@ double oracle_render(void* sp, float* film, int threads, int tileBegin, int tile
     };
     std::vector<std::thread> pool;
     for (int i = 0; i < threads; i++) pool.emplace_back(work);
+    for (auto& t : pool) t.join();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// AOV pass `aov` (0 UV, 1 denoising albedo, 2 denoising normal) over all tiles; the
+// AOV loops of Core/Petrichor.cpp:104-261 seed tile k with RandomSampler1D(k) and
+// RandomSampler2D(k, k + 1). dspp = RenderSetting::numSppForDenoising.
+double oracle_render_aov(void* sp, float* film, int threads, int aov, int dspp) {
+    Scene& s = *(Scene*)sp;
+    if (!s.built) BuildBVH(s);
+    const int nx = s.W / s.tileW, ny = s.H / s.tileH;
+    const int remW = s.W - nx * s.tileW, remH = s.H - ny * s.tileH;
+    const int nt = (nx + 1) * (ny + 1);
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next(0);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= nt) break;
+            const int i = k % (nx + 1), j = k / (nx + 1);
+            const int x0 = i * s.tileW, y0 = j * s.tileH;
+            const int w = i != nx ? s.tileW : remW, h = j != ny ? s.tileH : remH;
+            Sampler1D s1(k);
+            Sampler2D s2(k, k + 1);
+            for (int y = y0; y < y0 + h; y++)
+                for (int x = x0; x < x0 + w; x++) {
+                    if (aov == 0) RenderAovUV(s, x, y, film, s2);
+                    else RenderAovDenoise(s, aov == 2, dspp, x, y, film, s1, s2);
+                }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(work);
     for (auto& t : pool) t.join();
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }

@@ -99,6 +99,7 @@ struct Loaded {
     std::unique_ptr<Texture2D> film;
     std::vector<const MaterialBase*> materials;
     int integrator = 0;
+    int denoisingSpp = 1;
 };
 
 static Math::Vector3f V3(const float* p) { return Math::Vector3f(p[0], p[1], p[2]); }
@@ -114,7 +115,8 @@ static void Load(const std::string& path, const std::string& tmpPrefix, Loaded& 
         const std::string sp = tmpPrefix + ".settings.json";
         std::ofstream s(sp);
         s << "{\"outputWidth\": " << L.settings[0] << ", \"outputHeight\": " << L.settings[1]
-          << ", \"spp\": " << L.settings[2] << ", \"denoising_spp\": 1, \"maxBounces\": "
+          << ", \"spp\": " << L.settings[2] << ", \"denoising_spp\": " << L.denoisingSpp
+          << ", \"maxBounces\": "
           << L.settings[3] << ", \"tileWidth\": " << L.settings[4]
           << ", \"tileHeight\": " << L.settings[5] << ", \"numThreads\": " << L.settings[6]
           << "}\n";
@@ -250,6 +252,7 @@ int main(int argc, char** argv) {
     const std::string mode = argv[1], scenePath = argv[2], out = argv[3];
     try {
         Loaded L;
+        if (mode == "aov" && argc > 4) L.denoisingSpp = std::stoi(argv[4]);
         Load(scenePath, out, L);
         const Scene& scene = *L.scene;
         if (mode == "film") {
@@ -332,6 +335,22 @@ int main(int argc, char** argv) {
             put(ids.data(), ids.size() * 4);
             WriteAll(out, blob.data(), blob.size());
             std::printf("{\"bvh_build_s\": %.6f, \"nodes\": %d}\n", t1 - t0, nn);
+        } else if (mode == "aov") {
+            // the AOV passes of Petrichor::Render (Core/Petrichor.cpp:104-261), Rendered skipped
+            const int W = L.settings[0], H = L.settings[1];
+            Texture2D uv(W, H), albedo(W, H), normal(W, H);
+            L.scene->SetTargetTexture(Scene::AOVType::Rendered, nullptr);
+            L.scene->SetTargetTexture(Scene::AOVType::UV, &uv);
+            L.scene->SetTargetTexture(Scene::AOVType::DenoisingAlbedo, &albedo);
+            L.scene->SetTargetTexture(Scene::AOVType::DenoisingNormal, &normal);
+            Core::Petrichor renderer;
+            renderer.Render(scene);
+            const size_t n = (size_t)W * H * 3;
+            std::vector<float> o(3 * n);
+            std::memcpy(o.data(), uv.GetRawDataPtr(), n * 4);
+            std::memcpy(o.data() + n, albedo.GetRawDataPtr(), n * 4);
+            std::memcpy(o.data() + 2 * n, normal.GetRawDataPtr(), n * 4);
+            WriteAll(out, o.data(), o.size() * 4);
         } else if (mode == "env") {
             const int n = argc > 4 ? std::stoi(argv[4]) : 4096;
             RandomSampler2D s2(3, 4);

@@ -23,6 +23,7 @@ from .scene_io import Scene, INTEGRATOR_SIMPLE, INTEGRATOR_PT
 PT_OK = 0
 MODE_REPLAY = 0
 MODE_WAVEFRONT = 1
+AOV_UV, AOV_DENOISING_ALBEDO, AOV_DENOISING_NORMAL = 0, 1, 2
 
 _f3 = ctypes.c_float * 3
 
@@ -56,7 +57,8 @@ class PtSettings(ctypes.Structure):
                 ("max_bounces", ctypes.c_int32), ("tile_width", ctypes.c_int32),
                 ("tile_height", ctypes.c_int32), ("integrator", ctypes.c_int32),
                 ("mode", ctypes.c_int32), ("seed", ctypes.c_uint32),
-                ("wave_paths", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+                ("wave_paths", ctypes.c_int32), ("denoising_spp", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class PtJob(ctypes.Structure):
@@ -120,6 +122,7 @@ EXPORTED = [
     "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc", "pt_batch_render",
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
     "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
+    "pt_render_aov", "pt_render_aov_device",
 ]
 
 _lib = None
@@ -176,6 +179,9 @@ def load(build: bool = True):
     L.pt_autotune.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings), i32,
                               ctypes.POINTER(PtTuning)]
     L.pt_set_tuning.argtypes = [vp, ctypes.POINTER(PtTuning)]
+    L.pt_render_aov.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings), i32, vp]
+    L.pt_render_aov_device.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
+                                       i32, vp, vp]
     L.pt_get_tuning.argtypes = [vp, ctypes.POINTER(PtTuning)]
     L.pt_bvh_build.argtypes = [vp, u32, vp, u32, i32, ctypes.POINTER(u32), ctypes.POINTER(u32),
                                vp, vp, vp]
@@ -214,6 +220,7 @@ def settings_from_scene(scene: Scene, mode: int = MODE_REPLAY, seed: int = 1, **
     st.mode = mode
     st.seed = seed
     st.wave_paths = over.get("wave_paths", 0)
+    st.denoising_spp = over.get("denoising_spp", 0)
     return st
 
 
@@ -254,6 +261,7 @@ class Context:
     def upload(self, scene: Scene) -> int:
         pos = np.ascontiguousarray(scene.positions, np.float32)
         nrm = np.ascontiguousarray(scene.normals, np.float32)
+        uvs = np.ascontiguousarray(scene.uvs, np.float32)
         idx = np.ascontiguousarray(scene.indices, np.int32)
         tm = np.ascontiguousarray(scene.tri_material, np.int32)
         sh = np.ascontiguousarray(scene.tri_shading, np.uint8)
@@ -271,7 +279,7 @@ class Context:
         d.num_vertices = pos.shape[0]
         d.positions = pos.ctypes.data
         d.normals = nrm.ctypes.data
-        d.uvs = None
+        d.uvs = uvs.ctypes.data
         d.num_triangles = idx.shape[0]
         d.indices = idx.ctypes.data
         d.tri_material = tm.ctypes.data
@@ -310,6 +318,23 @@ class Context:
         self._check(self.L.pt_render(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
                                      out.ctypes.data), "pt_render")
         return out
+
+    def render_aov(self, sid: int, camera: PtCamera, settings: PtSettings, aov: int,
+                   out: Optional[np.ndarray] = None) -> np.ndarray:
+        """AOV pass (AOV_UV, AOV_DENOISING_ALBEDO, AOV_DENOISING_NORMAL) into a host film."""
+        if out is None:
+            out = np.empty((settings.height, settings.width, 3), np.float32)
+        assert out.flags.c_contiguous and out.dtype == np.float32
+        assert out.size == settings.width * settings.height * 3
+        self._check(self.L.pt_render_aov(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
+                                         aov, out.ctypes.data), "pt_render_aov")
+        return out
+
+    def render_aov_device(self, sid: int, camera: PtCamera, settings: PtSettings, aov: int,
+                          film_ptr: int, stream_ptr: int = 0):
+        self._check(self.L.pt_render_aov_device(self.h, sid, ctypes.byref(camera),
+                                                ctypes.byref(settings), aov, film_ptr,
+                                                stream_ptr or None), "pt_render_aov_device")
 
     def render_device(self, sid: int, camera: PtCamera, settings: PtSettings, film_ptr: int,
                       stream_ptr: int = 0):

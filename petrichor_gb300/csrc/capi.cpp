@@ -472,6 +472,21 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         shade[3 * (size_t)k + 1] = F4(n[1].x, n[1].y, n[1].z, IntBits(smooth));
         shade[3 * (size_t)k + 2] = F4(n[2].x, n[2].y, n[2].z, 0.0f);
     }
+    // vertex uvs in leaf order, for the UV pass (omitted when the scene has none)
+    std::vector<float4> uvs;
+    bool anyUV = false;
+    if (d->uvs)
+        for (size_t i = 0; i < (size_t)d->num_vertices * 3 && !anyUV; i++) anyUV = d->uvs[i] != 0.0f;
+    if (anyUV) {
+        uvs.resize((size_t)T * 3);
+        for (int k = 0; k < T; k++) {
+            const int t = bvh.primIds[k];
+            for (int v = 0; v < 3; v++) {
+                const float* u = d->uvs + 3 * (size_t)d->indices[3 * t + v];
+                uvs[3 * (size_t)k + v] = F4(u[0], u[1], u[2], 0.0f);
+            }
+        }
+    }
     // materials
     std::vector<DevMaterial> mats(d->num_materials);
     for (uint32_t m = 0; m < d->num_materials; m++) {
@@ -516,7 +531,8 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         (rc = Upload(ctx, s, shade, &D.shade)) != PT_OK ||
         (rc = Upload(ctx, s, mats, &D.mats)) != PT_OK ||
         (rc = Upload(ctx, s, lights, &D.lights)) != PT_OK ||
-        (rc = Upload(ctx, s, env, &D.env)) != PT_OK) {
+        (rc = Upload(ctx, s, env, &D.env)) != PT_OK ||
+        (anyUV && (rc = Upload(ctx, s, uvs, &D.uvs)) != PT_OK)) {
         for (auto& b : s.buffers) Free(ctx, b);
         return rc;
     }
@@ -605,6 +621,62 @@ int pt_render_device(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     if ((rc = SetDevice(ctx)) != PT_OK) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     return RenderOnStream(ctx, *sg, cam, st, dFilm, s);
+}
+
+// One AOV pass into a device film on `stream` (replay semantics, tile chunks).
+int AovOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt_settings* st, int aov,
+                float* dFilm, cudaStream_t stream) {
+    if (aov < PT_AOV_UV || aov > PT_AOV_DENOISING_NORMAL) return Fail(ctx, PT_ERR_INVALID_ARG, "bad AOV");
+    if (st->denoising_spp < 0) return Fail(ctx, PT_ERR_INVALID_ARG, "denoising_spp < 0");
+    const int dspp = st->denoising_spp > 0 ? st->denoising_spp : 128;  // RenderSetting.h default
+    const DevCamera C = ToDev(cam);
+    const DevSettings S = ToDev(st);
+    const int tiles = NumTiles(S);
+    int rc = Alloc(ctx, ctx->stack, (size_t)tiles * sg.dev.stackDepth * sizeof(int));
+    if (rc != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->status, 16)) != PT_OK) return rc;
+    cudaError_t e = cudaEventRecord(ctx->ev0, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.ptr, 0, sizeof(int), stream);
+    const int chunk = std::max(1, std::min(tiles, 8192));
+    int launches = 0;
+    for (int t0 = 0; t0 < tiles && e == cudaSuccess; t0 += chunk) {
+        e = LaunchAov(sg.dev, C, S, aov, dspp, dFilm, (int*)ctx->stack.ptr, (int*)ctx->status.ptr, t0,
+                      std::min(tiles, t0 + chunk), stream);
+        launches++;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "AOV render");
+    ctx->stats.kernel_launches += launches;
+    return PT_OK;
+}
+
+int pt_render_aov(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
+                  int32_t aov, float* film) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!film) return Fail(ctx, PT_ERR_INVALID_ARG, "film is NULL");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    const size_t bytes = (size_t)st->width * st->height * 3 * sizeof(float);
+    if ((rc = Alloc(ctx, ctx->film, bytes)) != PT_OK) return rc;
+    if ((rc = AovOnStream(ctx, *sg, cam, st, aov, (float*)ctx->film.ptr, ctx->stream)) != PT_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(film, ctx->film.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "film download");
+    return FinishStats(ctx, ctx->stream);
+}
+
+int pt_render_aov_device(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
+                         const pt_settings* st, int32_t aov, float* dFilm, void* stream) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!dFilm) return Fail(ctx, PT_ERR_INVALID_ARG, "film is NULL");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    return AovOnStream(ctx, *sg, cam, st, aov, dFilm, stream ? (cudaStream_t)stream : ctx->stream);
 }
 
 int pt_set_tuning(pt_context* ctx, const pt_tuning* t) {

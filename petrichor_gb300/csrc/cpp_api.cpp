@@ -230,12 +230,12 @@ void Petrichor::Render(const Scene& scene) {
     m_lastStatus = PT_OK;
     m_lastError.clear();
     Texture2D* target = scene.GetTargetTexture(Scene::AOVType::Rendered);
-    if (!target) return fail(PT_ERR_INVALID_ARG, "Target texture has not been set.");
+    bool anyTarget = target != nullptr;
+    for (int a = Scene::AOVType::UV; a < Scene::AOVType::NumAOVTypes; a++)
+        anyTarget = anyTarget || scene.GetTargetTexture((Scene::AOVType::Value)a) != nullptr;
+    if (!anyTarget) return fail(PT_ERR_INVALID_ARG, "Target texture has not been set.");
     const Camera* cam = scene.GetMainCamera();
     if (!cam) return fail(PT_ERR_INVALID_ARG, "Main camera is not found.");
-    for (int a = Scene::AOVType::UV; a < Scene::AOVType::NumAOVTypes; a++)
-        if (scene.GetTargetTexture((Scene::AOVType::Value)a))
-            std::cerr << "[petrichor_gb300] AOV target " << a << " is not rendered\n";
     if (!m_ctx) {
         const int rc = pt_context_create(0, 0, &m_ctx);
         if (rc != PT_OK) return fail(rc, std::string("no GPU context: ") + pt_status_string(rc));
@@ -364,8 +364,6 @@ void Petrichor::Render(const Scene& scene) {
 
     const RenderSetting& rs = scene.GetRenderSetting();
     pt_settings st{};
-    st.width = target->GetWidth();
-    st.height = target->GetHeight();
     st.spp = rs.numSamplesPerPixel;
     st.max_bounces = rs.numMaxBounces;
     st.tile_width = rs.tileWidth;
@@ -373,8 +371,27 @@ void Petrichor::Render(const Scene& scene) {
     st.integrator = m_integrator;
     st.mode = m_mode;
     st.seed = m_seed;
-    rc = pt_render(m_ctx, sid, &pc, &st, target->GetRawDataPtr());
-    if (rc != PT_OK) fail(rc, pt_last_error(m_ctx));
+    st.denoising_spp = rs.numSppForDenoising;
+    // the Rendered pass, then UV, DenoisingAlbedo and DenoisingNormal
+    // (Petrichor.cpp:50-261), each at its own target's size
+    const int32_t passes[Scene::AOVType::NumAOVTypes] = {-1, PT_AOV_UV, PT_AOV_DENOISING_ALBEDO,
+                                                          PT_AOV_DENOISING_NORMAL};
+    for (int a = Scene::AOVType::Rendered; a < Scene::AOVType::NumAOVTypes; a++) {
+        Texture2D* tex = scene.GetTargetTexture((Scene::AOVType::Value)a);
+        if (!tex) {
+            if (a == Scene::AOVType::Rendered) std::cerr << "[Error] Target texture has not been set.\n";
+            continue;
+        }
+        st.width = tex->GetWidth();
+        st.height = tex->GetHeight();
+        rc = a == Scene::AOVType::Rendered
+               ? pt_render(m_ctx, sid, &pc, &st, tex->GetRawDataPtr())
+               : pt_render_aov(m_ctx, sid, &pc, &st, passes[a], tex->GetRawDataPtr());
+        if (rc != PT_OK) {
+            fail(rc, pt_last_error(m_ctx));
+            break;
+        }
+    }
     pt_scene_release(m_ctx, sid);
     if (m_callback) {
         RenderingResult r;

@@ -239,6 +239,22 @@ __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V
     return si;
 }
 
+// The uv of Triangle::Interpolate (Triangle.cpp:90-110) at the hit of ray (o, d) on slot k.
+__device__ __forceinline__ V3 InterpolateUV(const DevScene& S, int k, V3 o, V3 d) {
+    if (!S.uvs) return V3();
+    V3 v0, e1, e2;
+    LoadTri(S.tris, k, v0, e1, e2);
+    const V3 ce = Cross(e1, e2);
+    const float invDet = 1.0f / Dot(-d, ce);
+    const V3 vec = o - v0;
+    const float w1 = Dot(vec, Cross(d, e2)) * invDet;
+    const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+    const float4 a = __ldg(S.uvs + 3 * k), b = __ldg(S.uvs + 3 * k + 1), c = __ldg(S.uvs + 3 * k + 2);
+    const V3 uv0(a.x, a.y, a.z), uv1(b.x, b.y, b.z), uv2(c.x, c.y, c.z);
+    const V3 duv1 = uv1 - uv0, duv2 = uv2 - uv0;
+    return w1 * duv1 + w2 * duv2 + uv0;
+}
+
 // Triangle::SampleSurface (Triangle.cpp:155-182) for light i; pdfArea not returned
 // (the per-light sum is precomputed in DevScene::lightPdfArea).
 template <class M>

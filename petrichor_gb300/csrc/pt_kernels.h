@@ -24,6 +24,12 @@ cudaError_t LaunchReplay(const DevScene& S, const DevCamera& C, const DevSetting
                          int* stackScratch, int* status, int tileBegin, int tileEnd,
                          cudaStream_t stream);
 
+// AOV pass (0 UV, 1 denoising albedo, 2 denoising normal) of tiles [tileBegin, tileEnd):
+// one thread per tile with the reference's per-tile stream; dspp = numSppForDenoising.
+cudaError_t LaunchAov(const DevScene& S, const DevCamera& C, const DevSettings& st, int aov,
+                      int dspp, float* film, int* stackScratch, int* status, int tileBegin,
+                      int tileEnd, cudaStream_t stream);
+
 // ---- wavefront (throughput) path
 // A job is one image: its resident scene, camera, settings, per-pixel running
 // sums and output film. Any number of jobs share a wave; every path carries its

@@ -20,6 +20,8 @@
 //              them (Core/Geometry/Triangle.cpp:53-54).
 //   shade      3 x float4 per primitive slot (48 B), in leaf order like tris:
 //                [0] n0.xyz material(bits) [1] n1.xyz smooth(bits) [2] n2.xyz 0
+//   uvs        3 x float4 per primitive slot (optional, for the UV pass): vertex uv0, uv1,
+//              uv2 (xyz; the reference's uv is a Vector3f)
 //   lights     3 x float4 per light: [0] v0.xyz tri(bits) [1] e0.xyz 0 [2] e1.xyz 0
 //   env        float4 RGB_ texels, row-major (H x W). The importance-sampling row
 //              tables are a function of H alone and are evaluated in the kernels.
@@ -62,6 +64,7 @@ struct DevScene {
     const float4* wide;  // 4-wide collapse of the same tree (throughput traversal)
     const float4* tris;
     const float4* shade;
+    const float4* uvs;  // nullptr: all vertex uvs are zero
     const DevMaterial* mats;
     const float4* lights;
     const float4* env;

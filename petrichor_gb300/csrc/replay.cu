@@ -248,6 +248,107 @@ __global__ void __launch_bounds__(64) ReplayKernel(DevScene S, DevCamera C, DevS
     if (status) atomicOr(statusOut, status);
 }
 
+// ---------------------------------------------------------------- AOV passes
+// Core/AOV/AOVUVCoordinate.cpp:11-51: numSamplesPerPixel camera rays, hit uvs summed.
+__device__ void AovUVPixel(const DevScene& S, const DevCamera& C, const DevSettings& st, int px,
+                           int py, float* film, RefSampler2D& s2, int* stack, int* status) {
+    V3 sum;
+    for (int sp = 0; sp < st.spp; sp++) {
+        float r0, r1, r2, r3;
+        s2.Next(r0, r1);
+        s2.Next(r2, r3);
+        const Ray ray = GenerateRay<ExactMath>(C, px, py, st.width, st.height, r0, r1, r2, r3);
+        float d;
+        const int k = TraverseReference(S, ray.o, ray.d, kEps, kInfinity, d, stack, status);
+        if (k >= 0) sum = sum + InterpolateUV(S, k, ray.o, ray.d);
+    }
+    const V3 avg = sum / (float)st.spp;
+    float* o = film + ((size_t)py * st.width + px) * 3;
+    o[0] = avg.x;
+    o[1] = avg.y;
+    o[2] = avg.z;
+}
+
+// AOVDenoisingAlbedo.cpp:56-133 (normal == false), AOVDenoisingNormal.cpp:54-128 (normal ==
+// true): glass and zero-roughness GGX are followed up to numMaxBounces; the first other
+// surface, or the environment, gives the value. Emission gives zero (the reference's
+// ASSERT(false) default branch in a release build).
+__device__ V3 AovPath(const DevScene& S, const DevSettings& st, Ray ray, bool normal,
+                      RefSampler1D& s1, RefSampler2D& s2, int* stack, int* status) {
+    for (int bounce = 0; bounce < st.maxBounces; bounce++) {
+        float d;
+        const int k = TraverseReference(S, ray.o, ray.d, kEps, kInfinity, d, stack, status);
+        if (k < 0) return normal ? ray.T * (-ray.d) : ray.T * EnvColor<ExactMath>(S, ray.d);
+        const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, k), s1.Next());
+        const Shading si = Interpolate(S, k, ray.o, ray.d, d);
+        const DevMaterial& M = S.mats[m];
+        if (M.kind == kLambert) return normal ? ray.T * si.n : ray.T * V3(1.f, 1.f, 1.f);
+        if (M.kind == kGlossy && M.alpha != 0) return normal ? ray.T * si.n : ray.T * GgxF0(M);
+        if (M.kind != kGlass && M.kind != kGlossy) return V3();
+        ray = NextRay<ExactMath>(M, ray, si, s2);  // Glass::GetAlpha is always 0
+    }
+    return V3();
+}
+
+__device__ void AovDenoisePixel(const DevScene& S, const DevCamera& C, const DevSettings& st,
+                                bool normal, int dspp, int px, int py, float* film, RefSampler1D& s1,
+                                RefSampler2D& s2, int* stack, int* status) {
+    V3 sum;
+    for (int sp = 0; sp < dspp; sp++) {
+        float r0, r1, r2, r3;
+        s2.Next(r0, r1);
+        s2.Next(r2, r3);
+        const Ray ray = GenerateRay<ExactMath>(C, px, py, st.width, st.height, r0, r1, r2, r3);
+        sum = sum + AovPath(S, st, ray, normal, s1, s2, stack, status);
+    }
+    const V3 avg = sum / (float)dspp;
+    float* o = film + ((size_t)py * st.width + px) * 3;
+    o[0] = avg.x;
+    o[1] = avg.y;
+    o[2] = avg.z;
+}
+
+// One thread per tile; unlike the Rendered pass, the AOV loops of Petrichor::Render
+// (Core/Petrichor.cpp:104-261) advance tileIndex: tile k is seeded
+// RandomSampler1D(k) / RandomSampler2D(k, k + 1).
+__global__ void __launch_bounds__(64) AovKernel(DevScene S, DevCamera C, DevSettings st, int aov,
+                                                int dspp, float* __restrict__ film,
+                                                int* __restrict__ stackScratch,
+                                                int* __restrict__ statusOut, int tileBegin,
+                                                int tileEnd) {
+    const int t = tileBegin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tileEnd) return;
+    const int nx = st.width / st.tileW, ny = st.height / st.tileH;
+    const int remW = st.width - nx * st.tileW, remH = st.height - ny * st.tileH;
+    const int ti = t % (nx + 1), tj = t / (nx + 1);
+    if (tj > ny) return;
+    const int x0 = ti * st.tileW, y0 = tj * st.tileH;
+    const int w = (ti != nx) ? st.tileW : remW, h = (tj != ny) ? st.tileH : remH;
+    int* stack = stackScratch + (size_t)(t - tileBegin) * S.stackDepth;
+    int status = 0;
+    RefSampler1D s1((uint32_t)t);
+    RefSampler2D s2((uint32_t)t, (uint32_t)t + 1u);
+    for (int y = y0; y < y0 + h; y++)
+        for (int x = x0; x < x0 + w; x++) {
+            if (aov == 0)
+                AovUVPixel(S, C, st, x, y, film, s2, stack, &status);
+            else
+                AovDenoisePixel(S, C, st, aov == 2, dspp, x, y, film, s1, s2, stack, &status);
+        }
+    if (status) atomicOr(statusOut, status);
+}
+
+cudaError_t LaunchAov(const DevScene& S, const DevCamera& C, const DevSettings& st, int aov,
+                      int dspp, float* film, int* stackScratch, int* status, int tileBegin,
+                      int tileEnd, cudaStream_t stream) {
+    const int n = tileEnd - tileBegin;
+    if (n <= 0) return cudaSuccess;
+    const int block = 64;
+    AovKernel<<<(n + block - 1) / block, block, 0, stream>>>(S, C, st, aov, dspp, film, stackScratch,
+                                                              status, tileBegin, tileEnd);
+    return cudaGetLastError();
+}
+
 int NumTiles(const DevSettings& st) {
     return (st.width / st.tileW + 1) * (st.height / st.tileH + 1);
 }

@@ -191,7 +191,11 @@ def _uv_sphere(center, radius, nu, nv):
     d = np.stack([np.sin(T) * np.cos(Ph), np.sin(T) * np.sin(Ph), np.cos(T)], -1).reshape(-1, 3)
     d = np.concatenate([[[0, 0, 1.0]], d, [[0, 0, -1.0]]])
     P = np.asarray(center) + radius * d
+    # texture coordinates (phi / 2 pi, theta / pi, 0); the poles take u = 0
     uv = np.zeros_like(P)
+    uv[1:-1, 0] = (Ph / (2.0 * math.pi)).reshape(-1)
+    uv[1:-1, 1] = (T / math.pi).reshape(-1)
+    uv[-1, 1] = 1.0
     rings = nv - 1
     idx = []
     ring = lambda r, k: 1 + r * nu + (k % nu)

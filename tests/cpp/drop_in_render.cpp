@@ -7,11 +7,13 @@
 // Camera(pos, dir)/SetFOV/SetFocalLength/FocusTo/SetApeture), renders it with
 // Petrichor::Render and writes the Rendered texture as raw float32 RGB rows.
 //
-//   drop_in_render <scene.ptscene> <film.bin> [wavefront]
+//   drop_in_render <scene.ptscene> <film.bin> [wavefront | aov <denoising spp>]
 //
 // Without "wavefront" the renderer keeps its defaults (replay mode with
-// SimplePathTracing: the reference's own Render output). Exit status: 0 on
-// success, 3 when Render reported an error (its status code is printed).
+// SimplePathTracing: the reference's own Render output). With "aov" the UV,
+// DenoisingAlbedo and DenoisingNormal targets are set too, and the file holds the
+// Rendered film followed by the three AOV films. Exit status: 0 on success, 3 when
+// Render reported an error (its status code is printed).
 #include <petrichor_gb300/Petrichor.hpp>
 #include <petrichor_gb300.h>
 
@@ -62,6 +64,8 @@ struct App {
     std::vector<Triangle> triangles;
     std::unique_ptr<Texture2D> film;
     int integrator = 0;
+    int denoisingSpp = 1;
+    std::unique_ptr<Texture2D> aov[3];
 };
 
 void BuildScene(const std::string& path, const std::string& scratch, App& app) {
@@ -76,7 +80,8 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
         const std::string json = scratch + ".settings.json";
         std::ofstream f(json);
         f << "{\n  \"outputWidth\": " << s[0] << ",\n  \"outputHeight\": " << s[1]
-          << ",\n  \"spp\": " << s[2] << ",\n  \"denoising_spp\": 1,\n  \"maxBounces\": " << s[3]
+          << ",\n  \"spp\": " << s[2] << ",\n  \"denoising_spp\": " << app.denoisingSpp
+          << ",\n  \"maxBounces\": " << s[3]
           << ",\n  \"tileWidth\": " << s[4] << ",\n  \"tileHeight\": " << s[5]
           << ",\n  \"numThreads\": " << s[6] << "\n}\n";
         f.close();
@@ -175,12 +180,22 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
 
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront | aov <spp>]\n", argv[0]);
         return 2;
     }
     try {
         App app;
+        const bool aov = argc > 4 && std::string(argv[3]) == "aov";
+        if (aov) app.denoisingSpp = std::stoi(argv[4]);
         BuildScene(argv[1], argv[2], app);
+        if (aov) {
+            const Scene::AOVType::Value kinds[3] = {Scene::AOVType::UV, Scene::AOVType::DenoisingAlbedo,
+                                                    Scene::AOVType::DenoisingNormal};
+            for (int k = 0; k < 3; k++) {
+                app.aov[k] = std::make_unique<Texture2D>(app.film->GetWidth(), app.film->GetHeight());
+                app.scene.SetTargetTexture(kinds[k], app.aov[k].get());
+            }
+        }
         Core::Petrichor renderer;
         if (argc > 3 && std::string(argv[3]) == "wavefront") renderer.SetMode(PT_MODE_WAVEFRONT);
         renderer.SetIntegrator(app.integrator);
@@ -194,10 +209,11 @@ int main(int argc, char** argv) {
             std::fprintf(stderr, "render failed: %s\n", renderer.GetLastError().c_str());
             return 3;
         }
-        const Texture2D& film = *app.film;
         std::ofstream f(argv[2], std::ios::binary);
-        f.write(reinterpret_cast<const char*>(film.GetRawDataPtr()),
-                (std::streamsize)((size_t)film.GetWidth() * film.GetHeight() * 3 * 4));
+        for (const Texture2D* t : {app.film.get(), app.aov[0].get(), app.aov[1].get(), app.aov[2].get()})
+            if (t)
+                f.write(reinterpret_cast<const char*>(t->GetRawDataPtr()),
+                        (std::streamsize)((size_t)t->GetWidth() * t->GetHeight() * 3 * 4));
         return f ? 0 : 1;
     } catch (const std::exception& e) {
         std::fprintf(stderr, "error: %s\n", e.what());

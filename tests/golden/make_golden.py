@@ -40,6 +40,17 @@ def cases():
     }
 
 
+def aov_cases():
+    """Scenes whose AOV passes (UV, denoising albedo, denoising normal) are pinned, with
+    their numSppForDenoising."""
+    return {
+        "aov_spheres": (synth.spheres_grids(tri_budget=4000, width=48, height=27, spp=2,
+                                            max_bounces=8, env_width=64, env_height=32), 3),
+        "aov_cornell_mixed": (synth.cornell(width=40, height=24, spp=3, mixed=True, aperture=0.05,
+                                            tile=7, max_bounces=5, env_texture=True), 2),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -68,6 +79,12 @@ def main():
     out["spheres_pt/hits"] = np.frombuffer(rh[n * 32:], np.int32).reshape(n, 2)
     out["spheres_pt/env"] = np.frombuffer(oracle.run_reference("env", sc, work, 256),
                                           np.float32).reshape(256, 8)
+    for name, (sc, dspp) in aov_cases().items():
+        out[f"{name}/scene"] = np.frombuffer(scene_io.scene_bytes(sc), np.uint8)
+        out[f"{name}/denoising_spp"] = np.array([dspp], np.int32)
+        aov = np.frombuffer(oracle.run_reference("aov", sc, work, dspp), np.float32)
+        out[f"{name}/aov"] = aov.reshape(3, sc.settings.height, sc.settings.width, 3)
+        print(name, "aov means", [float(a.mean()) for a in out[f"{name}/aov"]])
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 

@@ -12,7 +12,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, golden_scene
+from conftest import AOV_CASES, GOLDEN_CASES, golden_scene
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "drop_in_render.cpp")
@@ -71,3 +71,19 @@ def test_drop_in_wavefront_equals_c_abi(client, golden, gpu_ctx, tmp_path, name)
     ref = capi.render_scene(sc, mode=capi.MODE_WAVEFRONT, seed=1, ctx=gpu_ctx)
     got = np.fromfile(film, np.float32).reshape(ref.shape)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", AOV_CASES)
+def test_drop_in_render_fills_aov_targets(client, golden, tmp_path, name):
+    """Rendered + UV + DenoisingAlbedo + DenoisingNormal targets in one Render call."""
+    import oracle
+    dspp = int(golden[f"{name}/denoising_spp"][0])
+    r, film = _run(client, golden, name, tmp_path, "aov", str(dspp))
+    assert r.returncode == 0, r.stdout + r.stderr
+    ref = golden[f"{name}/aov"]
+    got = np.fromfile(film, np.float32).reshape((4,) + ref.shape[1:])
+    rendered, _ = oracle.OracleScene(golden_scene(golden, name)).render(threads=4)
+    assert np.array_equal(got[0].view(np.uint32), rendered.view(np.uint32))
+    for a in range(3):
+        assert np.array_equal(got[a + 1].view(np.uint32), ref[a].view(np.uint32)), a

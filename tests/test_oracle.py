@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import GOLDEN_CASES, golden_scene
+from conftest import AOV_CASES, GOLDEN_CASES, golden_scene
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
@@ -18,6 +18,19 @@ def test_oracle_film_matches_reference_bits(golden, name):
     ref = golden[f"{name}/film"]
     assert film.shape == ref.shape
     assert np.array_equal(film.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", AOV_CASES)
+def test_oracle_aov_passes_match_reference_bits(golden, name):
+    """UV, denoising albedo and denoising normal passes (Core/AOV/*.cpp), tile k seeded k."""
+    sc = golden_scene(golden, name)
+    dspp = int(golden[f"{name}/denoising_spp"][0])
+    ref = golden[f"{name}/aov"]
+    o = oracle.OracleScene(sc)
+    for a in range(3):
+        got = o.render_aov(a, dspp, threads=3)
+        assert np.array_equal(got.view(np.uint32), ref[a].view(np.uint32)), a
+    assert np.abs(ref[0]).max() > 0 or name != "aov_spheres"  # the spheres carry uvs
 
 
 def test_oracle_film_independent_of_thread_count(golden):
