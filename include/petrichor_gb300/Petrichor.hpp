@@ -6,6 +6,13 @@
 // Petrichor::Render(scene) fills the Rendered target texture, through the C ABI
 // in petrichor_gb300.h.
 //
+// Loaders: Scene::LoadAssets reads the reference's JSON scene format (materials,
+// camera, env, assets; SceneLoader.cpp:17-297), Scene::LoadModel reads OBJ meshes
+// (the reference uses Assimp; this is an own subset reader: v/vn/vt/f, one vertex per
+// face corner, the first three corners of a polygon), Texture2D::Load reads Radiance
+// .hdr and Texture2D::Save writes tone-mapped .png and .hdr (Texture2D.cpp:107-252).
+// PNG decoding and texture maps on materials are not supported.
+//
 // Differences, all additive: Petrichor::SetMode/SetIntegrator/SetSeed choose the
 // GB300 path (default: replay mode, SimplePathTracing, i.e. the reference's own
 // Render output bit for bit); Scene::SetRenderSetting sets settings without a
@@ -188,10 +195,14 @@ private:
 
 class Texture2D {
 public:
+    enum class TextureColorType { Color, NonColor };
     Texture2D() : Texture2D(0, 0) {}
     Texture2D(int width, int height);
-    // ".hdr": a raw container "PTRAWF32", uint32 width, uint32 height, RGB float32 rows.
-    bool Load(const std::filesystem::path& path);
+    // ".hdr": Radiance RGBE (flat or run-length encoded scanlines), or the raw container
+    // "PTRAWF32", uint32 width, uint32 height, RGB float32 rows.
+    bool Load(const std::filesystem::path& path, TextureColorType type = TextureColorType::Color);
+    // ".png": ACES + the reference's tone curve, 8-bit RGB; ".hdr": Radiance RGBE.
+    void Save(const std::filesystem::path& path) const;
     void Clear(const Color3f& color = Color3f::Zero());
     Color3f GetPixel(int i, int j) const;
     void SetPixel(int i, int j, const Color3f& color);
@@ -207,6 +218,18 @@ private:
     int m_width = 0, m_height = 0;
     std::vector<float> m_pixels;
     bool m_isLoaded = false;
+};
+
+class Mesh {
+public:
+    // OBJ subset (see the header comment); every triangle gets `material` and `shadingType`.
+    void Load(const std::filesystem::path& path, const MaterialBase* material,
+              ShadingTypes shadingType = ShadingTypes::Flat);
+    const std::vector<Triangle>& GetTriangles() const { return m_triangles; }
+
+private:
+    std::vector<Vertex> m_vertices;
+    std::vector<Triangle> m_triangles;
 };
 
 class Environment {
@@ -264,6 +287,21 @@ public:
 
     void AppendGeometry(const GeometryBase* geometry) { m_geometries.push_back(geometry); }
     void AppendLight(const GeometryBase* geometry) { m_lights.push_back(geometry); }
+    void AppendMesh(const Mesh& mesh) {
+        for (const Triangle& t : mesh.GetTriangles()) AppendGeometry(&t);
+    }
+    void AppendLightMesh(const Mesh& mesh) {
+        for (const Triangle& t : mesh.GetTriangles()) {
+            AppendGeometry(&t);
+            AppendLight(&t);
+        }
+    }
+    // Loads an OBJ with the "default" material (or the named one), smooth shading
+    // (Scene.cpp:29-52). The scene keeps the mesh.
+    void LoadModel(const std::filesystem::path& path);
+    void LoadModel(const std::filesystem::path& path, std::string_view materialName);
+    // The reference's JSON scene file (SceneLoaderJson, SceneLoader.cpp:17-297).
+    void LoadAssets(const std::filesystem::path& path);
     const std::vector<const GeometryBase*>& GetGeometries() const { return m_geometries; }
     const std::vector<const GeometryBase*>& GetLights() const { return m_lights; }
     const Camera* GetMainCamera() const { return m_mainCamera.get(); }
@@ -288,6 +326,7 @@ private:
     std::unique_ptr<Camera> m_mainCamera;
     std::array<Texture2D*, AOVType::NumAOVTypes> m_targets{};
     RenderSetting m_renderSetting;
+    std::vector<std::unique_ptr<Mesh>> m_meshes;
 };
 
 class Petrichor {

@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 CU_SOURCES = ["replay.cu", "wavefront.cu", "noalloc.cu"]
-CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp", "scheduler.cpp", "server.cpp", "cpp_api.cpp"]
+CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp", "scheduler.cpp", "server.cpp", "cpp_api.cpp",
+               "cpp_loaders.cpp"]
 
 
 def _nvcc() -> str:

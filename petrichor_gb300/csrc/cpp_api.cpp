@@ -114,24 +114,6 @@ void Texture2D::Clear(const Color3f& c) {
     }
 }
 
-bool Texture2D::Load(const std::filesystem::path& path) {
-    std::ifstream f(path, std::ios::binary);
-    char magic[8];
-    uint32_t dims[2];
-    if (!f || !f.read(magic, 8) || std::memcmp(magic, "PTRAWF32", 8) != 0 ||
-        !f.read((char*)dims, 8)) {
-        std::cerr << "Could not read texture. [" << path.string() << "]\n";
-        return false;
-    }
-    std::vector<float> px((size_t)dims[0] * dims[1] * 3);
-    if (!f.read((char*)px.data(), (std::streamsize)(px.size() * 4))) return false;
-    m_width = (int)dims[0];
-    m_height = (int)dims[1];
-    m_pixels = std::move(px);
-    m_isLoaded = true;
-    return true;
-}
-
 Color3f Texture2D::GetPixel(int i, int j) const {  // Texture2D.cpp:260-271
     if (!IsValid()) return Color3f(1.0f, 0.0f, 1.0f);
     const float* p = &m_pixels[((size_t)m_width * j + i) * 3];

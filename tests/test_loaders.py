@@ -1,0 +1,313 @@
+"""File loaders of the C++ API (petrichor_gb300/csrc/cpp_loaders.cpp): the reference's
+JSON scene format (SceneLoaderJson), OBJ assets, Radiance .hdr images and tone-mapped
+.png output, driven by tests/cpp/load_scene.cpp.
+
+CPU: what LoadRenderSetting + LoadAssets build (settings, camera in the reference's
+call order, environment texels, materials, triangles), and the image writers. GPU: the
+loaded scene renders through Petrichor::Render exactly as the oracle renders the same
+scene given as arrays.
+"""
+import math
+import os
+import struct
+import subprocess
+import zlib
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "load_scene.cpp")
+f32 = np.float32
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    from petrichor_gb300 import _build
+    lib = _build.build()
+    out = str(tmp_path_factory.mktemp("cpp") / "load_scene")
+    d = os.path.dirname(lib)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), SRC,
+                    "-L", d, "-lpetrichor_gb300", f"-Wl,-rpath,{d}", "-o", out], check=True)
+    return out
+
+
+def _rgbe_rows(W, H, seed):
+    rng = np.random.default_rng(seed)
+    px = rng.integers(0, 256, size=(H, W, 4), dtype=np.uint8)
+    px[..., 3] = rng.integers(120, 140, size=(H, W))
+    px[0, 0] = 0  # a black texel (exponent 0)
+    return px
+
+
+def _write_hdr(path, px, rle):
+    H, W, _ = px.shape
+    with open(path, "wb") as f:
+        f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {H} +X {W}\n".encode())
+        for y in range(H):
+            if not rle:
+                f.write(px[y].tobytes())
+                continue
+            f.write(bytes([2, 2, W >> 8, W & 255]))
+            for c in range(4):
+                row = px[y, :, c]
+                x = 0
+                while x < W:  # runs of equal bytes, else literal spans
+                    run = 1
+                    while x + run < W and run < 127 and row[x + run] == row[x]:
+                        run += 1
+                    if run >= 3:
+                        f.write(bytes([128 + run, int(row[x])]))
+                        x += run
+                        continue
+                    n = min(128, W - x)
+                    f.write(bytes([n]) + row[x:x + n].tobytes())
+                    x += n
+
+
+def _decode(px):
+    m = px[..., :3].astype(np.float64)
+    e = px[..., 3:4].astype(np.int64)
+    return np.where(e > 0, np.ldexp(m, e - 136), 0.0).astype(np.float32)
+
+
+OBJ_A = """# quad, textured triangles, negative indices
+v 0 0 0
+v 1 0 0
+v 1 1 0.25
+v 0 1 0
+v 0.5 0.5 1.5
+vt 0 0
+vt 1 0
+vt 1 1
+vt 0.25 0.75
+vn 0 0 2
+vn 0 1 1
+vn 1 0 1
+f 1/1/1 2/2/1 3/3/2 4/4/3
+f 1/1/1 3/3/2 5/4/3
+f -4/-3/-2 -3/-2/-1 -1/-1/-1
+"""
+OBJ_B = """o positions only
+v -1 -1 0
+v 2 -1 0
+v -1 2 0
+v 2 2 -0.5
+f 1 2 3
+f 2 4 3
+"""
+
+
+def _write_case(d):
+    with open(os.path.join(d, "settings.json"), "w") as f:
+        f.write('{"outputWidth": 24, "outputHeight": 16, "spp": 2, "denoising_spp": 4, "maxBounces": 3,'
+                ' "tileWidth": 8, "tileHeight": 8, "numThreads": 0}')
+    with open(os.path.join(d, "a.obj"), "w") as f:
+        f.write(OBJ_A)
+    with open(os.path.join(d, "b.obj"), "w") as f:
+        f.write(OBJ_B)
+    px = _rgbe_rows(16, 8, 5)
+    _write_hdr(os.path.join(d, "sky.hdr"), px, rle=True)
+    with open(os.path.join(d, "scene.json"), "w") as f:
+        f.write("""{
+ "materials": [
+  {"type": "lambert", "name": "white", "base_color": [0.7, 0.6, 0.5]},
+  {"type": "glossy", "name": "metal", "color": [0.9, 0.8, 0.4], "roughness": 0.3},
+  {"type": "glass", "name": "gl", "color": [1, 1, 1], "ior": 1.45},
+  {"type": "emission", "name": "light"},
+  {"type": "mix", "name": "mixed", "mat0_name": "white", "mat1_name": "metal", "mix": 0.3}
+ ],
+ "camera": {"position": [0.5, -3.0, 1.2], "look_at": [0.5, 0.5, 0.3], "focus_pos": [0.5, 0.5, 0.4],
+            "f_number": 4.0, "focal_length": 0.035},
+ "env": {"base_color": [1.0, 0.9, 0.8], "texture": "sky.hdr"},
+ "assets": [{"path": "a.obj", "mat": "mixed"}, {"path": "b.obj"}]
+}
+""")
+    return px
+
+
+def _parse_dump(path):
+    rec = {"texel": [], "material": {}, "tri": [], "mixof": {}}
+    h = lambda t: float.fromhex(t)
+    for line in open(path):
+        t = line.split()
+        if t[0] == "settings":
+            rec["settings"] = [int(x) for x in t[1:]]
+        elif t[0] == "camera":
+            v = [h(x) for x in t[1:]]
+            rec["camera"] = dict(pos=v[0:3], fwd=v[3:6], right=v[6:9], up=v[9:12], hperf=v[12],
+                                 focus=v[13], aperture=v[14])
+        elif t[0] == "env":
+            rec["env"] = ([h(x) for x in t[1:4]], int(t[4]), int(t[5]))
+        elif t[0] == "texel":
+            rec["texel"].append([h(x) for x in t[1:]])
+        elif t[0] == "material":
+            rec["material"][int(t[1])] = (int(t[2]), [h(x) for x in t[3:]])
+        elif t[0] == "mixof":
+            rec["mixof"][int(t[1])] = (int(t[2]), int(t[3]))
+        elif t[0] == "tri":
+            v = [h(x) for x in t[3:]]
+            rec["tri"].append((int(t[1]), int(t[2]), np.array(v, np.float32).reshape(3, 3, 3)))
+    return rec
+
+
+def test_load_assets_builds_the_reference_scene(exe, tmp_path):
+    px = _write_case(str(tmp_path))
+    out = tmp_path / "dump.txt"
+    r = subprocess.run([exe, "dump", str(tmp_path / "settings.json"), str(tmp_path / "scene.json"), str(out)],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    d = _parse_dump(out)
+    assert d["settings"] == [24, 16, 2, 4, 3, 8, 8, 0]
+    # camera: SetPosition, LookAt, FocusTo, SetFNumber (at the default 55 mm), SetFocalLength
+    c = d["camera"]
+    pos, look, focus = (np.array(v, f32) for v in ([0.5, -3.0, 1.2], [0.5, 0.5, 0.3], [0.5, 0.5, 0.4]))
+    assert np.array_equal(np.array(c["pos"], f32), pos)
+    dirv = look - pos
+    np.testing.assert_allclose(c["fwd"], dirv / np.linalg.norm(dirv), rtol=0, atol=1e-6)
+    assert f32(c["hperf"]) == f32(24e-3) / f32(0.035)
+    assert f32(c["focus"]) == f32(math.sqrt(float(np.dot(focus - pos, focus - pos))))
+    hperf0 = f32(24e-3) / f32(55e-3)
+    assert f32(c["aperture"]) == (f32(24e-3) / hperf0) / f32(4.0)
+    # environment: base colour and RGBE texels (run-length encoded file)
+    base, w, h = d["env"]
+    assert np.array_equal(np.array(base, f32), np.array([1.0, 0.9, 0.8], f32))
+    assert (w, h) == (16, 8)
+    assert np.array_equal(np.array(d["texel"], f32).reshape(8, 16, 3), _decode(px))
+    # triangles: the quad keeps its first three corners; one vertex per face corner
+    tris = d["tri"]
+    assert len(tris) == 3 + 2
+    P = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0.25], [0, 1, 0], [0.5, 0.5, 1.5]], f32)
+    T = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0.25, 0.75, 0]], f32)
+    N = np.array([[0, 0, 2], [0, 1, 1], [1, 0, 1]], f32)
+    N = N / np.linalg.norm(N, axis=1, keepdims=True)
+    faces = [[(0, 0, 0), (1, 1, 0), (2, 2, 1)], [(0, 0, 0), (2, 2, 1), (4, 3, 2)],
+             [(1, 1, 1), (2, 2, 2), (4, 3, 2)]]
+    for (m, smooth, v), face in zip(tris[:3], faces):
+        assert smooth == 1
+        for k, (pi, ti, ni) in enumerate(face):
+            assert np.array_equal(v[k, 0], P[pi])
+            assert np.array_equal(v[k, 2], T[ti])
+            np.testing.assert_allclose(v[k, 1], N[ni], rtol=0, atol=1e-6)
+    mats = d["material"]
+    mixed = tris[0][0]
+    assert mats[mixed][0] == 4 and np.isclose(mats[mixed][1][0], 0.3)
+    m0, m1 = d["mixof"][mixed]
+    assert mats[m0] == (0, [np.float32(0.7), np.float32(0.6), np.float32(0.5)])
+    assert mats[m1][0] == 3 and np.allclose(mats[m1][1], [0.9, 0.8, 0.4, 0.3])
+    for m, smooth, v in tris[3:]:  # positions-only mesh: default material, normal +Z
+        assert mats[m] == (0, [1.0, 1.0, 1.0])
+        assert np.array_equal(v[:, 1], np.tile(np.array([0, 0, 1], f32), (3, 1)))
+        assert np.array_equal(v[:, 2], np.zeros((3, 3), f32))
+
+
+def _aces(x):
+    a, b, c, d, e = f32(2.51), f32(0.03), f32(2.43), f32(0.59), f32(0.14)
+    return (x * (a * x + b)) / (x * (c * x + d) + e)
+
+
+def _tonemap_u8(rgb):
+    # dark values go negative before the power curves and become NaN, then 0, as in
+    # the reference's float code
+    with np.errstate(invalid="ignore"):
+        return _tonemap_u8_raw(rgb)
+
+
+def _tonemap_u8_raw(rgb):
+    g = lambda v, p: np.power(v.astype(np.float64), np.float64(f32(p))).astype(f32)
+    c = _aces(rgb.astype(f32))
+    c = g(c, 1.2)
+    x0, x1 = g(f32(0.05), 2.2), g(f32(0.9), 2.2)
+    c = (c - x0) / (x1 - x0)
+    c[..., 1] = g(c[..., 1], 1.3)
+    c[..., 2] = g(c[..., 2], 1.6)
+    v = np.power(c.astype(np.float64), 1.1).astype(f32)
+    v = np.clip(v, f32(0), f32(1))
+    v = np.power(v.astype(np.float64), np.float64(f32(1) / f32(2.2))).astype(f32)
+    return ((f32(255) - f32(1e-3)) * v).astype(np.uint8)
+
+
+def _read_png(path):
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    off, idat, W = 8, b"", None
+    while off < len(data):
+        n, = struct.unpack(">I", data[off:off + 4])
+        typ, body = data[off + 4:off + 8], data[off + 8:off + 8 + n]
+        crc, = struct.unpack(">I", data[off + 8 + n:off + 12 + n])
+        assert zlib.crc32(typ + body) & 0xffffffff == crc
+        if typ == b"IHDR":
+            W, H, depth, ctype = struct.unpack(">IIBB", body[:10])
+            assert (depth, ctype) == (8, 2)
+        elif typ == b"IDAT":
+            idat += body
+        off += 12 + n
+    raw = zlib.decompress(idat)
+    rows = np.frombuffer(raw, np.uint8).reshape(H, 1 + W * 3)
+    assert (rows[:, 0] == 0).all()
+    return rows[:, 1:].reshape(H, W, 3)
+
+
+def test_texture_save_png_and_hdr(exe, tmp_path):
+    px = _rgbe_rows(9, 5, 11)  # width < 8 would force flat scanlines; 9 tests flat rows too
+    src = tmp_path / "in.hdr"
+    _write_hdr(src, px, rle=False)
+    r = subprocess.run([exe, "save", str(src), str(tmp_path / "o.png"), str(tmp_path / "o.hdr")],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    img = _read_png(tmp_path / "o.png")
+    expect = _tonemap_u8(_decode(px))
+    assert img.shape == expect.shape
+    assert np.abs(img.astype(int) - expect.astype(int)).max() <= 1
+    # .hdr written back: same header form, values within RGBE precision
+    data = open(tmp_path / "o.hdr", "rb").read()
+    head, body = data.split(b"\n-Y 5 +X 9\n", 1)
+    assert head.startswith(b"#?RADIANCE")
+    back = _decode(np.frombuffer(body, np.uint8).reshape(5, 9, 4))
+    orig = _decode(px)
+    np.testing.assert_allclose(back, orig, rtol=1.0 / 128, atol=1e-30)
+
+
+@pytest.mark.gpu
+def test_loaded_scene_renders_like_the_oracle(exe, tmp_path):
+    """LoadAssets + Petrichor::Render (replay) equals the oracle on the same scene arrays."""
+    import oracle
+    from petrichor_gb300 import scene_io
+    px = _write_case(str(tmp_path))
+    dump = tmp_path / "dump.txt"
+    subprocess.run([exe, "dump", str(tmp_path / "settings.json"), str(tmp_path / "scene.json"), str(dump)],
+                   check=True, timeout=60)
+    d = _parse_dump(dump)
+    r = subprocess.run([exe, "render", str(tmp_path / "settings.json"), str(tmp_path / "scene.json"),
+                        str(tmp_path / "film.bin")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    film = np.fromfile(tmp_path / "film.bin", np.float32).reshape(16, 24, 3)
+    # the same scene as arrays
+    ids = sorted(d["material"])
+    kinds = {0: scene_io.MAT_LAMBERT, 3: scene_io.MAT_GLOSSY, 1: scene_io.MAT_GLASS, 4: scene_io.MAT_MIX}
+    mats = []
+    for k in ids:
+        kind, v = d["material"][k]
+        if kind == 0:
+            mats.append(scene_io.Material(scene_io.MAT_LAMBERT, color=tuple(v[:3])))
+        elif kind == 3:
+            mats.append(scene_io.Material(scene_io.MAT_GLOSSY, color=tuple(v[:3]), roughness=v[3]))
+        else:
+            a, b = d["mixof"][k]
+            mats.append(scene_io.Material(scene_io.MAT_MIX, mix=v[0], mat0=a, mat1=b))
+    V = np.concatenate([t[2] for t in d["tri"]])  # (3T, 3 attributes, 3)
+    n = len(d["tri"])
+    c = d["camera"]
+    cam = scene_io.Camera(pos=tuple(c["pos"]), view_dir=tuple(np.array([0.5, 0.5, 0.3], f32) -
+                                                                np.array(c["pos"], f32)),
+                          fov=0.0, focal_length=0.035, focus_target=(0.5, 0.5, 0.4),
+                          aperture=c["aperture"])
+    env = scene_io.Environment(base_color=(1.0, 0.9, 0.8), texture=_decode(px))
+    st = scene_io.Settings(width=24, height=16, spp=2, max_bounces=3, tile_width=8, tile_height=8,
+                           integrator=scene_io.INTEGRATOR_SIMPLE)
+    sc = scene_io.Scene(V[:, 0].copy(), V[:, 1].copy(), V[:, 2].copy(),
+                        np.arange(3 * n, dtype=np.int32).reshape(n, 3),
+                        np.array([t[0] for t in d["tri"]], np.int32), np.ones(n, np.uint8),
+                        np.zeros(0, np.int32), mats, cam, env, st)
+    ref, _ = oracle.OracleScene(sc).render(threads=2)
+    assert np.array_equal(film.view(np.uint32), ref.view(np.uint32))
