@@ -364,10 +364,36 @@ __device__ __forceinline__ V3 EnvColor(const DevScene& S, V3 d) {
 }
 // Environment::ImportanceSampling (Environment.cpp:130-220)
 template <class M>
+//
+// When W and H are powers of two (all configured maps) both searches have a closed
+// form, evaluated here bit for bit:
+//   row search: every compared midpoint v is an odd multiple of 2^-k with k <= log2 H,
+//     so y = v H is an integer, the lerp weight is exactly 0 and the table value is
+//     cdf1D[y] = (y + 1) / H = v + 1/H exactly: the comparisons reduce to v + 1/H - r0;
+//   column search: for u = 2^-k (k <= log2 W) and the row found above (a multiple of
+//     1/(2H)), every bilinear weight is 0, 1/2 or 1 and the unloaded-table read is
+//     exactly 1, so 1 - r1 >= 0 at every step: u shrinks to 0.5 / W whatever r1 is;
+//   pdf: the same weights at (0.5 / W, v0) give exactly 1 * 1.
 __device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, float& pdf) {
     const int W = S.envW, H = S.envH;
     const float tw = 1.0f / W, th = 1.0f / H;
     float v0 = 0.0f, v1 = 1.0f;
+    if (((W & (W - 1)) | (H & (H - 1))) == 0 && W <= (1 << 22) && H <= (1 << 22)) {
+        for (int it = 0; it < 64; it++) {
+            const float v = 0.5f * (v0 + v1);
+            const float diff = (v + th) - r0;
+            if (v1 - v0 <= th) { v0 = v1 = v; break; }
+            if (diff > 0) v1 = v;
+            else if (diff < 0) v0 = v;
+            else { v0 = v1 = v; break; }
+        }
+        const float u0 = 0.5f * tw;
+        pdf = 1.0f;
+        const float theta = v0 * kPi;
+        const float phi = 2.0f * kPi * (1.0f - u0) + S.envRot;
+        const float cx = M::SinCos(theta, phi), cy = M::SinSin(theta, phi), cz = M::Cos(theta);
+        return cx * V3(1.f, 0.f, 0.f) + cy * V3(0.f, 1.f, 0.f) + cz * V3(0.f, 0.f, 1.f);
+    }
     for (int it = 0; it < 64; it++) {
         const float v = 0.5f * (v0 + v1);
         const float y = v * H;

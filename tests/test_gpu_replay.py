@@ -1,4 +1,5 @@
 """Replay mode on the GPU against the reference's films (bit parity path)."""
+import dataclasses
 import numpy as np
 import pytest
 
@@ -53,6 +54,20 @@ def test_replay_ragged_tiles_and_tiny_images(gpu_ctx):
         film = _render(gpu_ctx, sc)
         close, _ = _close_fraction(film, ref)
         assert close >= 0.99, (w, h, t, close)
+
+
+@pytest.mark.parametrize("env_shape", [(24, 48), (32, 64), (20, 32), (32, 40)])
+def test_replay_env_sampling_any_map_size(gpu_ctx, env_shape):
+    """Environment next-event sampling: the closed form used for power-of-two maps and
+    the bisections used otherwise both give the reference's samples bit for bit."""
+    sc = synth.cornell(width=24, height=16, spp=4, mixed=True, integrator=1, max_bounces=4,
+                       env_texture=True)
+    rng = np.random.default_rng(env_shape[0] * 100 + env_shape[1])
+    tex = rng.lognormal(0.0, 0.7, size=env_shape + (3,)).astype(np.float32)
+    sc = sc.copy_with(env=dataclasses.replace(sc.env, texture=tex))
+    ref, _ = oracle.OracleScene(sc).render()
+    film = _render(gpu_ctx, sc)
+    assert np.array_equal(film.view(np.uint32), ref.view(np.uint32)), env_shape
 
 
 def test_replay_progress_counts_tiles(gpu_ctx, golden):
