@@ -221,7 +221,8 @@ namespace {
 
 struct WideCollapser {
     const BvhResult& b;
-    std::vector<float>& out;  // 32 floats per wide node
+    std::vector<float>& out;  // WideNodeFloats(K) floats per wide node
+    const int K;
     bool ok = true;
 
     static float Area(const BvhNodeOut& n) {
@@ -229,19 +230,20 @@ struct WideCollapser {
         return 2.0f * (dx * dy + dy * dz + dz * dx);
     }
     int NewNode() {
-        const int w = (int)(out.size() / 32);
-        out.resize(out.size() + 32, 0.0f);
-        int32_t* codes = reinterpret_cast<int32_t*>(&out[(size_t)w * 32 + 24]);
-        for (int i = 0; i < 4; i++) codes[i] = INT32_MIN;
+        const size_t nf = (size_t)WideNodeFloats(K);
+        const int w = (int)(out.size() / nf);
+        out.resize(out.size() + nf, 0.0f);
+        int32_t* codes = reinterpret_cast<int32_t*>(&out[(size_t)w * nf + 6 * K]);
+        for (int i = 0; i < K; i++) codes[i] = INT32_MIN;
         return w;
     }
     void SetChild(int w, int i, const float* lo, const float* hi, int32_t code) {
-        float* f = &out[(size_t)w * 32];
+        float* f = &out[(size_t)w * WideNodeFloats(K)];
         for (int a = 0; a < 3; a++) {
-            f[4 * a + i] = lo[a];
-            f[12 + 4 * a + i] = hi[a];
+            f[K * a + i] = lo[a];
+            f[K * (3 + a) + i] = hi[a];
         }
-        std::memcpy(&f[24 + i], &code, 4);
+        std::memcpy(&f[6 * K + i], &code, 4);
     }
     int32_t LeafCode(int first, int count) {
         if (first >= (1 << 25)) ok = false;
@@ -253,8 +255,8 @@ struct WideCollapser {
         if (count <= kWideLeafMax) return LeafCode(n.begin, count);
         const int w = NewNode();
         int first = n.begin, left = count;
-        for (int i = 0; i < 4 && left > 0; i++) {
-            if (i == 3 && left > kWideLeafMax) {
+        for (int i = 0; i < K && left > 0; i++) {
+            if (i == K - 1 && left > kWideLeafMax) {
                 BvhNodeOut rest = n;
                 rest.begin = first;
                 rest.end = n.end;
@@ -272,12 +274,11 @@ struct WideCollapser {
     int32_t Node(int bi) {
         const BvhNodeOut& n = b.nodes[bi];
         if (n.leaf) return Leaf(n);
-        int cand[4] = {n.child[0], n.child[1], -1, -1};
-        int k = 2;
-        while (k < 4) {
+        std::vector<int> cand = {n.child[0], n.child[1]};
+        while ((int)cand.size() < K) {
             int best = -1;
             float bestA = -1.0f;
-            for (int i = 0; i < k; i++)
+            for (int i = 0; i < (int)cand.size(); i++)
                 if (!b.nodes[cand[i]].leaf && Area(b.nodes[cand[i]]) > bestA) {
                     bestA = Area(b.nodes[cand[i]]);
                     best = i;
@@ -285,10 +286,10 @@ struct WideCollapser {
             if (best < 0) break;
             const int open = cand[best];
             cand[best] = b.nodes[open].child[0];
-            cand[k++] = b.nodes[open].child[1];
+            cand.push_back(b.nodes[open].child[1]);
         }
         const int w = NewNode();
-        for (int i = 0; i < k; i++) {
+        for (int i = 0; i < (int)cand.size(); i++) {
             const BvhNodeOut& c = b.nodes[cand[i]];
             const int32_t code = c.leaf ? Leaf(c) : Node(cand[i]);
             SetChild(w, i, c.lo, c.hi, code);
@@ -299,10 +300,11 @@ struct WideCollapser {
 
 }  // namespace
 
-bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide) {
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width) {
     wide->clear();
     if (bvh.primIds.empty()) return true;
-    WideCollapser c{bvh, *wide};
+    if (width < 2 || width > 8) return false;
+    WideCollapser c{bvh, *wide, width};
     const BvhNodeOut& root = bvh.nodes[0];
     if (root.leaf) {  // the root itself is a leaf: a wide root with that one leaf child
         const int w = c.NewNode();

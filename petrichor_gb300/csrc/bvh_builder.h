@@ -27,13 +27,16 @@ struct BvhResult {
     int height = 0;  // longest root-to-leaf edge count
 };
 
-// Collapses the binary tree into 4-wide nodes (8 float4 each; layout in
-// pt_layout.h): each wide node takes a binary node's children and repeatedly
-// opens the largest-area inner child until it has four. Leaves of more than 63
-// primitives become chains of leaf chunks. Returns false if a leaf starts beyond
-// the 2^25 slots the child code can hold.
-bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide);
+// Collapses the binary tree into `width`-wide nodes (width 4: 32 floats, width 8:
+// 64 floats each; layout in pt_layout.h): each wide node takes a binary node's
+// children and repeatedly opens the largest-area inner child until it has `width`.
+// Leaves of more than 63 primitives become chains of leaf chunks. Returns false if
+// a leaf starts beyond the 2^25 slots the child code can hold.
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width = 4);
 constexpr int kWideLeafMax = 63;
+// Floats per wide node of the given width (6 bounds + 1 code per child, padded to
+// whole 128-byte lines).
+constexpr int WideNodeFloats(int width) { return ((7 * width + 31) / 32) * 32; }
 
 // positions: V x 3 floats; indices: T x 3. threads <= 0: hardware concurrency.
 BvhResult BuildBinnedSah(const float* positions, const int32_t* indices, int numTriangles,

@@ -442,9 +442,9 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         nodes[2 * i] = F4(n.lo[0], n.lo[1], n.lo[2], n.hi[0]);
         nodes[2 * i + 1] = F4(n.hi[1], n.hi[2], IntBits(a), IntBits(b));
     }
-    // 4-wide collapse for the throughput traversal
+    // wide collapse for the throughput traversal
     std::vector<float> wideF;
-    if (!CollapseWide(bvh, &wideF))
+    if (!CollapseWide(bvh, &wideF, kWide))
         return Fail(ctx, PT_ERR_UNSUPPORTED, "too many triangles for the wide BVH leaf encoding");
     std::vector<float4> wide(wideF.size() / 4);
     std::memcpy(wide.data(), wideF.data(), wideF.size() * sizeof(float));
@@ -537,7 +537,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         return rc;
     }
     D.numNodes = T > 0 ? (int)bvh.nodes.size() : 0;
-    D.numWide = (int)(wide.size() / 8);
+    D.numWide = (int)(wide.size() / (kWideFloats / 4));
     D.numTris = T;
     D.numMats = (int)d->num_materials;
     D.numLights = (int)d->num_lights;

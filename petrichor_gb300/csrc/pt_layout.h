@@ -8,12 +8,11 @@
 //              Node order and leaf ranges are the reference binned-SAH tree's
 //              (Core/Accel/BinnedSAHBVH.cpp:15-225), so slot k of a leaf is
 //              m_primitiveIDs[k].
-//   wide       8 x float4 per 4-wide node (128 B, one L2 line), the binary tree
-//              collapsed for the throughput traversal:
-//                [0..5] lo.x lo.y lo.z hi.x hi.y hi.z of the four children (SoA)
-//                [6]    child codes: >= 0 wide node; < 0 leaf, -(first*64+count)-1;
-//                       INT_MIN empty slot
-//                [7]    unused
+//   wide       kWide-wide nodes of the binary tree collapsed for the throughput
+//              traversal, kWideFloats floats each (4-wide: 128 B, one L2 line):
+//                lo.x lo.y lo.z hi.x hi.y hi.z of the children (kWide floats each, SoA),
+//                then the child codes: >= 0 wide node; < 0 leaf, -(first*64+count)-1;
+//                INT_MIN empty slot; padding to whole 128-byte lines
 //   tris       3 x float4 per primitive slot (48 B), in leaf order:
 //                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) 0 0
 //              e1 = v1 - v0, e2 = v2 - v0 exactly as Triangle::Intersect forms
@@ -36,6 +35,13 @@
 #endif
 
 namespace ptg {
+
+// Width of the throughput traversal's BVH nodes (4 or 8).
+#ifndef PT_WIDE
+#define PT_WIDE 4
+#endif
+constexpr int kWide = PT_WIDE;
+constexpr int kWideFloats = ((7 * kWide + 31) / 32) * 32;
 
 enum MaterialKind : int32_t {
     kLambert = 0,

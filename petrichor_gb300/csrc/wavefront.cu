@@ -171,45 +171,72 @@ __device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur) 
     return false;
 }
 
-// Tests the four children of wide node `cur`; `cur` becomes the nearest hit child
-// and the other hit children are pushed farthest first (or the next stack item).
+// Tests the children of wide node `cur`; `cur` becomes the nearest hit child and
+// the other hit children are pushed farthest first (or the next stack item).
 __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur, int& err) {
-    const float4* n = r.nodes + 8 * (size_t)cur;
-    const float4 lx = __ldg(n), ly = __ldg(n + 1), lz = __ldg(n + 2);
-    const float4 hx = __ldg(n + 3), hy = __ldg(n + 4), hz = __ldg(n + 5);
-    const int4 code = __ldg(reinterpret_cast<const int4*>(n + 6));
+    constexpr int K = kWide, Q = kWide / 4;
+    const float4* n = r.nodes + (kWideFloats / 4) * (size_t)cur;
+    float b[6][K];
+#pragma unroll
+    for (int a = 0; a < 6; a++)
+#pragma unroll
+        for (int j = 0; j < Q; j++) {
+            const float4 v = __ldg(n + a * Q + j);
+            b[a][4 * j] = v.x;
+            b[a][4 * j + 1] = v.y;
+            b[a][4 * j + 2] = v.z;
+            b[a][4 * j + 3] = v.w;
+        }
+    int c[K];
+#pragma unroll
+    for (int j = 0; j < Q; j++) {
+        const int4 v = __ldg(reinterpret_cast<const int4*>(n + 6 * Q + j));
+        c[4 * j] = v.x;
+        c[4 * j + 1] = v.y;
+        c[4 * j + 2] = v.z;
+        c[4 * j + 3] = v.w;
+    }
     const float inf = __int_as_float(0x7f800000);
-    float t0 = inf, t1 = inf, t2 = inf, t3 = inf;
-    int c0 = code.x, c1 = code.y, c2 = code.z, c3 = code.w;
-    float te;
-    if (c0 != INT_MIN && SlabFast(make_float4(lx.x, ly.x, lz.x, hx.x), make_float4(hy.x, hz.x, 0.f, 0.f),
-                                  r.o, r.inv, 0.0f, r.tBest, te)) t0 = te;
-    if (c1 != INT_MIN && SlabFast(make_float4(lx.y, ly.y, lz.y, hx.y), make_float4(hy.y, hz.y, 0.f, 0.f),
-                                  r.o, r.inv, 0.0f, r.tBest, te)) t1 = te;
-    if (c2 != INT_MIN && SlabFast(make_float4(lx.z, ly.z, lz.z, hx.z), make_float4(hy.z, hz.z, 0.f, 0.f),
-                                  r.o, r.inv, 0.0f, r.tBest, te)) t2 = te;
-    if (c3 != INT_MIN && SlabFast(make_float4(lx.w, ly.w, lz.w, hx.w), make_float4(hy.w, hz.w, 0.f, 0.f),
-                                  r.o, r.inv, 0.0f, r.tBest, te)) t3 = te;
+    float t[K];
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        float te;
+        t[i] = (c[i] != INT_MIN && SlabFast(make_float4(b[0][i], b[1][i], b[2][i], b[3][i]),
+                                            make_float4(b[4][i], b[5][i], 0.f, 0.f), r.o, r.inv,
+                                            0.0f, r.tBest, te))
+                 ? te
+                 : inf;
+    }
     // sorting network, nearest first
-    SortPair(t0, c0, t1, c1);
-    SortPair(t2, c2, t3, c3);
-    SortPair(t0, c0, t2, c2);
-    SortPair(t1, c1, t3, c3);
-    SortPair(t1, c1, t2, c2);
-    if (t0 == inf) {
+    if (K == 4) {
+        SortPair(t[0], c[0], t[1], c[1]);
+        SortPair(t[2], c[2], t[3], c[3]);
+        SortPair(t[0], c[0], t[2], c[2]);
+        SortPair(t[1], c[1], t[3], c[3]);
+        SortPair(t[1], c[1], t[2], c[2]);
+    } else {
+        constexpr int kNet[19][2] = {{0, 2}, {1, 3}, {4, 6}, {5, 7}, {0, 4}, {1, 5}, {2, 6},
+                                     {3, 7}, {0, 1}, {2, 3}, {4, 5}, {6, 7}, {2, 4}, {3, 5},
+                                     {1, 4}, {3, 6}, {1, 2}, {3, 4}, {5, 6}};
+#pragma unroll
+        for (int k = 0; k < 19; k++) SortPair(t[kNet[k][0] % K], c[kNet[k][0] % K], t[kNet[k][1] % K], c[kNet[k][1] % K]);
+    }
+    if (t[0] == inf) {
         cur = stk.Pop(r.tBest);
         return;
     }
-    const int pushes = (t1 != inf) + (t2 != inf) + (t3 != inf);
+    int pushes = 0;
+#pragma unroll
+    for (int i = 1; i < K; i++) pushes += t[i] != inf;
     if (stk.sp + pushes > kWaveStackDepth) {
         err = 1;
         cur = kDone;
         return;
     }
-    if (t3 != inf) stk.Push(c3, t3);
-    if (t2 != inf) stk.Push(c2, t2);
-    if (t1 != inf) stk.Push(c1, t1);
-    cur = c0;
+#pragma unroll
+    for (int i = K - 1; i >= 1; i--)
+        if (t[i] != inf) stk.Push(c[i], t[i]);
+    cur = c[0];
 }
 
 // Q provides: void Load(int i, LaneRay&) (ray, range, and the scene: nodes = nullptr
