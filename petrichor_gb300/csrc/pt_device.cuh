@@ -82,6 +82,8 @@ struct ExactMath {
     static __device__ __forceinline__ float SinSin(float t, float p) {
         return (float)(sin((double)t) * sin((double)p));
     }
+    // Vector3f::Normalized: each component divided by the length
+    static __device__ __forceinline__ V3 Norm(V3 a) { return Normalized(a); }
     // -0.5f + 0.5f * sqrt(x) evaluated in double (GGX.cpp:148)
     static __device__ __forceinline__ float SmithLambda(float x) {
         return (float)((double)-0.5f + (double)0.5f * sqrt((double)x));
@@ -91,18 +93,24 @@ struct ExactMath {
         return (float)((double)ndn + sqrt((double)disc));
     }
 };
+// Sines and cosines go through sinpif/cospif of the angle in half turns: the angles
+// here are small (sampled on [0, 2 pi] or [0, pi]), the half-turn functions need no
+// large-argument reduction, and the shade kernel's code stays small enough for the
+// instruction cache. They agree with sinf/cosf to a few ulps.
 struct FastMath {
-    static __device__ __forceinline__ float Cos(float x) { return cosf(x); }
-    static __device__ __forceinline__ float Sin(float x) { return sinf(x); }
+    static __device__ __forceinline__ float Cos(float x) { return cospif(x * kInvPi); }
+    static __device__ __forceinline__ float Sin(float x) { return sinpif(x * kInvPi); }
     static __device__ __forceinline__ float Acos(float x) { return acosf(x); }
     static __device__ __forceinline__ float Atan2(float y, float x) { return atan2f(y, x); }
-    static __device__ __forceinline__ float MulCos(float a, float x) { return a * cosf(x); }
-    static __device__ __forceinline__ float MulSin(float a, float x) { return a * sinf(x); }
+    static __device__ __forceinline__ float MulCos(float a, float x) { return a * Cos(x); }
+    static __device__ __forceinline__ float MulSin(float a, float x) { return a * Sin(x); }
     static __device__ __forceinline__ float MulSinMul(float a, float x, float b) {
-        return a * sinf(x) * b;
+        return a * Sin(x) * b;
     }
-    static __device__ __forceinline__ float SinCos(float t, float p) { return sinf(t) * cosf(p); }
-    static __device__ __forceinline__ float SinSin(float t, float p) { return sinf(t) * sinf(p); }
+    static __device__ __forceinline__ float SinCos(float t, float p) { return Sin(t) * Cos(p); }
+    static __device__ __forceinline__ float SinSin(float t, float p) { return Sin(t) * Sin(p); }
+    // one division and three products instead of three divisions
+    static __device__ __forceinline__ V3 Norm(V3 a) { return a * (1.0f / Length(a)); }
     static __device__ __forceinline__ float SmithLambda(float x) { return -0.5f + 0.5f * sqrtf(x); }
     static __device__ __forceinline__ float RefractScale(float ndn, float disc) {
         return ndn + sqrtf(disc);
@@ -216,6 +224,7 @@ __device__ __forceinline__ int ResolveMaterial(const DevMaterial* __restrict__ m
 }
 
 // Triangle::Interpolate (Triangle.cpp:90-153); k = primitive slot
+template <class M>
 __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V3 d, float dist) {
     Shading si;
     si.pos = o + d * dist;
@@ -225,7 +234,7 @@ __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V
     const float4 s1 = __ldg(S.shade + 3 * k + 1);
     const V3 ce = Cross(e1, e2);
     if (__float_as_int(s1.w) == 0) {
-        si.n = Normalized(ce);
+        si.n = M::Norm(ce);
     } else {
         const float4 s2 = __ldg(S.shade + 3 * k + 2);
         const float invDet = 1.0f / Dot(-d, ce);
@@ -233,7 +242,7 @@ __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V
         const float w1 = Dot(vec, Cross(d, e2)) * invDet;
         const float w2 = Dot(vec, Cross(e1, d)) * invDet;
         const V3 n0(s0.x, s0.y, s0.z), n1(s1.x, s1.y, s1.z), n2(s2.x, s2.y, s2.z);
-        si.n = Normalized(w1 * (n1 - n0) + w2 * (n2 - n0) + n0);
+        si.n = M::Norm(w1 * (n1 - n0) + w2 * (n2 - n0) + n0);
     }
     si.mat = ResolveMaterial(S.mats, __float_as_int(s0.w), 0.0f);
     return si;
@@ -269,17 +278,19 @@ __device__ __forceinline__ V3 SampleLightPoint(const DevScene& S, int i, float u
 // ---------------------------------------------------------------- ONB
 struct ONB {  // Math/OrthonormalBasis.cpp:10-62
     V3 u, v, w;
+    template <class M>
     __device__ __forceinline__ void Build(V3 n) {
-        w = Normalized(n);
+        w = M::Norm(n);
         const float sign = copysignf(1.0f, w.z);
         const float a = -1.0f / (sign + w.z);
         const float b = w.x * w.y * a;
         u = V3(1.0f + sign * w.x * w.x * a, sign * b, -sign * w.x);
         v = V3(b, sign + w.y * w.y * a, -w.y);
     }
+    template <class M>
     __device__ __forceinline__ void Build(V3 ww, V3 uu) {
-        w = Normalized(ww);
-        u = Normalized(uu);
+        w = M::Norm(ww);
+        u = M::Norm(uu);
         v = Cross(w, u);
     }
     __device__ __forceinline__ V3 WorldToLocal(V3 a) const { return V3(Dot(a, u), Dot(a, v), Dot(a, w)); }
@@ -303,7 +314,7 @@ __device__ __forceinline__ Ray GenerateRay(const DevCamera& c, int i, int j, int
                       -up * 0.5f * c.aperture * r * M::Sin(theta);
     Ray ray;
     ray.o = onLens;
-    ray.d = Normalized(onSensor - onLens);
+    ray.d = M::Norm(onSensor - onLens);
     const float dd = Dot(ray.d, fwd);
     ray.T = V3(1.f, 1.f, 1.f) * dd * dd * c.focusDist * c.focusDist / SqLen(onSensor - onLens);
     return ray;
@@ -362,38 +373,13 @@ __device__ __forceinline__ V3 EnvColor(const DevScene& S, V3 d) {
     v = Mod1(v);
     return base * EnvBilinear(S, u * S.envW, v * S.envH);
 }
-// Environment::ImportanceSampling (Environment.cpp:130-220)
-template <class M>
-//
-// When W and H are powers of two (all configured maps) both searches have a closed
-// form, evaluated here bit for bit:
-//   row search: every compared midpoint v is an odd multiple of 2^-k with k <= log2 H,
-//     so y = v H is an integer, the lerp weight is exactly 0 and the table value is
-//     cdf1D[y] = (y + 1) / H = v + 1/H exactly: the comparisons reduce to v + 1/H - r0;
-//   column search: for u = 2^-k (k <= log2 W) and the row found above (a multiple of
-//     1/(2H)), every bilinear weight is 0, 1/2 or 1 and the unloaded-table read is
-//     exactly 1, so 1 - r1 >= 0 at every step: u shrinks to 0.5 / W whatever r1 is;
-//   pdf: the same weights at (0.5 / W, v0) give exactly 1 * 1.
-__device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, float& pdf) {
+// The two bisections of Environment::ImportanceSampling (Environment.cpp:150-200), used
+// for maps whose dimensions are not both powers of two.
+__device__ __forceinline__ void EnvSampleSearch(const DevScene& S, float r0, float r1, float& u0, float& v0, float& pdf) {
     const int W = S.envW, H = S.envH;
     const float tw = 1.0f / W, th = 1.0f / H;
-    float v0 = 0.0f, v1 = 1.0f;
-    if (((W & (W - 1)) | (H & (H - 1))) == 0 && W <= (1 << 22) && H <= (1 << 22)) {
-        for (int it = 0; it < 64; it++) {
-            const float v = 0.5f * (v0 + v1);
-            const float diff = (v + th) - r0;
-            if (v1 - v0 <= th) { v0 = v1 = v; break; }
-            if (diff > 0) v1 = v;
-            else if (diff < 0) v0 = v;
-            else { v0 = v1 = v; break; }
-        }
-        const float u0 = 0.5f * tw;
-        pdf = 1.0f;
-        const float theta = v0 * kPi;
-        const float phi = 2.0f * kPi * (1.0f - u0) + S.envRot;
-        const float cx = M::SinCos(theta, phi), cy = M::SinSin(theta, phi), cz = M::Cos(theta);
-        return cx * V3(1.f, 0.f, 0.f) + cy * V3(0.f, 1.f, 0.f) + cz * V3(0.f, 0.f, 1.f);
-    }
+    v0 = 0.0f;
+    float v1 = 1.0f;
     for (int it = 0; it < 64; it++) {
         const float v = 0.5f * (v0 + v1);
         const float y = v * H;
@@ -406,7 +392,8 @@ __device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, f
         else if (diff < 0) v0 = v;
         else { v0 = v1 = v; break; }
     }
-    float u0 = 0.0f, u1 = 1.0f;
+    float u1 = 1.0f;
+    u0 = 0.0f;
     for (int it = 0; it < 64; it++) {
         const float u = 0.5f * (u0 + u1);
         const float c = UnloadedTableBilinearX(u, v0, W, H);
@@ -421,6 +408,37 @@ __device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, f
         const int y1 = min(y0 + 1, H - 1);
         const float py = Lerp(kEnvRowPdf, kEnvRowPdf, y - y0);
         pdf = py * UnloadedTableBilinearX(u0, v0, W, H);
+    }
+}
+// Environment::ImportanceSampling (Environment.cpp:130-220)
+//
+// When W and H are powers of two (all configured maps) both searches have a closed
+// form, evaluated here bit for bit:
+//   row search: every compared midpoint v is an odd multiple of 2^-k with k <= log2 H,
+//     so y = v H is an integer, the lerp weight is exactly 0 and the table value is
+//     cdf1D[y] = (y + 1) / H = v + 1/H exactly: the comparisons reduce to v + 1/H - r0;
+//   column search: for u = 2^-k (k <= log2 W) and the row found above (a multiple of
+//     1/(2H)), every bilinear weight is 0, 1/2 or 1 and the unloaded-table read is
+//     exactly 1, so 1 - r1 >= 0 at every step: u shrinks to 0.5 / W whatever r1 is;
+//   pdf: the same weights at (0.5 / W, v0) give exactly 1 * 1.
+template <class M>
+__device__ __forceinline__ V3 EnvSample(const DevScene& S, float r0, float r1, float& pdf) {
+    const int W = S.envW, H = S.envH;
+    const float tw = 1.0f / W, th = 1.0f / H;
+    float u0, v0 = 0.0f, v1 = 1.0f;
+    if (((W & (W - 1)) | (H & (H - 1))) == 0 && W <= (1 << 22) && H <= (1 << 22)) {
+        for (int it = 0; it < 64; it++) {
+            const float v = 0.5f * (v0 + v1);
+            const float diff = (v + th) - r0;
+            if (v1 - v0 <= th) { v0 = v1 = v; break; }
+            if (diff > 0) v1 = v;
+            else if (diff < 0) v0 = v;
+            else { v0 = v1 = v; break; }
+        }
+        u0 = 0.5f * tw;
+        pdf = 1.0f;
+    } else {
+        EnvSampleSearch(S, r0, r1, u0, v0, pdf);
     }
     const float theta = v0 * kPi;
     const float phi = 2.0f * kPi * (1.0f - u0) + S.envRot;
@@ -464,7 +482,7 @@ template <class M>
 __device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) {
     if (m.kind == kLambert) return MatColor(m) * V3(1.f, 1.f, 1.f) * kInvPi;
     if (m.kind == kGlossy) {
-        const V3 h = Normalized(-din + dout);
+        const V3 h = M::Norm(-din + dout);
         const float hn = fabsf(Dot(h, n));
         const float a = m.alpha, a2 = a * a, hn2 = hn * hn;
         const float k = (a2 - 1.0f) * hn2 + 1.0f;
@@ -479,10 +497,11 @@ __device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) 
     return V3(0.f, 0.f, 0.f);
 }
 // MaterialBase::PDF (Lambert.cpp:33-47, GGX.cpp:59-76, Glass.cpp:20-27)
+template <class M>
 __device__ __forceinline__ float BsdfPdf(const DevMaterial& m, V3 din, V3 dout, V3 n) {
     if (m.kind == kLambert) return fabsf(Dot(dout, n)) * kInvPi;
     if (m.kind == kGlossy) {
-        const V3 h = Normalized(-din + dout);
+        const V3 h = M::Norm(-din + dout);
         const float hn = fabsf(Dot(h, n));
         const float a2 = m.alpha * m.alpha, hn2 = hn * hn;
         const float tmp = 1.0f - (1.0f - a2) * hn2;
@@ -496,12 +515,12 @@ __device__ __forceinline__ V3 SampleVNDF(const DevMaterial& m, V3 view, V3 n0, f
     const V3 n = n0 * copysignf(1.0f, Dot(view, n0));
     ONB surf;
     const V3 t = (fabsf(n.z) < 0.9999f) ? Cross(n, V3(0.f, 0.f, 1.f)) : V3(1.f, 0.f, 0.f);
-    surf.Build(n, t);
+    surf.template Build<M>(n, t);
     V3 v = surf.WorldToLocal(view);
     const float alpha = m.alpha;
     v = v * V3(alpha, alpha, 1.0f);
     v = v / Length(v);
-    const V3 t1 = (v.z < 0.9999f) ? Normalized(Cross(v, V3(0.f, 0.f, 1.f))) : V3(1.f, 0.f, 0.f);
+    const V3 t1 = (v.z < 0.9999f) ? M::Norm(Cross(v, V3(0.f, 0.f, 1.f))) : V3(1.f, 0.f, 0.f);
     const V3 t2 = Cross(t1, v);
     const float a = 1.0f / (1.0f + v.z);
     const float r = sqrtf(u0);
@@ -523,7 +542,7 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
     if (m.kind == kLambert) {
         const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
         ONB onb;
-        onb.Build(n);
+        onb.template Build<M>(n);
         float r0, r1;
         s2.Next(r0, r1);
         const float phi = 2.0f * kPi * r1;
@@ -563,7 +582,7 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         const float disc = dn * dn - 1 + eta * eta;
         if (disc < 0) {  // total internal reflection
             out.o = si.pos + kEps * n;
-            out.d = Normalized(Reflected(in.d, n));
+            out.d = M::Norm(Reflected(in.d, n));
             out.T = V3(0.f, 0.f, 0.f);
             out.bounce = 0 + 1;
             out.prob = in.prob;
@@ -571,7 +590,7 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
             return out;
         }
         const V3 rd = (1.0f / eta) * (in.d - si.n * M::RefractScale(-dn, disc));
-        out.d = Normalized(rd);
+        out.d = M::Norm(rd);
         const float nd = Dot(si.n, out.d);
         const float q = (1.0f - eta) / (1.0f + eta);
         const float f0 = q * q;

@@ -42,7 +42,7 @@ __device__ void ReplaySimplePixel(const DevScene& S, const DevCamera& C, const D
                 contrib = contrib + ray.T * MatColor(S.mats[m]);
                 break;
             }
-            const Shading si = Interpolate(S, k, ray.o, ray.d, dist);
+            const Shading si = Interpolate<ExactMath>(S, k, ray.o, ray.d, dist);
             ray = NextRay<ExactMath>(S.mats[m], ray, si, s2);
             if (ray.bounce > st.maxBounces) {
                 ray.prob *= 0.9f;
@@ -104,7 +104,7 @@ __device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1
         const int k = TraverseReference(S, p, ld, 0.0f, kFltMax, d, stack, status);
         if (k >= 0) {
             if (IsEmission(S, ResolveMaterial(S.mats, SlotMaterial(S.shade, k), s1.Next()))) {
-                const Shading sl = Interpolate(S, k, p, ld, d);
+                const Shading sl = Interpolate<ExactMath>(S, k, p, ld, d);
                 const float dist = SqLen(pl - sl.pos);
                 if (fabsf(dist - 0.0f) < kEps) {
                     const float l2 = SqLen(sl.pos - si.pos);
@@ -112,7 +112,7 @@ __device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1
                     float mis = 0.0f;
                     if (l2 > 0.0f) {
                         const float pL = pdfArea;
-                        const float pB = BsdfPdf(M, ray.d, ld, si.n) * cosP / l2;
+                        const float pB = BsdfPdf<ExactMath>(M, ray.d, ld, si.n) * cosP / l2;
                         mis = pL * pL / (pL * pL + pB * pB);
                     }
                     const V3 li = MatColor(S.mats[sl.mat]);
@@ -132,7 +132,7 @@ __device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1
         if (TraverseReference(S, eo, sd, 0.0f, kFltMax, d, stack, status) < 0) {
             const float c = fabsf(Dot(sd, si.n));
             const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf(M, ray.d, sd, si.n);
+            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<ExactMath>(M, ray.d, sd, si.n);
             const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
             const V3 li = EnvColor<ExactMath>(S, sd);
             const V3 f = BxDF<ExactMath>(M, ray.d, sd, si.n);
@@ -162,7 +162,7 @@ __device__ void ReplayPtPixel(const DevScene& S, const DevCamera& C, const DevSe
                 sum = sum + ray.T * EnvColor<ExactMath>(S, ray.d);
                 continue;
             }
-            si = Interpolate(S, k, ray.o, ray.d, d);
+            si = Interpolate<ExactMath>(S, k, ray.o, ray.d, d);
         }
         if (IsEmission(S, si.mat)) {
             sum = sum + ray.T * MatColor(S.mats[si.mat]);
@@ -177,14 +177,14 @@ __device__ void ReplayPtPixel(const DevScene& S, const DevCamera& C, const DevSe
             float d;
             const int k = TraverseReference(S, ray.o, ray.d, 0.0f, kFltMax, d, stack, status);
             if (k >= 0) {
-                const Shading sn = Interpolate(S, k, ray.o, ray.d, d);
+                const Shading sn = Interpolate<ExactMath>(S, k, ray.o, ray.d, d);
                 if (IsEmission(S, sn.mat)) {
                     const float l2 = SqLen(sn.pos - ray.o);
                     const float cosP = fabsf(Dot(ray.d, sn.n));
                     bool unused = false;
                     ReplaySampleLight(S, s1.Next(), s2, false, &unused);
                     const float pdfArea = S.lightPdfArea;
-                    const float pB = BsdfPdf(S.mats[m], prev.d, ray.d, si.n);
+                    const float pB = BsdfPdf<ExactMath>(S.mats[m], prev.d, ray.d, si.n);
                     const float pL = l2 / cosP * pdfArea;
                     const float mis = pB * pB / (pL * pL + pB * pB);
                     color = color + mis * ray.T * MatColor(S.mats[sn.mat]);
@@ -195,7 +195,7 @@ __device__ void ReplayPtPixel(const DevScene& S, const DevCamera& C, const DevSe
                 if (S.envValid) {
                     const float c = fabsf(Dot(si.n, ray.d));
                     const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-                    const float pB = BsdfPdf(S.mats[m], prev.d, ray.d, si.n);
+                    const float pB = BsdfPdf<ExactMath>(S.mats[m], prev.d, ray.d, si.n);
                     float mis = 0.0f;
                     if (ray.d.x != 0 && ray.d.y != 0 && sn > 0) {
                         const float pE = EnvPdf<ExactMath>(S, ray.d) / (2.0f * kPi * kPi * sn);
@@ -280,7 +280,7 @@ __device__ V3 AovPath(const DevScene& S, const DevSettings& st, Ray ray, bool no
         const int k = TraverseReference(S, ray.o, ray.d, kEps, kInfinity, d, stack, status);
         if (k < 0) return normal ? ray.T * (-ray.d) : ray.T * EnvColor<ExactMath>(S, ray.d);
         const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, k), s1.Next());
-        const Shading si = Interpolate(S, k, ray.o, ray.d, d);
+        const Shading si = Interpolate<ExactMath>(S, k, ray.o, ray.d, d);
         const DevMaterial& M = S.mats[m];
         if (M.kind == kLambert) return normal ? ray.T * si.n : ray.T * V3(1.f, 1.f, 1.f);
         if (M.kind == kGlossy && M.alpha != 0) return normal ? ray.T * si.n : ray.T * GgxF0(M);

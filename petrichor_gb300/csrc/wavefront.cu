@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                 if (S.mats[m].kind == kEmission) {
                     L = L + in.T * MatColor(S.mats[m]);
                 } else {
-                    const Shading si = Interpolate(S, slot, o, d, h.x);
+                    const Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
                     out = NextRay<FastMath>(S.mats[m], in, si, rng);
                     cont = true;
                     if (out.bounce > st.maxBounces) {
@@ -456,23 +456,17 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
             // PathTracing.cpp:38-196; k = BSDF bounces taken so far
             const int k = in.bounce;
             if (slot < 0) {
+                // one lookup for the three cases (mis = 1 multiplies exactly)
+                float mis = 1.0f;
                 if (k == 0) {
-                    L = L + in.T * EnvColor<FastMath>(S, d);
                     flags |= kFlagNoSignCheck;
-                } else if (S.envValid) {
-                    float mis;
-                    if (d.x != 0 && d.y != 0 && lastSin > 0) {
-                        const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
-                        mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
-                    } else {
-                        mis = 1.0f;
-                    }
-                    L = L + mis * in.T * EnvColor<FastMath>(S, d);
-                } else {
-                    L = L + in.T * EnvColor<FastMath>(S, d);
+                } else if (S.envValid && d.x != 0 && d.y != 0 && lastSin > 0) {
+                    const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
+                    mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
                 }
+                L = L + mis * in.T * EnvColor<FastMath>(S, d);
             } else {
-                const Shading si = Interpolate(S, slot, o, d, h.x);
+                const Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
                 const DevMaterial& M = S.mats[si.mat];
                 if (M.kind == kEmission) {
                     if (k == 0) {
@@ -500,7 +494,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                             const V3 sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
                             const float c = fabsf(Dot(sd, si.n));
                             const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-                            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf(M, d, sd, si.n);
+                            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, si.n);
                             const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
                             const V3 li = EnvColor<FastMath>(S, sd);
                             const V3 f = BxDF<FastMath>(M, d, sd, si.n);
@@ -528,7 +522,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                             shadow = true;
                             sh0 = make_float4(p.x, p.y, p.z, dist);
                             sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
-                            sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf(M, d, ld, si.n));
+                            sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf<FastMath>(M, d, ld, si.n));
                             sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, pick);
                         }
                     }
@@ -546,7 +540,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                     out = NextRay<FastMath>(M, in, si, rng);
                     if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
                         cont = true;
-                        lastPdf = BsdfPdf(M, d, out.d, si.n);
+                        lastPdf = BsdfPdf<FastMath>(M, d, out.d, si.n);
                         const float c = fabsf(Dot(si.n, out.d));
                         lastSin = sqrtf(SMax(0.0f, 1.0f - c * c));
                         out.bounce = k + 1;
@@ -609,7 +603,7 @@ struct ShadowQueue {
         const float4 e2 = entries[4 * j + 2], e3 = entries[4 * j + 3];
         const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, r.best), e3.w);
         if (S.mats[m].kind != kEmission) return;
-        const Shading sl = Interpolate(S, r.best, r.o, r.d, r.tBest);
+        const Shading sl = Interpolate<FastMath>(S, r.best, r.o, r.d, r.tBest);
         const V3 pl = r.o + r.d * e0.w;
         if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
         const V3 sipos(e3.x, e3.y, e3.z);
