@@ -23,6 +23,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 CU_SOURCES = ["replay.cu", "wavefront.cu", "noalloc.cu"]
+# The throughput kernels use approximate division and square root (a few ulps), except
+# where the code asks for correctly rounded results (traversal reciprocals, the
+# triangle test); the replay kernel keeps IEEE arithmetic throughout.
+FAST_DIV_SQRT = {"wavefront.cu": ["-prec-div=false", "-prec-sqrt=false"]}
 CPP_SOURCES = ["capi.cpp", "bvh_builder.cpp", "scheduler.cpp", "server.cpp", "cpp_api.cpp",
                "cpp_loaders.cpp"]
 
@@ -58,6 +62,7 @@ def build(force: bool = False, verbose: bool = False, defines=()) -> str:
     for s in CU_SOURCES:
         o = os.path.join(OBJ_DIR, s + ".o")
         jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
+                     *FAST_DIV_SQRT.get(s, []),
                      *[f"-D{d}" for d in defines],
                      "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", *inc, "-c",
                      os.path.join(CSRC, s), "-o", o])

@@ -47,6 +47,11 @@ __device__ __forceinline__ V3 Cross(V3 a, V3 b) {
 __device__ __forceinline__ float SqLen(V3 a) { return Dot(a, a); }
 __device__ __forceinline__ float Length(V3 a) { return sqrtf(Dot(a, a)); }  // = (float)sqrt(double)
 __device__ __forceinline__ V3 Normalized(V3 a) { return a / Length(a); }
+// 1 / d per component, correctly rounded whatever the file's division flags: the
+// traversal's slab tests and the triangle test keep the reference's arithmetic.
+__device__ __forceinline__ V3 ExactRecip(V3 d) {
+    return V3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
+}
 // std::min / std::max argument semantics (NaN handling included)
 __device__ __forceinline__ float SMin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float SMax(float a, float b) { return (a < b) ? b : a; }
@@ -100,7 +105,8 @@ struct ExactMath {
 struct FastMath {
     static __device__ __forceinline__ float Cos(float x) { return cospif(x * kInvPi); }
     static __device__ __forceinline__ float Sin(float x) { return sinpif(x * kInvPi); }
-    static __device__ __forceinline__ float Acos(float x) { return acosf(x); }
+    // clamped: directions normalised with approximate division may reach |z| > 1
+    static __device__ __forceinline__ float Acos(float x) { return acosf(fminf(fmaxf(x, -1.0f), 1.0f)); }
     static __device__ __forceinline__ float Atan2(float y, float x) { return atan2f(y, x); }
     static __device__ __forceinline__ float MulCos(float a, float x) { return a * Cos(x); }
     static __device__ __forceinline__ float MulSin(float a, float x) { return a * Sin(x); }
@@ -201,7 +207,7 @@ __device__ __forceinline__ int SlotMaterial(const float4* __restrict__ shade, in
 // Triangle::Intersect (Core/Geometry/Triangle.cpp:51-88)
 __device__ __forceinline__ bool TriIntersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& dist) {
     const V3 ce = Cross(e1, e2);
-    const float invDet = 1.0f / Dot(-d, ce);
+    const float invDet = __fdiv_rn(1.0f, Dot(-d, ce));  // correctly rounded in every build
     const V3 vec = o - v0;
     const float w1 = Dot(vec, Cross(d, e2)) * invDet;
     const float w2 = Dot(vec, Cross(e1, d)) * invDet;
@@ -549,7 +555,7 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         const float st = sqrtf(r0);
         const float cu = M::MulCos(st, phi);
         const float cv = M::MulSin(st, phi);
-        const float cw = sqrtf(1.0f - st * st);
+        const float cw = sqrtf(SMax(0.0f, 1.0f - st * st));  // >= 0 already with IEEE sqrt
         out.o = si.pos + kEps * n;
         out.d = cu * onb.u + cv * onb.v + cw * onb.w;
         out.T = in.T * V3(1.f, 1.f, 1.f);
@@ -626,7 +632,7 @@ __device__ int TraverseReference(const DevScene& S, V3 o, V3 d, float distMin, f
                                  float& bestD, int* __restrict__ stack, int* status,
                                  unsigned* nodeTests = nullptr, unsigned* triTests = nullptr) {
     if (S.numNodes == 0) return -1;
-    const V3 inv = 1.0f / d;
+    const V3 inv = ExactRecip(d);
     const int s0 = inv.x < 0.0f, s1 = inv.y < 0.0f, s2 = inv.z < 0.0f;
     int sp = 0;
     stack[sp++] = 0;

@@ -270,7 +270,7 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
                 if (i < n) {
                     idx = i;
                     q.Load(i, r);
-                    r.inv = 1.0f / r.d;
+                    r.inv = ExactRecip(r.d);
                     r.tBest = r.tmax;
                     r.best = -1;
                     stk.sp = 0;
