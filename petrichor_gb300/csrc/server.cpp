@@ -88,7 +88,9 @@ struct Request {
 class Server {
 public:
     Server(pt_context* ctx, const pt_serve_config& cfg) : ctx_(ctx), cfg_(cfg) {
-        if (cfg_.wave_paths <= 0) cfg_.wave_paths = 1 << 25;
+        // 2^26 paths (15.8 GB of wave state): at saturation the waves are full enough
+        // to beat one-request-at-a-time rendering; under light load they stay small
+        if (cfg_.wave_paths <= 0) cfg_.wave_paths = 1 << 26;
         if (cfg_.max_active <= 0) cfg_.max_active = 256;
         cfg_.max_active = std::min(cfg_.max_active, kMaxJobsPerCall);
         if (cfg_.state_budget == 0) cfg_.state_budget = uint64_t(4) << 30;
