@@ -135,6 +135,9 @@ struct Material {
     float ior;
     float mix;
     int mat0, mat1;
+    // texture maps (Scene::textures index or -1) and their strengths
+    int albedoTex = -1, f0Tex = -1, roughTex = -1, normalTex = -1;
+    float roughStrength = 1.0f, normalStrength = 1.0f;
 };
 struct Ray {  // Core/Ray.h:42-48
     V3 o, dir;
@@ -143,8 +146,8 @@ struct Ray {  // Core/Ray.h:42-48
     float prob = 1.0f;
     float ior = 1.0f;
 };
-struct Shading {  // Core/HitInfo.h:20-27 (tangent omitted: only normal maps read it)
-    V3 normal, pos, uv;
+struct Shading {  // Core/HitInfo.h:20-27
+    V3 normal, tangent, pos, uv;
     int material;
 };
 struct Texture {  // Core/Texture2D.h: AoS RGB float, row-major; "valid" = loaded
@@ -330,6 +333,7 @@ struct Scene {
     std::vector<int> idx, triMat;
     std::vector<uint8_t> shade;
     std::vector<int> lights;
+    std::vector<Texture> textures;  // material texture maps (loaded textures)
     // BVH
     std::vector<BVHNode> nodes;
     std::vector<int> primIDs;
@@ -380,12 +384,15 @@ static Shading Interpolate(const Scene& s, int t, const Ray& ray, float dist) {
     const V3 duv1 = s.UV[i1] - s.UV[i0];
     const V3 duv2 = s.UV[i2] - s.UV[i0];
     si.uv = w1 * duv1 + w2 * duv2 + s.UV[i0];
+    si.tangent = duv2.y * e1 - duv1.y * e2;
     if (s.shade[t] == 0) {
         si.normal = Normalized(ce);
     } else {
         si.normal = w1 * (s.N[i1] - s.N[i0]) + w2 * (s.N[i2] - s.N[i0]) + s.N[i0];
         si.normal = Normalized(si.normal);
+        si.tangent = si.tangent - Dot(si.normal, si.tangent) * si.normal;
     }
+    if (SqLen(si.tangent) == 0.0f) si.tangent = V3(1, 0, 0);
     si.material = s.GetMaterial(t, 0.0f);
     return si;
 }
@@ -581,10 +588,37 @@ static inline int IntersectDefault(const Scene& s, const Ray& r, float* d) {  //
 }
 
 // ---------------------------------------------------------------- materials
-static inline V3 LambertAlbedo(const Material&) { return V3(1, 1, 1); }  // Lambert.cpp:117-126 (untextured)
-static inline V3 GgxF0(const Material& m) {  // GGX.h:126-139 (metalness 0, no map)
-    const V3 refl = m.color;
+// Texture2D::GetPixelByUV (Texture2D.cpp:327-335): wrap, then bilinear at (u W, v H)
+static inline V3 TexByUV(const Texture& t, float u, float v) {
+    u = Mod1(u);
+    v = Mod1(v);
+    return t.Bilinear(u * t.W, v * t.H);
+}
+// Lambert::GetAlbedo (Lambert.cpp:117-126)
+static inline V3 LambertAlbedo(const Scene& s, const Material& m, const Shading& si) {
+    if (m.albedoTex < 0) return V3(1, 1, 1);
+    return m.color * TexByUV(s.textures[m.albedoTex], si.uv.x, si.uv.y);
+}
+// GGX::GetF0 (GGX.h:126-139), metalness 0
+static inline V3 GgxF0(const Scene& s, const Material& m, const Shading& si) {
+    V3 refl = m.color;
+    if (m.f0Tex >= 0) refl = refl * TexByUV(s.textures[m.f0Tex], si.uv.x, si.uv.y);
     return 0.16f * Pow2(refl) * (1.0f - 0.0f) + V3(1, 1, 1) * 0.0f;
+}
+// GGX::GetAlpha (GGX.h:57-73)
+static inline float GgxAlpha(const Scene& s, const Material& m, const Shading& si) {
+    if (m.roughTex < 0) return m.alpha;
+    const float r = m.roughStrength * Luminance(TexByUV(s.textures[m.roughTex], si.uv.x, si.uv.y));
+    return r * r;
+}
+// GGX::GetNormal (GGX.h:95-121)
+static inline V3 GgxNormal(const Scene& s, const Material& m, const Shading& si) {
+    if (m.normalTex < 0) return si.normal;
+    ONB b;
+    b.Build(si.normal, si.tangent);
+    const V3 nm = TexByUV(s.textures[m.normalTex], si.uv.x, si.uv.y);
+    const V3 ln = Normalized(2.0f * nm - V3(1, 1, 1));
+    return (1.0f - m.normalStrength) * ln.x * b.u + ln.y * b.v + (1.0f - m.normalStrength) * ln.z * b.w;
 }
 static inline float GgxLambda(V3 dir, V3 h, float alpha) {  // GGX.cpp:140-152
     const float a2 = alpha * alpha;
@@ -596,18 +630,18 @@ static V3 BxDF(const Scene& s, int m, const Ray& in, const Ray& out, const Shadi
     const Material& M = s.mats[m];
     switch (M.kind) {
     case kLambert:  // Lambert.cpp:27-31
-        return M.color * LambertAlbedo(M) * kInvPi;
+        return M.color * LambertAlbedo(s, M, si) * kInvPi;
     case kGlossy: {  // GGX.cpp:22-57
-        const V3 n = si.normal;
+        const V3 n = GgxNormal(s, M, si);
         const V3 h = Normalized(-in.dir + out.dir);
         const float hn = std::abs(Dot(h, n));
-        const float a = M.alpha, a2 = a * a, hn2 = hn * hn;
+        const float a = GgxAlpha(s, M, si), a2 = a * a, hn2 = hn * hn;
         const float k = (a2 - 1.0f) * hn2 + 1.0f;
         const float D = a2 / (kPi * k * k);
         const float li = GgxLambda(out.dir, h, a), lo = GgxLambda(-in.dir, h, a);
         const float G = 1.0f / (1.0f + li + lo);
         const float hl = std::abs(Dot(h, out.dir));
-        const V3 F = GgxF0(M) + (V3(1, 1, 1) - GgxF0(M)) * Pow5(1.0f - hl);
+        const V3 F = GgxF0(s, M, si) + (V3(1, 1, 1) - GgxF0(s, M, si)) * Pow5(1.0f - hl);
         const float ln = std::abs(Dot(out.dir, n)), vn = std::abs(Dot(-in.dir, n));
         return D * G * F / (4.0f * ln * vn);
     }
@@ -622,8 +656,9 @@ static float PDF(const Scene& s, int m, const Ray& in, const Ray& out, const Sha
         return std::abs(Dot(out.dir, si.normal)) * kInvPi;
     case kGlossy: {  // GGX.cpp:59-76
         const V3 h = Normalized(-in.dir + out.dir);
-        const float hn = std::abs(Dot(h, si.normal));
-        const float a2 = M.alpha * M.alpha, hn2 = hn * hn;
+        const float hn = std::abs(Dot(h, GgxNormal(s, M, si)));
+        const float alpha = GgxAlpha(s, M, si);
+        const float a2 = alpha * alpha, hn2 = hn * hn;
         const float tmp = 1.0f - (1.0f - a2) * hn2;
         return tmp > 0 ? kInvPi * a2 / (tmp * tmp) : kInfinity;
     }
@@ -632,14 +667,14 @@ static float PDF(const Scene& s, int m, const Ray& in, const Ray& out, const Sha
     }
 }
 // GGX.cpp:154-208
-static V3 SampleVNDF(const Material& M, V3 view, const Shading& si, Sampler2D& s2) {
-    const V3 n0 = si.normal;
+static V3 SampleVNDF(const Scene& s, const Material& M, V3 view, const Shading& si, Sampler2D& s2) {
+    const V3 n0 = GgxNormal(s, M, si);
     const V3 n = n0 * std::copysign(1.0f, Dot(view, n0));
     ONB surf;
     const V3 t = (std::abs(n.z) < 0.9999f) ? Cross(n, V3(0, 0, 1)) : V3(1, 0, 0);
     surf.Build(n, t);
     V3 v = surf.WorldToLocal(view);
-    const float alpha = M.alpha;
+    const float alpha = GgxAlpha(s, M, si);
     v = v * V3(alpha, alpha, 1.0f);
     v = v / Length(v);
     const V3 t1 = (v.z < 0.9999f) ? Normalized(Cross(v, V3(0, 0, 1))) : V3(1, 0, 0);
@@ -674,22 +709,24 @@ static Ray NextRay(const Scene& s, int m, const Ray& in, const Shading& si, Samp
         const float cw = (float)std::sqrt((double)(1.0f - st * st));
         out.o = si.pos + kEps * n;
         out.dir = cu * onb.u + cv * onb.v + cw * onb.w;
-        out.T = in.T * LambertAlbedo(M);
+        out.T = in.T * LambertAlbedo(s, M, si);
         out.bounce = in.bounce + 1;
         return out;
     }
     case kGlossy: {  // GGX.cpp:78-138
-        const V3 n = si.normal * std::copysign(1.0f, -Dot(in.dir, si.normal));
-        const V3 h = SampleVNDF(M, -in.dir, si, s2);
+        const V3 n0 = GgxNormal(s, M, si);
+        const V3 n = n0 * std::copysign(1.0f, -Dot(in.dir, n0));
+        const V3 h = SampleVNDF(s, M, -in.dir, si, s2);
         const V3 od = Reflected(in.dir, h);
         const float hl = std::abs(Dot(h, od));
-        const V3 f0 = GgxF0(M);
+        const V3 f0 = GgxF0(s, M, si);
         const V3 F = f0 + (V3(1, 1, 1) - f0) * Pow5(1.0f - hl);
         out.o = si.pos;
         out.dir = od;
         out.T = in.T;
         out.bounce = in.bounce + 1;
-        const float li = GgxLambda(od, h, M.alpha), lo = GgxLambda(-in.dir, h, M.alpha);
+        const float alpha = GgxAlpha(s, M, si);
+        const float li = GgxLambda(od, h, alpha), lo = GgxLambda(-in.dir, h, alpha);
         const float g2 = 1.0f / (1.0f + li + lo);
         const float g1 = 1.0f / (1.0f + li);
         out.T = out.T * (F * g2 / g1);
@@ -798,12 +835,12 @@ static V3 AovPath(const Scene& s, Ray ray, bool normal, Sampler1D& s1, Sampler2D
         const Material& M = s.mats[m];
         switch (M.kind) {
         case kLambert:
-            return normal ? ray.T * si.normal : ray.T * LambertAlbedo(M);
+            return normal ? ray.T * si.normal : ray.T * LambertAlbedo(s, M, si);
         case kGlass:  // Glass::GetAlpha is 0: always follows the refracted/reflected ray
             ray = NextRay(s, m, ray, si, s2);
             break;
         case kGlossy:
-            if (M.alpha != 0) return normal ? ray.T * si.normal : ray.T * GgxF0(M);
+            if (GgxAlpha(s, M, si) != 0) return normal ? ray.T * si.normal : ray.T * GgxF0(s, M, si);
             ray = NextRay(s, m, ray, si, s2);
             break;
         default:  // Emission: the ASSERT(false) branch returns zero in release builds
@@ -1035,6 +1072,13 @@ static Scene* Parse(const void* data, size_t size) {
         m.mix = mf[k * 8 + 5];
         m.mat0 = mi[k * 4 + 1];
         m.mat1 = mi[k * 4 + 2];
+        const uint32_t refs = (uint32_t)mi[k * 4 + 3];  // texture index + 1 per byte
+        m.albedoTex = (int)(refs & 255) - 1;
+        m.f0Tex = (int)((refs >> 8) & 255) - 1;
+        m.roughTex = (int)((refs >> 16) & 255) - 1;
+        m.normalTex = (int)((refs >> 24) & 255) - 1;
+        m.roughStrength = mf[k * 8 + 6];
+        m.normalStrength = mf[k * 8 + 7];
         s->mats.push_back(m);
     }
     const uint32_t V = b.get<uint32_t>();
@@ -1053,6 +1097,21 @@ static Scene* Parse(const void* data, size_t size) {
     const uint32_t L = b.get<uint32_t>();
     s->lights.resize(L);
     b.take(s->lights.data(), (size_t)L * 4);
+    if (b.off < b.n) {  // optional texture-map section
+        const uint32_t NT = b.get<uint32_t>();
+        for (uint32_t k = 0; k < NT; k++) {
+            Texture t;
+            t.W = b.get<int32_t>();
+            t.H = b.get<int32_t>();
+            t.valid = true;
+            t.px.resize((size_t)t.W * t.H);
+            b.take(t.px.data(), (size_t)t.W * t.H * 12);
+            s->textures.push_back(std::move(t));
+        }
+    }
+    for (const Material& m : s->mats)
+        for (int r : {m.albedoTex, m.f0Tex, m.roughTex, m.normalTex})
+            if (r >= (int)s->textures.size()) throw std::runtime_error("texture index out of range");
     return s.release();
 }
 

@@ -100,6 +100,7 @@ struct Loaded {
     std::vector<const MaterialBase*> materials;
     int integrator = 0;
     int denoisingSpp = 1;
+    std::vector<std::unique_ptr<Texture2D>> textures;  // material texture maps
 };
 
 static Math::Vector3f V3(const float* p) { return Math::Vector3f(p[0], p[1], p[2]); }
@@ -161,6 +162,8 @@ static void Load(const std::string& path, const std::string& tmpPrefix, Loaded& 
     r.take(mf.data(), mf.size() * 4);
     r.take(mi.data(), mi.size() * 4);
     L.materials.assign(M, nullptr);
+    std::vector<Lambert*> lamberts(M, nullptr);
+    std::vector<GGX*> ggxs(M, nullptr);
     for (int pass = 0; pass < 2; pass++) {
         for (uint32_t k = 0; k < M; k++) {
             const float* f = &mf[k * 8];
@@ -168,10 +171,20 @@ static void Load(const std::string& path, const std::string& tmpPrefix, Loaded& 
             std::unique_ptr<const MaterialBase> m;
             if (pass == 0) {
                 switch (q[0]) {
-                case 0: m = std::make_unique<Lambert>(V3(f)); break;
+                case 0: {
+                    auto l = std::make_unique<Lambert>(V3(f));
+                    lamberts[k] = l.get();
+                    m = std::move(l);
+                    break;
+                }
                 case 1: m = std::make_unique<Glass>(V3(f), f[4]); break;
                 case 2: m = std::make_unique<Emission>(V3(f)); break;
-                case 3: m = std::make_unique<GGX>(V3(f), f[3]); break;
+                case 3: {
+                    auto g = std::make_unique<GGX>(V3(f), f[3]);
+                    ggxs[k] = g.get();
+                    m = std::move(g);
+                    break;
+                }
                 default: break;
                 }
             } else if (q[0] == 4) {
@@ -209,6 +222,47 @@ static void Load(const std::string& path, const std::string& tmpPrefix, Loaded& 
     for (uint32_t t = 0; t < T; t++) L.scene->AppendGeometry(&L.triangles[t]);
     const uint32_t NL = r.get<uint32_t>();
     for (uint32_t i = 0; i < NL; i++) L.scene->AppendLight(&L.triangles.at(r.get<int32_t>()));
+    // optional texture maps: loaded through Texture2D::Load of raw .hdr files and attached
+    // with the materials' setters (Lambert::SetTexAlbedo, GGX::SetF0Texture/SetRoughnessMap/
+    // SetNormalMap and the map strengths)
+    if (r.off < r.buf.size()) {
+        const uint32_t NT = r.get<uint32_t>();
+        for (uint32_t k = 0; k < NT; k++) {
+            const int32_t tw = r.get<int32_t>(), th = r.get<int32_t>();
+            std::vector<float> px((size_t)tw * th * 3);
+            r.take(px.data(), px.size() * 4);
+            const std::string tp = tmpPrefix + ".tex" + std::to_string(k) + ".hdr";
+            std::ofstream h(tp, std::ios::binary);
+            const uint32_t dims[2] = {(uint32_t)tw, (uint32_t)th};
+            h.write("PTRAWF32", 8);
+            h.write((const char*)dims, 8);
+            h.write((const char*)px.data(), px.size() * 4);
+            h.close();
+            auto t = std::make_unique<Texture2D>();
+            if (!t->Load(tp, Texture2D::TextureColorType::NonColor)) throw std::runtime_error("texture");
+            std::remove(tp.c_str());
+            L.textures.push_back(std::move(t));
+        }
+        auto tex = [&](uint32_t refs, int j) -> const Texture2D* {
+            const int id = (int)((refs >> (8 * j)) & 255) - 1;
+            return id >= 0 ? L.textures.at(id).get() : nullptr;
+        };
+        for (uint32_t k = 0; k < M; k++) {
+            const uint32_t refs = (uint32_t)mi[k * 4 + 3];
+            if (lamberts[k] && tex(refs, 0)) lamberts[k]->SetTexAlbedo(tex(refs, 0));
+            if (ggxs[k]) {
+                if (tex(refs, 1)) ggxs[k]->SetF0Texture(tex(refs, 1));
+                if (tex(refs, 2)) {
+                    ggxs[k]->SetRoughnessMap(tex(refs, 2));
+                    ggxs[k]->SetRoughnessMapStrength(mf[k * 8 + 6]);
+                }
+                if (tex(refs, 3)) {
+                    ggxs[k]->SetNormalMap(tex(refs, 3));
+                    ggxs[k]->SetNormalMapStrength(mf[k * 8 + 7]);
+                }
+            }
+        }
+    }
 
     L.film = std::make_unique<Texture2D>(L.settings[0], L.settings[1]);
     L.scene->SetTargetTexture(Scene::AOVType::Rendered, L.film.get());

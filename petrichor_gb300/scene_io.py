@@ -51,6 +51,15 @@ class Material:
     mix: float = 0.0         # Mix
     mat0: int = -1           # Mix
     mat1: int = -1           # Mix
+    # texture maps (indices into Scene.textures, -1 = none): Lambert albedo
+    # (Lambert::SetTexAlbedo); GGX reflectance, roughness and normal maps
+    # (GGX::SetF0Texture / SetRoughnessMap / SetNormalMap) with their strengths
+    albedo_tex: int = -1
+    f0_tex: int = -1
+    roughness_tex: int = -1
+    normal_tex: int = -1
+    roughness_map_strength: float = 1.0
+    normal_map_strength: float = 1.0
 
 
 @dataclasses.dataclass
@@ -96,6 +105,7 @@ class Scene:
     camera: Camera
     env: Environment
     settings: Settings
+    textures: List[np.ndarray] = dataclasses.field(default_factory=list)  # (H, W, 3) float32
 
     @property
     def num_triangles(self) -> int:
@@ -113,8 +123,9 @@ def _f32(a, shape_last=None):
 def material_table(mats: List[Material]) -> np.ndarray:
     """Pack materials as a (M, 8) float32 table + (M, 4) int32 table.
 
-    float row: color.rgb, roughness, ior, mix, 0, 0
-    int row:   kind, mat0, mat1, 0
+    float row: color.rgb, roughness, ior, mix, roughness-map strength, normal-map strength
+    int row:   kind, mat0, mat1, texture references (one byte each, texture index + 1,
+               0 = none: albedo | f0 << 8 | roughness << 16 | normal << 24)
     """
     f = np.zeros((len(mats), 8), np.float32)
     i = np.zeros((len(mats), 4), np.int32)
@@ -123,9 +134,14 @@ def material_table(mats: List[Material]) -> np.ndarray:
         f[k, 3] = m.roughness
         f[k, 4] = m.ior
         f[k, 5] = m.mix
+        f[k, 6] = m.roughness_map_strength
+        f[k, 7] = m.normal_map_strength
         i[k, 0] = m.kind
         i[k, 1] = m.mat0
         i[k, 2] = m.mat1
+        refs = (m.albedo_tex, m.f0_tex, m.roughness_tex, m.normal_tex)
+        assert all(-1 <= r < 255 for r in refs)
+        i[k, 3] = np.int32(np.uint32(sum((r + 1) << (8 * j) for j, r in enumerate(refs))))
     return f, i
 
 
@@ -168,6 +184,12 @@ def write_scene(path_or_buf, sc: Scene) -> None:
     L = sc.lights.shape[0]
     w(struct.pack("<I", L))
     w(np.ascontiguousarray(sc.lights, np.int32).tobytes())
+    if sc.textures:  # optional trailing section: material texture maps
+        w(struct.pack("<I", len(sc.textures)))
+        for t in sc.textures:
+            t = np.ascontiguousarray(t, np.float32)
+            w(struct.pack("<ii", t.shape[1], t.shape[0]))
+            w(t.tobytes())
     data = out.getvalue()
     if hasattr(path_or_buf, "write"):
         path_or_buf.write(data)
@@ -215,9 +237,16 @@ def read_scene_bytes(data: bytes) -> Scene:
     (M,) = struct.unpack("<I", take(4))
     mf = np.frombuffer(take(M * 32), np.float32).reshape(M, 8)
     mi = np.frombuffer(take(M * 16), np.int32).reshape(M, 4)
+    def refs(v):
+        u = int(np.uint32(v))
+        return [((u >> (8 * j)) & 255) - 1 for j in range(4)]
     mats = [Material(kind=int(mi[k, 0]), color=tuple(float(x) for x in mf[k, 0:3]),
                      roughness=float(mf[k, 3]), ior=float(mf[k, 4]), mix=float(mf[k, 5]),
-                     mat0=int(mi[k, 1]), mat1=int(mi[k, 2])) for k in range(M)]
+                     mat0=int(mi[k, 1]), mat1=int(mi[k, 2]),
+                     albedo_tex=refs(mi[k, 3])[0], f0_tex=refs(mi[k, 3])[1],
+                     roughness_tex=refs(mi[k, 3])[2], normal_tex=refs(mi[k, 3])[3],
+                     roughness_map_strength=float(mf[k, 6]), normal_map_strength=float(mf[k, 7]))
+            for k in range(M)]
     (V,) = struct.unpack("<I", take(4))
     pos = np.frombuffer(take(V * 12), np.float32).reshape(V, 3).copy()
     nrm = np.frombuffer(take(V * 12), np.float32).reshape(V, 3).copy()
@@ -228,4 +257,10 @@ def read_scene_bytes(data: bytes) -> Scene:
     sh = np.frombuffer(take(T + ((-T) % 4)), np.uint8)[:T].copy()
     (L,) = struct.unpack("<I", take(4))
     lights = np.frombuffer(take(L * 4), np.int32).copy()
-    return Scene(pos, nrm, uv, idx, tm, sh, lights, mats, cam, env, settings)
+    textures = []
+    if off < len(data):
+        (NT,) = struct.unpack("<I", take(4))
+        for _ in range(NT):
+            tw, th = struct.unpack("<ii", take(8))
+            textures.append(np.frombuffer(take(tw * th * 12), np.float32).reshape(th, tw, 3).copy())
+    return Scene(pos, nrm, uv, idx, tm, sh, lights, mats, cam, env, settings, textures)

@@ -19,6 +19,7 @@ Workloads (sizes as named by the benchmark description):
 """
 from __future__ import annotations
 
+import dataclasses
 import math
 from typing import List, Tuple
 
@@ -329,6 +330,47 @@ def spheres_grids(seed: int = 2, tri_budget: int = 1_000_000, n_objects: int = 6
     st = Settings(width=width, height=height, spp=spp, max_bounces=max_bounces,
                   integrator=INTEGRATOR_PT)
     return Scene(pos, nrm, uv, idx, tm, sh, np.zeros(0, np.int32), mats, cam, env, st)
+
+
+def textured_spheres(seed: int = 4, tri_budget: int = 4000, width: int = 48, height: int = 27,
+                     spp: int = 2, max_bounces: int = 6, env_width: int = 64, env_height: int = 32,
+                     integrator: int = INTEGRATOR_PT) -> Scene:
+    """A small spheres_grids scene whose materials carry texture maps: Lambert albedo
+    maps, GGX reflectance, roughness and normal maps (with their strengths), on a few
+    procedural RGB textures. Spheres keep their (phi, theta) uvs; grids get planar uvs."""
+    sc = spheres_grids(seed=seed, tri_budget=tri_budget, width=width, height=height, spp=spp,
+                       max_bounces=max_bounces, env_width=env_width, env_height=env_height,
+                       sun_peak_over_median=30.0)
+    rng = Rng(seed + 1000)
+    textures = []
+    for k, (w, h) in enumerate([(32, 32), (48, 24), (16, 40), (24, 24)]):
+        y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+        f = rng.uniform(3, 1.0, 6.0)
+        base = 0.5 + 0.5 * np.sin(f[0] * 2 * math.pi * x / w)[..., None] * \
+            np.cos(f[1] * 2 * math.pi * y / h)[..., None] * np.array([1.0, 0.7, 0.4])
+        noise = np.array([rng.one() for _ in range(w * h * 3)]).reshape(h, w, 3)
+        textures.append(np.clip(0.05 + 0.8 * base + 0.15 * noise, 0.0, 1.0).astype(np.float32))
+    mats = []
+    for m in sc.materials:
+        m = dataclasses.replace(m)
+        if m.kind == MAT_LAMBERT and rng.one() < 0.7:
+            m.albedo_tex = int(rng.one() * 4) % 4
+        elif m.kind == MAT_GLOSSY:
+            if rng.one() < 0.5:
+                m.f0_tex = int(rng.one() * 4) % 4
+            if rng.one() < 0.5:
+                m.roughness_tex = int(rng.one() * 4) % 4
+                m.roughness_map_strength = rng.one(0.5, 1.5)
+            if rng.one() < 0.5:
+                m.normal_tex = int(rng.one() * 4) % 4
+                m.normal_map_strength = rng.one(0.0, 1.0)
+        mats.append(m)
+    uv = sc.uvs.copy()
+    flat = ~np.any(uv != 0.0, axis=1)
+    uv[flat, 0] = 0.37 * sc.positions[flat, 0]
+    uv[flat, 1] = 0.29 * sc.positions[flat, 1]
+    st = dataclasses.replace(sc.settings, integrator=integrator)
+    return sc.copy_with(materials=mats, uvs=uv.astype(np.float32), textures=textures, settings=st)
 
 
 def terrain_rocks(seed: int = 5, terrain_n: int = 3000, n_rocks: int = 4000, rock_tris: int = 500,

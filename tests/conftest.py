@@ -27,8 +27,8 @@ def golden_scene(golden, name):
 
 
 GOLDEN_CASES = ["cornell_simple", "cornell_mixed_simple", "cornell_mixed_pt", "cornell_lambert_pt",
-                "spheres_pt"]
-AOV_CASES = ["aov_spheres", "aov_cornell_mixed"]  # UV, denoising albedo, denoising normal
+                "spheres_pt", "textured_pt", "textured_simple"]
+AOV_CASES = ["aov_spheres", "aov_cornell_mixed", "aov_textured"]  # UV, denoising albedo, normal
 
 
 @pytest.fixture(scope="session")

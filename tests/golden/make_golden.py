@@ -37,6 +37,8 @@ def cases():
         "cornell_lambert_pt": synth.cornell(width=40, height=40, spp=8, integrator=1, max_bounces=5),
         "spheres_pt": synth.spheres_grids(tri_budget=4000, width=48, height=27, spp=2,
                                           max_bounces=8, env_width=64, env_height=32),
+        "textured_pt": synth.textured_spheres(integrator=1),
+        "textured_simple": synth.textured_spheres(seed=6, integrator=0, spp=3),
     }
 
 
@@ -48,6 +50,7 @@ def aov_cases():
                                             max_bounces=8, env_width=64, env_height=32), 3),
         "aov_cornell_mixed": (synth.cornell(width=40, height=24, spp=3, mixed=True, aperture=0.05,
                                             tile=7, max_bounces=5, env_texture=True), 2),
+        "aov_textured": (synth.textured_spheres(seed=7), 3),
     }
 
 
