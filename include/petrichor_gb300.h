@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define PT_ABI_VERSION 1
+#define PT_ABI_VERSION 2
 
 /* status codes */
 #define PT_OK 0
@@ -77,7 +77,10 @@ typedef struct pt_context pt_context;
 typedef int32_t pt_scene_id;
 
 /* One material (Lambert(kd) / GGX(f0, roughness) / Glass(color, ior) /
- * Emission(color) / MixMaterial(mat0, mat1, mix)). */
+ * Emission(color) / MixMaterial(mat0, mat1, mix)), with the texture maps of
+ * Lambert::SetTexAlbedo and GGX::SetF0Texture / SetRoughnessMap / SetNormalMap
+ * (LibPetrichor/Core/Material/Lambert.h, GGX.h). Texture references are
+ * 1 + an index into pt_scene_desc.textures; 0 = none, so a zeroed struct has no maps. */
 typedef struct pt_material {
   int32_t kind;
   float color[3];  /* Lambert kd, GGX reflectance ("f0" argument), Glass color, Emission radiance */
@@ -86,7 +89,20 @@ typedef struct pt_material {
   float mix;       /* Mix */
   int32_t mat0;    /* Mix: index of the material picked when mix <= r */
   int32_t mat1;    /* Mix: the other one */
+  int32_t tex_albedo;          /* Lambert: albedo = kd * texel */
+  int32_t tex_f0;              /* GGX: reflectance = color * texel */
+  int32_t tex_roughness;       /* GGX: alpha = (roughness_strength * luminance(texel))^2 */
+  int32_t tex_normal;          /* GGX: tangent-space normal map */
+  float roughness_strength;    /* GGX::SetRoughnessMap strength */
+  float normal_strength;       /* GGX::SetNormalMap strength, clamped to [0, 1] */
 } pt_material;
+
+/* An RGB texture (Texture2D): height rows of width texels, sampled bilinearly
+ * with wrap-around (Texture2D::GetPixelByUV). */
+typedef struct pt_texture {
+  int32_t width, height;
+  const float* rgb; /* height * width * 3 */
+} pt_texture;
 
 /* Scene geometry, materials, lights and environment (host memory; copied). */
 typedef struct pt_scene_desc {
@@ -106,6 +122,8 @@ typedef struct pt_scene_desc {
   float env_z_rotation;
   int32_t env_width, env_height; /* 0 = no texture (base colour only) */
   const float* env_rgb;          /* env_height rows of env_width RGB texels */
+  uint32_t num_textures;         /* material texture maps (pt_material.tex_*) */
+  const pt_texture* textures;
 } pt_scene_desc;
 
 /* Derived camera state (the private members of Petrichor's Camera). Fill it with

@@ -93,14 +93,22 @@ public:
     virtual MaterialTypes GetMaterialType() const = 0;
 };
 
+class Texture2D;
+
+// Texture maps are sampled bilinearly with wrap-around at the shading point's uv;
+// the texture must outlive the render (the scene keeps pointers, as the reference does).
 class Lambert : public MaterialBase {
 public:
     explicit Lambert(const Color3f& kd) : m_kd(kd) {}
     MaterialTypes GetMaterialType() const override { return MaterialTypes::Lambert; }
     const Color3f& GetKd() const { return m_kd; }
+    // Lambert.h:37-41: albedo = kd * texel
+    void SetTexAlbedo(const Texture2D* texAlbedo) { m_texAlbedo = texAlbedo; }
+    const Texture2D* GetTexAlbedo() const { return m_texAlbedo; }
 
 private:
     Color3f m_kd;
+    const Texture2D* m_texAlbedo = nullptr;
 };
 
 class GGX : public MaterialBase {
@@ -109,10 +117,29 @@ public:
     MaterialTypes GetMaterialType() const override { return MaterialTypes::Glossy; }
     const Color3f& GetReflectance() const { return m_f0; }
     float GetRoughness() const { return m_roughness; }
+    // GGX.h:43-93: reflectance = f0 * texel; alpha = (strength * luminance(texel))^2;
+    // tangent-space normal map blended by its strength (clamped to [0, 1])
+    void SetF0Texture(const Texture2D* texture) { m_f0Map = texture; }
+    void SetRoughnessMap(const Texture2D* roughnessMap) { m_roughnessMap = roughnessMap; }
+    void SetNormalMap(const Texture2D* normalMap) { m_normalMap = normalMap; }
+    void SetRoughnessMapStrength(float strength) { m_roughnessMapStrength = strength; }
+    void SetNormalMapStrength(float strength) {
+        m_normalMapStrength = strength < 0.0f ? 0.0f : (strength > 1.0f ? 1.0f : strength);
+    }
+    const Texture2D* GetF0Texture() const { return m_f0Map; }
+    const Texture2D* GetRoughnessMap() const { return m_roughnessMap; }
+    const Texture2D* GetNormalMap() const { return m_normalMap; }
+    float GetRoughnessMapStrength() const { return m_roughnessMapStrength; }
+    float GetNormalMapStrength() const { return m_normalMapStrength; }
 
 private:
     Color3f m_f0;
     float m_roughness;
+    const Texture2D* m_f0Map = nullptr;
+    const Texture2D* m_roughnessMap = nullptr;
+    const Texture2D* m_normalMap = nullptr;
+    float m_roughnessMapStrength = 1.0f;
+    float m_normalMapStrength = 1.0f;
 };
 
 class Glass : public MaterialBase {

@@ -31,7 +31,14 @@ _f3 = ctypes.c_float * 3
 class PtMaterial(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("color", _f3), ("roughness", ctypes.c_float),
                 ("ior", ctypes.c_float), ("mix", ctypes.c_float), ("mat0", ctypes.c_int32),
-                ("mat1", ctypes.c_int32)]
+                ("mat1", ctypes.c_int32), ("tex_albedo", ctypes.c_int32),
+                ("tex_f0", ctypes.c_int32), ("tex_roughness", ctypes.c_int32),
+                ("tex_normal", ctypes.c_int32), ("roughness_strength", ctypes.c_float),
+                ("normal_strength", ctypes.c_float)]
+
+
+class PtTexture(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("rgb", ctypes.c_void_p)]
 
 
 class PtSceneDesc(ctypes.Structure):
@@ -43,7 +50,8 @@ class PtSceneDesc(ctypes.Structure):
                 ("num_lights", ctypes.c_uint32), ("lights", ctypes.c_void_p),
                 ("env_base_color", _f3), ("env_z_rotation", ctypes.c_float),
                 ("env_width", ctypes.c_int32), ("env_height", ctypes.c_int32),
-                ("env_rgb", ctypes.c_void_p)]
+                ("env_rgb", ctypes.c_void_p), ("num_textures", ctypes.c_uint32),
+                ("textures", ctypes.POINTER(PtTexture))]
 
 
 class PtCamera(ctypes.Structure):
@@ -275,7 +283,21 @@ class Context:
             mats[k].mix = m.mix
             mats[k].mat0 = m.mat0
             mats[k].mat1 = m.mat1
+            # texture references are 1 + index (0: none)
+            mats[k].tex_albedo = m.albedo_tex + 1
+            mats[k].tex_f0 = m.f0_tex + 1
+            mats[k].tex_roughness = m.roughness_tex + 1
+            mats[k].tex_normal = m.normal_tex + 1
+            mats[k].roughness_strength = m.roughness_map_strength
+            mats[k].normal_strength = m.normal_map_strength
+        texels = [np.ascontiguousarray(t, np.float32) for t in scene.textures]
+        texs = (PtTexture * max(1, len(texels)))()
+        for k, t in enumerate(texels):
+            texs[k].width, texs[k].height = t.shape[1], t.shape[0]
+            texs[k].rgb = t.ctypes.data
         d = PtSceneDesc()
+        d.num_textures = len(texels)
+        d.textures = texs
         d.num_vertices = pos.shape[0]
         d.positions = pos.ctypes.data
         d.normals = nrm.ctypes.data

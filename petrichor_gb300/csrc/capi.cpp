@@ -148,7 +148,29 @@ int Validate(pt_context* ctx, const pt_scene_desc* d) {
     if ((d->env_width > 0) != (d->env_height > 0) || d->env_width < 0 || d->env_height < 0)
         return Fail(ctx, PT_ERR_INVALID_ARG, "environment size is invalid");
     if (d->env_width > 0 && !d->env_rgb) return Fail(ctx, PT_ERR_INVALID_ARG, "environment texels missing");
+    if (d->num_textures && !d->textures) return Fail(ctx, PT_ERR_INVALID_ARG, "textures missing");
+    int64_t texels = 0;
+    for (uint32_t t = 0; t < d->num_textures; t++) {
+        const pt_texture& X = d->textures[t];
+        if (X.width <= 0 || X.height <= 0 || !X.rgb)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "texture " + std::to_string(t) + " is empty");
+        texels += (int64_t)X.width * X.height;
+    }
+    if (texels >= (int64_t)1 << 31) return Fail(ctx, PT_ERR_INVALID_ARG, "textures too large");
+    for (uint32_t m = 0; m < d->num_materials; m++) {
+        const pt_material& M = d->materials[m];
+        for (int32_t r : {M.tex_albedo, M.tex_f0, M.tex_roughness, M.tex_normal})
+            if (r < 0 || (uint32_t)r > d->num_textures)
+                return Fail(ctx, PT_ERR_INVALID_ARG, "material texture reference out of range");
+    }
     return PT_OK;
+}
+
+// Texture maps a material's kind reads (Lambert: albedo; GGX: f0, roughness, normal).
+bool HasTextureMaps(const pt_material& M) {
+    if (M.kind == PT_MAT_LAMBERT) return M.tex_albedo > 0;
+    if (M.kind == PT_MAT_GLOSSY) return M.tex_f0 > 0 || M.tex_roughness > 0 || M.tex_normal > 0;
+    return false;
 }
 
 int SetDevice(pt_context* ctx) {
@@ -472,19 +494,34 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         shade[3 * (size_t)k + 1] = F4(n[1].x, n[1].y, n[1].z, IntBits(smooth));
         shade[3 * (size_t)k + 2] = F4(n[2].x, n[2].y, n[2].z, 0.0f);
     }
-    // vertex uvs in leaf order, for the UV pass (omitted when the scene has none)
+    // vertex uvs in leaf order, for the UV pass and texture maps (omitted when the
+    // scene has neither)
+    bool anyTex = false;
+    for (uint32_t m = 0; m < d->num_materials; m++) anyTex = anyTex || HasTextureMaps(d->materials[m]);
     std::vector<float4> uvs;
     bool anyUV = false;
     if (d->uvs)
         for (size_t i = 0; i < (size_t)d->num_vertices * 3 && !anyUV; i++) anyUV = d->uvs[i] != 0.0f;
-    if (anyUV) {
-        uvs.resize((size_t)T * 3);
-        for (int k = 0; k < T; k++) {
+    if (anyUV || anyTex) {
+        uvs.assign((size_t)std::max(T, 1) * 3, F4(0.0f, 0.0f, 0.0f, 0.0f));
+        for (int k = 0; k < T && d->uvs; k++) {
             const int t = bvh.primIds[k];
             for (int v = 0; v < 3; v++) {
                 const float* u = d->uvs + 3 * (size_t)d->indices[3 * t + v];
                 uvs[3 * (size_t)k + v] = F4(u[0], u[1], u[2], 0.0f);
             }
+        }
+    }
+    // material texture maps: texels as {r, g, b, 0}, one texture after another
+    std::vector<float4> texels(1, F4(0.0f, 0.0f, 0.0f, 0.0f));
+    std::vector<int4> texInfo(std::max<uint32_t>(d->num_textures, 1), int4{0, 0, 0, 0});
+    if (anyTex) {
+        texels.clear();
+        for (uint32_t t = 0; t < d->num_textures; t++) {
+            const pt_texture& X = d->textures[t];
+            texInfo[t] = int4{(int)texels.size(), X.width, X.height, 0};
+            for (size_t i = 0; i < (size_t)X.width * X.height; i++)
+                texels.push_back(F4(X.rgb[3 * i], X.rgb[3 * i + 1], X.rgb[3 * i + 2], 0.0f));
         }
     }
     // materials
@@ -500,6 +537,15 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         o.ior = M.ior;
         o.mix = M.mix;
         o.mat01 = M.kind == PT_MAT_MIX ? (M.mat0 | (M.mat1 << 16)) : 0;
+        o.ar = o.ag = o.ab = 1.0f;  // Lambert::GetAlbedo without a texture
+        const bool lam = M.kind == PT_MAT_LAMBERT, ggx = M.kind == PT_MAT_GLOSSY;
+        o.texAlbedo = lam ? M.tex_albedo - 1 : -1;
+        o.texF0 = ggx ? M.tex_f0 - 1 : -1;
+        o.texRough = ggx ? M.tex_roughness - 1 : -1;
+        o.texNormal = ggx ? M.tex_normal - 1 : -1;
+        o.texMask = HasTextureMaps(M) ? 1 : 0;
+        o.roughStrength = M.roughness_strength;
+        o.normalStrength = std::min(1.0f, std::max(0.0f, M.normal_strength));  // GGX::SetNormalMap
     }
     // lights and 1 / sum(1 / pdfArea_i) (PathTracing.cpp:363-383, Triangle.cpp:155-182)
     std::vector<float4> lights((size_t)std::max<uint32_t>(d->num_lights, 1) * 3);
@@ -532,7 +578,9 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         (rc = Upload(ctx, s, mats, &D.mats)) != PT_OK ||
         (rc = Upload(ctx, s, lights, &D.lights)) != PT_OK ||
         (rc = Upload(ctx, s, env, &D.env)) != PT_OK ||
-        (anyUV && (rc = Upload(ctx, s, uvs, &D.uvs)) != PT_OK)) {
+        (anyTex && (rc = Upload(ctx, s, texels, &D.texels)) != PT_OK) ||
+        (anyTex && (rc = Upload(ctx, s, texInfo, &D.texInfo)) != PT_OK) ||
+        ((anyUV || anyTex) && (rc = Upload(ctx, s, uvs, &D.uvs)) != PT_OK)) {
         for (auto& b : s.buffers) Free(ctx, b);
         return rc;
     }
@@ -541,6 +589,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     D.numTris = T;
     D.numMats = (int)d->num_materials;
     D.numLights = (int)d->num_lights;
+    D.numTextures = anyTex ? (int)d->num_textures : 0;
     D.envW = W;
     D.envH = H;
     D.envValid = W > 0 ? 1 : 0;

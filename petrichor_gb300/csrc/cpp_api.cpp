@@ -228,6 +228,18 @@ void Petrichor::Render(const Scene& scene) {
     std::vector<int32_t> idx, triMat, lights;
     std::vector<uint8_t> shading;
     std::vector<pt_material> mats;
+    std::vector<pt_texture> textures;
+    std::unordered_map<const Texture2D*, int32_t> texIndex;
+    std::string texError;
+    // texture reference of a material map: 1 + index, 0 for none
+    auto addTexture = [&](const Texture2D* t) -> int32_t {
+        if (!t) return 0;
+        auto it = texIndex.find(t);
+        if (it != texIndex.end()) return it->second;
+        if (t->GetWidth() <= 0 || t->GetHeight() <= 0) texError = "material texture is empty";
+        textures.push_back(pt_texture{t->GetWidth(), t->GetHeight(), t->GetRawDataPtr()});
+        return texIndex[t] = (int32_t)textures.size();
+    };
     std::unordered_map<const Vertex*, int32_t> vertexIndex;
     std::unordered_map<const MaterialBase*, int32_t> matIndex;
     std::unordered_map<const GeometryBase*, int32_t> triIndex;
@@ -240,6 +252,7 @@ void Petrichor::Render(const Scene& scene) {
             const auto* l = static_cast<const Lambert*>(m);
             pm.kind = PT_MAT_LAMBERT;
             pm.color[0] = l->GetKd().x, pm.color[1] = l->GetKd().y, pm.color[2] = l->GetKd().z;
+            pm.tex_albedo = addTexture(l->GetTexAlbedo());
             break;
         }
         case MaterialTypes::Glossy: {
@@ -248,6 +261,11 @@ void Petrichor::Render(const Scene& scene) {
             const Color3f& c = g->GetReflectance();
             pm.color[0] = c.x, pm.color[1] = c.y, pm.color[2] = c.z;
             pm.roughness = g->GetRoughness();
+            pm.tex_f0 = addTexture(g->GetF0Texture());
+            pm.tex_roughness = addTexture(g->GetRoughnessMap());
+            pm.tex_normal = addTexture(g->GetNormalMap());
+            pm.roughness_strength = g->GetRoughnessMapStrength();
+            pm.normal_strength = g->GetNormalMapStrength();
             break;
         }
         case MaterialTypes::Glass: {
@@ -300,6 +318,7 @@ void Petrichor::Render(const Scene& scene) {
         lights.push_back(it->second);
     }
     if (mats.empty()) mats.push_back(pt_material{});  // an empty scene still needs one
+    if (!texError.empty()) return fail(PT_ERR_INVALID_ARG, texError);
 
     pt_scene_desc d{};
     d.num_vertices = (uint32_t)(pos.size() / 3);
@@ -324,6 +343,8 @@ void Petrichor::Render(const Scene& scene) {
         d.env_height = env.GetTexture()->GetHeight();
         d.env_rgb = env.GetTexture()->GetRawDataPtr();
     }
+    d.num_textures = (uint32_t)textures.size();
+    d.textures = textures.data();
     pt_scene_id sid = 0;
     int rc = pt_scene_upload(m_ctx, &d, &sid);
     if (rc != PT_OK) return fail(rc, pt_last_error(m_ctx));

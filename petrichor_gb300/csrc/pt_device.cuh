@@ -185,9 +185,10 @@ struct Ray {  // Core/Ray.h:42-48
     float prob, ior;
     __device__ Ray() : T(1.f, 1.f, 1.f), bounce(0), prob(1.0f), ior(1.0f) {}
 };
-struct Shading {  // Core/HitInfo.h:20-27 (tangent/uv unused without textures)
+struct Shading {  // Core/HitInfo.h:20-27 (uv and tangent formed on demand for texture maps)
     V3 n, pos;
     int mat;
+    int slot;  // primitive slot of the hit
 };
 
 __device__ __forceinline__ void LoadTri(const float4* __restrict__ tris, int k, V3& v0, V3& e1, V3& e2) {
@@ -251,6 +252,7 @@ __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V
         si.n = M::Norm(w1 * (n1 - n0) + w2 * (n2 - n0) + n0);
     }
     si.mat = ResolveMaterial(S.mats, __float_as_int(s0.w), 0.0f);
+    si.slot = k;
     return si;
 }
 
@@ -471,6 +473,94 @@ __device__ __forceinline__ float EnvPdf(const DevScene& S, V3 d) {
 // ---------------------------------------------------------------- materials
 __device__ __forceinline__ V3 MatColor(const DevMaterial& m) { return V3(m.cr, m.cg, m.cb); }
 // GGX::GetF0 with metalness 0 and no map (GGX.h:126-139)
+// Texture2D::GetPixelByUV (Texture2D.cpp:327-335) on material texture t: wrap, then the
+// bilinear fetch of Texture2D::GetPixel at (u W, v H) with edge clamping.
+__device__ __forceinline__ V3 TexByUV(const DevScene& S, int t, float u, float v) {
+    const int4 info = __ldg(S.texInfo + t);
+    const int W = info.y, H = info.z;
+    u = Mod1(u);
+    v = Mod1(v);
+    const float x = u * W, y = v * H;
+    int ix0 = (int)x, ix1 = (int)(x + 1.0f), iy0 = (int)y, iy1 = (int)(y + 1.0f);
+    const float wx0 = x - ix0, wy0 = y - iy0, wx1 = ix1 - x, wy1 = iy1 - y;
+    ix0 = IClamp(ix0, 0, W - 1);
+    ix1 = IClamp(ix1, 0, W - 1);
+    iy0 = IClamp(iy0, 0, H - 1);
+    iy1 = IClamp(iy1, 0, H - 1);
+    const float4* px = S.texels + info.x;
+    const float4 a = __ldg(px + (size_t)W * iy0 + ix0), b = __ldg(px + (size_t)W * iy0 + ix1);
+    const float4 c = __ldg(px + (size_t)W * iy1 + ix0), d = __ldg(px + (size_t)W * iy1 + ix1);
+    const V3 c00(a.x, a.y, a.z), c10(b.x, b.y, b.z), c01(c.x, c.y, c.z), c11(d.x, d.y, d.z);
+    const V3 cm0 = wx1 * c00 + wx0 * c10;
+    const V3 cm1 = wx1 * c01 + wx0 * c11;
+    return wy1 * cm0 + wy0 * cm1;
+}
+
+// Material parameters at a shading point of a material with texture maps
+// (Lambert::GetAlbedo, Lambert.cpp:117-126; GGX::GetAlpha / GetF0 / GetNormal,
+// GGX.h:57-139), with uv and tangent as Triangle::Interpolate forms them
+// (Triangle.cpp:90-145). Kept out of line: untextured scenes never run it, and the
+// shading kernels are instruction-fetch bound, so its code stays out of their loop.
+struct PointTextures {
+    V3 albedo;  // Lambert: kd * texel (1 without an albedo map)
+    V3 refl;    // GGX reflectance: color * texel (GgxF0 squares it)
+    float alpha;
+    V3 n;       // the normal the GGX functions use
+};
+template <class M>
+__device__ __noinline__ PointTextures TexturedPoint(const DevScene& S, int mat, int k, V3 o, V3 d,
+                                                     V3 n) {
+    const DevMaterial m = S.mats[mat];
+    PointTextures r;
+    r.albedo = V3(m.ar, m.ag, m.ab);
+    r.refl = MatColor(m);
+    r.alpha = m.alpha;
+    r.n = n;
+    const bool smooth = __float_as_int(__ldg(&S.shade[3 * k + 1].w)) != 0;
+    V3 v0, e1, e2;
+    LoadTri(S.tris, k, v0, e1, e2);
+    const V3 ce = Cross(e1, e2);
+    const float invDet = __fdiv_rn(1.0f, Dot(-d, ce));
+    const V3 vec = o - v0;
+    const float w1 = Dot(vec, Cross(d, e2)) * invDet;
+    const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+    const float4 a = __ldg(S.uvs + 3 * k), b = __ldg(S.uvs + 3 * k + 1), c = __ldg(S.uvs + 3 * k + 2);
+    const V3 uv0(a.x, a.y, a.z), uv1(b.x, b.y, b.z), uv2(c.x, c.y, c.z);
+    const V3 duv1 = uv1 - uv0, duv2 = uv2 - uv0;
+    const V3 uv = w1 * duv1 + w2 * duv2 + uv0;
+    if (m.texAlbedo >= 0) r.albedo = MatColor(m) * TexByUV(S, m.texAlbedo, uv.x, uv.y);
+    if (m.texF0 >= 0) r.refl = MatColor(m) * TexByUV(S, m.texF0, uv.x, uv.y);
+    if (m.texRough >= 0) {
+        const V3 t = TexByUV(S, m.texRough, uv.x, uv.y);
+        const float rs = m.roughStrength * (0.2126f * t.x + 0.7152f * t.y + 0.0722f * t.z);
+        r.alpha = rs * rs;
+    }
+    if (m.texNormal < 0) return r;
+    V3 tangent = duv2.y * e1 - duv1.y * e2;
+    if (smooth) tangent = tangent - Dot(n, tangent) * n;
+    if (SqLen(tangent) == 0.0f) tangent = V3(1.f, 0.f, 0.f);
+    const V3 bw = M::Norm(n), bu = M::Norm(tangent), bv = Cross(bw, bu);
+    const V3 nm = TexByUV(S, m.texNormal, uv.x, uv.y);
+    const V3 ln = M::Norm(2.0f * nm - V3(1.f, 1.f, 1.f));
+    const float s = 1.0f - m.normalStrength;
+    r.n = s * ln.x * bu + ln.y * bv + s * ln.z * bw;
+    return r;
+}
+
+// The material of slot k's shading point and the normal its BSDF uses: untextured
+// materials are returned as stored with the shading normal.
+template <class M>
+__device__ __forceinline__ V3 PointMaterial(const DevScene& S, int mat, int k, V3 o, V3 d, V3 n,
+                                           DevMaterial& m) {
+    m = S.mats[mat];
+    if (m.texMask == 0) return n;
+    const PointTextures t = TexturedPoint<M>(S, mat, k, o, d, n);
+    m.ar = t.albedo.x, m.ag = t.albedo.y, m.ab = t.albedo.z;
+    m.cr = t.refl.x, m.cg = t.refl.y, m.cb = t.refl.z;
+    m.alpha = t.alpha;
+    return m.kind == kGlossy ? t.n : n;
+}
+
 __device__ __forceinline__ V3 GgxF0(const DevMaterial& m) {
     const V3 c = MatColor(m);
     return 0.16f * (c * c) * (1.0f - 0.0f) + V3(1.f, 1.f, 1.f) * 0.0f;
@@ -486,7 +576,7 @@ __device__ __forceinline__ float GgxLambda(V3 dir, V3 h, float alpha) {  // GGX.
 // (GGX.cpp:22-57); Glass returns zero (Glass.cpp:11-18).
 template <class M>
 __device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) {
-    if (m.kind == kLambert) return MatColor(m) * V3(1.f, 1.f, 1.f) * kInvPi;
+    if (m.kind == kLambert) return MatColor(m) * V3(m.ar, m.ag, m.ab) * kInvPi;
     if (m.kind == kGlossy) {
         const V3 h = M::Norm(-din + dout);
         const float hn = fabsf(Dot(h, n));
@@ -558,7 +648,7 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         const float cw = sqrtf(SMax(0.0f, 1.0f - st * st));  // >= 0 already with IEEE sqrt
         out.o = si.pos + kEps * n;
         out.d = cu * onb.u + cv * onb.v + cw * onb.w;
-        out.T = in.T * V3(1.f, 1.f, 1.f);
+        out.T = in.T * V3(m.ar, m.ag, m.ab);
         out.bounce = in.bounce + 1;
         return out;
     }

@@ -51,13 +51,17 @@ enum MaterialKind : int32_t {
     kMix = 4,
 };
 
-struct DevMaterial {  // 32 B
+struct DevMaterial {  // 64 B
     int32_t kind;
     float cr, cg, cb;  // Lambert kd / GGX reflectance strength / Glass color / Emission radiance
     float alpha;       // GGX roughness^2 (GGX.cpp:16-20)
     float ior;         // Glass
     float mix;         // Mix: mix <= r picks mat0 (MixMaterial.h:45-50)
     int32_t mat01;     // Mix: mat0 | (mat1 << 16)
+    float ar, ag, ab;  // Lambert::GetAlbedo: 1 untextured; per shading point kd * texel
+    int32_t texMask;   // 0: no texture maps (then the texture fields are unused)
+    int32_t texAlbedo, texF0, texRough, texNormal;  // texture index or -1
+    float roughStrength, normalStrength;             // GGX map strengths (normal clamped to [0, 1])
 };
 
 struct DevCamera {  // derived Camera state (Core/Camera.h:121-130)
@@ -74,12 +78,15 @@ struct DevScene {
     const DevMaterial* mats;
     const float4* lights;
     const float4* env;
+    const float4* texels;  // material texture maps, RGB_ rows, one after another
+    const int4* texInfo;   // per texture: first texel, width, height, 0
     int32_t numNodes, numTris, numMats, numLights;
     int32_t envW, envH, envValid, stackDepth;  // stackDepth: max traversal stack entries
     float envBase[3], envRot;
     float lightPdfArea;  // 1 / sum(1/pdfArea_i), PathTracing.cpp:363-383 (summed in light order)
     int32_t numWide;
-    int32_t pad[2];
+    int32_t numTextures;
+    int32_t pad;
 };
 
 // Integrators

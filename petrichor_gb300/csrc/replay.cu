@@ -42,8 +42,10 @@ __device__ void ReplaySimplePixel(const DevScene& S, const DevCamera& C, const D
                 contrib = contrib + ray.T * MatColor(S.mats[m]);
                 break;
             }
-            const Shading si = Interpolate<ExactMath>(S, k, ray.o, ray.d, dist);
-            ray = NextRay<ExactMath>(S.mats[m], ray, si, s2);
+            Shading si = Interpolate<ExactMath>(S, k, ray.o, ray.d, dist);
+            DevMaterial Mh;
+            si.n = PointMaterial<ExactMath>(S, m, k, ray.o, ray.d, si.n, Mh);
+            ray = NextRay<ExactMath>(Mh, ray, si, s2);
             if (ray.bounce > st.maxBounces) {
                 ray.prob *= 0.9f;
                 ray.prob = SMax(0.1f, ray.prob);
@@ -88,15 +90,16 @@ __device__ V3 ReplaySampleLight(const DevScene& S, float rv, RefSampler2D& s2, b
 }
 
 // PathTracing::CalcLightContribution (PathTracing.cpp:202-327)
-__device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1, RefSampler2D& s2,
-                          const Ray& ray, int* stack, int* status) {
+// M and nb: the shading point's material and BSDF normal (texture maps applied)
+__device__ V3 ReplayLight(const DevScene& S, const Shading& si, const DevMaterial& M, V3 nb,
+                          RefSampler1D& s1, RefSampler2D& s2, const Ray& ray, int* stack,
+                          int* status) {
     V3 lc;
     const float dt = -Dot(ray.d, si.n);
     const V3 p = si.pos + kEps * copysignf(1.0f, dt) * si.n;
     const float pdfArea = S.lightPdfArea;
     bool sampleEnv = false;
     const V3 pl = ReplaySampleLight(S, s1.Next(), s2, true, &sampleEnv);
-    const DevMaterial& M = S.mats[si.mat];
     if (!sampleEnv) {
         if (S.numLights == 0) return V3();
         const V3 ld = Normalized(pl - p);
@@ -112,11 +115,11 @@ __device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1
                     float mis = 0.0f;
                     if (l2 > 0.0f) {
                         const float pL = pdfArea;
-                        const float pB = BsdfPdf<ExactMath>(M, ray.d, ld, si.n) * cosP / l2;
+                        const float pB = BsdfPdf<ExactMath>(M, ray.d, ld, nb) * cosP / l2;
                         mis = pL * pL / (pL * pL + pB * pB);
                     }
                     const V3 li = MatColor(S.mats[sl.mat]);
-                    const V3 f = BxDF<ExactMath>(M, ray.d, ld, si.n);
+                    const V3 f = BxDF<ExactMath>(M, ray.d, ld, nb);
                     const float c = fabsf(Dot(ld, si.n));
                     lc = lc + mis * ray.T * (li * f * c * cosP / (pdfArea * l2));
                 }
@@ -132,10 +135,10 @@ __device__ V3 ReplayLight(const DevScene& S, const Shading& si, RefSampler1D& s1
         if (TraverseReference(S, eo, sd, 0.0f, kFltMax, d, stack, status) < 0) {
             const float c = fabsf(Dot(sd, si.n));
             const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<ExactMath>(M, ray.d, sd, si.n);
+            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<ExactMath>(M, ray.d, sd, nb);
             const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
             const V3 li = EnvColor<ExactMath>(S, sd);
-            const V3 f = BxDF<ExactMath>(M, ray.d, sd, si.n);
+            const V3 f = BxDF<ExactMath>(M, ray.d, sd, nb);
             lc = lc + mis * ray.T * (li * f * sn * c * 2.0f * kPi * kPi) / pdfuv;
         }
     }
@@ -169,10 +172,13 @@ __device__ void ReplayPtPixel(const DevScene& S, const DevCamera& C, const DevSe
             continue;
         }
         for (int bounce = 0; bounce < st.maxBounces; bounce++) {
-            color = color + ReplayLight(S, si, s1, s2, ray, stack, status);
+            DevMaterial Mh;
+            const V3 nb = PointMaterial<ExactMath>(S, si.mat, si.slot, ray.o, ray.d, si.n, Mh);
+            color = color + ReplayLight(S, si, Mh, nb, s1, s2, ray, stack, status);
             prev = ray;
-            const int m = si.mat;
-            ray = NextRay<ExactMath>(S.mats[m], ray, si, s2);
+            Shading sb = si;
+            sb.n = nb;
+            ray = NextRay<ExactMath>(Mh, ray, sb, s2);
             if (fabsf(SqLen(ray.T) - 0.0f) < kEps) break;
             float d;
             const int k = TraverseReference(S, ray.o, ray.d, 0.0f, kFltMax, d, stack, status);
@@ -184,7 +190,7 @@ __device__ void ReplayPtPixel(const DevScene& S, const DevCamera& C, const DevSe
                     bool unused = false;
                     ReplaySampleLight(S, s1.Next(), s2, false, &unused);
                     const float pdfArea = S.lightPdfArea;
-                    const float pB = BsdfPdf<ExactMath>(S.mats[m], prev.d, ray.d, si.n);
+                    const float pB = BsdfPdf<ExactMath>(Mh, prev.d, ray.d, nb);
                     const float pL = l2 / cosP * pdfArea;
                     const float mis = pB * pB / (pL * pL + pB * pB);
                     color = color + mis * ray.T * MatColor(S.mats[sn.mat]);
@@ -195,7 +201,7 @@ __device__ void ReplayPtPixel(const DevScene& S, const DevCamera& C, const DevSe
                 if (S.envValid) {
                     const float c = fabsf(Dot(si.n, ray.d));
                     const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-                    const float pB = BsdfPdf<ExactMath>(S.mats[m], prev.d, ray.d, si.n);
+                    const float pB = BsdfPdf<ExactMath>(Mh, prev.d, ray.d, nb);
                     float mis = 0.0f;
                     if (ray.d.x != 0 && ray.d.y != 0 && sn > 0) {
                         const float pE = EnvPdf<ExactMath>(S, ray.d) / (2.0f * kPi * kPi * sn);
@@ -281,11 +287,13 @@ __device__ V3 AovPath(const DevScene& S, const DevSettings& st, Ray ray, bool no
         if (k < 0) return normal ? ray.T * (-ray.d) : ray.T * EnvColor<ExactMath>(S, ray.d);
         const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, k), s1.Next());
         const Shading si = Interpolate<ExactMath>(S, k, ray.o, ray.d, d);
-        const DevMaterial& M = S.mats[m];
-        if (M.kind == kLambert) return normal ? ray.T * si.n : ray.T * V3(1.f, 1.f, 1.f);
+        DevMaterial M;
+        Shading sb = si;
+        sb.n = PointMaterial<ExactMath>(S, m, k, ray.o, ray.d, si.n, M);
+        if (M.kind == kLambert) return normal ? ray.T * si.n : ray.T * V3(M.ar, M.ag, M.ab);
         if (M.kind == kGlossy && M.alpha != 0) return normal ? ray.T * si.n : ray.T * GgxF0(M);
         if (M.kind != kGlass && M.kind != kGlossy) return V3();
-        ray = NextRay<ExactMath>(M, ray, si, s2);  // Glass::GetAlpha is always 0
+        ray = NextRay<ExactMath>(M, ray, sb, s2);  // Glass::GetAlpha is always 0
     }
     return V3();
 }

@@ -439,8 +439,10 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                 if (S.mats[m].kind == kEmission) {
                     L = L + in.T * MatColor(S.mats[m]);
                 } else {
-                    const Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
-                    out = NextRay<FastMath>(S.mats[m], in, si, rng);
+                    Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
+                    DevMaterial Mh;
+                    si.n = PointMaterial<FastMath>(S, m, slot, o, d, si.n, Mh);
+                    out = NextRay<FastMath>(Mh, in, si, rng);
                     cont = true;
                     if (out.bounce > st.maxBounces) {
                         out.prob *= 0.9f;
@@ -467,8 +469,8 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                 L = L + mis * in.T * EnvColor<FastMath>(S, d);
             } else {
                 const Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
-                const DevMaterial& M = S.mats[si.mat];
-                if (M.kind == kEmission) {
+                if (S.mats[si.mat].kind == kEmission) {
+                    const DevMaterial& M = S.mats[si.mat];
                     if (k == 0) {
                         L = L + in.T * MatColor(M);
                         flags |= kFlagNoSignCheck;
@@ -480,6 +482,9 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                         L = L + mis * in.T * MatColor(M);
                     }
                 } else if (k < st.maxBounces) {
+                    // material and BSDF normal at the shading point (texture maps applied)
+                    DevMaterial M;
+                    const V3 nb = PointMaterial<FastMath>(S, si.mat, slot, o, d, si.n, M);
                     // ---- next-event estimation (PathTracing.cpp:202-327)
                     const float dt = -Dot(d, si.n);
                     const V3 p = si.pos + kEps * copysignf(1.0f, dt) * si.n;
@@ -494,10 +499,10 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                             const V3 sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
                             const float c = fabsf(Dot(sd, si.n));
                             const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-                            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, si.n);
+                            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, nb);
                             const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
                             const V3 li = EnvColor<FastMath>(S, sd);
-                            const V3 f = BxDF<FastMath>(M, d, sd, si.n);
+                            const V3 f = BxDF<FastMath>(M, d, sd, nb);
                             const V3 contrib = mis * in.T * (li * f * sn * c * 2.0f * kPi * kPi) / pdfuv;
                             if (contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f) {
                                 shadow = true;
@@ -514,7 +519,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                         const V3 dl = pl - p;
                         const float dist = Length(dl);
                         const V3 ld = dl / dist;
-                        const V3 f = BxDF<FastMath>(M, d, ld, si.n);
+                        const V3 f = BxDF<FastMath>(M, d, ld, nb);
                         // emitter material pick for the visibility test (GetMaterial with a draw)
                         const float pick = rng.Next();
                         if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
@@ -522,7 +527,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                             shadow = true;
                             sh0 = make_float4(p.x, p.y, p.z, dist);
                             sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
-                            sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf<FastMath>(M, d, ld, si.n));
+                            sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf<FastMath>(M, d, ld, nb));
                             sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, pick);
                         }
                     }
@@ -537,10 +542,12 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                         e[3] = sh3;
                     }
                     // ---- continuation
-                    out = NextRay<FastMath>(M, in, si, rng);
+                    Shading sb = si;
+                    sb.n = nb;
+                    out = NextRay<FastMath>(M, in, sb, rng);
                     if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
                         cont = true;
-                        lastPdf = BsdfPdf<FastMath>(M, d, out.d, si.n);
+                        lastPdf = BsdfPdf<FastMath>(M, d, out.d, nb);
                         const float c = fabsf(Dot(si.n, out.d));
                         lastSin = sqrtf(SMax(0.0f, 1.0f - c * c));
                         out.bounce = k + 1;

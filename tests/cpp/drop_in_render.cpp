@@ -4,8 +4,10 @@
 // makes (Vertex, Triangle, Lambert/GGX/Glass/Emission/MixMaterial,
 // Scene::RegisterMaterial/AppendGeometry/AppendLight/SetMainCamera/
 // SetEnvironment/SetTargetTexture/LoadRenderSetting, Environment::Load,
-// Camera(pos, dir)/SetFOV/SetFocalLength/FocusTo/SetApeture), renders it with
-// Petrichor::Render and writes the Rendered texture as raw float32 RGB rows.
+// Camera(pos, dir)/SetFOV/SetFocalLength/FocusTo/SetApeture, Texture2D::Load with
+// Lambert::SetTexAlbedo and GGX::SetF0Texture/SetRoughnessMap/SetNormalMap and their
+// strengths), renders it with Petrichor::Render and writes the Rendered texture as
+// raw float32 RGB rows.
 //
 //   drop_in_render <scene.ptscene> <film.bin> [wavefront | aov <denoising spp>]
 //
@@ -43,6 +45,7 @@ public:
         std::memcpy(dst, m_buf.data() + m_off, n);
         m_off += n;
     }
+    bool AtEnd() const { return m_off >= m_buf.size(); }
     template <typename T>
     T Get() {
         T v;
@@ -66,7 +69,18 @@ struct App {
     int integrator = 0;
     int denoisingSpp = 1;
     std::unique_ptr<Texture2D> aov[3];
+    std::vector<std::unique_ptr<Texture2D>> maps;  // material texture maps
 };
+
+// Writes RGB rows as the raw float container Texture2D::Load reads.
+void WriteRawImage(const std::string& path, int w, int h, const float* px) {
+    std::ofstream f(path, std::ios::binary);
+    const uint32_t dims[2] = {(uint32_t)w, (uint32_t)h};
+    f.write("PTRAWF32", 8);
+    f.write(reinterpret_cast<const char*>(dims), 8);
+    f.write(reinterpret_cast<const char*>(px), (std::streamsize)((size_t)w * h * 12));
+    if (!f) throw std::runtime_error("cannot write " + path);
+}
 
 void BuildScene(const std::string& path, const std::string& scratch, App& app) {
     Bytes r(path);
@@ -108,12 +122,7 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
         std::vector<float> px((size_t)ew * eh * 3);
         r.Take(px.data(), px.size() * 4);
         const std::string hdr = scratch + ".env.hdr";
-        std::ofstream f(hdr, std::ios::binary);
-        const uint32_t dims[2] = {(uint32_t)ew, (uint32_t)eh};
-        f.write("PTRAWF32", 8);
-        f.write(reinterpret_cast<const char*>(dims), 8);
-        f.write(reinterpret_cast<const char*>(px.data()), (std::streamsize)(px.size() * 4));
-        f.close();
+        WriteRawImage(hdr, ew, eh, px.data());
         env.Load(hdr);
     }
     app.scene.SetEnvironment(env);
@@ -123,16 +132,68 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
     std::vector<int32_t> mi((size_t)M * 4);
     r.Take(mf.data(), mf.size() * 4);
     r.Take(mi.data(), mi.size() * 4);
+
+    const uint32_t NV = r.Get<uint32_t>();
+    std::vector<float> pos((size_t)NV * 3), nrm((size_t)NV * 3), uv((size_t)NV * 3);
+    r.Take(pos.data(), pos.size() * 4);
+    r.Take(nrm.data(), nrm.size() * 4);
+    r.Take(uv.data(), uv.size() * 4);
+    const uint32_t T = r.Get<uint32_t>();
+    std::vector<int32_t> idx((size_t)T * 3), tm(T);
+    std::vector<uint8_t> sh(T + (4 - T % 4) % 4);
+    r.Take(idx.data(), idx.size() * 4);
+    r.Take(tm.data(), tm.size() * 4);
+    r.Take(sh.data(), sh.size());
+    const uint32_t NL = r.Get<uint32_t>();
+    std::vector<int32_t> lights(NL);
+    r.Take(lights.data(), lights.size() * 4);
+    if (!r.AtEnd()) {  // material texture maps, each loaded from an image file
+        const uint32_t NT = r.Get<uint32_t>();
+        for (uint32_t t = 0; t < NT; t++) {
+            const int32_t tw = r.Get<int32_t>(), th = r.Get<int32_t>();
+            std::vector<float> px((size_t)tw * th * 3);
+            r.Take(px.data(), px.size() * 4);
+            const std::string path = scratch + ".map" + std::to_string(t) + ".hdr";
+            WriteRawImage(path, tw, th, px.data());
+            app.maps.push_back(std::make_unique<Texture2D>());
+            if (!app.maps.back()->Load(path, Texture2D::TextureColorType::NonColor))
+                throw std::runtime_error("cannot load " + path);
+        }
+    }
+    // texture reference byte j of a material's int row: texture index + 1, 0 = none
+    auto map = [&](int32_t refs, int j) -> const Texture2D* {
+        const int r8 = (int)(((uint32_t)refs >> (8 * j)) & 0xffu);
+        return r8 ? app.maps.at(r8 - 1).get() : nullptr;
+    };
     std::vector<const MaterialBase*> mats(M, nullptr);
     auto name = [](uint32_t k) { return "material" + std::to_string(k); };
     for (uint32_t k = 0; k < M; k++) {  // plain materials, then mixes of them
         const float* f = &mf[(size_t)k * 8];
         std::unique_ptr<const MaterialBase> m;
+        const int32_t refs = mi[(size_t)k * 4 + 3];
         switch (mi[(size_t)k * 4]) {
-        case 0: m = std::make_unique<Lambert>(V(f)); break;
+        case 0: {
+            auto l = std::make_unique<Lambert>(V(f));
+            if (map(refs, 0)) l->SetTexAlbedo(map(refs, 0));
+            m = std::move(l);
+            break;
+        }
         case 1: m = std::make_unique<Glass>(V(f), f[4]); break;
         case 2: m = std::make_unique<Emission>(V(f)); break;
-        case 3: m = std::make_unique<GGX>(V(f), f[3]); break;
+        case 3: {
+            auto g = std::make_unique<GGX>(V(f), f[3]);
+            if (map(refs, 1)) g->SetF0Texture(map(refs, 1));
+            if (map(refs, 2)) {
+                g->SetRoughnessMap(map(refs, 2));
+                g->SetRoughnessMapStrength(f[6]);
+            }
+            if (map(refs, 3)) {
+                g->SetNormalMap(map(refs, 3));
+                g->SetNormalMapStrength(f[7]);
+            }
+            m = std::move(g);
+            break;
+        }
         default: continue;
         }
         app.scene.RegisterMaterial(name(k), std::move(m));
@@ -147,20 +208,9 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
         mats[k] = app.scene.GetMaterial(name(k));
     }
 
-    const uint32_t NV = r.Get<uint32_t>();
-    std::vector<float> pos((size_t)NV * 3), nrm((size_t)NV * 3), uv((size_t)NV * 3);
-    r.Take(pos.data(), pos.size() * 4);
-    r.Take(nrm.data(), nrm.size() * 4);
-    r.Take(uv.data(), uv.size() * 4);
     app.vertices.reserve(NV);
     for (uint32_t i = 0; i < NV; i++)
         app.vertices.emplace_back(V(&pos[i * 3]), V(&nrm[i * 3]), V(&uv[i * 3]));
-    const uint32_t T = r.Get<uint32_t>();
-    std::vector<int32_t> idx((size_t)T * 3), tm(T);
-    std::vector<uint8_t> sh(T + (4 - T % 4) % 4);
-    r.Take(idx.data(), idx.size() * 4);
-    r.Take(tm.data(), tm.size() * 4);
-    r.Take(sh.data(), sh.size());
     app.triangles.reserve(T);
     for (uint32_t t = 0; t < T; t++) {
         app.triangles.emplace_back(&app.vertices.at(idx[t * 3]), &app.vertices.at(idx[t * 3 + 1]),
@@ -169,8 +219,7 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
         app.triangles.back().SetMaterial(mats.at(tm[t]));
     }
     for (const Triangle& t : app.triangles) app.scene.AppendGeometry(&t);
-    const uint32_t NL = r.Get<uint32_t>();
-    for (uint32_t i = 0; i < NL; i++) app.scene.AppendLight(&app.triangles.at(r.Get<int32_t>()));
+    for (int32_t t : lights) app.scene.AppendLight(&app.triangles.at(t));
 
     app.film = std::make_unique<Texture2D>(s[0], s[1]);
     app.scene.SetTargetTexture(Scene::AOVType::Rendered, app.film.get());

@@ -81,7 +81,19 @@ def _cases():
         "spheres_pt_soft_sun": synth.spheres_grids(tri_budget=20000, width=32, height=18, spp=1,
                                                    max_bounces=8, env_width=128, env_height=64,
                                                    sun_peak_over_median=30.0),
+        # Lambert albedo maps and GGX reflectance / roughness / normal maps. The
+        # reference's normal map yields an unnormalised normal, with which the
+        # next-event GGX term 1 / (4 |l.n| |v.n|) has unbounded variance (the
+        # 65536-spp image holds infinities), so the MIS integrator is compared without
+        # normal maps; the replay films cover them bit for bit.
+        "textured_pt": _without_normal_maps(synth.textured_spheres(width=32, height=18, spp=1)),
+        "textured_simple": synth.textured_spheres(width=32, height=18, spp=1, integrator=0),
     }
+
+
+def _without_normal_maps(sc):
+    mats = [dataclasses.replace(m, normal_tex=-1) for m in sc.materials]
+    return sc.copy_with(materials=mats)
 
 
 def _with_spp(sc, spp):
