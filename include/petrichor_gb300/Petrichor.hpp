@@ -9,9 +9,12 @@
 // Loaders: Scene::LoadAssets reads the reference's JSON scene format (materials,
 // camera, env, assets; SceneLoader.cpp:17-297), Scene::LoadModel reads OBJ meshes
 // (the reference uses Assimp; this is an own subset reader: v/vn/vt/f, one vertex per
-// face corner, the first three corners of a polygon), Texture2D::Load reads Radiance
-// .hdr and Texture2D::Save writes tone-mapped .png and .hdr (Texture2D.cpp:107-252).
-// PNG decoding and texture maps on materials are not supported.
+// face corner, the first three corners of a polygon), Texture2D::Load reads PNG
+// (colour textures linearised with a 2.2 power, as the reference does) and Radiance
+// .hdr, and Texture2D::Save writes tone-mapped .png and .hdr (Texture2D.cpp:107-252).
+// Material texture maps (Lambert albedo; GGX reflectance, roughness and normal maps)
+// are rendered by every pass, and LoadAssets attaches the "color_tex" and
+// "roughness_tex" maps of the JSON format.
 //
 // Differences, all additive: Petrichor::SetMode/SetIntegrator/SetSeed choose the
 // GB300 path (default: replay mode, SimplePathTracing, i.e. the reference's own
@@ -26,6 +29,7 @@
 #include <cstdint>
 #include <filesystem>
 #include <functional>
+#include <map>
 #include <memory>
 #include <string>
 #include <string_view>
@@ -306,6 +310,10 @@ private:
     float m_apeture = 25e-3f;
 };
 
+struct TextureHandle {  // Scene.h:24-27
+    std::string filePath;
+};
+
 class Scene {
 public:
     struct AOVType {
@@ -337,6 +345,16 @@ public:
         m_materials[std::string(name)] = std::move(material);
     }
     const MaterialBase* GetMaterial(std::string_view name) { return m_materials[std::string(name)].get(); }
+    // Scene.h:131-158: textures kept by the scene under their file path; the first
+    // registration of a path wins, and the pointers stay valid for the scene's life.
+    TextureHandle RegisterTexture(const std::filesystem::path& filePath, const Texture2D& texture) {
+        m_textures.emplace(filePath.string(), texture);
+        return TextureHandle{filePath.string()};
+    }
+    const Texture2D* GetTexture(const TextureHandle& handle) {
+        auto it = m_textures.find(handle.filePath);
+        return it == m_textures.end() ? nullptr : &it->second;
+    }
     const Environment& GetEnvironment() const { return m_environment; }
     void SetEnvironment(const Environment& environment) { m_environment = environment; }
     void SetTargetTexture(AOVType::Value type, Texture2D* target) { m_targets[type] = target; }
@@ -349,6 +367,7 @@ public:
 private:
     std::vector<const GeometryBase*> m_geometries, m_lights;
     std::unordered_map<std::string, std::unique_ptr<const MaterialBase>> m_materials;
+    std::map<std::string, Texture2D> m_textures;
     Environment m_environment;
     std::unique_ptr<Camera> m_mainCamera;
     std::array<Texture2D*, AOVType::NumAOVTypes> m_targets{};

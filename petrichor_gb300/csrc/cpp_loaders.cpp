@@ -15,6 +15,7 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <iterator>
 #include <map>
 #include <sstream>
 
@@ -324,14 +325,348 @@ float Degamma(float v) {
     return (float)std::pow((double)v, (double)(1 / 2.2f));
 }
 
+
+// ---- PNG reading (what stbi_load(path, 3 channels) returns to Texture2D::Load,
+// Texture2D.cpp:118-160). An own decoder written from the zlib / DEFLATE formats
+// (RFC 1950, RFC 1951) and the PNG specification: all colour types and bit depths,
+// Adam7 interlacing, the five scanline filters. The result is 8-bit RGB: grey is
+// replicated, palette indices are looked up, alpha is dropped, 16-bit samples keep
+// their high byte, and 1/2/4-bit grey is scaled to 0..255.
+
+class BitStream {  // DEFLATE bit order: least significant bit of each byte first
+public:
+    BitStream(const uint8_t* p, size_t n) : m_p(p), m_n(n) {}
+    bool Bits(int count, uint32_t* out) {
+        uint32_t v = 0;
+        for (int i = 0; i < count; i++) {
+            if (m_byte >= m_n) return false;
+            v |= (uint32_t)((m_p[m_byte] >> m_bit) & 1u) << i;
+            if (++m_bit == 8) m_bit = 0, m_byte++;
+        }
+        *out = v;
+        return true;
+    }
+    void AlignToByte() {
+        if (m_bit) m_bit = 0, m_byte++;
+    }
+    bool Bytes(size_t count, const uint8_t** out) {
+        if (m_byte + count > m_n) return false;
+        *out = m_p + m_byte;
+        m_byte += count;
+        return true;
+    }
+
+private:
+    const uint8_t* m_p;
+    size_t m_n, m_byte = 0;
+    int m_bit = 0;
+};
+
+// Canonical Huffman code given by its code lengths (RFC 1951 section 3.2.2), decoded
+// one bit at a time: codes of each length are consecutive, ordered by symbol.
+class Huffman {
+public:
+    bool Build(const uint8_t* lengths, int n) {
+        std::fill(std::begin(m_count), std::end(m_count), 0);
+        for (int i = 0; i < n; i++) m_count[lengths[i]]++;
+        m_count[0] = 0;
+        int left = 1;  // reject over-subscribed sets
+        for (int len = 1; len < 16; len++) {
+            left = 2 * left - m_count[len];
+            if (left < 0) return false;
+        }
+        int offset[16] = {0};
+        for (int len = 1; len < 15; len++) offset[len + 1] = offset[len] + m_count[len];
+        m_symbol.assign(n, 0);
+        for (int i = 0; i < n; i++)
+            if (lengths[i]) m_symbol[offset[lengths[i]]++] = (uint16_t)i;
+        return true;
+    }
+    int Decode(BitStream& in) const {
+        int code = 0, first = 0, index = 0;
+        for (int len = 1; len < 16; len++) {
+            uint32_t b;
+            if (!in.Bits(1, &b)) return -1;
+            code |= (int)b;
+            const int count = m_count[len];
+            if (code - first < count) return m_symbol[index + code - first];
+            index += count;
+            first = (first + count) << 1;
+            code <<= 1;
+        }
+        return -1;
+    }
+
+private:
+    int m_count[16];
+    std::vector<uint16_t> m_symbol;
+};
+
+// Length and distance codes (RFC 1951 section 3.2.5).
+constexpr uint16_t kLenBase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                   31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+constexpr uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                   2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+constexpr uint16_t kDistBase[30] = {1,   2,   3,   4,   5,   7,    9,    13,   17,   25,
+                                    33,  49,  65,  97,  129, 193,  257,  385,  513,  769,
+                                    1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+constexpr uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2,  3,  3,  4,  4,  5,  5,  6,
+                                    6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+
+bool InflateBlock(BitStream& in, const Huffman& lit, const Huffman& dist, std::vector<uint8_t>& out,
+                  size_t limit) {
+    for (;;) {
+        const int sym = lit.Decode(in);
+        if (sym < 0) return false;
+        if (sym < 256) {
+            if (out.size() >= limit) return false;
+            out.push_back((uint8_t)sym);
+            continue;
+        }
+        if (sym == 256) return true;
+        const int li = sym - 257;
+        if (li >= 29) return false;
+        uint32_t e;
+        if (!in.Bits(kLenExtra[li], &e)) return false;
+        const size_t len = kLenBase[li] + e;
+        const int di = dist.Decode(in);
+        if (di < 0 || di >= 30) return false;
+        if (!in.Bits(kDistExtra[di], &e)) return false;
+        const size_t d = kDistBase[di] + e;
+        if (d > out.size() || out.size() + len > limit) return false;
+        for (size_t k = 0; k < len; k++) {
+            const uint8_t v = out[out.size() - d];
+            out.push_back(v);
+        }
+    }
+}
+
+// zlib stream -> bytes (at most `limit`); false on any malformed input.
+bool Inflate(const std::vector<uint8_t>& z, std::vector<uint8_t>& out, size_t limit) {
+    if (z.size() < 2 || (z[0] & 15) != 8 || ((z[0] << 8) | z[1]) % 31 != 0 || (z[1] & 32))
+        return false;
+    BitStream in(z.data() + 2, z.size() - 2);
+    Huffman fixedLit, fixedDist;
+    {
+        uint8_t l[288], d[30];
+        for (int i = 0; i < 288; i++) l[i] = i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8;
+        std::fill(d, d + 30, 5);
+        fixedLit.Build(l, 288);
+        fixedDist.Build(d, 30);
+    }
+    uint32_t last = 0;
+    while (!last) {
+        uint32_t type;
+        if (!in.Bits(1, &last) || !in.Bits(2, &type)) return false;
+        if (type == 0) {  // stored
+            in.AlignToByte();
+            const uint8_t* h;
+            if (!in.Bytes(4, &h)) return false;
+            const uint32_t len = h[0] | (h[1] << 8), nlen = h[2] | (h[3] << 8);
+            if ((len ^ 0xffffu) != nlen || out.size() + len > limit) return false;
+            const uint8_t* p;
+            if (!in.Bytes(len, &p)) return false;
+            out.insert(out.end(), p, p + len);
+        } else if (type == 1) {
+            if (!InflateBlock(in, fixedLit, fixedDist, out, limit)) return false;
+        } else if (type == 2) {  // dynamic codes
+            uint32_t hlit, hdist, hclen;
+            if (!in.Bits(5, &hlit) || !in.Bits(5, &hdist) || !in.Bits(4, &hclen)) return false;
+            hlit += 257, hdist += 1, hclen += 4;
+            if (hlit > 286 || hdist > 30) return false;
+            static constexpr uint8_t kOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5,
+                                                   11, 4,  12, 3, 13, 2, 14, 1, 15};
+            uint8_t cl[19] = {0};
+            for (uint32_t i = 0; i < hclen; i++) {
+                uint32_t v;
+                if (!in.Bits(3, &v)) return false;
+                cl[kOrder[i]] = (uint8_t)v;
+            }
+            Huffman clCode;
+            if (!clCode.Build(cl, 19)) return false;
+            uint8_t lens[286 + 30] = {0};
+            for (uint32_t i = 0; i < hlit + hdist;) {
+                const int sym = clCode.Decode(in);
+                if (sym < 0) return false;
+                if (sym < 16) {
+                    lens[i++] = (uint8_t)sym;
+                    continue;
+                }
+                uint32_t rep, v = 0;
+                if (sym == 16) {
+                    if (i == 0 || !in.Bits(2, &rep)) return false;
+                    rep += 3, v = lens[i - 1];
+                } else if (sym == 17) {
+                    if (!in.Bits(3, &rep)) return false;
+                    rep += 3;
+                } else {
+                    if (!in.Bits(7, &rep)) return false;
+                    rep += 11;
+                }
+                if (i + rep > hlit + hdist) return false;
+                while (rep--) lens[i++] = (uint8_t)v;
+            }
+            if (lens[256] == 0) return false;
+            Huffman lit, dist;
+            if (!lit.Build(lens, (int)hlit) || !dist.Build(lens + hlit, (int)hdist)) return false;
+            if (!InflateBlock(in, lit, dist, out, limit)) return false;
+        } else {
+            return false;
+        }
+    }
+    return true;
+}
+
+uint32_t BigEndian32(const uint8_t* p) {
+    return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+}
+
+int Paeth(int a, int b, int c) {
+    const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+    return (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+}
+
+// Reverses the scanline filters of one (sub)image in place; rows of `stride` bytes
+// each preceded by their filter byte; bpp = bytes per complete pixel (at least 1).
+bool Unfilter(uint8_t* data, int rows, size_t stride, int bpp, std::vector<uint8_t>& out) {
+    out.assign((size_t)rows * stride, 0);
+    for (int y = 0; y < rows; y++) {
+        const uint8_t f = data[(size_t)y * (stride + 1)];
+        const uint8_t* src = data + (size_t)y * (stride + 1) + 1;
+        uint8_t* row = out.data() + (size_t)y * stride;
+        const uint8_t* up = y ? row - stride : nullptr;
+        for (size_t x = 0; x < stride; x++) {
+            const int a = x >= (size_t)bpp ? row[x - bpp] : 0, b = up ? up[x] : 0;
+            const int c = (up && x >= (size_t)bpp) ? up[x - bpp] : 0;
+            int v = src[x];
+            switch (f) {
+            case 0: break;
+            case 1: v += a; break;
+            case 2: v += b; break;
+            case 3: v += (a + b) >> 1; break;
+            case 4: v += Paeth(a, b, c); break;
+            default: return false;
+            }
+            row[x] = (uint8_t)v;
+        }
+    }
+    return true;
+}
+
+bool ReadPng(const std::filesystem::path& path, int* W, int* H, std::vector<uint8_t>& rgb) {
+    std::ifstream f(path, std::ios::binary);
+    std::vector<uint8_t> file((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    static constexpr uint8_t kSig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    if (file.size() < 8 || std::memcmp(file.data(), kSig, 8) != 0) return false;
+    uint32_t width = 0, height = 0;
+    int depth = 0, color = -1, interlace = 0;
+    std::vector<uint8_t> idat, palette;
+    for (size_t off = 8; off + 12 <= file.size();) {
+        const uint32_t len = BigEndian32(&file[off]);
+        if (len > file.size() - off - 12) return false;
+        const char* type = (const char*)&file[off + 4];
+        const uint8_t* d = &file[off + 8];
+        if (std::memcmp(type, "IHDR", 4) == 0 && len >= 13) {
+            width = BigEndian32(d), height = BigEndian32(d + 4);
+            depth = d[8], color = d[9], interlace = d[12];
+            if (d[10] != 0 || d[11] != 0) return false;
+        } else if (std::memcmp(type, "PLTE", 4) == 0) {
+            palette.assign(d, d + len);
+        } else if (std::memcmp(type, "IDAT", 4) == 0) {
+            idat.insert(idat.end(), d, d + len);
+        } else if (std::memcmp(type, "IEND", 4) == 0) {
+            break;
+        }
+        off += 12 + (size_t)len;
+    }
+    const int channels = color == 0 ? 1 : color == 2 ? 3 : color == 3 ? 1 : color == 4 ? 2 : color == 6 ? 4 : 0;
+    const bool depthOk = (color == 0 && (depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)) ||
+                         (color == 3 && (depth == 1 || depth == 2 || depth == 4 || depth == 8)) ||
+                         ((color == 2 || color == 4 || color == 6) && (depth == 8 || depth == 16));
+    if (!channels || !depthOk || width == 0 || height == 0 || width > (1u << 24) || height > (1u << 24) ||
+        (uint64_t)width * height > (1ull << 28) || interlace > 1 || (color == 3 && palette.size() < 3))
+        return false;
+    const int bitsPerPixel = channels * depth, bpp = std::max(1, bitsPerPixel / 8);
+    auto stride = [&](uint32_t w) { return ((size_t)w * bitsPerPixel + 7) / 8; };
+    // Adam7 passes (start and step in x and y); a non-interlaced image is one pass
+    static constexpr int kX0[7] = {0, 4, 0, 2, 0, 1, 0}, kY0[7] = {0, 0, 4, 0, 2, 0, 1};
+    static constexpr int kDX[7] = {8, 8, 4, 4, 2, 2, 1}, kDY[7] = {8, 8, 8, 4, 4, 2, 2};
+    const int passes = interlace ? 7 : 1;
+    size_t expected = 0;
+    uint32_t pw[7], ph[7];
+    for (int p = 0; p < passes; p++) {
+        pw[p] = interlace ? (width > (uint32_t)kX0[p] ? (width - kX0[p] + kDX[p] - 1) / kDX[p] : 0) : width;
+        ph[p] = interlace ? (height > (uint32_t)kY0[p] ? (height - kY0[p] + kDY[p] - 1) / kDY[p] : 0) : height;
+        if (pw[p] && ph[p]) expected += (size_t)ph[p] * (stride(pw[p]) + 1);
+    }
+    std::vector<uint8_t> raw;
+    if (!Inflate(idat, raw, expected) || raw.size() != expected) return false;
+    rgb.assign((size_t)width * height * 3, 0);
+    const int maxSample = (1 << depth) - 1;
+    size_t pos = 0;
+    std::vector<uint8_t> rows;
+    for (int p = 0; p < passes; p++) {
+        if (!pw[p] || !ph[p]) continue;
+        const size_t st = stride(pw[p]);
+        if (!Unfilter(raw.data() + pos, (int)ph[p], st, bpp, rows)) return false;
+        pos += (size_t)ph[p] * (st + 1);
+        for (uint32_t y = 0; y < ph[p]; y++) {
+            const uint8_t* row = rows.data() + (size_t)y * st;
+            // sample c of pixel x as 0..255 (or the raw index for palettes)
+            auto sample = [&](uint32_t x, int c) -> int {
+                const size_t bit = ((size_t)x * channels + c) * depth;
+                if (depth == 16) return row[bit / 8];  // high byte
+                if (depth == 8) return row[bit / 8];
+                const int v = (row[bit / 8] >> (8 - depth - (int)(bit % 8))) & maxSample;
+                return color == 3 ? v : v * (255 / maxSample);
+            };
+            for (uint32_t x = 0; x < pw[p]; x++) {
+                const uint32_t ox = interlace ? kX0[p] + x * kDX[p] : x;
+                const uint32_t oy = interlace ? kY0[p] + y * kDY[p] : y;
+                uint8_t* o = &rgb[((size_t)oy * width + ox) * 3];
+                if (color == 3) {
+                    const int i = sample(x, 0);
+                    if ((size_t)i * 3 + 2 >= palette.size()) return false;
+                    o[0] = palette[3 * i], o[1] = palette[3 * i + 1], o[2] = palette[3 * i + 2];
+                } else if (channels <= 2) {
+                    o[0] = o[1] = o[2] = (uint8_t)sample(x, 0);
+                } else {
+                    for (int c = 0; c < 3; c++) o[c] = (uint8_t)sample(x, c);
+                }
+            }
+        }
+    }
+    *W = (int)width;
+    *H = (int)height;
+    return true;
+}
 }  // namespace
 
 // ---------------------------------------------------------------- Texture2D
-bool Texture2D::Load(const std::filesystem::path& path, TextureColorType) {
+bool Texture2D::Load(const std::filesystem::path& path, TextureColorType type) {
     std::ifstream f(path, std::ios::binary);
     if (!f) {
         Error("Texture not found. " + path.string());
         return false;
+    }
+    if (path.extension() == ".png") {  // Texture2D.cpp:118-160
+        int W = 0, H = 0;
+        std::vector<uint8_t> rgb;
+        if (!ReadPng(path, &W, &H, rgb)) {
+            Error("Could not read png file. [" + path.string() + "]");
+            return false;
+        }
+        std::vector<float> px(rgb.size());
+        for (size_t i = 0; i < rgb.size(); i++) {
+            px[i] = static_cast<float>(rgb[i]) / static_cast<float>(255);
+            // colour textures are linearised with ApplyGamma (std::pow(v, 2.2f))
+            if (type == TextureColorType::Color) px[i] = std::pow(px[i], 2.2f);
+        }
+        m_width = W;
+        m_height = H;
+        m_pixels = std::move(px);
+        m_isLoaded = true;
+        return true;
     }
     char magic[8] = {};
     f.read(magic, 8);
@@ -507,7 +842,12 @@ void Scene::LoadAssets(const std::filesystem::path& path) {
             auto mat = std::make_unique<Lambert>(LoadVector3f(m, "base_color"));
             std::string tex;
             LoadValue(&tex, m, "color_tex");
-            if (!tex.empty()) Error("[SceneLoaderJson] texture maps are not supported; '" + tex + "' ignored.");
+            if (!tex.empty()) {  // relative to the scene file, registered under that path
+                const std::filesystem::path tp = dir / tex;
+                Texture2D t;
+                if (t.Load(tp, Texture2D::TextureColorType::Color))
+                    mat->SetTexAlbedo(GetTexture(RegisterTexture(tp, t)));
+            }
             RegisterMaterial(name, std::move(mat));
         } else if (type == "glass") {
             const Color3f color = LoadVector3f(m, "color");
@@ -518,13 +858,22 @@ void Scene::LoadAssets(const std::filesystem::path& path) {
             const Color3f color = LoadVector3f(m, "color");
             float roughness = 0.0f;
             LoadValue(&roughness, m, "roughness");
+            auto mat = std::make_unique<GGX>(color, roughness);
             std::string tex;
             LoadValue(&tex, m, "color_tex");
-            if (!tex.empty()) Error("[SceneLoaderJson] texture maps are not supported; '" + tex + "' ignored.");
+            if (!tex.empty()) {  // read relative to the scene file, registered under the key as written
+                Texture2D t;
+                if (t.Load(dir / tex, Texture2D::TextureColorType::Color))
+                    mat->SetF0Texture(GetTexture(RegisterTexture(tex, t)));
+            }
             tex.clear();
             LoadValue(&tex, m, "roughness_tex");
-            if (!tex.empty()) Error("[SceneLoaderJson] texture maps are not supported; '" + tex + "' ignored.");
-            RegisterMaterial(name, std::make_unique<GGX>(color, roughness));
+            if (!tex.empty()) {  // the reference reads this one relative to the working directory
+                Texture2D t;
+                if (t.Load(tex, Texture2D::TextureColorType::NonColor))
+                    mat->SetRoughnessMap(GetTexture(RegisterTexture(tex, t)));
+            }
+            RegisterMaterial(name, std::move(mat));
         } else if (type == "emission") {
             // the reference registers nothing for an emission entry (SceneLoader.cpp:189-191)
         } else if (type == "mix") {

@@ -5,6 +5,8 @@
 //   load_scene dump   <settings> <scene.json> <out.txt>  writes what was loaded as text
 //   load_scene render <settings> <scene.json> <out.bin>  renders (replay) and writes the film
 //   load_scene save   <in.hdr> <out.png> <out.hdr>       loads an image and saves it both ways
+//   load_scene tex    <in> <out.bin> color|noncolor        loads an image (Texture2D::Load) and
+//                                                          writes int32 width, height, RGB floats
 //
 // The text dump holds one record per line with floats as C99 hex literals, so the
 // test reads back exact values.
@@ -15,6 +17,8 @@
 #include <fstream>
 #include <map>
 #include <string>
+#include <utility>
+#include <vector>
 
 using namespace Petrichor;
 using namespace Petrichor::Core;
@@ -56,10 +60,20 @@ int Dump(const Scene& scene, const char* out) {
         const int k = (int)ids.size();
         ids[m] = k;
         std::fprintf(f, "material %d %d", k, m ? (int)m->GetMaterialType() : -1);
-        if (m && m->GetMaterialType() == MaterialTypes::Lambert) Put(f, static_cast<const Lambert*>(m)->GetKd());
+        // texture maps: "map <material> <slot> <width> <height> <strength> <texels...>"
+        std::vector<std::pair<int, const Texture2D*>> maps;
+        float strength = 1.0f;
+        if (m && m->GetMaterialType() == MaterialTypes::Lambert) {
+            Put(f, static_cast<const Lambert*>(m)->GetKd());
+            maps.push_back({0, static_cast<const Lambert*>(m)->GetTexAlbedo()});
+        }
         if (m && m->GetMaterialType() == MaterialTypes::Glossy) {
-            Put(f, static_cast<const GGX*>(m)->GetReflectance());
-            std::fprintf(f, " %a", static_cast<const GGX*>(m)->GetRoughness());
+            const auto* g = static_cast<const GGX*>(m);
+            Put(f, g->GetReflectance());
+            std::fprintf(f, " %a", g->GetRoughness());
+            maps.push_back({1, g->GetF0Texture()});
+            maps.push_back({2, g->GetRoughnessMap()});
+            strength = g->GetRoughnessMapStrength();
         }
         if (m && m->GetMaterialType() == MaterialTypes::Glass) {
             Put(f, static_cast<const Glass*>(m)->GetColor());
@@ -70,6 +84,13 @@ int Dump(const Scene& scene, const char* out) {
             std::fprintf(f, " %a", x->GetMix());
         }
         std::fprintf(f, "\n");
+        for (const auto& [slot, t] : maps) {
+            if (!t) continue;
+            std::fprintf(f, "map %d %d %d %d %a", k, slot, t->GetWidth(), t->GetHeight(), strength);
+            for (int j = 0; j < t->GetHeight(); j++)
+                for (int i = 0; i < t->GetWidth(); i++) Put(f, t->GetPixel(i, j));
+            std::fprintf(f, "\n");
+        }
         return k;
     };
     for (const GeometryBase* g : scene.GetGeometries()) {
@@ -100,6 +121,19 @@ int main(int argc, char** argv) {
         return 2;
     }
     const std::string mode = argv[1];
+    if (mode == "tex") {
+        Texture2D tex;
+        const bool color = std::string(argv[4]) == "color";
+        if (!tex.Load(argv[2], color ? Texture2D::TextureColorType::Color
+                                     : Texture2D::TextureColorType::NonColor))
+            return 4;
+        std::ofstream o(argv[3], std::ios::binary);
+        const int32_t dims[2] = {tex.GetWidth(), tex.GetHeight()};
+        o.write(reinterpret_cast<const char*>(dims), 8);
+        o.write(reinterpret_cast<const char*>(tex.GetRawDataPtr()),
+                (std::streamsize)((size_t)dims[0] * dims[1] * 3 * 4));
+        return o ? 0 : 1;
+    }
     if (mode == "save") {
         Texture2D tex;
         if (!tex.Load(argv[2])) return 4;
