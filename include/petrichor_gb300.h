@@ -27,6 +27,8 @@
  *                        (LibPetrichor/Core/Logger.h:63-94, used at Petrichor.cpp:106,124)
  *   pt_bvh_build         BinnedSAHBVH::Build alone, on the host, returning the tree
  *                        (LibPetrichor/Core/Accel/BinnedSAHBVH.cpp:15-225)
+ *   pt_bvh_build_device  the same build on the GPU (the same tree, node for node)
+ *   pt_set_bvh_builder   which of the two pt_scene_upload runs
  */
 #ifndef PETRICHOR_GB300_H_
 #define PETRICHOR_GB300_H_
@@ -154,7 +156,9 @@ typedef struct pt_settings {
 typedef struct pt_scene_info {
   uint32_t num_triangles, num_nodes, tree_height, num_lights;
   uint64_t device_bytes;
-  double build_seconds; /* host binned-SAH build */
+  double build_seconds;  /* binned-SAH build, wall time */
+  int32_t bvh_builder;   /* PT_BVH_BUILDER_* that built the tree */
+  int32_t reserved;
 } pt_scene_info;
 
 typedef struct pt_stats {
@@ -280,6 +284,28 @@ int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float*
 int pt_bvh_build(const float* positions, uint32_t num_vertices, const int32_t* indices,
                  uint32_t num_triangles, int32_t threads, uint32_t* num_nodes,
                  uint32_t* tree_height, float* bounds, int32_t* node_ints, int32_t* prim_ids);
+
+/* The same build on the context's GPU: the reference's tree node for node, including
+ * the order std::sort leaves equal keys in. Outputs as pt_bvh_build, sized for
+ * max(1, 2 * num_triangles) nodes; *num_nodes receives the count; stats may be NULL.
+ * Synchronous; temporary device memory of about 250 bytes per triangle. */
+typedef struct pt_bvh_build_stats {
+  double device_ms;   /* device time, uploads to tree read back */
+  int32_t levels;     /* tree levels built */
+  int32_t rounds;     /* parallel partition rounds of the per-node sorts */
+  int32_t heapsorts;  /* sort subranges that ran out of depth budget (heapsorted) */
+  int32_t launches;   /* kernels launched */
+} pt_bvh_build_stats;
+int pt_bvh_build_device(pt_context* ctx, const float* positions, uint32_t num_vertices,
+                        const int32_t* indices, uint32_t num_triangles, uint32_t* num_nodes,
+                        uint32_t* tree_height, float* bounds, int32_t* node_ints,
+                        int32_t* prim_ids, pt_bvh_build_stats* stats);
+
+/* Builder pt_scene_upload uses: both give the same tree; the device builder is the
+ * default. */
+#define PT_BVH_BUILDER_HOST 0
+#define PT_BVH_BUILDER_DEVICE 1
+int pt_set_bvh_builder(pt_context* ctx, int32_t builder);
 
 /* Per-stage device times (CUDA events around every stage launch) and work tallies
  * of one wavefront render. With count_reference != 0 every extended ray is also

@@ -88,10 +88,16 @@ class PtRequestStatus(ctypes.Structure):
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 
+class PtBvhBuildStats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("levels", ctypes.c_int32), ("rounds", ctypes.c_int32),
+                ("heapsorts", ctypes.c_int32), ("launches", ctypes.c_int32)]
+
+
 class PtSceneInfo(ctypes.Structure):
     _fields_ = [("num_triangles", ctypes.c_uint32), ("num_nodes", ctypes.c_uint32),
                 ("tree_height", ctypes.c_uint32), ("num_lights", ctypes.c_uint32),
-                ("device_bytes", ctypes.c_uint64), ("build_seconds", ctypes.c_double)]
+                ("device_bytes", ctypes.c_uint64), ("build_seconds", ctypes.c_double),
+                ("bvh_builder", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class PtStats(ctypes.Structure):
@@ -130,8 +136,10 @@ EXPORTED = [
     "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc", "pt_batch_render",
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
     "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
-    "pt_render_aov", "pt_render_aov_device",
+    "pt_render_aov", "pt_render_aov_device", "pt_bvh_build_device", "pt_set_bvh_builder",
 ]
+
+BVH_BUILDER_HOST, BVH_BUILDER_DEVICE = 0, 1
 
 _lib = None
 
@@ -193,6 +201,9 @@ def load(build: bool = True):
     L.pt_get_tuning.argtypes = [vp, ctypes.POINTER(PtTuning)]
     L.pt_bvh_build.argtypes = [vp, u32, vp, u32, i32, ctypes.POINTER(u32), ctypes.POINTER(u32),
                                vp, vp, vp]
+    L.pt_bvh_build_device.argtypes = [vp, vp, u32, vp, u32, ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                      vp, vp, vp, ctypes.POINTER(PtBvhBuildStats)]
+    L.pt_set_bvh_builder.argtypes = [vp, i32]
     _lib = L
     return L
 
@@ -427,6 +438,24 @@ class Context:
         self._check(self.L.pt_autotune(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
                                        probe_spp, ctypes.byref(t)), "pt_autotune")
         return t
+
+    def set_bvh_builder(self, builder: int):
+        self._check(self.L.pt_set_bvh_builder(self.h, builder), "pt_set_bvh_builder")
+
+    def bvh_build_device(self, positions: np.ndarray, indices: np.ndarray):
+        """Device binned-SAH build: (bounds (N,6), ints (N,5), prim_ids (T,), height, stats)."""
+        pos = np.ascontiguousarray(positions, np.float32)
+        idx = np.ascontiguousarray(indices, np.int32)
+        cap = max(1, 2 * idx.shape[0])
+        b = np.zeros((cap, 6), np.float32)
+        q = np.zeros((cap, 5), np.int32)
+        ids = np.zeros(idx.shape[0], np.int32)
+        n, h, st = ctypes.c_uint32(), ctypes.c_uint32(), PtBvhBuildStats()
+        self._check(self.L.pt_bvh_build_device(self.h, pos.ctypes.data, pos.shape[0], idx.ctypes.data,
+                                               idx.shape[0], ctypes.byref(n), ctypes.byref(h),
+                                               b.ctypes.data, q.ctypes.data, ids.ctypes.data,
+                                               ctypes.byref(st)), "pt_bvh_build_device")
+        return b[:n.value], q[:n.value], ids, h.value, st
 
     def set_tuning(self, wave_paths: int = 0, blocks_per_sm: int = 0, band_rows: int = 0,
                    use_graphs: int = 1):

@@ -138,6 +138,11 @@ struct Builder {
             }
         }
         if (bestBin == 0) return;
+        // The child bounds are merges in range order (BinnedSAHBVH.cpp:163-186), where the
+        // first of equal extremes wins (+0 against -0): merge the right child's bins in
+        // ascending order rather than take the suffix, which merged them descending.
+        bestR = Box();
+        for (int k = bestBin; k < kBins; k++) bestR.Merge(binBox[k]);
         n->left = arena.New(bestL, b, b + bestLeft);
         n->right = arena.New(bestR, b + bestLeft, e);
     }

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "bvh_builder.h"
+#include "bvh_gpu.h"
 #include "pt_kernels.h"
 #include "pt_layout.h"
 #include "context.h"
@@ -148,6 +149,9 @@ int Validate(pt_context* ctx, const pt_scene_desc* d) {
     if ((d->env_width > 0) != (d->env_height > 0) || d->env_width < 0 || d->env_height < 0)
         return Fail(ctx, PT_ERR_INVALID_ARG, "environment size is invalid");
     if (d->env_width > 0 && !d->env_rgb) return Fail(ctx, PT_ERR_INVALID_ARG, "environment texels missing");
+    for (size_t i = 0; i < (size_t)d->num_vertices * 3 && d->num_triangles; i++)
+        if (!std::isfinite(d->positions[i]))
+            return Fail(ctx, PT_ERR_INVALID_ARG, "vertex positions must be finite");
     if (d->num_textures && !d->textures) return Fail(ctx, PT_ERR_INVALID_ARG, "textures missing");
     int64_t texels = 0;
     for (uint32_t t = 0; t < d->num_textures; t++) {
@@ -452,7 +456,16 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     auto sg = std::make_unique<SceneGpu>();
     const int T = (int)d->num_triangles;
     const auto t0 = std::chrono::steady_clock::now();
-    BvhResult bvh = BuildBinnedSah(d->positions, d->indices, T, 0);
+    BvhResult bvh;
+    if (ctx->bvhBuilder == PT_BVH_BUILDER_DEVICE) {
+        std::string why;
+        const cudaError_t be = BuildBinnedSahDevice(d->positions, (int)d->num_vertices, d->indices, T,
+                                                    ctx->stream, &bvh, &why, nullptr);
+        if (be != cudaSuccess)
+            return Fail(ctx, be == cudaErrorMemoryAllocation ? PT_ERR_OUT_OF_MEMORY : PT_ERR_CUDA, why);
+    } else {
+        bvh = BuildBinnedSah(d->positions, d->indices, T, 0);
+    }
     const double buildSec =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     // nodes
@@ -612,6 +625,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     s.info.tree_height = bvh.height;
     s.info.num_lights = d->num_lights;
     s.info.build_seconds = buildSec;
+    s.info.bvh_builder = ctx->bvhBuilder;
     for (auto& b : s.buffers) s.info.device_bytes += b.bytes;
     const int id = ctx->nextId++;
     ctx->scenes[id] = std::move(sg);
@@ -986,6 +1000,63 @@ int pt_bvh_build(const float* positions, uint32_t numVertices, const int32_t* in
         }
     }
     if (primIds) std::memcpy(primIds, r.primIds.data(), r.primIds.size() * sizeof(int32_t));
+    return PT_OK;
+}
+
+int pt_bvh_build_device(pt_context* ctx, const float* positions, uint32_t numVertices,
+                        const int32_t* indices, uint32_t numTriangles, uint32_t* numNodes,
+                        uint32_t* height, float* bounds, int32_t* nodeInts, int32_t* primIds,
+                        pt_bvh_build_stats* stats) {
+    if (!ctx || !numNodes || (numTriangles && (!positions || !indices))) return PT_ERR_INVALID_ARG;
+    if (numTriangles > (1u << 30)) return Fail(ctx, PT_ERR_INVALID_ARG, "too many triangles");
+    for (uint32_t t = 0; t < numTriangles * 3; t++)
+        if (indices[t] < 0 || (uint32_t)indices[t] >= numVertices)
+            return Fail(ctx, PT_ERR_INVALID_ARG, "triangle vertex index out of range");
+    for (size_t i = 0; i < (size_t)numVertices * 3; i++)
+        if (!std::isfinite(positions[i])) return Fail(ctx, PT_ERR_INVALID_ARG, "vertex positions must be finite");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    int rc = SetDevice(ctx);
+    if (rc != PT_OK) return rc;
+    BvhResult r;
+    std::string why;
+    DeviceBuildStats st;
+    const cudaError_t e = BuildBinnedSahDevice(positions, (int)numVertices, indices, (int)numTriangles,
+                                               ctx->stream, &r, &why, &st);
+    if (e != cudaSuccess)
+        return Fail(ctx, e == cudaErrorMemoryAllocation ? PT_ERR_OUT_OF_MEMORY : PT_ERR_CUDA, why);
+    *numNodes = (uint32_t)r.nodes.size();
+    if (height) *height = (uint32_t)r.height;
+    if (stats) {
+        stats->device_ms = st.ms;
+        stats->levels = st.levels;
+        stats->rounds = st.rounds;
+        stats->heapsorts = st.heapsorts;
+        stats->launches = st.launches;
+    }
+    if (bounds && nodeInts) {
+        for (size_t i = 0; i < r.nodes.size(); i++) {
+            const BvhNodeOut& n = r.nodes[i];
+            for (int a = 0; a < 3; a++) {
+                bounds[6 * i + a] = n.lo[a];
+                bounds[6 * i + 3 + a] = n.hi[a];
+            }
+            nodeInts[5 * i] = n.child[0];
+            nodeInts[5 * i + 1] = n.child[1];
+            nodeInts[5 * i + 2] = n.begin;
+            nodeInts[5 * i + 3] = n.end;
+            nodeInts[5 * i + 4] = n.leaf ? 1 : 0;
+        }
+    }
+    if (primIds && !r.primIds.empty()) std::memcpy(primIds, r.primIds.data(), r.primIds.size() * sizeof(int32_t));
+    return PT_OK;
+}
+
+int pt_set_bvh_builder(pt_context* ctx, int32_t builder) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    if (builder != PT_BVH_BUILDER_HOST && builder != PT_BVH_BUILDER_DEVICE)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "unknown BVH builder");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->bvhBuilder = builder;
     return PT_OK;
 }
 

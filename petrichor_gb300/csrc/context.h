@@ -63,6 +63,7 @@ struct pt_context {
     int tunedWavePaths = 0;  // 0: the automatic wave size
     double tunedProbeMs = 0.0;
     ptg::WaveGraphCache* graphs = nullptr;
+    int bvhBuilder = PT_BVH_BUILDER_DEVICE;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_stats stats{};
     uint32_t tilesDone = 0, tilesTotal = 0;

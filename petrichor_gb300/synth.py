@@ -411,6 +411,40 @@ def terrain_rocks(seed: int = 5, terrain_n: int = 3000, n_rocks: int = 4000, roc
     return Scene(pos, nrm, uv, idx, tm, sh, np.zeros(0, np.int32), mats, cam, env, st)
 
 
+def bvh_ties(seed: int = 6, n_lattice: int = 2400, n_zero: int = 500, n_free: int = 300,
+             width: int = 32, height: int = 18, spp: int = 1) -> Scene:
+    """Triangles whose binned-SAH tree depends on how std::sort orders equal keys and on
+    signed zeros: centroids on a coarse lattice (exact, with many equal keys on every
+    axis and exact duplicates), a slab in the plane x = 0 whose vertices carry +0.0 or
+    -0.0, and a few free triangles; all shuffled together."""
+    rng = Rng(seed)
+    tris = []
+    cell = np.floor(rng.uniform(3 * n_lattice).reshape(n_lattice, 3) * [12, 10, 8])
+    lift = np.floor(rng.uniform(n_lattice) * 2) * 3.0
+    for (ix, iy, iz), s in zip(cell, lift):
+        o = np.array([3 * ix, 3 * iy, 3 * iz])
+        tris.append([o, o + [3, 0, 0], o + [0, 3, s]])
+    for k in range(n_zero):
+        yz = rng.uniform(6).reshape(3, 2) * 30.0
+        sign = np.where(rng.uniform(3) < 0.5, -0.0, 0.0)
+        tris.append([[sign[j], yz[j, 0], yz[j, 1]] for j in range(3)])
+    for k in range(n_free):
+        c = rng.uniform(3) * [36, 30, 24]
+        tris.append([c + (rng.uniform(3) - 0.5) * 2.0 for _ in range(3)])
+    order = np.argsort(rng.uniform(len(tris)), kind="stable")
+    P = np.array([tris[i] for i in order], np.float64).reshape(-1, 3)
+    I = np.arange(P.shape[0]).reshape(-1, 3)
+    b = _Builder()
+    b.add(P, I, 0, SHADING_FLAT)
+    pos, nrm, uv, idx, tm, sh = b.arrays()
+    mats = [Material(MAT_LAMBERT, color=(0.6, 0.6, 0.6))]
+    env = Environment(base_color=(1.0, 1.0, 1.0), texture=None)
+    cam = Camera(pos=(18.0, -40.0, 30.0), view_dir=(0.0, 40.0, -18.0), fov=math.radians(50.0),
+                 focus_target=None, aperture=0.0)
+    st = Settings(width=width, height=height, spp=spp, max_bounces=3)
+    return Scene(pos, nrm, uv, idx, tm, sh, np.zeros(0, np.int32), mats, cam, env, st)
+
+
 def batch_instances(seed: int = 3, n: int = 64, tri_lo: float = 1e4, tri_hi: float = 2e6,
                     px_lo: float = 256 ** 2, px_hi: float = 1024 ** 2, spps=(4, 16, 64, 256),
                     env_width: int = 1024, env_height: int = 512, max_bounces: int = 16):

@@ -67,15 +67,20 @@ def main():
         film = np.frombuffer(oracle.run_reference("film", sc, work), np.float32)
         out[f"{name}/film"] = film.reshape(sc.settings.height, sc.settings.width, 3)
         print(name, "film mean", float(film.mean()))
-    # BVH, primary hits and environment samples of the triangle-soup case
+    # BVH of the triangle-soup case and of a scene of equal sort keys and signed zeros;
+    # primary hits and environment samples of the triangle-soup case
+    bvh_scenes = {"spheres_pt": cases()["spheres_pt"], "bvh_ties": synth.bvh_ties()}
+    for name, sc in bvh_scenes.items():
+        if name not in cases():
+            out[f"{name}/scene"] = np.frombuffer(scene_io.scene_bytes(sc), np.uint8)
+        rb = oracle.run_reference("bvh", sc, work)
+        nn, ni, depth = np.frombuffer(rb[:12], np.int32)
+        arr = np.frombuffer(rb[12:12 + nn * 44], np.uint8).reshape(nn, 44)
+        out[f"{name}/bvh_bounds"] = arr[:, :24].copy().view(np.float32).reshape(nn, 6)
+        out[f"{name}/bvh_ints"] = arr[:, 24:].copy().view(np.int32).reshape(nn, 5)
+        out[f"{name}/bvh_ids"] = np.frombuffer(rb[12 + nn * 44:], np.int32).copy()
+        out[f"{name}/bvh_depth"] = np.array([depth], np.int32)
     sc = cases()["spheres_pt"]
-    rb = oracle.run_reference("bvh", sc, work)
-    nn, ni, depth = np.frombuffer(rb[:12], np.int32)
-    arr = np.frombuffer(rb[12:12 + nn * 44], np.uint8).reshape(nn, 44)
-    out["spheres_pt/bvh_bounds"] = arr[:, :24].copy().view(np.float32).reshape(nn, 6)
-    out["spheres_pt/bvh_ints"] = arr[:, 24:].copy().view(np.int32).reshape(nn, 5)
-    out["spheres_pt/bvh_ids"] = np.frombuffer(rb[12 + nn * 44:], np.int32).copy()
-    out["spheres_pt/bvh_depth"] = np.array([depth], np.int32)
     n = sc.settings.width * sc.settings.height
     rh = oracle.run_reference("hits", sc, work, 7, 11)
     out["spheres_pt/hit_rays"] = np.frombuffer(rh[:n * 32], np.float32).reshape(n, 8)

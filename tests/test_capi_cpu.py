@@ -89,6 +89,16 @@ def test_product_bvh_matches_reference_tree(golden, threads):
     assert np.array_equal(ids, golden["spheres_pt/bvh_ids"])
 
 
+def test_product_bvh_matches_reference_tree_on_equal_keys_and_signed_zeros(golden):
+    """Equal sort keys on every axis and node bounds at +0 and -0: the host build must
+    leave std::sort's order and the reference's first-of-equal bound merges."""
+    sc = golden_scene(golden, "bvh_ties")
+    b, q, ids, h = capi.bvh_build(sc.positions, sc.indices, threads=4)
+    assert np.array_equal(b.view(np.uint32), golden["bvh_ties/bvh_bounds"].view(np.uint32))
+    assert np.array_equal(q, golden["bvh_ties/bvh_ints"])
+    assert np.array_equal(ids, golden["bvh_ties/bvh_ids"])
+
+
 def test_product_bvh_matches_oracle_on_large_parallel_build():
     sc = synth.spheres_grids(tri_budget=150_000, width=8, height=8, spp=1, env_width=8, env_height=4)
     ob, oq, oids, _ = oracle.OracleScene(sc).bvh()

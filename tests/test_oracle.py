@@ -41,12 +41,13 @@ def test_oracle_film_independent_of_thread_count(golden):
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-def test_oracle_bvh_node_for_node(golden):
-    b, q, ids, depth = oracle.OracleScene(golden_scene(golden, "spheres_pt")).bvh()
-    assert np.array_equal(b.view(np.uint32), golden["spheres_pt/bvh_bounds"].view(np.uint32))
-    assert np.array_equal(q, golden["spheres_pt/bvh_ints"])
-    assert np.array_equal(ids, golden["spheres_pt/bvh_ids"])
-    assert depth == int(golden["spheres_pt/bvh_depth"][0])
+@pytest.mark.parametrize("name", ["spheres_pt", "bvh_ties"])
+def test_oracle_bvh_node_for_node(golden, name):
+    b, q, ids, depth = oracle.OracleScene(golden_scene(golden, name)).bvh()
+    assert np.array_equal(b.view(np.uint32), golden[f"{name}/bvh_bounds"].view(np.uint32))
+    assert np.array_equal(q, golden[f"{name}/bvh_ints"])
+    assert np.array_equal(ids, golden[f"{name}/bvh_ids"])
+    assert depth == int(golden[f"{name}/bvh_depth"][0])
 
 
 def test_oracle_primary_rays_and_hits(golden):
