@@ -29,6 +29,8 @@
  *                        (LibPetrichor/Core/Accel/BinnedSAHBVH.cpp:15-225)
  *   pt_bvh_build_device  the same build on the GPU (the same tree, node for node)
  *   pt_set_bvh_builder   which of the two pt_scene_upload runs
+ *   pt_denoise           IntelOpenImageDenoiser::Denoise
+ *                        (LibPetrichor/Core/Denoiser/IntelOpenImageDenoiser.cpp:15-101)
  */
 #ifndef PETRICHOR_GB300_H_
 #define PETRICHOR_GB300_H_
@@ -303,6 +305,20 @@ int pt_bvh_build_device(pt_context* ctx, const float* positions, uint32_t num_ve
 
 /* Builder pt_scene_upload uses: both give the same tree; the device builder is the
  * default. */
+/* Denoiser in place of IntelOpenImageDenoiser::Denoise(color[, albedo, normal], isHDR):
+ * Intel Open Image Denoise is not part of this library, so the images are not the
+ * reference's. An edge-avoiding à-trous wavelet filter on the GPU (Dammertz et al.
+ * 2010) with a per-pixel noise estimate, guided by the DenoisingAlbedo and
+ * DenoisingNormal AOVs when given. Images are width x height RGB float rows; albedo
+ * and normal may be NULL; hdr != 0 for unbounded radiance. out may equal color.
+ * pt_denoise: host buffers, synchronous. pt_denoise_device: device buffers, enqueued
+ * on `stream` (NULL: the context's stream). */
+int pt_denoise(pt_context* ctx, int32_t width, int32_t height, const float* color,
+               const float* albedo, const float* normal, int32_t hdr, float* out);
+int pt_denoise_device(pt_context* ctx, int32_t width, int32_t height, const float* color,
+                      const float* albedo, const float* normal, int32_t hdr, float* out,
+                      void* stream);
+
 #define PT_BVH_BUILDER_HOST 0
 #define PT_BVH_BUILDER_DEVICE 1
 int pt_set_bvh_builder(pt_context* ctx, int32_t builder);

@@ -401,5 +401,28 @@ private:
     std::string m_lastError;
 };
 
+// Core/Denoiser/IntelOpenImageDenoiser.h:10-38, with the same calls. Intel Open Image
+// Denoise is not part of this library: Denoise runs the GPU filter of pt_denoise
+// (edge-avoiding à-trous, guided by the albedo and normal AOVs when given), so the
+// images differ from the reference's. On an error the message goes to stderr and the
+// returned texture is black, as the reference leaves its output on an OIDN error.
+class IntelOpenImageDenoiser {
+public:
+    struct ImageType {
+        enum Type { Color, Albedo, Normal };
+    };
+    IntelOpenImageDenoiser();
+    ~IntelOpenImageDenoiser();
+    IntelOpenImageDenoiser(const IntelOpenImageDenoiser&) = delete;
+    IntelOpenImageDenoiser& operator=(const IntelOpenImageDenoiser&) = delete;
+    Texture2D Denoise(const Texture2D& color, bool isHDR);
+    Texture2D Denoise(const Texture2D& color, const Texture2D& albedo, const Texture2D& normal,
+                      bool isHDR);
+
+private:
+    Texture2D Run(const Texture2D& color, const Texture2D* albedo, const Texture2D* normal, bool isHDR);
+    pt_context* m_ctx = nullptr;
+};
+
 }  // namespace Core
 }  // namespace Petrichor

@@ -137,6 +137,7 @@ EXPORTED = [
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
     "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
     "pt_render_aov", "pt_render_aov_device", "pt_bvh_build_device", "pt_set_bvh_builder",
+    "pt_denoise", "pt_denoise_device",
 ]
 
 BVH_BUILDER_HOST, BVH_BUILDER_DEVICE = 0, 1
@@ -204,6 +205,8 @@ def load(build: bool = True):
     L.pt_bvh_build_device.argtypes = [vp, vp, u32, vp, u32, ctypes.POINTER(u32), ctypes.POINTER(u32),
                                       vp, vp, vp, ctypes.POINTER(PtBvhBuildStats)]
     L.pt_set_bvh_builder.argtypes = [vp, i32]
+    L.pt_denoise.argtypes = [vp, i32, i32, vp, vp, vp, i32, vp]
+    L.pt_denoise_device.argtypes = [vp, i32, i32, vp, vp, vp, i32, vp, vp]
     _lib = L
     return L
 
@@ -438,6 +441,32 @@ class Context:
         self._check(self.L.pt_autotune(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
                                        probe_spp, ctypes.byref(t)), "pt_autotune")
         return t
+
+    def denoise(self, color: np.ndarray, albedo: Optional[np.ndarray] = None,
+                normal: Optional[np.ndarray] = None, hdr: bool = True) -> np.ndarray:
+        """GPU denoiser (pt_denoise) on (H, W, 3) float32 images; albedo/normal optional."""
+        c = np.ascontiguousarray(color, np.float32)
+        H, W, _ = c.shape
+        guides = []
+        for g in (albedo, normal):
+            if g is None:
+                guides.append(None)
+                continue
+            g = np.ascontiguousarray(g, np.float32)
+            assert g.shape == c.shape
+            guides.append(g)
+        out = np.empty_like(c)
+        self._check(self.L.pt_denoise(self.h, W, H, c.ctypes.data,
+                                      guides[0].ctypes.data if guides[0] is not None else None,
+                                      guides[1].ctypes.data if guides[1] is not None else None,
+                                      1 if hdr else 0, out.ctypes.data), "pt_denoise")
+        return out
+
+    def denoise_device(self, width: int, height: int, color_ptr: int, albedo_ptr: int, normal_ptr: int,
+                       hdr: bool, out_ptr: int, stream_ptr: int = 0):
+        self._check(self.L.pt_denoise_device(self.h, width, height, color_ptr, albedo_ptr or None,
+                                             normal_ptr or None, 1 if hdr else 0, out_ptr,
+                                             stream_ptr or None), "pt_denoise_device")
 
     def set_bvh_builder(self, builder: int):
         self._check(self.L.pt_set_bvh_builder(self.h, builder), "pt_set_bvh_builder")

@@ -20,6 +20,7 @@
 
 #include "bvh_builder.h"
 #include "bvh_gpu.h"
+#include "denoise.h"
 #include "pt_kernels.h"
 #include "pt_layout.h"
 #include "context.h"
@@ -410,6 +411,8 @@ int pt_context_destroy(pt_context* ctx) {
         Free(ctx, ctx->unitTable);
         Free(ctx, ctx->jobList);
         Free(ctx, ctx->accum);
+        Free(ctx, ctx->denoiseScratch);
+        Free(ctx, ctx->denoiseImages);
         FreeWaveGraphCache(ctx->graphs);
         ctx->graphs = nullptr;
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -1049,6 +1052,56 @@ int pt_bvh_build_device(pt_context* ctx, const float* positions, uint32_t numVer
     }
     if (primIds && !r.primIds.empty()) std::memcpy(primIds, r.primIds.data(), r.primIds.size() * sizeof(int32_t));
     return PT_OK;
+}
+
+namespace {
+int DenoiseArgs(pt_context* ctx, int32_t width, int32_t height, const float* color, const float* out) {
+    if (!ctx || !color || !out) return PT_ERR_INVALID_ARG;
+    if (width <= 0 || height <= 0 || (int64_t)width * height > (int64_t)1 << 28)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "image size is invalid");
+    return PT_OK;
+}
+}  // namespace
+
+int pt_denoise_device(pt_context* ctx, int32_t width, int32_t height, const float* color,
+                      const float* albedo, const float* normal, int32_t hdr, float* out,
+                      void* stream) {
+    int rc = DenoiseArgs(ctx, width, height, color, out);
+    if (rc != PT_OK) return rc;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->denoiseScratch, DenoiseScratchBytes(width, height))) != PT_OK) return rc;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    int launches = 0;
+    const cudaError_t e = Denoise(width, height, color, albedo, normal, hdr, out,
+                                  ctx->denoiseScratch.ptr, s, &launches);
+    ctx->stats.kernel_launches += launches;
+    return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "denoise");
+}
+
+int pt_denoise(pt_context* ctx, int32_t width, int32_t height, const float* color,
+               const float* albedo, const float* normal, int32_t hdr, float* out) {
+    int rc = DenoiseArgs(ctx, width, height, color, out);
+    if (rc != PT_OK) return rc;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    const size_t img = (size_t)width * height * 3 * sizeof(float);
+    if ((rc = Alloc(ctx, ctx->denoiseScratch, DenoiseScratchBytes(width, height))) != PT_OK ||
+        (rc = Alloc(ctx, ctx->denoiseImages, 4 * img)) != PT_OK)
+        return rc;
+    float* d = static_cast<float*>(ctx->denoiseImages.ptr);
+    float *dc = d, *da = d + img / 4, *dn = d + img / 2, *dout = d + 3 * img / 4;
+    cudaStream_t s = ctx->stream;
+    cudaMemcpyAsync(dc, color, img, cudaMemcpyHostToDevice, s);
+    if (albedo) cudaMemcpyAsync(da, albedo, img, cudaMemcpyHostToDevice, s);
+    if (normal) cudaMemcpyAsync(dn, normal, img, cudaMemcpyHostToDevice, s);
+    int launches = 0;
+    cudaError_t e = Denoise(width, height, dc, albedo ? da : nullptr, normal ? dn : nullptr, hdr, dout,
+                            ctx->denoiseScratch.ptr, s, &launches);
+    ctx->stats.kernel_launches += launches;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, img, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "denoise");
 }
 
 int pt_set_bvh_builder(pt_context* ctx, int32_t builder) {

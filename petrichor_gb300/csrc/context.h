@@ -64,6 +64,7 @@ struct pt_context {
     double tunedProbeMs = 0.0;
     ptg::WaveGraphCache* graphs = nullptr;
     int bvhBuilder = PT_BVH_BUILDER_DEVICE;
+    ptg::DeviceBuffer denoiseScratch, denoiseImages;  // pt_denoise
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_stats stats{};
     uint32_t tilesDone = 0, tilesTotal = 0;

@@ -185,6 +185,45 @@ void Scene::LoadRenderSetting(const std::filesystem::path& path) {
 }
 
 // ---------------------------------------------------------------- Petrichor::Render
+IntelOpenImageDenoiser::IntelOpenImageDenoiser() = default;
+IntelOpenImageDenoiser::~IntelOpenImageDenoiser() {
+    if (m_ctx) pt_context_destroy(m_ctx);
+}
+
+Texture2D IntelOpenImageDenoiser::Run(const Texture2D& color, const Texture2D* albedo,
+                                      const Texture2D* normal, bool isHDR) {
+    Texture2D out(color.GetWidth(), color.GetHeight());
+    auto error = [&](const std::string& msg) {
+        std::cerr << "[Error] " << msg << "\n";
+        return out;
+    };
+    for (const Texture2D* t : {albedo, normal})
+        if (t && (t->GetWidth() != color.GetWidth() || t->GetHeight() != color.GetHeight()))
+            return error("denoiser guide image size differs from the colour image");
+    if (!m_ctx) {
+        const int rc = pt_context_create(0, 0, &m_ctx);
+        if (rc != PT_OK) {
+            m_ctx = nullptr;
+            return error(std::string("no GPU context: ") + pt_status_string(rc));
+        }
+    }
+    const int rc = pt_denoise(m_ctx, color.GetWidth(), color.GetHeight(), color.GetRawDataPtr(),
+                              albedo ? albedo->GetRawDataPtr() : nullptr,
+                              normal ? normal->GetRawDataPtr() : nullptr, isHDR ? 1 : 0,
+                              out.GetRawDataPtr());
+    if (rc != PT_OK) return error(pt_last_error(m_ctx));
+    return out;
+}
+
+Texture2D IntelOpenImageDenoiser::Denoise(const Texture2D& color, bool isHDR) {
+    return Run(color, nullptr, nullptr, isHDR);
+}
+
+Texture2D IntelOpenImageDenoiser::Denoise(const Texture2D& color, const Texture2D& albedo,
+                                          const Texture2D& normal, bool isHDR) {
+    return Run(color, &albedo, &normal, isHDR);
+}
+
 Petrichor::Petrichor() = default;
 Petrichor::~Petrichor() {
     if (m_ctx) pt_context_destroy(m_ctx);
