@@ -345,6 +345,8 @@ typedef struct pt_tuning {
   int32_t blocks_per_sm; /* stage kernel grid, blocks of 128 threads per SM (0: occupancy) */
   int32_t band_rows;     /* rows per pixel band of the path order (0: 8) */
   int32_t use_graphs;    /* 1: replay each wave's stage sequence from a captured CUDA graph */
+  int32_t sort_rays;     /* 1: reorder each bounce's rays by direction and origin cell */
+  int32_t reserved;
   double probe_ms;       /* pt_autotune: probe render time of the chosen configuration */
 } pt_tuning;
 /* Times candidate grids, pixel bands and graph replay on probe renders of one job

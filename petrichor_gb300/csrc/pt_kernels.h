@@ -76,7 +76,12 @@ struct WaveBuffers {
     float4* shadow;                // 4 float4 per next-event entry
     int* counts;                   // [0],[1] ray queues; [2] shadow queue; [3] error bits; [4],[5] fetch
     int* hostCount;                // pinned host word for queue-size polls
+    unsigned* sortKey;             // per entry of the next queue: coherence key (ray sorting)
+    unsigned* sortBins;            // kSortBins counts, then kSortBins offsets
 };
+// Bins of the ray-coherence key: 64 direction cells x 4096 origin cells.
+constexpr int kSortOriginBits = 12;
+constexpr int kSortBins = 64 << kSortOriginBits;
 // Device bytes of the wave buffers for `capacity` paths, and their carving out of
 // one 256-byte-aligned allocation (hostCount is left for the caller).
 size_t WaveBuffersBytes(int capacity);
@@ -106,6 +111,7 @@ struct WaveTuning {
     int blocksPerSm = 0;  // stage grid: blocks of 128 threads per SM (0: occupancy of the trace kernels)
     int band = 0;         // rows per pixel band of the path order (0: 8)
     int graphs = 1;       // replay each wave's stage sequence from a captured CUDA graph
+    int sortRays = 0;     // reorder each bounce's rays by direction and origin cell before tracing
 };
 // Captured stage sequences, keyed by wave shape and buffers (owned by a context or server).
 struct WaveGraphCache;

@@ -348,6 +348,8 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         wb.counts[cur] = n;
         wb.counts[4] = 0;
     }
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kSortBins; k += gridDim.x * blockDim.x)
+        wb.sortBins[k] = 0;  // ray-sort counts start at zero in every wave
 }
 
 __device__ __forceinline__ int JobOf(const int* __restrict__ pathJob, int soleJob, int path) {
@@ -783,6 +785,118 @@ size_t Up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // The one layout of the wave buffers: offsets from `base` (0 to measure the size).
 // Returns the bytes used; fills *w when given.
+
+// ---- ray reordering (WaveTuning::sortRays): a counting sort of the next queue by a
+// coherence key, so that a warp's rays start in similar places and directions.
+// Key: 64 octahedral direction cells (major), then a 12-bit Morton code of the origin's
+// cell on a 16x16x16 grid over the scene bounds. The order within a bin is arbitrary;
+// results do not depend on queue order (each path's state travels with its ray and
+// pixel sums are formed in sample order).
+__device__ __forceinline__ unsigned Spread3(unsigned v) {  // 4 bits -> every third bit
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+__device__ __forceinline__ unsigned RayKey(const DevScene& S, float4 a, float4 b) {
+    unsigned cell = 0;
+    if (S.numNodes > 0) {
+        const float4 n0 = __ldg(S.nodes), n1 = __ldg(S.nodes + 1);
+        const float lo[3] = {n0.x, n0.y, n0.z}, hi[3] = {n0.w, n1.x, n1.y}, o[3] = {a.x, a.y, a.z};
+        for (int k = 0; k < 3; k++) {
+            const float ext = hi[k] - lo[k];
+            const int c = ext > 0.0f ? (int)((o[k] - lo[k]) * (16.0f / ext)) : 0;
+            cell |= Spread3((unsigned)min(max(c, 0), 15)) << k;
+        }
+    }
+    const float s = fabsf(b.x) + fabsf(b.y) + fabsf(b.z);
+    float px = s > 0.0f ? b.x / s : 0.0f, py = s > 0.0f ? b.y / s : 0.0f;
+    if (b.z < 0.0f) {
+        const float qx = (1.0f - fabsf(py)) * copysignf(1.0f, px);
+        const float qy = (1.0f - fabsf(px)) * copysignf(1.0f, py);
+        px = qx;
+        py = qy;
+    }
+    const int ix = min(max((int)((px + 1.0f) * 4.0f), 0), 7);
+    const int iy = min(max((int)((py + 1.0f) * 4.0f), 0), 7);
+    return ((unsigned)(iy * 8 + ix) << kSortOriginBits) | cell;
+}
+
+__global__ void __launch_bounds__(128) SortKeysKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+                                                      int q) {
+    const int n = wb.counts[q];
+    const int soleJob = wb.desc->soleJob;
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        unsigned key = 0xffffffffu;
+        if (i < n) {
+            const float4 a = wb.ray[q][2 * i], b = wb.ray[q][2 * i + 1];
+            key = RayKey(jobs[JobOf(wb.pathJob, soleJob, __float_as_int(a.w))].S, a, b);
+            wb.sortKey[i] = key;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (i < n && lane == __ffs(peers) - 1) atomicAdd(&wb.sortBins[key], (unsigned)__popc(peers));
+    }
+}
+
+// One block: exclusive scan of the counts into offsets; the counts are cleared for the
+// next bounce.
+__global__ void __launch_bounds__(1024) SortScanKernel(WaveBuffers wb) {
+    __shared__ unsigned warpSums[32];
+    constexpr int kPer = kSortBins / 1024;
+    unsigned* hist = wb.sortBins;
+    unsigned* off = wb.sortBins + kSortBins;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned v[kPer], sum = 0;
+    for (int j = 0; j < kPer; j++) {
+        v[j] = hist[t * kPer + j];
+        hist[t * kPer + j] = 0;
+        sum += v[j];
+    }
+    unsigned inc = sum;
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned x = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += x;
+    }
+    if (lane == 31) warpSums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = warpSums[lane];
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned x = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += x;
+        }
+        warpSums[lane] = w;
+    }
+    __syncthreads();
+    unsigned run = inc - sum + (warp > 0 ? warpSums[warp - 1] : 0u);
+    for (int j = 0; j < kPer; j++) {
+        off[t * kPer + j] = run;
+        run += v[j];
+    }
+}
+
+__global__ void __launch_bounds__(128) SortScatterKernel(WaveBuffers wb, int src, int dst) {
+    const int n = wb.counts[src];
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[dst] = n;
+    unsigned* off = wb.sortBins + kSortBins;
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        const unsigned key = i < n ? wb.sortKey[i] : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if (i < n && lane == leader) base = atomicAdd(&off[key], (unsigned)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (i >= n) continue;
+        const int pos = (int)(base + __popc(peers & ((1u << lane) - 1u)));
+        wb.ray[dst][2 * pos] = wb.ray[src][2 * i];
+        wb.ray[dst][2 * pos + 1] = wb.ray[src][2 * i + 1];
+        wb.qs0[dst][pos] = wb.qs0[src][i];
+        wb.qs1[dst][pos] = wb.qs1[src][i];
+        wb.qrng[dst][pos] = wb.qrng[src][i];
+    }
+}
+
 static size_t LayOutWaveBuffers(uintptr_t base, int capacity, WaveBuffers* w) {
     const size_t C = (size_t)capacity;
     uintptr_t p = base;
@@ -803,6 +917,8 @@ static size_t LayOutWaveBuffers(uintptr_t base, int capacity, WaveBuffers* w) {
     v.desc = (WaveDesc*)take(sizeof(WaveDesc));
     v.shadow = (float4*)take(C * 4 * sizeof(float4));
     v.counts = (int*)take(16 * sizeof(int));
+    v.sortKey = (unsigned*)take(C * sizeof(unsigned));
+    v.sortBins = (unsigned*)take(2 * (size_t)kSortBins * sizeof(unsigned));
     if (w) *w = v;
     return (size_t)(p - base);
 }
@@ -852,12 +968,14 @@ int StageGrid(const WaveTuning& tune) {
 
 // The bounce iterations [it0, it0 + count) of a wave (queue parity from it0).
 static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integrator, int grid,
-                          int it0, int count, cudaStream_t stream, WaveProfile* prof, int* nl) {
+                          int it0, int count, cudaStream_t stream, WaveProfile* prof, int* nl,
+                          bool sort) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     const int block = kTraceBlock;
     const int sgrid = ShadeGrid(grid);
     for (int it = it0; it < it0 + count; it++) {
-        const int cur = it & 1;
+        // sorted bounces trace queue 0 and reorder the rays shade appends to queue 1 back into it
+        const int cur = sort ? 0 : (it & 1);
         if (ev) ev->Begin(1, stream);
         ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
         if (ev) {
@@ -880,6 +998,12 @@ static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integra
         ShadowKernel<<<grid, block, 0, stream>>>(jobs, wb);
         if (ev) ev->End(3, stream);
         *nl += 3;
+        if (sort) {
+            SortKeysKernel<<<grid, block, 0, stream>>>(jobs, wb, 1);
+            SortScanKernel<<<1, 1024, 0, stream>>>(wb);
+            SortScatterKernel<<<grid, block, 0, stream>>>(wb, 1, 0);
+            *nl += 3;
+        }
         if (prof) {
             prof->extendLaunches++;
             prof->shadowLaunches++;
@@ -894,10 +1018,10 @@ struct WaveGraphKey {
     const void* jobs;
     const void* units;
     const void* buffers;
-    int capacity, iters, integrator, grid;
+    int capacity, iters, integrator, grid, sort;
     bool operator==(const WaveGraphKey& o) const {
         return jobs == o.jobs && units == o.units && buffers == o.buffers && capacity == o.capacity &&
-               iters == o.iters && integrator == o.integrator && grid == o.grid;
+               iters == o.iters && integrator == o.integrator && grid == o.grid && sort == o.sort;
     }
 };
 struct WaveGraph {
@@ -968,11 +1092,13 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     cudaError_t e = cudaMemcpyAsync(wb.desc, &d, sizeof(d), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     int nl = 0;
-    const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid};
+    const bool sort = tune.sortRays != 0;
+    const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
+                           sort ? 1 : 0};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort);
             AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             *n += 2;
         };
@@ -982,7 +1108,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             if (ev) ev->Begin(0, stream);
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
             if (ev) ev->End(0, stream);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort);
             if (ev) ev->Begin(4, stream);
             AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             if (ev) ev->End(4, stream);
@@ -1004,11 +1130,11 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
                 WaveGraphKey k = key;
                 k.iters = -kPollEvery;
                 e = ReplayCaptured(graphs, k, stream, &nl, [&](int* n) {
-                    LaunchBounces(jobs, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n);
+                    LaunchBounces(jobs, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n, sort);
                 });
                 if (e != cudaSuccess) break;
             } else {
-                LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl);
+                LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort);
             }
         }
         if (e == cudaSuccess) {

@@ -19,6 +19,8 @@ CONFIGS = [
     dict(blocks_per_sm=4, band_rows=16, use_graphs=1),
     dict(blocks_per_sm=24, band_rows=4, use_graphs=0),
     dict(blocks_per_sm=12, band_rows=1, use_graphs=1, wave_paths=3000),
+    dict(sort_rays=1),
+    dict(sort_rays=1, use_graphs=0, wave_paths=3000),
 ]
 
 
@@ -89,10 +91,10 @@ def test_autotune_picks_a_valid_configuration(tuned_ctx):
     assert t.probe_ms > 0
     assert t.blocks_per_sm in (0, 4, 12, 16, 24)
     assert t.band_rows in (0, 4, 8, 16, 32)
-    assert t.use_graphs in (0, 1)
+    assert t.use_graphs in (0, 1) and t.sort_rays in (0, 1)
     got = ctx.get_tuning()
-    assert (got.blocks_per_sm, got.band_rows, got.use_graphs) == (t.blocks_per_sm, t.band_rows,
-                                                                    t.use_graphs)
+    assert (got.blocks_per_sm, got.band_rows, got.use_graphs, got.sort_rays) == (
+        t.blocks_per_sm, t.band_rows, t.use_graphs, t.sort_rays)
     film = _render(ctx, sid, cam, st)
     assert np.array_equal(film.view(np.uint32), ref.view(np.uint32))
     ctx.set_tuning()
@@ -101,7 +103,7 @@ def test_autotune_picks_a_valid_configuration(tuned_ctx):
 def test_set_tuning_rejects_bad_values(tuned_ctx):
     ctx, _ = tuned_ctx
     for bad in (dict(blocks_per_sm=-1), dict(blocks_per_sm=65), dict(band_rows=-2),
-                dict(wave_paths=-5), dict(use_graphs=2)):
+                dict(wave_paths=-5), dict(use_graphs=2), dict(sort_rays=3)):
         with pytest.raises(capi.PtError):
             ctx.set_tuning(**bad)
     ctx.set_tuning()
