@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--width", type=int, default=0, help="override (profiling runs only)")
     ap.add_argument("--height", type=int, default=0, help="override (profiling runs only)")
     ap.add_argument("--spp", type=int, default=0, help="override (profiling runs only)")
+    ap.add_argument("--ref-seconds", type=float, default=20.0,
+                    help="CPU seconds of the reference arm's sample per step (--impl reference)")
     ap.add_argument("--stress", action="store_true",
                     help="memory-bound stress scene: 20M triangles, 3840x2160, 256 spp, 8192x4096 env")
     ap.add_argument("--batch", action="store_true",
@@ -134,13 +136,6 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def dist_setup():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
-
-
 def cpu_baseline(scene, seconds: float, threads: int = 0):
     """The CPU oracle (a restatement of the reference renderer) on the host cores, on a
     bounded sample of the same workload: tiles spread evenly over the image at full spp."""
@@ -169,8 +164,9 @@ def cpu_baseline(scene, seconds: float, threads: int = 0):
 
 
 def run_reference_arm(args):
-    rank, world, local = dist_setup()
-    if rank != 0:
+    from petrichor_gb300 import replicas
+    rank, world, local = replicas.rank_world_local()
+    if rank != 0:  # the reference arm runs once, on rank 0's host cores
         return
     scene = make_scene(args)
     import numpy as np
@@ -182,7 +178,7 @@ def run_reference_arm(args):
     order = np.random.default_rng(0).permutation(n_tiles)
     _, secs, _ = o.render_tiles(order[:ncores])
     per_tile = secs
-    n = int(min(n_tiles, max(ncores, 20.0 / max(per_tile, 1e-6) * ncores)))
+    n = int(min(n_tiles, max(ncores, args.ref_seconds / max(per_tile, 1e-6) * ncores)))
     tiles = order[:n]
     for _ in range(args.warmup):
         o.render_tiles(tiles[:ncores])
@@ -387,7 +383,8 @@ def main():
     import torch
     from petrichor_gb300 import capi
 
-    rank, world, local = dist_setup()
+    from petrichor_gb300 import replicas
+    rank, world, local = replicas.rank_world_local()
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -409,7 +406,7 @@ def main():
     upload_s = time.perf_counter() - t0
     info = ctx.scene_info(sid)
     cam = capi.camera_from_scene(scene)
-    sets = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=1 + rank)
+    sets = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=replicas.replica_seed(1, rank))
     npx = st.width * st.height
     samples_per_step = npx * st.spp
     film = torch.empty(npx * 3, dtype=torch.float32, device="cuda")
@@ -438,11 +435,8 @@ def main():
     barrier()
     secs = e0.elapsed_time(e1) / 1e3
     launches = ctx.stats().kernel_launches - launches0
-    if dist is not None:
-        t = torch.tensor([secs], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
-    value = world * samples_per_step * args.steps / secs / 1e6
+    secs = replicas.max_over_ranks(secs, dist, "cuda")
+    value = replicas.job_throughput(world, samples_per_step * args.steps, secs) / 1e6
 
     # ---- end to end through the C ABI with a host film (pinned): per step the
     # camera + settings go in (kernel arguments) and the film comes back.
@@ -455,11 +449,8 @@ def main():
         ctx.render(sid, cam, sets, out=host_np)
         _ = float(host_np[0, 0, 0])
     e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * samples_per_step * args.steps / e2e_s / 1e6
+    e2e_s = replicas.max_over_ranks(e2e_s, dist, "cuda")
+    e2e = replicas.job_throughput(world, samples_per_step * args.steps, e2e_s) / 1e6
     img_mean = float(host_np.mean())
 
     # ---- roofline of the dominant kernel (CUDA events around every stage launch)
