@@ -268,6 +268,11 @@ int pt_serve_poll(pt_context* ctx, uint64_t request_id, pt_request_status* out);
 /* Waits until the request is done, cancelled or failed (PT_ERR_TIMEOUT after timeout_s). */
 int pt_serve_wait(pt_context* ctx, uint64_t request_id, double timeout_s, pt_request_status* out);
 int pt_serve_cancel(pt_context* ctx, uint64_t request_id);
+/* A deadline `seconds` after the request's submission (0 clears it): a request not
+ * done by then takes no further samples and, once its waves in flight retire, ends
+ * PT_REQ_FAILED with status PT_ERR_TIMEOUT. Checked between waves (at least every
+ * 20 ms while the server idles). PT_ERR_BUSY if the request already finished. */
+int pt_serve_set_deadline(pt_context* ctx, uint64_t request_id, double seconds);
 /* Forgets a finished request (its status can no longer be polled). */
 int pt_serve_release(pt_context* ctx, uint64_t request_id);
 /* Stops the server after the wave in flight; queued and running requests are cancelled. */

@@ -45,29 +45,40 @@ def _sources():
           os.path.join(ROOT, "include", "petrichor_gb300", "Petrichor.hpp")]
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
+def _stale(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return any(os.path.getmtime(s) > t for s in _sources())
 
 
-def build(force: bool = False, verbose: bool = False, defines=()) -> str:
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OBJ_DIR, exist_ok=True)
+# The checked build (device-side bounds checks on every node, primitive and queue
+# index, recorded as an error bit): a separate library, for the test suite.
+CHECK_DIR = os.path.join(PKG, "_lib_check")
+
+
+def build_checked(force: bool = False, verbose: bool = False) -> str:
+    return build(force, verbose, defines=("PT_CHECK=1",), out_dir=CHECK_DIR)
+
+
+def build(force: bool = False, verbose: bool = False, defines=(), out_dir: str = OUT_DIR) -> str:
+    lib_path = os.path.join(out_dir, "libpetrichor_gb300.so")
+    obj_dir = os.path.join(out_dir, "obj")
+    if not force and not _stale(lib_path):
+        return lib_path
+    os.makedirs(obj_dir, exist_ok=True)
     nvcc = _nvcc()
     inc = ["-I", CSRC, "-I", os.path.join(ROOT, "include")]
     jobs = []
     for s in CU_SOURCES:
-        o = os.path.join(OBJ_DIR, s + ".o")
+        o = os.path.join(obj_dir, s + ".o")
         jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
                      *FAST_DIV_SQRT.get(s, []),
                      *[f"-D{d}" for d in defines],
                      "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", *inc, "-c",
                      os.path.join(CSRC, s), "-o", o])
     for s in CPP_SOURCES:
-        o = os.path.join(OBJ_DIR, s + ".o")
+        o = os.path.join(obj_dir, s + ".o")
         jobs.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
                      "-pthread", "-Wall", *[f"-D{d}" for d in defines], *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c",
                      os.path.join(CSRC, s), "-o", o])
@@ -82,11 +93,11 @@ def build(force: bool = False, verbose: bool = False, defines=()) -> str:
 
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
-    objs = [os.path.join(OBJ_DIR, s + ".o") for s in CU_SOURCES + CPP_SOURCES]
-    tmp = LIB + ".tmp"
+    objs = [os.path.join(obj_dir, s + ".o") for s in CU_SOURCES + CPP_SOURCES]
+    tmp = lib_path + ".tmp"
     run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

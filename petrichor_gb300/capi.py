@@ -138,7 +138,7 @@ EXPORTED = [
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
     "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
     "pt_render_aov", "pt_render_aov_device", "pt_bvh_build_device", "pt_set_bvh_builder",
-    "pt_denoise", "pt_denoise_device",
+    "pt_denoise", "pt_denoise_device", "pt_serve_set_deadline",
 ]
 
 BVH_BUILDER_HOST, BVH_BUILDER_DEVICE = 0, 1
@@ -153,11 +153,15 @@ class PtError(RuntimeError):
 
 
 def load(build: bool = True):
-    """Load (building first if needed) the in-tree CUDA library."""
+    """Load (building first if needed) the in-tree CUDA library. PT_GB300_CHECKED=1
+    loads the checked build instead (device-side bounds checks; for the tests)."""
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.build() if build else _build.LIB
+    if os.environ.get("PT_GB300_CHECKED") == "1":
+        path = _build.build_checked() if build else os.path.join(_build.CHECK_DIR, "libpetrichor_gb300.so")
+    else:
+        path = _build.build() if build else _build.LIB
     if not os.path.exists(path):
         raise RuntimeError(f"CUDA library not built: {path}")
     L = ctypes.CDLL(path)
@@ -207,6 +211,7 @@ def load(build: bool = True):
                                       vp, vp, vp, ctypes.POINTER(PtBvhBuildStats)]
     L.pt_set_bvh_builder.argtypes = [vp, i32]
     L.pt_denoise.argtypes = [vp, i32, i32, vp, vp, vp, i32, vp]
+    L.pt_serve_set_deadline.argtypes = [vp, ctypes.c_uint64, ctypes.c_double]
     L.pt_denoise_device.argtypes = [vp, i32, i32, vp, vp, vp, i32, vp, vp]
     _lib = L
     return L
@@ -419,6 +424,9 @@ class Context:
         if rc not in (PT_OK, -4):
             self._check(rc, "pt_serve_wait")
         return st
+
+    def serve_set_deadline(self, rid: int, seconds: float):
+        self._check(self.L.pt_serve_set_deadline(self.h, rid, seconds), "pt_serve_set_deadline")
 
     def serve_cancel(self, rid: int):
         self._check(self.L.pt_serve_cancel(self.h, rid), "pt_serve_cancel")

@@ -710,7 +710,14 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
 
 // ---------------------------------------------------------------- reference traversal
 // Per-ray error bits reported through the status word.
-enum : int { kErrStackOverflow = 1, kErrBounceCap = 2 };
+enum : int { kErrStackOverflow = 1, kErrBounceCap = 2, kErrBounds = 4 };
+
+// Checked build (-DPT_CHECK=1): every node, primitive, material and queue index is
+// tested against its array before the access; a bad one sets kErrBounds in the
+// status word and the access is skipped. The shipped build has no checks (0).
+#ifndef PT_CHECK
+#define PT_CHECK 0
+#endif
 
 // BinnedSAHBVH::Intersect (Core/Accel/BinnedSAHBVH.cpp:272-374) with the slab test
 // of BinnedSAHBVH.h:95-170: pop order, culling rule and child push order as the
@@ -730,6 +737,10 @@ __device__ int TraverseReference(const DevScene& S, V3 o, V3 d, float distMin, f
     bestD = kInfinity;
     while (sp > 0) {
         const int ni = stack[--sp];
+        if (PT_CHECK && (unsigned)ni >= (unsigned)S.numNodes) {
+            *status |= kErrBounds;
+            return best;
+        }
         if (kCount) (*nodeTests)++;
         const float4 na = __ldg(S.nodes + 2 * ni), nb = __ldg(S.nodes + 2 * ni + 1);
         const V3 lo(na.x, na.y, na.z), hi(na.w, nb.x, nb.y);
@@ -758,6 +769,11 @@ __device__ int TraverseReference(const DevScene& S, V3 o, V3 d, float distMin, f
             if (!inside && bestD < nd) continue;
         }
         const int a = __float_as_int(nb.z), cnt = __float_as_int(nb.w);
+        if (PT_CHECK && (cnt >= 0 ? (a < 0 || a + cnt > S.numTris)
+                                  : (a < 0 || a + 1 >= S.numNodes))) {
+            *status |= kErrBounds;
+            return best;
+        }
         if (cnt >= 0) {
             for (int k = a; k < a + cnt; k++) {
                 V3 v0, e1, e2;

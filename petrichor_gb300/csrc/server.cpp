@@ -82,6 +82,8 @@ struct Request {
     size_t accumOff = 0, accumBytes = 0, filmOff = 0, filmBytes = 0;
     int inFlight = 0;  // waves holding this request's samples
     bool cancel = false;
+    double deadline = 0;    // seconds since the server started; 0: none
+    bool timedOut = false;  // cancelled by its deadline (fails with PT_ERR_TIMEOUT)
 };
 }  // namespace
 
@@ -186,6 +188,18 @@ public:
         return PT_OK;
     }
 
+    // seconds after submission; 0 clears
+    int SetDeadline(uint64_t id, double seconds) {
+        std::lock_guard<std::mutex> g(mu_);
+        auto it = reqs_.find(id);
+        if (it == reqs_.end()) return PT_ERR_NOT_FOUND;
+        Request& r = *it->second;
+        if (r.state != PT_REQ_QUEUED && r.state != PT_REQ_RUNNING) return PT_ERR_BUSY;
+        r.deadline = seconds > 0.0 ? r.submit + seconds : 0.0;
+        cv_.notify_all();
+        return PT_OK;
+    }
+
     int Release(uint64_t id) {
         std::lock_guard<std::mutex> g(mu_);
         auto it = reqs_.find(id);
@@ -236,6 +250,11 @@ private:
     }
 
     // mu_ held. Releases the request's slot and arena space.
+    void FinishCancelled(Request& r) {
+        if (r.timedOut) Finish(r, PT_REQ_FAILED, PT_ERR_TIMEOUT);
+        else Finish(r, PT_REQ_CANCELLED, PT_OK);
+    }
+
     void Finish(Request& r, int state, int status) {
         r.state = state;
         r.status = status;
@@ -289,14 +308,24 @@ private:
     // with the next wave).
     std::vector<Request*> Admit() {
         std::vector<Request*> admitted;
+        // requests past their deadline stop taking samples and fail once their waves retire
+        const double now = Now();
+        for (uint64_t id : active_) {
+            Request& r = *reqs_[id];
+            if (r.deadline > 0.0 && now > r.deadline && !r.cancel) r.cancel = r.timedOut = true;
+        }
+        for (uint64_t id : queue_) {
+            Request& r = *reqs_[id];
+            if (r.deadline > 0.0 && now > r.deadline && !r.cancel) r.cancel = r.timedOut = true;
+        }
         for (uint64_t id : std::vector<uint64_t>(active_)) {
             Request& r = *reqs_[id];
-            if (r.cancel && r.inFlight == 0) Finish(r, PT_REQ_CANCELLED, PT_OK);
+            if (r.cancel && r.inFlight == 0) FinishCancelled(r);
         }
         for (auto it = queue_.begin(); it != queue_.end();) {
             Request& r = *reqs_[*it];
             if (r.cancel) {
-                Finish(r, PT_REQ_CANCELLED, PT_OK);
+                FinishCancelled(r);
                 it = queue_.erase(it);
             } else {
                 ++it;
@@ -531,6 +560,12 @@ int pt_serve_wait(pt_context* ctx, uint64_t id, double timeout, pt_request_statu
     if (!ctx || !out) return PT_ERR_INVALID_ARG;
     if (!ctx->server) return PT_ERR_NOT_FOUND;
     return ctx->server->Wait(id, timeout, out);
+}
+
+int pt_serve_set_deadline(pt_context* ctx, uint64_t id, double seconds) {
+    if (!ctx || !(seconds >= 0.0)) return PT_ERR_INVALID_ARG;
+    if (!ctx->server) return PT_ERR_NOT_FOUND;
+    return ctx->server->SetDeadline(id, seconds);
 }
 
 int pt_serve_cancel(pt_context* ctx, uint64_t id) {

@@ -89,6 +89,9 @@ struct LaneRay {
     bool anyHit;
     const float4* nodes;  // the lane's 4-wide tree (rays of different jobs share a warp)
     const float4* tris;
+#if PT_CHECK
+    int numWide, numTris;  // bounds of nodes and tris, tested before every access
+#endif
 };
 
 __device__ __forceinline__ void SortPair(float& ta, int& ca, float& tb, int& cb) {
@@ -154,9 +157,16 @@ struct TravStack {
 
 // Tests the triangles of leaf `cur`; returns true when an any-hit ray is done.
 // Otherwise `cur` becomes the next item from the stack (or kDone).
-__device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur) {
+__device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur, int& err) {
     const int v = -cur - 1;
     const int first = v >> 6, cnt = v & 63;
+#if PT_CHECK
+    if (first < 0 || first + cnt > r.numTris) {
+        err |= kErrBounds;
+        cur = kDone;
+        return true;
+    }
+#endif
     for (int k = first; k < first + cnt; k++) {
         V3 v0, e1, e2;
         LoadTri(r.tris, k, v0, e1, e2);
@@ -175,6 +185,13 @@ __device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur) 
 // the other hit children are pushed farthest first (or the next stack item).
 __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur, int& err) {
     constexpr int K = kWide, Q = kWide / 4;
+#if PT_CHECK
+    if ((unsigned)cur >= (unsigned)r.numWide) {
+        err |= kErrBounds;
+        cur = kDone;
+        return;
+    }
+#endif
     const float4* n = r.nodes + (kWideFloats / 4) * (size_t)cur;
     float b[6][K];
 #pragma unroll
@@ -229,7 +246,7 @@ __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur,
 #pragma unroll
     for (int i = 1; i < K; i++) pushes += t[i] != inf;
     if (stk.sp + pushes > kWaveStackDepth) {
-        err = 1;
+        err |= kErrStackOverflow;
         cur = kDone;
         return;
     }
@@ -295,10 +312,10 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
 #if PT_WHILE_WHILE
             while (cur >= 0) VisitInner(r, stk, cur, err);
             __syncwarp(busy);  // the lanes' leaves are intersected together
-            if (cur != kDone) done = VisitLeaf(r, stk, cur);
+            if (cur != kDone) done = VisitLeaf(r, stk, cur, err);
 #else
             if (cur >= 0) VisitInner(r, stk, cur, err);
-            else if (cur != kDone) done = VisitLeaf(r, stk, cur);
+            else if (cur != kDone) done = VisitLeaf(r, stk, cur, err);
 #endif
             if (done || cur == kDone) {
                 q.Finish(idx, r);
@@ -374,6 +391,10 @@ struct ExtendQueue {
         r.anyHit = false;
         r.nodes = J.S.numWide > 0 ? J.S.wide : nullptr;
         r.tris = J.S.tris;
+#if PT_CHECK
+        r.numWide = J.S.numWide;
+        r.numTris = J.S.numTris;
+#endif
     }
     __device__ void Finish(int i, const LaneRay& r) const {
         hit[i] = make_float2(r.tBest, __int_as_float(r.best));
@@ -393,7 +414,7 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const D
     int err = 0;
     ExtendQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.ray[cur], wb.hit};
     TraceQueue(q, n, wb.counts + 4, err);
-    if (err) atomicOr(wb.counts + 3, 1);
+    if (err) atomicOr(wb.counts + 3, err);
 }
 
 // kInteg: the integrator of every job in the wave, or -1 when the wave mixes them
@@ -424,6 +445,12 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
         in.bounce = __float_as_int(s2.z);
         int flags = __float_as_int(s2.w);
         const int slot = __float_as_int(h.y);
+#if PT_CHECK
+        if (slot >= S.numTris || (unsigned)path >= (unsigned)wb.capacity) {
+            atomicOr(wb.counts + 3, kErrBounds);
+            continue;  // appends below are aggregated over the lanes that reach them
+        }
+#endif
         bool cont = false;
         Ray out;
         float lastPdf = s2.x, lastSin = s2.y;
@@ -535,7 +562,13 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
                     }
                     // the next-event entry is queued before the BSDF sample, so its
                     // registers are free for it
-                    const int sslot = WarpAppend(wb.counts + 2, shadow);
+                    int sslot = WarpAppend(wb.counts + 2, shadow);
+#if PT_CHECK
+                    if (shadow && sslot >= wb.capacity) {
+                        atomicOr(wb.counts + 3, kErrBounds);
+                        shadow = false;
+                    }
+#endif
                     if (shadow) {
                         float4* e = wb.shadow + 4 * (size_t)sslot;
                         e[0] = sh0;
@@ -558,7 +591,13 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
             }
         }
         // ---- write back and append
-        const int rslot = WarpAppend(wb.counts + nxt, cont);
+        int rslot = WarpAppend(wb.counts + nxt, cont);
+#if PT_CHECK
+        if (cont && rslot >= wb.capacity) {
+            atomicOr(wb.counts + 3, kErrBounds);
+            cont = false;
+        }
+#endif
         if (cont) {
             wb.ray[nxt][2 * rslot] = make_float4(out.o.x, out.o.y, out.o.z, __int_as_float(path));
             wb.ray[nxt][2 * rslot + 1] = make_float4(out.d.x, out.d.y, out.d.z, out.ior);
@@ -584,6 +623,10 @@ struct ShadowQueue {
         const DevScene& S = jobs[JobOf(pathJob, soleJob, __float_as_int(e1.w) & 0x7FFFFFFF)].S;
         r.nodes = S.numWide > 0 ? S.wide : nullptr;
         r.tris = S.tris;
+#if PT_CHECK
+        r.numWide = S.numWide;
+        r.numTris = S.numTris;
+#endif
         r.o = V3(e0.x, e0.y, e0.z);
         r.d = V3(e1.x, e1.y, e1.z);
         r.tmin = 0.0f;
@@ -640,7 +683,7 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ShadowKernel(const D
     int err = 0;
     ShadowQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.shadow, wb.pathL};
     TraceQueue(q, n, wb.counts + 5, err);
-    if (err) atomicOr(wb.counts + 3, 1);
+    if (err) atomicOr(wb.counts + 3, err);
 }
 
 __global__ void AccumulateKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
@@ -689,6 +732,7 @@ __global__ void FinalizeKernel(const DevJob* __restrict__ jobs, const int* __res
 struct RayBatchQueue {
     const float4* nodes;
     const float4* tris;
+    int numWide, numTris;
     const float* rays;
     float tmin, tmax;
     int* triOut;
@@ -702,6 +746,10 @@ struct RayBatchQueue {
         r.anyHit = false;
         r.nodes = nodes;
         r.tris = tris;
+#if PT_CHECK
+        r.numWide = numWide;
+        r.numTris = numTris;
+#endif
     }
     __device__ void Finish(int i, const LaneRay& r) const {
         triOut[i] = r.best >= 0 ? TriId(tris, r.best) : -1;
@@ -712,7 +760,8 @@ struct RayBatchQueue {
 __global__ void __launch_bounds__(128) TraceKernel(DevScene S, int n, const float* __restrict__ rays,
                                                    float tmin, float tmax, int* __restrict__ triOut,
                                                    float* __restrict__ distOut, int* fetch) {
-    RayBatchQueue q{S.numWide > 0 ? S.wide : nullptr, S.tris, rays, tmin, tmax, triOut, distOut};
+    RayBatchQueue q{S.numWide > 0 ? S.wide : nullptr, S.tris, S.numWide, S.numTris, rays, tmin, tmax,
+                    triOut, distOut};
     int err = 0;
     TraceQueue(q, n, fetch, err);
 }

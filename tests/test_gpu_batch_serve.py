@@ -149,3 +149,33 @@ def test_serve_cancel_budget_and_busy_scene(served):
             ctx.serve_poll(r1)
     finally:
         ctx.serve_stop()
+
+
+def test_serve_deadline_fails_late_request_and_spares_others(served):
+    """A request past its deadline stops taking samples and fails with PT_ERR_TIMEOUT;
+    a request rendering beside it is unaffected (film equal to its solo film)."""
+    ctx, jobs, solo = served
+    ctx.serve_start(wave_paths=1 << 14)
+    try:
+        sid, cam, _ = jobs[1]
+        long = capi.settings_from_scene(_scenes()[1], capi.MODE_WAVEFRONT, spp=1 << 16)
+        hl = np.empty((long.height, long.width, 3), np.float32)
+        r_late = ctx.serve_submit(sid, cam, long, film_host=hl)
+        ctx.serve_set_deadline(r_late, 0.05)
+        sid0, cam0, st0 = jobs[0]
+        h0 = np.empty((st0.height, st0.width, 3), np.float32)
+        r_ok = ctx.serve_submit(sid0, cam0, st0, film_host=h0)
+        s_ok = ctx.serve_wait(r_ok, 120)
+        s_late = ctx.serve_wait(r_late, 120)
+        assert s_ok.state == capi.REQ_DONE and s_ok.status == 0
+        assert np.array_equal(h0.reshape(-1).view(np.uint32), solo[0].view(np.uint32))
+        assert s_late.state == capi.REQ_FAILED and s_late.status == -4
+        assert s_late.samples_done < s_late.samples_total
+        assert s_late.done_s - s_late.submit_s < 30.0
+        # a finished request takes no deadline; unknown ids are reported
+        with pytest.raises(capi.PtError):
+            ctx.serve_set_deadline(r_ok, 1.0)
+        with pytest.raises(capi.PtError):
+            ctx.serve_set_deadline(123456789, 1.0)
+    finally:
+        ctx.serve_stop()
