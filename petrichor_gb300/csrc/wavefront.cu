@@ -363,7 +363,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wb.counts[cur] = n;
-        wb.counts[4] = 0;
+        wb.counts[2] = wb.counts[4] = wb.counts[5] = wb.counts[6] = 0;
     }
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kSortBins; k += gridDim.x * blockDim.x)
         wb.sortBins[k] = 0;  // ray-sort counts start at zero in every wave
@@ -402,15 +402,11 @@ struct ExtendQueue {
 };
 
 // counts: [0],[1] ray queues, [2] shadow queue, [3] error bits,
-//         [4] extend fetch counter, [5] shadow fetch counter
+//         [4] extend fetch counter, [5] shadow fetch counter, [6] shadow blocks finished
 __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                     int cur) {
     const int n = wb.counts[cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        wb.counts[cur ^ 1] = 0;
-        wb.counts[2] = 0;
-        wb.counts[5] = 0;  // the shadow kernel that follows fetches from zero
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur ^ 1] = 0;
     int err = 0;
     ExtendQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.ray[cur], wb.hit};
     TraceQueue(q, n, wb.counts + 4, err);
@@ -425,6 +421,7 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
     const int n = wb.counts[cur];
     const int nxt = cur ^ 1;
     const int sole = wb.desc->soleJob;
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // the next extend fetches from zero
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
         const float2 h = wb.hit[i];
@@ -677,13 +674,24 @@ struct ShadowQueue {
     }
 };
 
+// It may run beside the next bounce's extend kernel (which touches neither the
+// shadow queue nor its counters); its last block to finish clears the shadow queue
+// size and fetch counter for the next shade.
 __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ShadowKernel(const DevJob* __restrict__ jobs, WaveBuffers wb) {
     const int n = wb.counts[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // next extend fetches from zero
     int err = 0;
     ShadowQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.shadow, wb.pathL};
     TraceQueue(q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, err);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(wb.counts + 6, 1) == (int)gridDim.x - 1) {
+            wb.counts[2] = 0;
+            wb.counts[5] = 0;
+            wb.counts[6] = 0;
+        }
+    }
 }
 
 __global__ void AccumulateKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
@@ -1016,12 +1024,37 @@ int StageGrid(const WaveTuning& tune) {
 }
 
 // The bounce iterations [it0, it0 + count) of a wave (queue parity from it0).
+// A second stream and fork/join events: each bounce's shadow stage runs beside the
+// next bounce's extend stage (they share no buffers), and the next shade waits for it.
+struct StageOverlap {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    bool Ready() {
+        if (side) return true;
+        if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join, cudaEventDisableTiming) != cudaSuccess) {
+            Release();
+            return false;
+        }
+        return true;
+    }
+    void Release() {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
+        side = nullptr;
+        fork = join = nullptr;
+    }
+};
+
 static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integrator, int grid,
                           int it0, int count, cudaStream_t stream, WaveProfile* prof, int* nl,
-                          bool sort) {
+                          bool sort, StageOverlap* ov) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     const int block = kTraceBlock;
     const int sgrid = ShadeGrid(grid);
+    bool pendingShadow = false;  // a shadow stage on the side stream the next shade must wait for
     for (int it = it0; it < it0 + count; it++) {
         // sorted bounces trace queue 0 and reorder the rays shade appends to queue 1 back into it
         const int cur = sort ? 0 : (it & 1);
@@ -1032,6 +1065,10 @@ static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integra
             if (prof->countReference)
                 RefCountKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, prof->devCounters);
             ev->Begin(2, stream);
+        }
+        if (pendingShadow) {
+            cudaStreamWaitEvent(stream, ov->join, 0);
+            pendingShadow = false;
         }
         if (integrator == kPathTracing)
             ShadeKernel<kPathTracing><<<sgrid, block, 0, stream>>>(jobs, wb, cur);
@@ -1044,7 +1081,15 @@ static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integra
             TallyKernel<<<1, 1, 0, stream>>>(wb.counts, cur, prof->devCounters);
             ev->Begin(3, stream);
         }
-        ShadowKernel<<<grid, block, 0, stream>>>(jobs, wb);
+        if (ov) {
+            cudaEventRecord(ov->fork, stream);
+            cudaStreamWaitEvent(ov->side, ov->fork, 0);
+            ShadowKernel<<<grid, block, 0, ov->side>>>(jobs, wb);
+            cudaEventRecord(ov->join, ov->side);
+            pendingShadow = true;
+        } else {
+            ShadowKernel<<<grid, block, 0, stream>>>(jobs, wb);
+        }
         if (ev) ev->End(3, stream);
         *nl += 3;
         if (sort) {
@@ -1058,6 +1103,7 @@ static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integra
             prof->shadowLaunches++;
         }
     }
+    if (pendingShadow) cudaStreamWaitEvent(stream, ov->join, 0);
 }
 
 // A captured sequence: for fixed-depth waves the whole wave (raygen, iters
@@ -1081,8 +1127,10 @@ struct WaveGraph {
 struct WaveGraphCache {
     std::vector<WaveGraph> graphs;  // few shapes per owner; least recently added dropped first
     static constexpr size_t kMax = 16;
+    StageOverlap overlap;           // the owner's side stream
     ~WaveGraphCache() {
         for (WaveGraph& g : graphs) cudaGraphExecDestroy(g.exec);
+        overlap.Release();
     }
 };
 WaveGraphCache* NewWaveGraphCache() { return new WaveGraphCache(); }
@@ -1142,12 +1190,15 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     if (e != cudaSuccess) return e;
     int nl = 0;
     const bool sort = tune.sortRays != 0;
+    // shadow stages beside the next extend, on the owner's side stream (not when profiling,
+    // whose stage timers need one stream)
+    StageOverlap* ov = (graphs && !prof && graphs->overlap.Ready()) ? &graphs->overlap : nullptr;
     const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
                            sort ? 1 : 0};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort, ov);
             AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             *n += 2;
         };
@@ -1157,7 +1208,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             if (ev) ev->Begin(0, stream);
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
             if (ev) ev->End(0, stream);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort, ov);
             if (ev) ev->Begin(4, stream);
             AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             if (ev) ev->End(4, stream);
@@ -1179,11 +1230,12 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
                 WaveGraphKey k = key;
                 k.iters = -kPollEvery;
                 e = ReplayCaptured(graphs, k, stream, &nl, [&](int* n) {
-                    LaunchBounces(jobs, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n, sort);
+                    LaunchBounces(jobs, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n, sort,
+                                  ov);
                 });
                 if (e != cudaSuccess) break;
             } else {
-                LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort);
+                LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort, ov);
             }
         }
         if (e == cudaSuccess) {

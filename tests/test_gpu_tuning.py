@@ -107,3 +107,18 @@ def test_set_tuning_rejects_bad_values(tuned_ctx):
         with pytest.raises(capi.PtError):
             ctx.set_tuning(**bad)
     ctx.set_tuning()
+
+
+@pytest.mark.parametrize("name", ["pt", "simple", "tris"])
+def test_overlapped_shadow_stage_equals_sequential(tuned_ctx, name):
+    """Renders run each bounce's shadow stage beside the next extend on a second stream;
+    the profiled render runs every stage in order on one stream. Same film bits."""
+    ctx, jobs = tuned_ctx
+    sid, cam, st = jobs[name]
+    ctx.set_tuning()
+    overlapped = _render(ctx, sid, cam, st)
+    film = torch.full((st.width * st.height * 3,), float("nan"), device="cuda")
+    ctx.render_profile(sid, cam, st, film.data_ptr(), count_reference=False)
+    torch.cuda.synchronize()
+    sequential = film.cpu().numpy()
+    assert np.array_equal(overlapped.view(np.uint32), sequential.view(np.uint32))
