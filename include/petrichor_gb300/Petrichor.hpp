@@ -236,6 +236,11 @@ public:
     void Save(const std::filesystem::path& path) const;
     void Clear(const Color3f& color = Color3f::Zero());
     Color3f GetPixel(int i, int j) const;
+    // Texture2D.h:27-71: point or bilinear lookup at texel coordinates (x = u * width, no
+    // half-texel shift, edges clamped), and at wrapped uv
+    enum class InterplationTypes { Point, Bilinear };
+    Color3f GetPixel(float x, float y, InterplationTypes type = InterplationTypes::Bilinear) const;
+    Color3f GetPixelByUV(float u, float v, InterplationTypes type = InterplationTypes::Bilinear) const;
     void SetPixel(int i, int j, const Color3f& color);
     int GetWidth() const { return m_width; }
     int GetHeight() const { return m_height; }

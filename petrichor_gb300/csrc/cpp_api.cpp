@@ -114,6 +114,26 @@ void Texture2D::Clear(const Color3f& c) {
     }
 }
 
+Color3f Texture2D::GetPixel(float x, float y, InterplationTypes type) const {  // Texture2D.cpp:273-326
+    if (type == InterplationTypes::Point) return GetPixel(static_cast<int>(x), static_cast<int>(y));
+    int ix0 = static_cast<int>(x), ix1 = static_cast<int>(x + 1.0f);
+    int iy0 = static_cast<int>(y), iy1 = static_cast<int>(y + 1.0f);
+    const float wx0 = x - ix0, wy0 = y - iy0, wx1 = ix1 - x, wy1 = iy1 - y;
+    ix0 = std::clamp(ix0, 0, GetWidth() - 1);
+    ix1 = std::clamp(ix1, 0, GetWidth() - 1);
+    iy0 = std::clamp(iy0, 0, GetHeight() - 1);
+    iy1 = std::clamp(iy1, 0, GetHeight() - 1);
+    const Color3f top = wx1 * GetPixel(ix0, iy0) + wx0 * GetPixel(ix1, iy0);
+    const Color3f bottom = wx1 * GetPixel(ix0, iy1) + wx0 * GetPixel(ix1, iy1);
+    return wy1 * top + wy0 * bottom;
+}
+
+Color3f Texture2D::GetPixelByUV(float u, float v, InterplationTypes type) const {  // Texture2D.cpp:328-335
+    u = u - 1.0f * std::floor(u / 1.0f);  // Math::Mod (MathUtils.h:32-36)
+    v = v - 1.0f * std::floor(v / 1.0f);
+    return GetPixel(u * m_width, v * m_height, type);
+}
+
 Color3f Texture2D::GetPixel(int i, int j) const {  // Texture2D.cpp:260-271
     if (!IsValid()) return Color3f(1.0f, 0.0f, 1.0f);
     const float* p = &m_pixels[((size_t)m_width * j + i) * 3];

@@ -7,6 +7,7 @@
 //   load_scene save   <in.hdr> <out.png> <out.hdr>       loads an image and saves it both ways
 //   load_scene tex    <in> <out.bin> color|noncolor        loads an image (Texture2D::Load) and
 //                                                          writes int32 width, height, RGB floats
+//   load_scene sample <in> <out.txt> <u v>...              GetPixelByUV (bilinear, then point)
 //
 // The text dump holds one record per line with floats as C99 hex literals, so the
 // test reads back exact values.
@@ -14,6 +15,7 @@
 #include <petrichor_gb300.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <map>
 #include <string>
@@ -121,6 +123,20 @@ int main(int argc, char** argv) {
         return 2;
     }
     const std::string mode = argv[1];
+    if (mode == "sample") {
+        Texture2D tex;
+        if (!tex.Load(argv[2], Texture2D::TextureColorType::NonColor)) return 4;
+        FILE* f = std::fopen(argv[3], "w");
+        if (!f) return 1;
+        for (int k = 4; k + 1 < argc; k += 2) {
+            const float u = std::strtof(argv[k], nullptr), v = std::strtof(argv[k + 1], nullptr);
+            Put(f, tex.GetPixelByUV(u, v));
+            Put(f, tex.GetPixelByUV(u, v, Texture2D::InterplationTypes::Point));
+            std::fprintf(f, "\n");
+        }
+        std::fclose(f);
+        return 0;
+    }
     if (mode == "tex") {
         Texture2D tex;
         const bool color = std::string(argv[4]) == "color";

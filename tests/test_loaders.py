@@ -464,6 +464,38 @@ def test_load_assets_attaches_texture_maps(exe, tmp_path):
     assert {slot for (m, slot) in _parse_dump(out)["maps"]} == {0, 1}
 
 
+def test_texture_sampling_by_uv(exe, tmp_path):
+    """Texture2D::GetPixelByUV (Texture2D.cpp:273-335): wrapped uv, x = u * width with no
+    half-texel shift, clamped edges; bilinear weights as the reference forms them."""
+    rng = np.random.default_rng(21)
+    W, H = 7, 5
+    img = rng.random((H, W, 3), dtype=np.float32)
+    path = tmp_path / "t.hdr"
+    with open(path, "wb") as f:
+        f.write(b"PTRAWF32" + struct.pack("<II", W, H) + img.tobytes())
+    uvs = [(0.0, 0.0), (0.31, 0.77), (0.999, 0.5), (1.25, -0.4), (-2.6, 3.1), (0.5, 0.9999)]
+    out = tmp_path / "s.txt"
+    args = [str(x) for uv in uvs for x in uv]
+    r = subprocess.run([exe, "sample", str(path), str(out), *args], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 0, r.stderr
+    got = np.array([[float.fromhex(t) for t in line.split()] for line in open(out)], np.float32)
+    f32 = np.float32
+    for (u, v), row in zip(uvs, got):
+        u, v = f32(u), f32(v)
+        u = u - f32(1) * np.floor(u / f32(1))
+        v = v - f32(1) * np.floor(v / f32(1))
+        x, y = u * f32(W), v * f32(H)
+        ix0, ix1, iy0, iy1 = int(x), int(x + f32(1)), int(y), int(y + f32(1))
+        wx0, wy0 = x - f32(ix0), y - f32(iy0)
+        wx1, wy1 = f32(ix1) - x, f32(iy1) - y
+        c = lambda i, j: img[min(max(j, 0), H - 1), min(max(i, 0), W - 1)]
+        top = wx1 * c(ix0, iy0) + wx0 * c(ix1, iy0)
+        bot = wx1 * c(ix0, iy1) + wx0 * c(ix1, iy1)
+        want = wy1 * top + wy0 * bot
+        assert np.array_equal(row[:3].view(np.uint32), want.astype(np.float32).view(np.uint32))
+        assert np.array_equal(row[3:], img[int(y), int(x)])
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("textured", [False, True])
 def test_loaded_scene_renders_like_the_oracle(exe, tmp_path, textured):
