@@ -206,11 +206,13 @@ int EnsureWaveBuffers(pt_context* ctx, int capacity) {
     for (auto& b : ctx->wbBuffers) Free(ctx, b);
     ctx->wbBuffers.assign(1, DeviceBuffer{});
     ctx->wbCapacity = 0;
-    const int rc = Alloc(ctx, ctx->wbBuffers[0], WaveBuffersBytes(capacity));
+    const size_t bytes = WaveBuffersBytesTwoLanes(capacity);
+    const int rc = Alloc(ctx, ctx->wbBuffers[0], bytes);
     if (rc != PT_OK) return rc;
     int* hostCount = ctx->wb.hostCount;
     ctx->wb = CarveWaveBuffers(ctx->wbBuffers[0].ptr, capacity);
     ctx->wb.hostCount = hostCount;
+    ctx->wb.bytes = bytes;
     cudaMemsetAsync(ctx->wb.counts, 0, 16 * sizeof(int), ctx->stream);
     if (!ctx->wb.hostCount) {
         const cudaError_t e = cudaMallocHost(&ctx->wb.hostCount, sizeof(int) * 4);
@@ -223,7 +225,7 @@ int EnsureWaveBuffers(pt_context* ctx, int capacity) {
 int EnsureTables(pt_context* ctx, int nJobs, size_t accumPixels) {
     int rc;
     if ((rc = Alloc(ctx, ctx->jobTable, sizeof(DevJob) * (size_t)std::max(nJobs, 1))) != PT_OK) return rc;
-    if ((rc = Alloc(ctx, ctx->unitTable, sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK) return rc;
+    if ((rc = Alloc(ctx, ctx->unitTable, 2 * sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK) return rc;
     if ((rc = Alloc(ctx, ctx->jobList, sizeof(int) * (size_t)std::max(nJobs, 1))) != PT_OK) return rc;
     if ((rc = Alloc(ctx, ctx->accum, sizeof(float4) * std::max<size_t>(accumPixels, 1))) != PT_OK) return rc;
     return PT_OK;
@@ -233,6 +235,7 @@ WaveTables Tables(pt_context* ctx) {
     WaveTables t;
     t.jobs = (DevJob*)ctx->jobTable.ptr;
     t.units = (WaveUnit*)ctx->unitTable.ptr;
+    t.units2 = t.units + kMaxUnitsPerWave;
     t.jobList = (int*)ctx->jobList.ptr;
     t.maxUnits = kMaxUnitsPerWave;
     return t;

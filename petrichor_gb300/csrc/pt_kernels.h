@@ -78,6 +78,7 @@ struct WaveBuffers {
     int* hostCount;                // pinned host word for queue-size polls
     unsigned* sortKey;             // per entry of the next queue: coherence key (ray sorting)
     unsigned* sortBins;            // kSortBins counts, then kSortBins offsets
+    size_t bytes;                  // size of the allocation carved (0: unknown)
 };
 // Bins of the ray-coherence key: 64 direction cells x 4096 origin cells.
 constexpr int kSortOriginBits = 12;
@@ -86,6 +87,8 @@ constexpr int kSortBins = 64 << kSortOriginBits;
 // one 256-byte-aligned allocation (hostCount is left for the caller).
 size_t WaveBuffersBytes(int capacity);
 WaveBuffers CarveWaveBuffers(void* base, int capacity);
+// Bytes for `capacity` paths that also hold two sets of capacity / 2 (two wave lanes).
+size_t WaveBuffersBytesTwoLanes(int capacity);
 
 
 // Optional per-stage profile (CUDA events around every stage launch; ray tallies;
@@ -118,12 +121,23 @@ struct WaveGraphCache;
 WaveGraphCache* NewWaveGraphCache();
 void FreeWaveGraphCache(WaveGraphCache* cache);
 
-// One wave: raygen over `units` (device), the bounce loop, and accumulation into
-// each job's sums. With a cache and no profile, the launches of each wave shape
-// are captured once into a CUDA graph and replayed.
+// One wave: raygen over `units` (device), the bounce loop, and (accumulate) the
+// accumulation into each job's sums. With a cache and no profile, the launches of each
+// wave shape are captured once into a CUDA graph and replayed. lane (0 or 1) picks the
+// cache's shadow-stage side stream for waves run on two streams at once.
 cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& shape,
                     const WaveBuffers& wb, cudaStream_t stream, int* launches, WaveProfile* prof,
-                    const WaveTuning& tune, WaveGraphCache* graphs);
+                    const WaveTuning& tune, WaveGraphCache* graphs, int lane = 0,
+                    bool accumulate = true);
+// The accumulation pass of a wave run with accumulate = false.
+cudaError_t AccumulateWave(const DevJob* jobs, const WaveUnit* units, const WaveBuffers& wb,
+                           const WaveTuning& tune, cudaStream_t stream, int* launches);
+// The cache's second wave stream and the two lanes' completion events (created on
+// first use); false when they cannot be had.
+bool WavePipeline(WaveGraphCache* cache, cudaStream_t* side, cudaEvent_t* done);
+// into.counts[3] = a.counts[3] | b.counts[3] (error bits of two wave lanes).
+cudaError_t MergeWaveErrors(const WaveBuffers& into, const WaveBuffers& a, const WaveBuffers& b,
+                            cudaStream_t stream);
 // film = accum / spp for the listed jobs (device list of job indices).
 cudaError_t FinalizeJobs(const DevJob* jobs, const int* jobList, int nJobs, int maxPixels,
                          cudaStream_t stream, int* launches, WaveProfile* prof);

@@ -70,12 +70,73 @@ int WaveSoleJob(const std::vector<WaveUnit>& units) {
     return units.empty() ? -1 : units.front().job;
 }
 
+namespace {
+
+WaveShape ShapeOf(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units) {
+    WaveShape shape;
+    for (const WaveUnit& u : units) {
+        const int P = jobs[u.job].st.width * jobs[u.job].st.height;
+        shape.nPaths += P * u.sw;
+        shape.nPixelUnits += P;
+    }
+    shape.nUnits = (int)units.size();
+    shape.iters = WaveIterations(jobs, units);
+    shape.integrator = WaveIntegrator(jobs, units);
+    shape.soleJob = WaveSoleJob(units);
+    return shape;
+}
+
+// Finalises the jobs whose last wave is w (film = sums / spp), on `stream`.
+cudaError_t FinalizeDone(const std::vector<DevJob>& jobs, const WaveTables& T,
+                         const std::vector<int>& lastWave, size_t w, cudaStream_t stream,
+                         int* launches, WaveProfile* prof) {
+    std::vector<int> done;
+    int maxPx = 0;
+    for (size_t j = 0; j < jobs.size(); j++)
+        if (lastWave[j] == (int)w) {
+            done.push_back((int)j);
+            maxPx = std::max(maxPx, jobs[j].st.width * jobs[j].st.height);
+        }
+    if (done.empty()) return cudaSuccess;
+    cudaError_t e = cudaMemcpyAsync(T.jobList, done.data(), done.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    return FinalizeJobs(T.jobs, T.jobList, (int)done.size(), maxPx, stream, launches, prof);
+}
+
+}  // namespace
+
+// Waves run one after another on `stream`, or, when a render needs more than one wave
+// and the buffers hold two half-size sets, on two streams in turn: wave w+1 starts
+// while wave w finishes its last, sparse bounces, so the late-bounce tail of every wave
+// but the last is hidden. Each wave accumulates only after the previous wave has
+// accumulated and finalised (an event chain), so pixels still sum their samples in
+// sample order and films do not depend on the lane schedule.
 cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, const WaveBuffers& wb,
                        int cap, cudaStream_t stream, int* launches, WaveProfile* prof,
                        const WaveTuning& tune, WaveGraphCache* graphs) {
     std::vector<std::vector<WaveUnit>> waves;
     if (!PlanWaves(jobs, std::min(cap, wb.capacity), T.maxUnits, &waves))
         return cudaErrorInvalidValue;
+    // two lanes: half-capacity sets carved from the same allocation
+    WaveBuffers lane[2];
+    cudaStream_t laneStream[2] = {stream, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    bool twoLanes = false;
+    if (waves.size() > 1 && !prof && graphs && T.units2 && wb.bytes > 0 &&
+        wb.bytes >= 2 * WaveBuffersBytes(wb.capacity / 2) &&
+        WavePipeline(graphs, &laneStream[1], done)) {
+        std::vector<std::vector<WaveUnit>> half;
+        if (PlanWaves(jobs, std::min(cap, wb.capacity) / 2, T.maxUnits, &half)) {
+            char* base = reinterpret_cast<char*>(wb.ray[0]);
+            lane[0] = CarveWaveBuffers(base, wb.capacity / 2);
+            lane[1] = CarveWaveBuffers(base + WaveBuffersBytes(wb.capacity / 2), wb.capacity / 2);
+            lane[0].hostCount = wb.hostCount;
+            lane[1].hostCount = wb.hostCount ? wb.hostCount + 1 : nullptr;
+            waves.swap(half);
+            twoLanes = true;
+        }
+    }
     cudaError_t e = cudaMemcpyAsync(T.jobs, jobs.data(), jobs.size() * sizeof(DevJob),
                                     cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
@@ -87,41 +148,45 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
     std::vector<int> lastWave(jobs.size(), -1);
     for (size_t w = 0; w < waves.size(); w++)
         for (const WaveUnit& u : waves[w]) lastWave[u.job] = (int)w;
-    for (size_t w = 0; w < waves.size(); w++) {
-        const std::vector<WaveUnit>& units = waves[w];
-        // pageable source: the copy is staged before the call returns, so the
-        // next wave may reuse the host vector
-        e = cudaMemcpyAsync(T.units, units.data(), units.size() * sizeof(WaveUnit),
-                            cudaMemcpyHostToDevice, stream);
-        if (e != cudaSuccess) return e;
-        WaveShape shape;
-        for (const WaveUnit& u : units) {
-            const int P = jobs[u.job].st.width * jobs[u.job].st.height;
-            shape.nPaths += P * u.sw;
-            shape.nPixelUnits += P;
-        }
-        shape.nUnits = (int)units.size();
-        shape.iters = WaveIterations(jobs, units);
-        shape.integrator = WaveIntegrator(jobs, units);
-        shape.soleJob = WaveSoleJob(units);
-        e = RunWave(T.jobs, T.units, shape, wb, stream, launches, prof, tune, graphs);
-        if (e != cudaSuccess) return e;
-        std::vector<int> done;
-        int maxPx = 0;
-        for (size_t j = 0; j < jobs.size(); j++)
-            if (lastWave[j] == (int)w) {
-                done.push_back((int)j);
-                maxPx = std::max(maxPx, jobs[j].st.width * jobs[j].st.height);
-            }
-        if (!done.empty()) {
-            e = cudaMemcpyAsync(T.jobList, done.data(), done.size() * sizeof(int),
+    if (!twoLanes) {
+        e = cudaMemsetAsync(wb.counts, 0, 16 * sizeof(int), stream);
+        for (size_t w = 0; w < waves.size() && e == cudaSuccess; w++) {
+            const std::vector<WaveUnit>& units = waves[w];
+            // pageable source: the copy is staged before the call returns, so the
+            // next wave may reuse the host vector
+            e = cudaMemcpyAsync(T.units, units.data(), units.size() * sizeof(WaveUnit),
                                 cudaMemcpyHostToDevice, stream);
-            if (e != cudaSuccess) return e;
-            e = FinalizeJobs(T.jobs, T.jobList, (int)done.size(), maxPx, stream, launches, prof);
-            if (e != cudaSuccess) return e;
+            if (e == cudaSuccess)
+                e = RunWave(T.jobs, T.units, ShapeOf(jobs, units), wb, stream, launches, prof, tune, graphs);
+            if (e == cudaSuccess) e = FinalizeDone(jobs, T, lastWave, w, stream, launches, prof);
         }
+        return e;
     }
-    return cudaSuccess;
+    // the side lane starts after the job table, sums and counters are in place
+    for (int k = 0; k < 2 && e == cudaSuccess; k++)
+        e = cudaMemsetAsync(lane[k].counts, 0, 16 * sizeof(int), stream);
+    if (e == cudaSuccess) e = cudaEventRecord(done[1], stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(laneStream[1], done[1], 0);
+    WaveUnit* unitTable[2] = {T.units, T.units2};
+    for (size_t w = 0; w < waves.size() && e == cudaSuccess; w++) {
+        const int k = (int)(w & 1);
+        cudaStream_t s = laneStream[k];
+        const std::vector<WaveUnit>& units = waves[w];
+        e = cudaMemcpyAsync(unitTable[k], units.data(), units.size() * sizeof(WaveUnit),
+                            cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = RunWave(T.jobs, unitTable[k], ShapeOf(jobs, units), lane[k], s, launches, nullptr, tune,
+                        graphs, k, false);
+        // accumulate and finalise after the previous wave did
+        if (e == cudaSuccess && w > 0) e = cudaStreamWaitEvent(s, done[k ^ 1], 0);
+        if (e == cudaSuccess) e = AccumulateWave(T.jobs, unitTable[k], lane[k], tune, s, launches);
+        if (e == cudaSuccess) e = FinalizeDone(jobs, T, lastWave, w, s, launches, nullptr);
+        if (e == cudaSuccess) e = cudaEventRecord(done[k], s);
+    }
+    // the caller's stream continues after the last wave (whose chain covers every wave)
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, done[(waves.size() - 1) & 1], 0);
+    if (e == cudaSuccess) e = MergeWaveErrors(wb, lane[0], lane[1], stream);
+    return e;
 }
 
 }  // namespace ptg

@@ -13,6 +13,7 @@ namespace ptg {
 struct WaveTables {      // device buffers owned by the caller
     DevJob* jobs;        // >= number of jobs
     WaveUnit* units;     // >= maxUnits
+    WaveUnit* units2;    // >= maxUnits: the second wave lane's units (may be null: one lane)
     int* jobList;        // >= number of jobs
     int maxUnits;
 };

@@ -982,6 +982,10 @@ static size_t LayOutWaveBuffers(uintptr_t base, int capacity, WaveBuffers* w) {
 
 size_t WaveBuffersBytes(int capacity) { return LayOutWaveBuffers(0, capacity, nullptr); }
 
+size_t WaveBuffersBytesTwoLanes(int capacity) {
+    return std::max(WaveBuffersBytes(capacity), 2 * WaveBuffersBytes(capacity / 2));
+}
+
 WaveBuffers CarveWaveBuffers(void* base, int capacity) {
     WaveBuffers w{};
     LayOutWaveBuffers(reinterpret_cast<uintptr_t>(base), capacity, &w);
@@ -1113,10 +1117,11 @@ struct WaveGraphKey {
     const void* jobs;
     const void* units;
     const void* buffers;
-    int capacity, iters, integrator, grid, sort;
+    int capacity, iters, integrator, grid, sort, accum;
     bool operator==(const WaveGraphKey& o) const {
         return jobs == o.jobs && units == o.units && buffers == o.buffers && capacity == o.capacity &&
-               iters == o.iters && integrator == o.integrator && grid == o.grid && sort == o.sort;
+               iters == o.iters && integrator == o.integrator && grid == o.grid && sort == o.sort &&
+               accum == o.accum;
     }
 };
 struct WaveGraph {
@@ -1127,12 +1132,49 @@ struct WaveGraph {
 struct WaveGraphCache {
     std::vector<WaveGraph> graphs;  // few shapes per owner; least recently added dropped first
     static constexpr size_t kMax = 16;
-    StageOverlap overlap;           // the owner's side stream
+    StageOverlap overlap[2];        // shadow-stage side streams of the two wave lanes
+    // the second wave lane: its stream and each lane's "accumulated and finalised" event
+    cudaStream_t waveSide = nullptr;
+    cudaEvent_t waveDone[2] = {nullptr, nullptr};
     ~WaveGraphCache() {
         for (WaveGraph& g : graphs) cudaGraphExecDestroy(g.exec);
-        overlap.Release();
+        for (StageOverlap& o : overlap) o.Release();
+        for (cudaEvent_t e : waveDone)
+            if (e) cudaEventDestroy(e);
+        if (waveSide) cudaStreamDestroy(waveSide);
     }
 };
+
+bool WavePipeline(WaveGraphCache* cache, cudaStream_t* side, cudaEvent_t* done) {
+    if (!cache) return false;
+    if (!cache->waveSide) {
+        if (cudaStreamCreateWithFlags(&cache->waveSide, cudaStreamNonBlocking) != cudaSuccess) {
+            cache->waveSide = nullptr;
+            return false;
+        }
+        for (cudaEvent_t& e : cache->waveDone)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    }
+    *side = cache->waveSide;
+    done[0] = cache->waveDone[0];
+    done[1] = cache->waveDone[1];
+    return done[0] && done[1];
+}
+
+__global__ void OrErrorsKernel(int* dst, const int* a, const int* b) { *dst = *a | *b; }
+
+cudaError_t MergeWaveErrors(const WaveBuffers& into, const WaveBuffers& a, const WaveBuffers& b,
+                            cudaStream_t stream) {
+    OrErrorsKernel<<<1, 1, 0, stream>>>(into.counts + 3, a.counts + 3, b.counts + 3);
+    return cudaGetLastError();
+}
+
+cudaError_t AccumulateWave(const DevJob* jobs, const WaveUnit* units, const WaveBuffers& wb,
+                           const WaveTuning& tune, cudaStream_t stream, int* launches) {
+    AccumulateKernel<<<StageGrid(tune), kTraceBlock, 0, stream>>>(jobs, units, wb);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
 WaveGraphCache* NewWaveGraphCache() { return new WaveGraphCache(); }
 void FreeWaveGraphCache(WaveGraphCache* cache) { delete cache; }
 
@@ -1167,7 +1209,7 @@ static cudaError_t ReplayCaptured(WaveGraphCache* cache, const WaveGraphKey& key
 
 cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& shape,
                     const WaveBuffers& wb, cudaStream_t stream, int* launches, WaveProfile* prof,
-                    const WaveTuning& tune, WaveGraphCache* graphs) {
+                    const WaveTuning& tune, WaveGraphCache* graphs, int lane, bool accumulate) {
     if (shape.nPaths <= 0) return cudaSuccess;
     if (shape.nPaths > wb.capacity) return cudaErrorInvalidValue;
     const int grid = StageGrid(tune);
@@ -1192,15 +1234,16 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     const bool sort = tune.sortRays != 0;
     // shadow stages beside the next extend, on the owner's side stream (not when profiling,
     // whose stage timers need one stream)
-    StageOverlap* ov = (graphs && !prof && graphs->overlap.Ready()) ? &graphs->overlap : nullptr;
+    StageOverlap* ov =
+      (graphs && !prof && graphs->overlap[lane & 1].Ready()) ? &graphs->overlap[lane & 1] : nullptr;
     const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
-                           sort ? 1 : 0};
+                           sort ? 1 : 0, accumulate ? 1 : 0};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
             LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort, ov);
-            AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
-            *n += 2;
+            if (accumulate) AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
+            *n += accumulate ? 2 : 1;
         };
         if (useGraphs) {
             e = ReplayCaptured(graphs, key, stream, &nl, record);
@@ -1209,10 +1252,13 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
             if (ev) ev->End(0, stream);
             LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort, ov);
-            if (ev) ev->Begin(4, stream);
-            AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
-            if (ev) ev->End(4, stream);
-            nl += 2;
+            if (accumulate) {
+                if (ev) ev->Begin(4, stream);
+                AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
+                if (ev) ev->End(4, stream);
+                nl++;
+            }
+            nl++;
         }
     } else {
         // SimplePathTracing has no depth cap: run blocks of bounces until the queue drains
@@ -1238,7 +1284,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
                 LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort, ov);
             }
         }
-        if (e == cudaSuccess) {
+        if (e == cudaSuccess && accumulate) {
             if (ev) ev->Begin(4, stream);
             AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             if (ev) ev->End(4, stream);
