@@ -351,7 +351,7 @@ typedef struct pt_tuning {
   int32_t band_rows;     /* rows per pixel band of the path order (0: 8) */
   int32_t use_graphs;    /* 1: replay each wave's stage sequence from a captured CUDA graph */
   int32_t sort_rays;     /* 1: reorder each bounce's rays by direction and origin cell */
-  int32_t reserved;
+  int32_t tail_bounce;   /* > 0: from this bounce on, one launch finishes every path (0: off) */
   double probe_ms;       /* pt_autotune: probe render time of the chosen configuration */
 } pt_tuning;
 /* Times candidate grids, pixel bands and graph replay on probe renders of one job

@@ -753,13 +753,14 @@ int pt_set_tuning(pt_context* ctx, const pt_tuning* t) {
     std::lock_guard<std::mutex> g(ctx->mu);
     if (t->wave_paths < 0 || t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->band_rows < 0 ||
         t->band_rows > 4096 || (t->use_graphs != 0 && t->use_graphs != 1) ||
-        (t->sort_rays != 0 && t->sort_rays != 1))
+        (t->sort_rays != 0 && t->sort_rays != 1) || t->tail_bounce < 0 || t->tail_bounce > 64)
         return Fail(ctx, PT_ERR_INVALID_ARG, "bad tuning");
     ctx->tunedWavePaths = t->wave_paths;
     ctx->tuning.blocksPerSm = t->blocks_per_sm;
     ctx->tuning.band = t->band_rows;
     ctx->tuning.graphs = t->use_graphs;
     ctx->tuning.sortRays = t->sort_rays;
+    ctx->tuning.tailBounce = t->tail_bounce;
     return PT_OK;
 }
 
@@ -771,6 +772,7 @@ int pt_get_tuning(pt_context* ctx, pt_tuning* out) {
     out->band_rows = ctx->tuning.band;
     out->use_graphs = ctx->tuning.graphs;
     out->sort_rays = ctx->tuning.sortRays;
+    out->tail_bounce = ctx->tuning.tailBounce;
     out->probe_ms = ctx->tunedProbeMs;
     return PT_OK;
 }
@@ -810,12 +812,17 @@ int pt_autotune(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const 
     const int bands[] = {8, 4, 16, 32};
     const int graphs[] = {1, 0};
     const int sorts[] = {0, 1};
-    for (int knob = 0; knob < 4; knob++) {
-        const int* vals = knob == 0 ? grids : knob == 1 ? bands : knob == 2 ? graphs : sorts;
+    const int tails[] = {0, 8};
+    for (int knob = 0; knob < 5; knob++) {
+        const int* vals = knob == 0 ? grids : knob == 1 ? bands : knob == 2 ? graphs : knob == 3 ? sorts : tails;
         const int nv = knob == 0 ? 5 : knob == 1 ? 4 : 2;
         for (int i = 0; i < nv; i++) {
             WaveTuning t = best;
-            int& field = knob == 0 ? t.blocksPerSm : knob == 1 ? t.band : knob == 2 ? t.graphs : t.sortRays;
+            int& field = knob == 0 ? t.blocksPerSm
+                         : knob == 1 ? t.band
+                         : knob == 2 ? t.graphs
+                         : knob == 3 ? t.sortRays
+                                     : t.tailBounce;
             if (field == vals[i]) continue;
             field = vals[i];
             double ms = 0.0;
@@ -837,6 +844,7 @@ int pt_autotune(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const 
         out->band_rows = best.band;
         out->use_graphs = best.graphs;
         out->sort_rays = best.sortRays;
+        out->tail_bounce = best.tailBounce;
         out->probe_ms = bestMs;
     }
     return PT_OK;

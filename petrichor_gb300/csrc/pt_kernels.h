@@ -115,6 +115,7 @@ struct WaveTuning {
     int band = 0;         // rows per pixel band of the path order (0: 8)
     int graphs = 1;       // replay each wave's stage sequence from a captured CUDA graph
     int sortRays = 0;     // reorder each bounce's rays by direction and origin cell before tracing
+    int tailBounce = 0;   // > 0: from this bounce on, one launch finishes every path (TailKernel)
 };
 // Captured stage sequences, keyed by wave shape and buffers (owned by a context or server).
 struct WaveGraphCache;

@@ -415,179 +415,30 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const D
 
 // kInteg: the integrator of every job in the wave, or -1 when the wave mixes them
 // (then read per path). A fixed integrator halves the kernel's code.
-template <int kInteg>
-__global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
-                                                   int cur) {
-    const int n = wb.counts[cur];
-    const int nxt = cur ^ 1;
-    const int sole = wb.desc->soleJob;
-    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // the next extend fetches from zero
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
-        const float2 h = wb.hit[i];
-        const int path = __float_as_int(ra.w);
-        const DevJob& J = jobs[JobOf(wb.pathJob, sole, path)];
-        const DevScene& S = J.S;
-        const DevSettings& st = J.st;
-        const V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
-        const float4 s0 = wb.qs0[cur][i], s2 = wb.qs1[cur][i];
-        PathRng rng(wb.qrng[cur][i]);
-        V3 L;  // radiance this shade adds (terminations); next-event adds come later
-        Ray in;
-        in.o = o;
-        in.d = d;
-        in.T = V3(s0.x, s0.y, s0.z);
-        in.prob = s0.w;
-        in.ior = rb.w;
-        in.bounce = __float_as_int(s2.z);
-        int flags = __float_as_int(s2.w);
-        const int slot = __float_as_int(h.y);
+// The staged shade kernel's sink: next-event entries and continuation rays go to the
+// queues (warp-aggregated appends), terminated paths add their radiance.
+struct StageSink {
+    WaveBuffers& wb;
+    int nxt, path;
+    PathRng* rng;
+    __device__ __forceinline__ void Shadow(bool shadow, float4 sh0, float4 sh1, float4 sh2, float4 sh3) {
+        int sslot = WarpAppend(wb.counts + 2, shadow);
 #if PT_CHECK
-        if (slot >= S.numTris || (unsigned)path >= (unsigned)wb.capacity) {
+        if (shadow && sslot >= wb.capacity) {
             atomicOr(wb.counts + 3, kErrBounds);
-            continue;  // appends below are aggregated over the lanes that reach them
+            shadow = false;
         }
 #endif
-        bool cont = false;
-        Ray out;
-        float lastPdf = s2.x, lastSin = s2.y;
-        // next-event entry
-        bool shadow = false;
-        float4 sh0, sh1, sh2, sh3;
-
-        if ((kInteg >= 0 ? kInteg : st.integrator) == kSimplePathTracing) {
-            // SimplePathTracing.cpp:45-126
-            flags |= kFlagNoSignCheck;
-            if (slot < 0) {
-                L = L + in.T * EnvColor<FastMath>(S, d);
-            } else {
-                const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, slot), rng.Next());
-                if (S.mats[m].kind == kEmission) {
-                    L = L + in.T * MatColor(S.mats[m]);
-                } else {
-                    Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
-                    DevMaterial Mh;
-                    si.n = PointMaterial<FastMath>(S, m, slot, o, d, si.n, Mh);
-                    out = NextRay<FastMath>(Mh, in, si, rng);
-                    cont = true;
-                    if (out.bounce > st.maxBounces) {
-                        out.prob *= 0.9f;
-                        out.prob = SMax(0.1f, out.prob);
-                        if (rng.Next() < out.prob) out.T = out.T / out.prob;
-                        else cont = false;
-                    }
-                    // a path with exactly zero throughput adds nothing more
-                    if (out.T.x == 0.0f && out.T.y == 0.0f && out.T.z == 0.0f) cont = false;
-                }
-            }
-        } else {
-            // PathTracing.cpp:38-196; k = BSDF bounces taken so far
-            const int k = in.bounce;
-            if (slot < 0) {
-                // one lookup for the three cases (mis = 1 multiplies exactly)
-                float mis = 1.0f;
-                if (k == 0) {
-                    flags |= kFlagNoSignCheck;
-                } else if (S.envValid && d.x != 0 && d.y != 0 && lastSin > 0) {
-                    const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
-                    mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
-                }
-                L = L + mis * in.T * EnvColor<FastMath>(S, d);
-            } else {
-                const Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
-                if (S.mats[si.mat].kind == kEmission) {
-                    const DevMaterial& M = S.mats[si.mat];
-                    if (k == 0) {
-                        L = L + in.T * MatColor(M);
-                        flags |= kFlagNoSignCheck;
-                    } else {
-                        const float l2 = SqLen(si.pos - o);
-                        const float cosP = fabsf(Dot(d, si.n));
-                        const float pL = l2 / cosP * S.lightPdfArea;
-                        const float mis = lastPdf * lastPdf / (pL * pL + lastPdf * lastPdf);
-                        L = L + mis * in.T * MatColor(M);
-                    }
-                } else if (k < st.maxBounces) {
-                    // material and BSDF normal at the shading point (texture maps applied)
-                    DevMaterial M;
-                    const V3 nb = PointMaterial<FastMath>(S, si.mat, slot, o, d, si.n, M);
-                    // ---- next-event estimation (PathTracing.cpp:202-327)
-                    const float dt = -Dot(d, si.n);
-                    const V3 p = si.pos + kEps * copysignf(1.0f, dt) * si.n;
-                    const int nl = S.numLights;
-                    int index = (int)(rng.Next() * (float)(nl + 1));
-                    index = min(index, nl);
-                    if (index >= nl) {
-                        if (S.envValid && M.kind != kGlass) {
-                            float e0, e1;
-                            rng.Next(e0, e1);
-                            float pdfuv = 0.0f;
-                            const V3 sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
-                            const float c = fabsf(Dot(sd, si.n));
-                            const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
-                            const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, nb);
-                            const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
-                            const V3 li = EnvColor<FastMath>(S, sd);
-                            const V3 f = BxDF<FastMath>(M, d, sd, nb);
-                            const V3 contrib = mis * in.T * (li * f * sn * c * 2.0f * kPi * kPi) / pdfuv;
-                            if (contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f) {
-                                shadow = true;
-                                sh0 = make_float4(p.x, p.y, p.z, kFltMax);
-                                sh1 = make_float4(sd.x, sd.y, sd.z, __int_as_float(path));
-                                sh2 = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
-                                sh3 = make_float4(0.f, 0.f, 0.f, 0.f);
-                            }
-                        }  // glass: BxDF = 0 (Glass.cpp:11-18), nothing to add
-                    } else {
-                        float u0, u1;
-                        rng.Next(u0, u1);
-                        const V3 pl = SampleLightPoint<FastMath>(S, index, u0, u1);
-                        const V3 dl = pl - p;
-                        const float dist = Length(dl);
-                        const V3 ld = dl / dist;
-                        const V3 f = BxDF<FastMath>(M, d, ld, nb);
-                        // emitter material pick for the visibility test (GetMaterial with a draw)
-                        const float pick = rng.Next();
-                        if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
-                            const V3 Tfc = in.T * f * fabsf(Dot(ld, si.n));
-                            shadow = true;
-                            sh0 = make_float4(p.x, p.y, p.z, dist);
-                            sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
-                            sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf<FastMath>(M, d, ld, nb));
-                            sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, pick);
-                        }
-                    }
-                    // the next-event entry is queued before the BSDF sample, so its
-                    // registers are free for it
-                    int sslot = WarpAppend(wb.counts + 2, shadow);
-#if PT_CHECK
-                    if (shadow && sslot >= wb.capacity) {
-                        atomicOr(wb.counts + 3, kErrBounds);
-                        shadow = false;
-                    }
-#endif
-                    if (shadow) {
-                        float4* e = wb.shadow + 4 * (size_t)sslot;
-                        e[0] = sh0;
-                        e[1] = sh1;
-                        e[2] = sh2;
-                        e[3] = sh3;
-                    }
-                    // ---- continuation
-                    Shading sb = si;
-                    sb.n = nb;
-                    out = NextRay<FastMath>(M, in, sb, rng);
-                    if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
-                        cont = true;
-                        lastPdf = BsdfPdf<FastMath>(M, d, out.d, nb);
-                        const float c = fabsf(Dot(si.n, out.d));
-                        lastSin = sqrtf(SMax(0.0f, 1.0f - c * c));
-                        out.bounce = k + 1;
-                    }
-                }
-            }
+        if (shadow) {
+            float4* e = wb.shadow + 4 * (size_t)sslot;
+            e[0] = sh0;
+            e[1] = sh1;
+            e[2] = sh2;
+            e[3] = sh3;
         }
-        // ---- write back and append
+    }
+    __device__ __forceinline__ void Done(bool cont, const Ray& out, float lastPdf, float lastSin,
+                                         int flags, V3 L) {
         int rslot = WarpAppend(wb.counts + nxt, cont);
 #if PT_CHECK
         if (cont && rslot >= wb.capacity) {
@@ -601,12 +452,246 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
             wb.qs0[nxt][rslot] = make_float4(out.T.x, out.T.y, out.T.z, out.prob);
             wb.qs1[nxt][rslot] = make_float4(lastPdf, lastSin, __int_as_float(out.bounce),
                                              __int_as_float(flags));
-            wb.qrng[nxt][rslot] = rng.s;
+            wb.qrng[nxt][rslot] = rng->s;
         } else {
             float4 l = wb.pathL[path];  // next-event radiance added so far
             wb.pathL[path] = make_float4(l.x + L.x, l.y + L.y, l.z + L.z, __int_as_float(flags));
         }
     }
+};
+
+// One path's shade step (SimplePathTracing.cpp:45-126, PathTracing.cpp:38-327): the
+// radiance it adds at termination, its next-event entry and its continuation ray. The
+// sink takes the next-event entry (Shadow, called where the entry is complete) and the
+// outcome (Done). Shared by the staged shade kernel, whose sink appends to the queues,
+// and the tail kernel, whose sink keeps both for the same thread.
+template <int kInteg, class Sink>
+__device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, float4 s0, float4 s2,
+                                         float ior, float2 h, PathRng& rng, Sink& sink) {
+    const DevScene& S = J.S;
+    const DevSettings& st = J.st;
+    V3 L;  // radiance this shade adds (terminations); next-event adds come later
+    Ray in;
+    in.o = o;
+    in.d = d;
+    in.T = V3(s0.x, s0.y, s0.z);
+    in.prob = s0.w;
+    in.ior = ior;
+    in.bounce = __float_as_int(s2.z);
+    int flags = __float_as_int(s2.w);
+    const int slot = __float_as_int(h.y);
+    bool cont = false;
+    Ray out;
+    float lastPdf = s2.x, lastSin = s2.y;
+    // next-event entry
+    bool shadow = false;
+    float4 sh0, sh1, sh2, sh3;
+
+    if ((kInteg >= 0 ? kInteg : st.integrator) == kSimplePathTracing) {
+        // SimplePathTracing.cpp:45-126
+        flags |= kFlagNoSignCheck;
+        if (slot < 0) {
+            L = L + in.T * EnvColor<FastMath>(S, d);
+        } else {
+            const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, slot), rng.Next());
+            if (S.mats[m].kind == kEmission) {
+                L = L + in.T * MatColor(S.mats[m]);
+            } else {
+                Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
+                DevMaterial Mh;
+                si.n = PointMaterial<FastMath>(S, m, slot, o, d, si.n, Mh);
+                out = NextRay<FastMath>(Mh, in, si, rng);
+                cont = true;
+                if (out.bounce > st.maxBounces) {
+                    out.prob *= 0.9f;
+                    out.prob = SMax(0.1f, out.prob);
+                    if (rng.Next() < out.prob) out.T = out.T / out.prob;
+                    else cont = false;
+                }
+                // a path with exactly zero throughput adds nothing more
+                if (out.T.x == 0.0f && out.T.y == 0.0f && out.T.z == 0.0f) cont = false;
+            }
+        }
+    } else {
+        // PathTracing.cpp:38-196; k = BSDF bounces taken so far
+        const int k = in.bounce;
+        if (slot < 0) {
+            // one lookup for the three cases (mis = 1 multiplies exactly)
+            float mis = 1.0f;
+            if (k == 0) {
+                flags |= kFlagNoSignCheck;
+            } else if (S.envValid && d.x != 0 && d.y != 0 && lastSin > 0) {
+                const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
+                mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
+            }
+            L = L + mis * in.T * EnvColor<FastMath>(S, d);
+        } else {
+            const Shading si = Interpolate<FastMath>(S, slot, o, d, h.x);
+            if (S.mats[si.mat].kind == kEmission) {
+                const DevMaterial& M = S.mats[si.mat];
+                if (k == 0) {
+                    L = L + in.T * MatColor(M);
+                    flags |= kFlagNoSignCheck;
+                } else {
+                    const float l2 = SqLen(si.pos - o);
+                    const float cosP = fabsf(Dot(d, si.n));
+                    const float pL = l2 / cosP * S.lightPdfArea;
+                    const float mis = lastPdf * lastPdf / (pL * pL + lastPdf * lastPdf);
+                    L = L + mis * in.T * MatColor(M);
+                }
+            } else if (k < st.maxBounces) {
+                // material and BSDF normal at the shading point (texture maps applied)
+                DevMaterial M;
+                const V3 nb = PointMaterial<FastMath>(S, si.mat, slot, o, d, si.n, M);
+                // ---- next-event estimation (PathTracing.cpp:202-327)
+                const float dt = -Dot(d, si.n);
+                const V3 p = si.pos + kEps * copysignf(1.0f, dt) * si.n;
+                const int nl = S.numLights;
+                int index = (int)(rng.Next() * (float)(nl + 1));
+                index = min(index, nl);
+                if (index >= nl) {
+                    if (S.envValid && M.kind != kGlass) {
+                        float e0, e1;
+                        rng.Next(e0, e1);
+                        float pdfuv = 0.0f;
+                        const V3 sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
+                        const float c = fabsf(Dot(sd, si.n));
+                        const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
+                        const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, nb);
+                        const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
+                        const V3 li = EnvColor<FastMath>(S, sd);
+                        const V3 f = BxDF<FastMath>(M, d, sd, nb);
+                        const V3 contrib = mis * in.T * (li * f * sn * c * 2.0f * kPi * kPi) / pdfuv;
+                        if (contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f) {
+                            shadow = true;
+                            sh0 = make_float4(p.x, p.y, p.z, kFltMax);
+                            sh1 = make_float4(sd.x, sd.y, sd.z, __int_as_float(path));
+                            sh2 = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
+                            sh3 = make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
+                    }  // glass: BxDF = 0 (Glass.cpp:11-18), nothing to add
+                } else {
+                    float u0, u1;
+                    rng.Next(u0, u1);
+                    const V3 pl = SampleLightPoint<FastMath>(S, index, u0, u1);
+                    const V3 dl = pl - p;
+                    const float dist = Length(dl);
+                    const V3 ld = dl / dist;
+                    const V3 f = BxDF<FastMath>(M, d, ld, nb);
+                    // emitter material pick for the visibility test (GetMaterial with a draw)
+                    const float pick = rng.Next();
+                    if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
+                        const V3 Tfc = in.T * f * fabsf(Dot(ld, si.n));
+                        shadow = true;
+                        sh0 = make_float4(p.x, p.y, p.z, dist);
+                        sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
+                        sh2 = make_float4(Tfc.x, Tfc.y, Tfc.z, BsdfPdf<FastMath>(M, d, ld, nb));
+                        sh3 = make_float4(si.pos.x, si.pos.y, si.pos.z, pick);
+                    }
+                }
+                // the next-event entry is handed over before the BSDF sample, so its
+                // registers are free for it
+                sink.Shadow(shadow, sh0, sh1, sh2, sh3);
+                // ---- continuation
+                Shading sb = si;
+                sb.n = nb;
+                out = NextRay<FastMath>(M, in, sb, rng);
+                if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
+                    cont = true;
+                    lastPdf = BsdfPdf<FastMath>(M, d, out.d, nb);
+                    const float c = fabsf(Dot(si.n, out.d));
+                    lastSin = sqrtf(SMax(0.0f, 1.0f - c * c));
+                    out.bounce = k + 1;
+                }
+            }
+        }
+    }
+    sink.Done(cont, out, lastPdf, lastSin, flags, L);
+}
+
+template <int kInteg>
+__global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+                                                   int cur) {
+    const int n = wb.counts[cur];
+    const int nxt = cur ^ 1;
+    const int sole = wb.desc->soleJob;
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // the next extend fetches from zero
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
+        const float2 h = wb.hit[i];
+        const int path = __float_as_int(ra.w);
+        const DevJob& J = jobs[JobOf(wb.pathJob, sole, path)];
+#if PT_CHECK
+        if (__float_as_int(h.y) >= J.S.numTris || (unsigned)path >= (unsigned)wb.capacity) {
+            atomicOr(wb.counts + 3, kErrBounds);
+            continue;  // the appends are aggregated over the lanes that reach them
+        }
+#endif
+        PathRng rng(wb.qrng[cur][i]);
+        StageSink sink{wb, nxt, path, &rng};
+        ShadeOne<kInteg>(J, path, V3(ra.x, ra.y, ra.z), V3(rb.x, rb.y, rb.z), wb.qs0[cur][i],
+                         wb.qs1[cur][i], rb.w, h, rng, sink);
+    }
+}
+
+// A next-event entry's visibility ray (PathTracing.cpp:202-327): environment entries
+// are any-hit rays, area-light entries closest-hit rays bounded just past the light.
+__device__ __forceinline__ void ShadowRay(const DevScene& S, float4 e0, float4 e1, LaneRay& r) {
+    r.nodes = S.numWide > 0 ? S.wide : nullptr;
+    r.tris = S.tris;
+#if PT_CHECK
+    r.numWide = S.numWide;
+    r.numTris = S.numTris;
+#endif
+    r.o = V3(e0.x, e0.y, e0.z);
+    r.d = V3(e1.x, e1.y, e1.z);
+    r.tmin = 0.0f;
+    const bool env = __float_as_int(e1.w) >= 0;
+    r.anyHit = env;
+    r.tmax = env ? kFltMax : e0.w + 0.05f;
+}
+
+// Adds a traced next-event entry's contribution to its path's radiance; e holds the
+// entry's four float4 (read only as needed: an occluded environment entry reads one).
+__device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, const LaneRay& r,
+                                            float4* pathL) {
+    const float4 e1 = e[1];
+    const int tag = __float_as_int(e1.w);
+    const int path = tag & 0x7FFFFFFF;
+    if (tag >= 0) {  // environment: adds when unoccluded
+        if (r.best >= 0) return;
+        const float4 e2 = e[2];
+        float4 l = pathL[path];
+        l.x += e2.x;
+        l.y += e2.y;
+        l.z += e2.z;
+        pathL[path] = l;
+        return;
+    }
+    // area light: the closest hit must be an emitter at the sampled point
+    if (r.best < 0) return;
+    const float4 e0 = e[0], e2 = e[2], e3 = e[3];
+    const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, r.best), e3.w);
+    if (S.mats[m].kind != kEmission) return;
+    const Shading sl = Interpolate<FastMath>(S, r.best, r.o, r.d, r.tBest);
+    const V3 pl = r.o + r.d * e0.w;
+    if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
+    const V3 sipos(e3.x, e3.y, e3.z);
+    const float l2 = SqLen(sl.pos - sipos);
+    const float cosP = fabsf(Dot(r.d, sl.n));
+    const float pdfArea = S.lightPdfArea;
+    float mis = 0.0f;
+    if (l2 > 0.0f) {
+        const float pB = e2.w * cosP / l2;
+        mis = pdfArea * pdfArea / (pdfArea * pdfArea + pB * pB);
+    }
+    const V3 li = MatColor(S.mats[sl.mat]);
+    const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * cosP / (pdfArea * l2));
+    float4 l = pathL[path];
+    l.x += c.x;
+    l.y += c.y;
+    l.z += c.z;
+    pathL[path] = l;
 }
 
 struct ShadowQueue {
@@ -617,62 +702,123 @@ struct ShadowQueue {
     float4* pathL;
     __device__ void Load(int j, LaneRay& r) const {
         const float4 e0 = entries[4 * j], e1 = entries[4 * j + 1];
-        const DevScene& S = jobs[JobOf(pathJob, soleJob, __float_as_int(e1.w) & 0x7FFFFFFF)].S;
-        r.nodes = S.numWide > 0 ? S.wide : nullptr;
-        r.tris = S.tris;
-#if PT_CHECK
-        r.numWide = S.numWide;
-        r.numTris = S.numTris;
-#endif
-        r.o = V3(e0.x, e0.y, e0.z);
-        r.d = V3(e1.x, e1.y, e1.z);
-        r.tmin = 0.0f;
-        const bool env = __float_as_int(e1.w) >= 0;
-        r.anyHit = env;
-        r.tmax = env ? kFltMax : e0.w + 0.05f;
+        ShadowRay(jobs[JobOf(pathJob, soleJob, __float_as_int(e1.w) & 0x7FFFFFFF)].S, e0, e1, r);
     }
     __device__ void Finish(int j, const LaneRay& r) const {
-        const float4 e1 = entries[4 * j + 1];
-        const int tag = __float_as_int(e1.w);
-        const int path = tag & 0x7FFFFFFF;
-        if (tag >= 0) {  // environment: adds when unoccluded
-            if (r.best >= 0) return;
-            const float4 c = entries[4 * j + 2];
-            float4 l = pathL[path];
-            l.x += c.x;
-            l.y += c.y;
-            l.z += c.z;
-            pathL[path] = l;
-            return;
-        }
-        // area light: the closest hit must be an emitter at the sampled point
-        if (r.best < 0) return;
-        const DevScene& S = jobs[JobOf(pathJob, soleJob, path)].S;
-        const float4 e0 = entries[4 * j];
-        const float4 e2 = entries[4 * j + 2], e3 = entries[4 * j + 3];
-        const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, r.best), e3.w);
-        if (S.mats[m].kind != kEmission) return;
-        const Shading sl = Interpolate<FastMath>(S, r.best, r.o, r.d, r.tBest);
-        const V3 pl = r.o + r.d * e0.w;
-        if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
-        const V3 sipos(e3.x, e3.y, e3.z);
-        const float l2 = SqLen(sl.pos - sipos);
-        const float cosP = fabsf(Dot(r.d, sl.n));
-        const float pdfArea = S.lightPdfArea;
-        float mis = 0.0f;
-        if (l2 > 0.0f) {
-            const float pB = e2.w * cosP / l2;
-            mis = pdfArea * pdfArea / (pdfArea * pdfArea + pB * pB);
-        }
-        const V3 li = MatColor(S.mats[sl.mat]);
-        const V3 c = mis * (V3(e2.x, e2.y, e2.z) * li * cosP / (pdfArea * l2));
-        float4 l = pathL[path];
-        l.x += c.x;
-        l.y += c.y;
-        l.z += c.z;
-        pathL[path] = l;
+        const int path = __float_as_int(entries[4 * j + 1].w) & 0x7FFFFFFF;
+        ApplyShadow(jobs[JobOf(pathJob, soleJob, path)].S, entries + 4 * j, r, pathL);
     }
 };
+
+// One ray traversed by one thread (the tail kernel's form): the same node and leaf
+// order as TraceQueue gives the ray.
+__device__ __forceinline__ void TraceOne(LaneRay& r, TravStack& stk, int& err) {
+    r.inv = ExactRecip(r.d);
+    r.tBest = r.tmax;
+    r.best = -1;
+    stk.sp = 0;
+    if (!r.nodes) return;
+    int cur = 0;  // wide root
+    while (cur != kDone) {
+        if (cur >= 0) VisitInner(r, stk, cur, err);
+        else if (VisitLeaf(r, stk, cur, err)) break;
+    }
+}
+
+// The tail kernel's sink: the thread keeps its next-event entry and continuation;
+// a terminated path adds its radiance at once (before its next-event entry is traced,
+// the order the staged kernels add them in).
+struct TailSink {
+    float4* pathL;
+    int path;
+    bool shadow = false, cont = false;
+    float4 sh[4];
+    Ray out;
+    float lastPdf = 0.0f, lastSin = 0.0f;
+    int flags = 0;
+    __device__ __forceinline__ void Shadow(bool s, float4 a, float4 b, float4 c, float4 d) {
+        shadow = s;
+        sh[0] = a;
+        sh[1] = b;
+        sh[2] = c;
+        sh[3] = d;
+    }
+    __device__ __forceinline__ void Done(bool c, const Ray& o, float lp, float ls, int f, V3 L) {
+        cont = c;
+        out = o;
+        lastPdf = lp;
+        lastSin = ls;
+        flags = f;
+        if (!c) {
+            const float4 l = pathL[path];
+            pathL[path] = make_float4(l.x + L.x, l.y + L.y, l.z + L.z, __int_as_float(f));
+        }
+    }
+};
+
+// The last `iters` bounces of a wave in one launch: each thread takes a path from the
+// queue and runs its closest hit, shade and next-event ray, bounce after bounce, until
+// the path ends or the wave's iterations are used up, exactly as the staged kernels
+// would (same functions, same per-path random stream, same order of radiance adds).
+// Late bounces hold few rays, and one launch spares each of them a sweep of three
+// latency-bound launches.
+template <int kInteg>
+__global__ void __launch_bounds__(128) TailKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
+                                                  int cur, int iters) {
+    __shared__ int sCode[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
+    __shared__ float sDist[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
+    TravStack stk;
+    stk.code = sCode;
+    stk.dist = sDist;
+    stk.sp = 0;
+    const int n = wb.counts[cur];
+    const int sole = wb.desc->soleJob;
+    int err = 0;
+    for (;;) {
+        const int i = atomicAdd(wb.counts + 4, 1);  // reset by the shade before
+        if (i >= n) break;
+        const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
+        const int path = __float_as_int(ra.w);
+        const DevJob& J = jobs[JobOf(wb.pathJob, sole, path)];
+        const DevScene& S = J.S;
+        V3 o(ra.x, ra.y, ra.z), d(rb.x, rb.y, rb.z);
+        float ior = rb.w;
+        float4 s0 = wb.qs0[cur][i], s2 = wb.qs1[cur][i];
+        PathRng rng(wb.qrng[cur][i]);
+        for (int it = 0; it < iters; it++) {
+            LaneRay r;
+            r.o = o;
+            r.d = d;
+            r.tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;  // as ExtendQueue
+            r.tmax = kFltMax;
+            r.anyHit = false;
+            r.nodes = S.numWide > 0 ? S.wide : nullptr;
+            r.tris = S.tris;
+#if PT_CHECK
+            r.numWide = S.numWide;
+            r.numTris = S.numTris;
+#endif
+            TraceOne(r, stk, err);
+            TailSink sink{wb.pathL, path};
+            ShadeOne<kInteg>(J, path, o, d, s0, s2, ior, make_float2(r.tBest, __int_as_float(r.best)), rng,
+                             sink);
+            if (sink.shadow) {
+                LaneRay sr;
+                ShadowRay(S, sink.sh[0], sink.sh[1], sr);
+                TraceOne(sr, stk, err);
+                ApplyShadow(S, sink.sh, sr, wb.pathL);
+            }
+            if (!sink.cont) break;
+            o = sink.out.o;
+            d = sink.out.d;
+            ior = sink.out.ior;
+            s0 = make_float4(sink.out.T.x, sink.out.T.y, sink.out.T.z, sink.out.prob);
+            s2 = make_float4(sink.lastPdf, sink.lastSin, __int_as_float(sink.out.bounce),
+                             __int_as_float(sink.flags));
+        }
+    }
+    if (err) atomicOr(wb.counts + 3, err);
+}
 
 // It may run beside the next bounce's extend kernel (which touches neither the
 // shadow queue nor its counters); its last block to finish clears the shadow queue
@@ -1052,9 +1198,10 @@ struct StageOverlap {
     }
 };
 
+// tailFrom > 0: bounces from it0 + tailFrom on run in one TailKernel launch.
 static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integrator, int grid,
                           int it0, int count, cudaStream_t stream, WaveProfile* prof, int* nl,
-                          bool sort, StageOverlap* ov) {
+                          bool sort, StageOverlap* ov, int tailFrom = 0) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     const int block = kTraceBlock;
     const int sgrid = ShadeGrid(grid);
@@ -1062,6 +1209,21 @@ static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integra
     for (int it = it0; it < it0 + count; it++) {
         // sorted bounces trace queue 0 and reorder the rays shade appends to queue 1 back into it
         const int cur = sort ? 0 : (it & 1);
+        if (tailFrom > 0 && it - it0 == tailFrom) {
+            if (pendingShadow) {  // the tail adds radiance the pending shadow stage also adds to
+                cudaStreamWaitEvent(stream, ov->join, 0);
+                pendingShadow = false;
+            }
+            const int left = it0 + count - it;
+            if (integrator == kPathTracing)
+                TailKernel<kPathTracing><<<grid, block, 0, stream>>>(jobs, wb, cur, left);
+            else if (integrator == kSimplePathTracing)
+                TailKernel<kSimplePathTracing><<<grid, block, 0, stream>>>(jobs, wb, cur, left);
+            else
+                TailKernel<-1><<<grid, block, 0, stream>>>(jobs, wb, cur, left);
+            *nl += 1;
+            break;
+        }
         if (ev) ev->Begin(1, stream);
         ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
         if (ev) {
@@ -1117,11 +1279,11 @@ struct WaveGraphKey {
     const void* jobs;
     const void* units;
     const void* buffers;
-    int capacity, iters, integrator, grid, sort, accum;
+    int capacity, iters, integrator, grid, sort, accum, tail;
     bool operator==(const WaveGraphKey& o) const {
         return jobs == o.jobs && units == o.units && buffers == o.buffers && capacity == o.capacity &&
                iters == o.iters && integrator == o.integrator && grid == o.grid && sort == o.sort &&
-               accum == o.accum;
+               accum == o.accum && tail == o.tail;
     }
 };
 struct WaveGraph {
@@ -1232,16 +1394,20 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     if (e != cudaSuccess) return e;
     int nl = 0;
     const bool sort = tune.sortRays != 0;
+    // the last bounces in one launch (fixed-depth waves; profiled renders keep every stage)
+    const int tailFrom = (!prof && !sort && tune.tailBounce > 0 && shape.iters > tune.tailBounce)
+                           ? tune.tailBounce : 0;
     // shadow stages beside the next extend, on the owner's side stream (not when profiling,
     // whose stage timers need one stream)
     StageOverlap* ov =
       (graphs && !prof && graphs->overlap[lane & 1].Ready()) ? &graphs->overlap[lane & 1] : nullptr;
     const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
-                           sort ? 1 : 0, accumulate ? 1 : 0};
+                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort, ov);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort, ov,
+                          tailFrom);
             if (accumulate) AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             *n += accumulate ? 2 : 1;
         };
@@ -1251,7 +1417,8 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             if (ev) ev->Begin(0, stream);
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
             if (ev) ev->End(0, stream);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort, ov);
+            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort, ov,
+                          tailFrom);
             if (accumulate) {
                 if (ev) ev->Begin(4, stream);
                 AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);

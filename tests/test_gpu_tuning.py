@@ -21,6 +21,8 @@ CONFIGS = [
     dict(blocks_per_sm=12, band_rows=1, use_graphs=1, wave_paths=3000),
     dict(sort_rays=1),
     dict(sort_rays=1, use_graphs=0, wave_paths=3000),
+    dict(tail_bounce=1),                                      # one launch from bounce 1 on
+    dict(tail_bounce=3, use_graphs=0, wave_paths=3000),
 ]
 
 
@@ -103,7 +105,8 @@ def test_autotune_picks_a_valid_configuration(tuned_ctx):
 def test_set_tuning_rejects_bad_values(tuned_ctx):
     ctx, _ = tuned_ctx
     for bad in (dict(blocks_per_sm=-1), dict(blocks_per_sm=65), dict(band_rows=-2),
-                dict(wave_paths=-5), dict(use_graphs=2), dict(sort_rays=3)):
+                dict(wave_paths=-5), dict(use_graphs=2), dict(sort_rays=3), dict(tail_bounce=-2),
+                dict(tail_bounce=65)):
         with pytest.raises(capi.PtError):
             ctx.set_tuning(**bad)
     ctx.set_tuning()
