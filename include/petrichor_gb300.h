@@ -77,6 +77,12 @@ extern "C" {
 #define PT_MODE_REPLAY 0    /* reproduces the reference's per-tile random stream: same film bits */
 #define PT_MODE_WAVEFRONT 1 /* throughput path: per-(pixel, sample) stream, same estimator */
 
+/* environment light sampling in the PathTracing integrator's next-event step */
+#define PT_ENV_SAMPLING_REFERENCE 0 /* the reference's tables (Environment.cpp:56-244) */
+#define PT_ENV_SAMPLING_ALIAS 1     /* opt-in, wavefront mode: alias table over the map's
+                                       texels (Math::AliasMethod); a different, unbiased
+                                       estimator, so the film differs from the reference's */
+
 typedef struct pt_context pt_context;
 typedef int32_t pt_scene_id;
 
@@ -152,7 +158,7 @@ typedef struct pt_settings {
                              not depend on it */
   int32_t denoising_spp;  /* numSppForDenoising: samples of the denoising AOV passes
                              (0 = the reference's default, 128) */
-  int32_t reserved;
+  int32_t env_sampling;   /* PT_ENV_SAMPLING_* (0, the reference's, when unset) */
 } pt_settings;
 
 typedef struct pt_scene_info {

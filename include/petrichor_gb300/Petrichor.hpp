@@ -67,6 +67,66 @@ inline Vector3f Cross(const Vector3f& a, const Vector3f& b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 
+// Math/AliasMethod.h:26-105: Walker's alias table over a discrete distribution, built
+// here with Vose's linear construction (M. D. Vose, IEEE TSE 17(9), 1991). Sample(r0,
+// r1) with r0, r1 uniform in [0, 1): column int(r0 n), then its own index when r1 is
+// below the column's threshold, else its alias. The wavefront path's optional
+// environment importance sampling (pt_settings.env_sampling) uses the same table.
+class AliasMethod {
+public:
+    template <class T>
+    void Construct(const std::vector<T>& distribution) {
+        std::vector<double> w(distribution.size());
+        for (size_t i = 0; i < w.size(); i++) w[i] = static_cast<double>(distribution[i]);
+        Build(w);
+    }
+    int Sample(float r0, float r1) const {
+        const int n = static_cast<int>(m_threshold.size());
+        int i = static_cast<int>(r0 * static_cast<float>(n));
+        i = i < 0 ? 0 : (i >= n ? n - 1 : i);
+        return r1 < m_threshold[i] ? i : m_alias[i];
+    }
+    // the table: per column the probability of keeping it, and its alias
+    const std::vector<float>& GetThresholds() const { return m_threshold; }
+    const std::vector<int32_t>& GetAliases() const { return m_alias; }
+    bool IsValid() const { return !m_threshold.empty(); }
+
+private:
+    void Build(const std::vector<double>& w) {
+        m_threshold.assign(w.size(), 1.0f);
+        m_alias.resize(w.size());
+        double total = 0.0;
+        for (double x : w) total += x > 0.0 ? x : 0.0;
+        if (w.empty() || !(total > 0.0)) {
+            m_threshold.clear();
+            m_alias.clear();
+            return;
+        }
+        const double n = static_cast<double>(w.size());
+        std::vector<double> p(w.size());
+        std::vector<int32_t> small, large;
+        for (size_t i = 0; i < w.size(); i++) {
+            m_alias[i] = static_cast<int32_t>(i);
+            p[i] = (w[i] > 0.0 ? w[i] : 0.0) * n / total;
+            (p[i] < 1.0 ? small : large).push_back(static_cast<int32_t>(i));
+        }
+        while (!small.empty() && !large.empty()) {
+            const int32_t s = small.back(), l = large.back();
+            small.pop_back();
+            m_threshold[s] = static_cast<float>(p[s]);
+            m_alias[s] = l;
+            p[l] = (p[l] + p[s]) - 1.0;
+            if (p[l] < 1.0) {
+                large.pop_back();
+                small.push_back(l);
+            }
+        }
+        // what is left (large columns, and small ones from rounding) keeps itself
+    }
+    std::vector<float> m_threshold;
+    std::vector<int32_t> m_alias;
+};
+
 }  // namespace Math
 
 using Color3f = Math::Vector3f;

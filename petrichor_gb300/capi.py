@@ -23,6 +23,7 @@ from .scene_io import Scene, INTEGRATOR_SIMPLE, INTEGRATOR_PT
 PT_OK = 0
 MODE_REPLAY = 0
 MODE_WAVEFRONT = 1
+ENV_SAMPLING_REFERENCE, ENV_SAMPLING_ALIAS = 0, 1
 AOV_UV, AOV_DENOISING_ALBEDO, AOV_DENOISING_NORMAL = 0, 1, 2
 
 _f3 = ctypes.c_float * 3
@@ -66,7 +67,7 @@ class PtSettings(ctypes.Structure):
                 ("tile_height", ctypes.c_int32), ("integrator", ctypes.c_int32),
                 ("mode", ctypes.c_int32), ("seed", ctypes.c_uint32),
                 ("wave_paths", ctypes.c_int32), ("denoising_spp", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("env_sampling", ctypes.c_int32)]
 
 
 class PtJob(ctypes.Structure):
@@ -249,6 +250,7 @@ def settings_from_scene(scene: Scene, mode: int = MODE_REPLAY, seed: int = 1, **
     st.seed = seed
     st.wave_paths = over.get("wave_paths", 0)
     st.denoising_spp = over.get("denoising_spp", 0)
+    st.env_sampling = over.get("env_sampling", ENV_SAMPLING_REFERENCE)
     return st
 
 

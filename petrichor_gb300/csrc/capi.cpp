@@ -4,6 +4,7 @@
 // here (camera basis, light area sum, environment row tables) are computed with
 // the reference's operation order so the replay path stays bit-exact.
 #include "petrichor_gb300.h"
+#include "petrichor_gb300/Petrichor.hpp"  // Math::AliasMethod
 
 #include <cuda_runtime.h>
 
@@ -241,6 +242,70 @@ WaveTables Tables(pt_context* ctx) {
     return t;
 }
 
+// Alias table of the optional environment sampler (PT_ENV_SAMPLING_ALIAS). Cell (ix, iy)
+// of the map is the region EnvColor fills by blending texels ix..ix+1 and iy..iy+1
+// (clamped at the last row and column). Its weight is the largest Rec. 709 luminance of
+// those four texels times sin theta at the cell centre (the area of the cell on the
+// sphere), so the table follows the radiance the cell can return. A map without
+// positive luminance falls back to sin theta alone. Stored per cell as {keep threshold,
+// alias index (bits), density over (u, v) = weight / mean weight, 0}. Built on the host
+// with Math::AliasMethod (Vose's construction) from the texels already on the device;
+// ctx->mu held.
+int EnsureEnvAlias(pt_context* ctx, SceneGpu& s) {
+    if (s.envAlias || !s.dev.envValid) return PT_OK;
+    const int W = s.dev.envW, H = s.dev.envH;
+    const size_t N = (size_t)W * H;
+    std::vector<float4> tex(N);
+    cudaError_t e = cudaMemcpyAsync(tex.data(), s.dev.env, N * sizeof(float4), cudaMemcpyDeviceToHost,
+                                    ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "environment read-back");
+    auto lum = [&](int x, int y) {
+        const float4 t = tex[(size_t)y * W + x];
+        const double l = 0.2126 * t.x + 0.7152 * t.y + 0.0722 * t.z;
+        return std::isfinite(l) && l > 0.0 ? l : 0.0;
+    };
+    std::vector<double> w(N);
+    double total = 0.0;
+    for (int pass = 0; pass < 2 && !(total > 0.0); pass++) {
+        total = 0.0;
+        for (int iy = 0; iy < H; iy++) {
+            const double sinT = std::sin(M_PI * (iy + 0.5) / H);
+            const int iy1 = std::min(iy + 1, H - 1);
+            for (int ix = 0; ix < W; ix++) {
+                const int ix1 = std::min(ix + 1, W - 1);
+                const double l = pass == 0 ? std::max(std::max(lum(ix, iy), lum(ix1, iy)),
+                                                      std::max(lum(ix, iy1), lum(ix1, iy1)))
+                                           : 1.0;
+                w[(size_t)iy * W + ix] = l * sinT;
+                total += l * sinT;
+            }
+        }
+    }
+    Petrichor::Math::AliasMethod am;
+    am.Construct(w);
+    if (!am.IsValid()) return Fail(ctx, PT_ERR_INVALID_ARG, "environment map has no sampling weight");
+    std::vector<float> thr = am.GetThresholds();
+    std::vector<int32_t> alias = am.GetAliases();
+    // a column of zero weight never keeps itself (leftovers of rounding keep threshold 1),
+    // so every drawn cell has a positive density
+    const size_t heaviest = (size_t)(std::max_element(w.begin(), w.end()) - w.begin());
+    for (size_t i = 0; i < N; i++)
+        if (!(w[i] > 0.0) && alias[i] == (int32_t)i) {
+            thr[i] = 0.0f;
+            alias[i] = (int32_t)heaviest;
+        }
+    std::vector<float4> table(N);
+    for (size_t i = 0; i < N; i++)
+        table[i] = F4(thr[i], IntBits(alias[i]), (float)(w[i] / total * (double)N), 0.0f);
+    const int rc = Upload(ctx, s, table, &s.envAlias);
+    if (rc != PT_OK) return rc;
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "environment alias upload");
+    s.info.device_bytes += s.buffers.back().bytes;
+    return PT_OK;
+}
+
 int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
               SceneGpu** out) {
     if (!ctx) return PT_ERR_INVALID_ARG;
@@ -256,10 +321,24 @@ int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt
     if (st->mode != PT_MODE_REPLAY && st->mode != PT_MODE_WAVEFRONT)
         return Fail(ctx, PT_ERR_INVALID_ARG, "unknown mode");
     if (st->wave_paths < 0) return Fail(ctx, PT_ERR_INVALID_ARG, "wave_paths must be >= 0");
+    if (st->env_sampling != PT_ENV_SAMPLING_REFERENCE && st->env_sampling != PT_ENV_SAMPLING_ALIAS)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "unknown env_sampling");
+    if (st->env_sampling == PT_ENV_SAMPLING_ALIAS && st->mode != PT_MODE_WAVEFRONT)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "the alias environment sampler is a wavefront-mode option");
     auto it = ctx->scenes.find(scene);
     if (it == ctx->scenes.end()) return Fail(ctx, PT_ERR_NOT_FOUND, "unknown scene id");
+    if (st->env_sampling == PT_ENV_SAMPLING_ALIAS) {
+        const int rc = EnsureEnvAlias(ctx, *it->second);
+        if (rc != PT_OK) return rc;
+    }
     *out = it->second.get();
     return PT_OK;
+}
+
+DevScene JobScene(const SceneGpu& s, const pt_settings* st) {
+    DevScene S = s.dev;
+    S.envAlias = st->env_sampling == PT_ENV_SAMPLING_ALIAS ? s.envAlias : nullptr;
+    return S;
 }
 
 DevCamera ToDev(const pt_camera* c) {
@@ -322,7 +401,7 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
         if (rc != PT_OK) return rc;
         if ((rc = EnsureTables(ctx, 1, (size_t)st->width * st->height)) != PT_OK) return rc;
         DevJob job{};
-        job.S = sg.dev;
+        job.S = JobScene(sg, st);
         job.C = C;
         job.st = S;
         job.accum = (float4*)ctx->accum.ptr;
@@ -872,7 +951,7 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     prof.devCounters = (unsigned long long*)counters.ptr;
     int launches = 0;
     DevJob job{};
-    job.S = sg->dev;
+    job.S = JobScene(*sg, st);
     job.C = ToDev(cam);
     job.st = ToDev(st);
     job.accum = (float4*)ctx->accum.ptr;
@@ -915,7 +994,7 @@ int pt_batch_render(pt_context* ctx, int32_t n, const pt_job* jobs, void* stream
         if (jobs[i].settings.mode != PT_MODE_WAVEFRONT)
             return Fail(ctx, PT_ERR_INVALID_ARG, "batched renders use the wavefront mode");
         if (!jobs[i].film_device) return Fail(ctx, PT_ERR_INVALID_ARG, "job film is NULL");
-        dj[i].S = sg->dev;
+        dj[i].S = JobScene(*sg, &jobs[i].settings);
         dj[i].C = ToDev(&jobs[i].camera);
         dj[i].st = ToDev(&jobs[i].settings);
         dj[i].film = jobs[i].film_device;

@@ -26,6 +26,9 @@ struct SceneGpu {
     std::vector<DeviceBuffer> buffers;
     pt_scene_info info{};
     std::atomic<int> refs{0};  // serving requests that use the scene
+    // alias table of the optional environment sampler, built at the first render that
+    // asks for it (owned by buffers)
+    const float4* envAlias = nullptr;
 };
 
 class Server;  // server.cpp
@@ -87,5 +90,8 @@ int CheckArgs(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt
               SceneGpu** out);
 DevCamera ToDev(const pt_camera* c);
 DevSettings ToDev(const pt_settings* s);
+// The scene as one job sees it: the environment alias table attached when the
+// settings ask for it (CheckArgs has built it).
+DevScene JobScene(const SceneGpu& s, const pt_settings* st);
 
 }  // namespace ptg

@@ -470,6 +470,41 @@ __device__ __forceinline__ float EnvPdf(const DevScene& S, V3 d) {
     return py * UnloadedTableBilinearX(u0, v0, S.envW, S.envH);
 }
 
+// Optional environment importance sampling from an alias table over the map's texels
+// (weights: the largest luminance of the texel's bilinear footprint times sin theta at
+// its centre, built at the first render that asks for it). A texel is drawn from
+// (r0, r1) and a point inside it from (j0, j1), uniform in (u, v): the density over
+// (u, v) is the texel's table pdf, which the reference's MIS formulas take as pdfuv
+// (PathTracing.cpp:282-327 convert it to solid angle with 2 pi^2 sin theta). Directions
+// map to (u, v) exactly as EnvColor reads the map. Out of line: a render without it
+// never runs this code.
+template <class M>
+__device__ __noinline__ V3 EnvSampleAlias(const DevScene& S, float r0, float r1, float j0, float j1,
+                                          float& pdfuv) {
+    const int W = S.envW, H = S.envH, N = W * H;
+    int i = (int)(r0 * (float)N);
+    i = min(max(i, 0), N - 1);
+    const float4 col = __ldg(S.envAlias + i);
+    const int t = r1 < col.x ? i : __float_as_int(col.y);
+    pdfuv = t == i ? col.z : __ldg(S.envAlias + t).z;
+    const int ix = t % W, iy = t / W;
+    const float u0 = ((float)ix + j0) / (float)W, v0 = ((float)iy + j1) / (float)H;
+    const float theta = v0 * kPi;
+    const float phi = 2.0f * kPi * (1.0f - u0) + S.envRot;
+    const float cx = M::SinCos(theta, phi), cy = M::SinSin(theta, phi), cz = M::Cos(theta);
+    return V3(cx, cy, cz);
+}
+template <class M>
+__device__ __noinline__ float EnvPdfAlias(const DevScene& S, V3 d) {
+    const float theta = M::Acos(d.z);
+    const float phi = M::Atan2(d.y, d.x);
+    const float u = Mod1(1.0f - (phi - S.envRot) * 0.5f * kInvPi);
+    const float v = Mod1(theta * kInvPi);
+    const int ix = min((int)(u * (float)S.envW), S.envW - 1);
+    const int iy = min((int)(v * (float)S.envH), S.envH - 1);
+    return __ldg(S.envAlias + (size_t)iy * S.envW + ix).z;
+}
+
 // ---------------------------------------------------------------- materials
 __device__ __forceinline__ V3 MatColor(const DevMaterial& m) { return V3(m.cr, m.cg, m.cb); }
 // GGX::GetF0 with metalness 0 and no map (GGX.h:126-139)

@@ -80,6 +80,10 @@ struct DevScene {
     const float4* env;
     const float4* texels;  // material texture maps, RGB_ rows, one after another
     const int4* texInfo;   // per texture: first texel, width, height, 0
+    // optional environment importance sampling (throughput path): per env texel
+    // {keep threshold, alias index (bits), pdf over (u, v), 0}; nullptr: the reference's
+    // sampler
+    const float4* envAlias;
     int32_t numNodes, numTris, numMats, numLights;
     int32_t envW, envH, envValid, stackDepth;  // stackDepth: max traversal stack entries
     float envBase[3], envRot;

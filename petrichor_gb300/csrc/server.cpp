@@ -393,7 +393,7 @@ private:
         for (Request* r : admitted) {
             DevJob& J = slotJobs_[r->slot];
             J = DevJob{};
-            J.S = r->scene->dev;
+            J.S = JobScene(*r->scene, &r->job.settings);
             J.C = ToDev(&r->job.camera);
             J.st = ToDev(&r->job.settings);
             J.accum = (float4*)((char*)arena_.ptr + r->accumOff);

@@ -520,6 +520,14 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
             float mis = 1.0f;
             if (k == 0) {
                 flags |= kFlagNoSignCheck;
+            } else if (S.envAlias) {
+                // alias sampler: densities in solid angle with the map's own sin theta; a
+                // bounce off glass (pdf 0) had no environment sample to share the weight
+                const float se = sqrtf(SMax(0.0f, 1.0f - d.z * d.z));
+                if (lastPdf > 0.0f && se > 0.0f) {
+                    const float pE = EnvPdfAlias<FastMath>(S, d) / (2.0f * kPi * kPi * se);
+                    mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
+                }
             } else if (S.envValid && d.x != 0 && d.y != 0 && lastSin > 0) {
                 const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
                 mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
@@ -554,9 +562,19 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                         float e0, e1;
                         rng.Next(e0, e1);
                         float pdfuv = 0.0f;
-                        const V3 sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
+                        V3 sd;
+                        float sn;  // sin theta of the (u, v) -> solid angle Jacobian
+                        if (S.envAlias) {
+                            float j0, j1;
+                            rng.Next(j0, j1);
+                            sd = EnvSampleAlias<FastMath>(S, e0, e1, j0, j1, pdfuv);
+                            sn = sqrtf(SMax(0.0f, 1.0f - sd.z * sd.z));
+                        } else {
+                            sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
+                        }
                         const float c = fabsf(Dot(sd, si.n));
-                        const float sn = sqrtf(SMax(0.0f, 1.0f - c * c));
+                        // the reference measures theta from the shading normal
+                        if (!S.envAlias) sn = sqrtf(SMax(0.0f, 1.0f - c * c));
                         const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, nb);
                         const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
                         const V3 li = EnvColor<FastMath>(S, sd);
