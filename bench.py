@@ -54,6 +54,9 @@ def parse():
                     help="serving loop: Poisson request stream, p50/p99 latency vs the plain path")
     ap.add_argument("--requests", type=int, default=100, help="requests per arrival rate (--serve)")
     ap.add_argument("--wave-paths", type=int, default=0, help="serving wave size (0: auto)")
+    ap.add_argument("--env-sampling", default="reference", choices=["reference", "alias"],
+                    help="environment next-event sampler: the reference's tables, or the opt-in "
+                         "alias table (a different, unbiased estimator)")
     return ap.parse_args()
 
 
@@ -80,6 +83,8 @@ def workload_name(args):
         name = WORKLOAD + ("_SMALL" if args.small else "")
     if args.width or args.height or args.spp:
         name += "_OVERRIDE"
+    if getattr(args, "env_sampling", "reference") == "alias":
+        name += "_ENV_ALIAS"
     return name
 
 
@@ -167,6 +172,10 @@ def run_reference_arm(args):
     from petrichor_gb300 import replicas
     rank, world, local = replicas.rank_world_local()
     if rank != 0:  # the reference arm runs once, on rank 0's host cores
+        return
+    if args.env_sampling == "alias":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no alias-table "
+                          "environment sampler (its AliasMethod is never called on the render path)"}))
         return
     scene = make_scene(args)
     import numpy as np
@@ -406,7 +415,9 @@ def main():
     upload_s = time.perf_counter() - t0
     info = ctx.scene_info(sid)
     cam = capi.camera_from_scene(scene)
-    sets = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=replicas.replica_seed(1, rank))
+    env = capi.ENV_SAMPLING_ALIAS if args.env_sampling == "alias" else capi.ENV_SAMPLING_REFERENCE
+    sets = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=replicas.replica_seed(1, rank),
+                                    env_sampling=env)
     npx = st.width * st.height
     samples_per_step = npx * st.spp
     film = torch.empty(npx * 3, dtype=torch.float32, device="cuda")
@@ -489,6 +500,7 @@ def main():
                    "triangles": info.num_triangles, "bvh_nodes": info.num_nodes,
                    "resolution": [st.width, st.height], "spp": st.spp, "max_bounces": st.max_bounces,
                    "env": list(scene.env.texture.shape[:2][::-1]), "mode": "wavefront",
+                   "env_sampling": args.env_sampling,
                    "parallelism": f"replicas{world}",
                    "l2": "working set > L2 (scene ~%.0f MB resident + wave state)" % (
                        info.device_bytes / 1e6),

@@ -16,9 +16,10 @@
 // are rendered by every pass, and LoadAssets attaches the "color_tex" and
 // "roughness_tex" maps of the JSON format.
 //
-// Differences, all additive: Petrichor::SetMode/SetIntegrator/SetSeed choose the
-// GB300 path (default: replay mode, SimplePathTracing, i.e. the reference's own
-// Render output bit for bit); Scene::SetRenderSetting sets settings without a
+// Differences, all additive: Petrichor::SetMode/SetIntegrator/SetSeed/SetEnvSampling
+// choose the GB300 path (default: replay mode, SimplePathTracing, the reference's
+// environment tables, i.e. the reference's own Render output bit for bit);
+// Scene::SetRenderSetting sets settings without a
 // file; Environment::SetTexture takes a texture from memory. The Rendered pass and
 // the UV / DenoisingAlbedo / DenoisingNormal AOV passes are produced for the
 // targets that are set, each equal to the reference's; only triangle geometry is
@@ -453,6 +454,9 @@ public:
     void SetMode(int mode) { m_mode = mode; }
     void SetIntegrator(int integrator) { m_integrator = integrator; }
     void SetSeed(uint32_t seed) { m_seed = seed; }
+    // Environment next-event sampling: PT_ENV_SAMPLING_REFERENCE, or PT_ENV_SAMPLING_ALIAS
+    // (wavefront mode; an alias table over the map, a different unbiased estimator).
+    void SetEnvSampling(int sampling) { m_envSampling = sampling; }
     // Status of the last Render (PT_OK or a PT_ERR_* code) and its message.
     int GetLastStatus() const { return m_lastStatus; }
     const std::string& GetLastError() const { return m_lastError; }
@@ -460,7 +464,7 @@ public:
 private:
     pt_context* m_ctx = nullptr;
     std::function<void(const RenderingResult&)> m_callback;
-    int m_mode = 0, m_integrator = 0;
+    int m_mode = 0, m_integrator = 0, m_envSampling = 0;
     uint32_t m_seed = 1;
     int m_lastStatus = 0;
     std::string m_lastError;

@@ -433,6 +433,7 @@ void Petrichor::Render(const Scene& scene) {
     st.integrator = m_integrator;
     st.mode = m_mode;
     st.seed = m_seed;
+    st.env_sampling = m_envSampling;
     st.denoising_spp = rs.numSppForDenoising;
     // the Rendered pass, then UV, DenoisingAlbedo and DenoisingNormal
     // (Petrichor.cpp:50-261), each at its own target's size

@@ -229,7 +229,7 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
 
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront | aov <spp>]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront | wavefront-alias | aov <spp>]\n", argv[0]);
         return 2;
     }
     try {
@@ -246,7 +246,9 @@ int main(int argc, char** argv) {
             }
         }
         Core::Petrichor renderer;
-        if (argc > 3 && std::string(argv[3]) == "wavefront") renderer.SetMode(PT_MODE_WAVEFRONT);
+        const std::string mode = argc > 3 ? argv[3] : "";
+        if (mode == "wavefront" || mode == "wavefront-alias") renderer.SetMode(PT_MODE_WAVEFRONT);
+        if (mode == "wavefront-alias") renderer.SetEnvSampling(PT_ENV_SAMPLING_ALIAS);
         renderer.SetIntegrator(app.integrator);
         float seconds = -1.0f;
         renderer.SetRenderCallback([&](const RenderingResult& r) { seconds = r.totalSec; });

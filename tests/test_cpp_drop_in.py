@@ -62,13 +62,15 @@ def test_drop_in_render_matches_reference_film(client, golden, tmp_path, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cornell_mixed_pt", "spheres_pt"])
-def test_drop_in_wavefront_equals_c_abi(client, golden, gpu_ctx, tmp_path, name):
+@pytest.mark.parametrize("name, mode", [("cornell_mixed_pt", "wavefront"), ("spheres_pt", "wavefront"),
+                                        ("spheres_pt", "wavefront-alias")])
+def test_drop_in_wavefront_equals_c_abi(client, golden, gpu_ctx, tmp_path, name, mode):
     from petrichor_gb300 import capi
-    r, film = _run(client, golden, name, tmp_path, "wavefront")
+    r, film = _run(client, golden, name, tmp_path, mode)
     assert r.returncode == 0, r.stdout + r.stderr
     sc = golden_scene(golden, name)
-    ref = capi.render_scene(sc, mode=capi.MODE_WAVEFRONT, seed=1, ctx=gpu_ctx)
+    env = capi.ENV_SAMPLING_ALIAS if mode == "wavefront-alias" else capi.ENV_SAMPLING_REFERENCE
+    ref = capi.render_scene(sc, mode=capi.MODE_WAVEFRONT, seed=1, ctx=gpu_ctx, env_sampling=env)
     got = np.fromfile(film, np.float32).reshape(ref.shape)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
 
