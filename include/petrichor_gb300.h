@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PT_ABI_VERSION 2
+#define PT_ABI_VERSION 3
 
 /* status codes */
 #define PT_OK 0
@@ -105,6 +105,8 @@ typedef struct pt_material {
   int32_t tex_normal;          /* GGX: tangent-space normal map */
   float roughness_strength;    /* GGX::SetRoughnessMap strength */
   float normal_strength;       /* GGX::SetNormalMap strength, clamped to [0, 1] */
+  int32_t uniform_sampling;    /* Lambert: 1 = MaterialBase::EnableImportanceSampling(false),
+                                  uniform hemisphere sampling; 0 = the default (cosine) */
 } pt_material;
 
 /* An RGB texture (Texture2D): height rows of width texels, sampled bilinearly

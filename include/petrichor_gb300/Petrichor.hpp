@@ -156,6 +156,13 @@ class MaterialBase {
 public:
     virtual ~MaterialBase() = default;
     virtual MaterialTypes GetMaterialType() const = 0;
+    // MaterialBase.h:52-62; Lambert reads it (off: uniform hemisphere sampling,
+    // Lambert.cpp:40-47,85-107), the other materials ignore it
+    void EnableImportanceSampling(bool isEnabled) { m_isImportanceSamplingEnabled = isEnabled; }
+    bool IsImportanceSamplingEnabled() const { return m_isImportanceSamplingEnabled; }
+
+private:
+    bool m_isImportanceSamplingEnabled = true;
 };
 
 class Texture2D;

@@ -138,6 +138,7 @@ struct Material {
     // texture maps (Scene::textures index or -1) and their strengths
     int albedoTex = -1, f0Tex = -1, roughTex = -1, normalTex = -1;
     float roughStrength = 1.0f, normalStrength = 1.0f;
+    bool uniform = false;  // MaterialBase::EnableImportanceSampling(false) (read by Lambert)
 };
 struct Ray {  // Core/Ray.h:42-48
     V3 o, dir;
@@ -652,7 +653,8 @@ static V3 BxDF(const Scene& s, int m, const Ray& in, const Ray& out, const Shadi
 static float PDF(const Scene& s, int m, const Ray& in, const Ray& out, const Shading& si) {
     const Material& M = s.mats[m];
     switch (M.kind) {
-    case kLambert:  // Lambert.cpp:33-47 (importance sampling on)
+    case kLambert:  // Lambert.cpp:33-47
+        if (M.uniform) return 0.5f * kInvPi;
         return std::abs(Dot(out.dir, si.normal)) * kInvPi;
     case kGlossy: {  // GGX.cpp:59-76
         const V3 h = Normalized(-in.dir + out.dir);
@@ -702,6 +704,20 @@ static Ray NextRay(const Scene& s, int m, const Ray& in, const Shading& si, Samp
         onb.Build(n);
         float r0, r1;
         s2.Next(&r0, &r1);
+        if (M.uniform) {  // Lambert.cpp:85-107
+            const float ct = r0;
+            const float st = (float)std::sqrt((double)(1.0f - ct * ct));
+            const float phi = 2.0f * kPi * r1;
+            const float cu = (float)((double)st * std::cos((double)phi));
+            const float cv = (float)((double)st * std::sin((double)phi));
+            out.o = si.pos + kEps * n;
+            out.dir = cu * onb.u + cv * onb.v + ct * onb.w;
+            out.T = in.T;
+            out.bounce = in.bounce + 1;
+            const V3 f = BxDF(s, m, in, out, si);
+            out.T = out.T * (f * ct / PDF(s, m, in, out, si));
+            return out;
+        }
         const float phi = 2.0f * kPi * r1;
         const float st = (float)std::sqrt((double)r0);
         const float cu = (float)((double)st * std::cos((double)phi));
@@ -1108,6 +1124,11 @@ static Scene* Parse(const void* data, size_t size) {
             b.take(t.px.data(), (size_t)t.W * t.H * 12);
             s->textures.push_back(std::move(t));
         }
+    }
+    if (b.off < b.n) {  // optional material-flag section: bit 0 = importance sampling off
+        const uint32_t NM = b.get<uint32_t>();
+        if (NM != s->mats.size()) throw std::runtime_error("material flag count");
+        for (uint32_t k = 0; k < NM; k++) s->mats[k].uniform = (b.get<uint32_t>() & 1u) != 0;
     }
     for (const Material& m : s->mats)
         for (int r : {m.albedoTex, m.f0Tex, m.roughTex, m.normalTex})

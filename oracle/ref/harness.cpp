@@ -263,6 +263,16 @@ static void Load(const std::string& path, const std::string& tmpPrefix, Loaded& 
             }
         }
     }
+    // optional per-material flags: bit 0 = MaterialBase::EnableImportanceSampling(false)
+    if (r.off < r.buf.size()) {
+        const uint32_t NM = r.get<uint32_t>();
+        if (NM != M) throw std::runtime_error("material flag count");
+        for (uint32_t k = 0; k < NM; k++) {
+            const bool off = (r.get<uint32_t>() & 1u) != 0;
+            if (lamberts[k]) lamberts[k]->EnableImportanceSampling(!off);
+            if (ggxs[k]) ggxs[k]->EnableImportanceSampling(!off);
+        }
+    }
 
     L.film = std::make_unique<Texture2D>(L.settings[0], L.settings[1]);
     L.scene->SetTargetTexture(Scene::AOVType::Rendered, L.film.get());

@@ -35,7 +35,7 @@ class PtMaterial(ctypes.Structure):
                 ("mat1", ctypes.c_int32), ("tex_albedo", ctypes.c_int32),
                 ("tex_f0", ctypes.c_int32), ("tex_roughness", ctypes.c_int32),
                 ("tex_normal", ctypes.c_int32), ("roughness_strength", ctypes.c_float),
-                ("normal_strength", ctypes.c_float)]
+                ("normal_strength", ctypes.c_float), ("uniform_sampling", ctypes.c_int32)]
 
 
 class PtTexture(ctypes.Structure):
@@ -312,6 +312,7 @@ class Context:
             mats[k].tex_normal = m.normal_tex + 1
             mats[k].roughness_strength = m.roughness_map_strength
             mats[k].normal_strength = m.normal_map_strength
+            mats[k].uniform_sampling = 0 if m.importance_sampling else 1
         texels = [np.ascontiguousarray(t, np.float32) for t in scene.textures]
         texs = (PtTexture * max(1, len(texels)))()
         for k, t in enumerate(texels):

@@ -642,6 +642,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         o.texRough = ggx ? M.tex_roughness - 1 : -1;
         o.texNormal = ggx ? M.tex_normal - 1 : -1;
         o.texMask = HasTextureMaps(M) ? 1 : 0;
+        o.uniform = M.uniform_sampling != 0 ? 1 : 0;
         o.roughStrength = M.roughness_strength;
         o.normalStrength = std::min(1.0f, std::max(0.0f, M.normal_strength));  // GGX::SetNormalMap
     }

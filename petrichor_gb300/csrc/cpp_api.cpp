@@ -312,6 +312,7 @@ void Petrichor::Render(const Scene& scene) {
             pm.kind = PT_MAT_LAMBERT;
             pm.color[0] = l->GetKd().x, pm.color[1] = l->GetKd().y, pm.color[2] = l->GetKd().z;
             pm.tex_albedo = addTexture(l->GetTexAlbedo());
+            pm.uniform_sampling = l->IsImportanceSamplingEnabled() ? 0 : 1;
             break;
         }
         case MaterialTypes::Glossy: {

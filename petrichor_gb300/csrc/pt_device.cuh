@@ -630,7 +630,7 @@ __device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) 
 // MaterialBase::PDF (Lambert.cpp:33-47, GGX.cpp:59-76, Glass.cpp:20-27)
 template <class M>
 __device__ __forceinline__ float BsdfPdf(const DevMaterial& m, V3 din, V3 dout, V3 n) {
-    if (m.kind == kLambert) return fabsf(Dot(dout, n)) * kInvPi;
+    if (m.kind == kLambert) return m.uniform ? 0.5f * kInvPi : fabsf(Dot(dout, n)) * kInvPi;
     if (m.kind == kGlossy) {
         const V3 h = M::Norm(-din + dout);
         const float hn = fabsf(Dot(h, n));
@@ -676,6 +676,20 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         onb.template Build<M>(n);
         float r0, r1;
         s2.Next(r0, r1);
+        if (m.uniform) {
+            // importance sampling off (Lambert.cpp:85-107): cos theta = r0, weight f cos / pdf
+            const float ct = r0;
+            const float st = sqrtf(1.0f - ct * ct);
+            const float phi = 2.0f * kPi * r1;
+            const float cu = M::MulCos(st, phi);
+            const float cv = M::MulSin(st, phi);
+            out.o = si.pos + kEps * n;
+            out.d = cu * onb.u + cv * onb.v + ct * onb.w;
+            const V3 f = BxDF<M>(m, in.d, out.d, n);
+            out.T = in.T * ((f * ct) / (0.5f * kInvPi));
+            out.bounce = in.bounce + 1;
+            return out;
+        }
         const float phi = 2.0f * kPi * r1;
         const float st = sqrtf(r0);
         const float cu = M::MulCos(st, phi);

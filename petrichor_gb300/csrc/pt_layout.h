@@ -51,7 +51,7 @@ enum MaterialKind : int32_t {
     kMix = 4,
 };
 
-struct DevMaterial {  // 64 B
+struct DevMaterial {  // 76 B
     int32_t kind;
     float cr, cg, cb;  // Lambert kd / GGX reflectance strength / Glass color / Emission radiance
     float alpha;       // GGX roughness^2 (GGX.cpp:16-20)
@@ -62,6 +62,7 @@ struct DevMaterial {  // 64 B
     int32_t texMask;   // 0: no texture maps (then the texture fields are unused)
     int32_t texAlbedo, texF0, texRough, texNormal;  // texture index or -1
     float roughStrength, normalStrength;             // GGX map strengths (normal clamped to [0, 1])
+    int32_t uniform;   // Lambert: importance sampling off (uniform hemisphere, Lambert.cpp:85-107)
 };
 
 struct DevCamera {  // derived Camera state (Core/Camera.h:121-130)

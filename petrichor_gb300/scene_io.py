@@ -60,6 +60,9 @@ class Material:
     normal_tex: int = -1
     roughness_map_strength: float = 1.0
     normal_map_strength: float = 1.0
+    # MaterialBase::EnableImportanceSampling (MaterialBase.h:52-62); only Lambert reads it
+    # (Lambert.cpp:40-47,66-107: off = uniform hemisphere sampling)
+    importance_sampling: bool = True
 
 
 @dataclasses.dataclass
@@ -184,12 +187,16 @@ def write_scene(path_or_buf, sc: Scene) -> None:
     L = sc.lights.shape[0]
     w(struct.pack("<I", L))
     w(np.ascontiguousarray(sc.lights, np.int32).tobytes())
-    if sc.textures:  # optional trailing section: material texture maps
+    flags = [0 if m.importance_sampling else 1 for m in sc.materials]
+    if sc.textures or any(flags):  # optional trailing section: material texture maps
         w(struct.pack("<I", len(sc.textures)))
         for t in sc.textures:
             t = np.ascontiguousarray(t, np.float32)
             w(struct.pack("<ii", t.shape[1], t.shape[0]))
             w(t.tobytes())
+    if any(flags):  # optional trailing section: per-material flags (bit 0: importance sampling off)
+        w(struct.pack("<I", len(flags)))
+        w(np.asarray(flags, np.uint32).tobytes())
     data = out.getvalue()
     if hasattr(path_or_buf, "write"):
         path_or_buf.write(data)
@@ -263,4 +270,10 @@ def read_scene_bytes(data: bytes) -> Scene:
         for _ in range(NT):
             tw, th = struct.unpack("<ii", take(8))
             textures.append(np.frombuffer(take(tw * th * 12), np.float32).reshape(th, tw, 3).copy())
+    if off < len(data):
+        (NM,) = struct.unpack("<I", take(4))
+        if NM != M:
+            raise ValueError("material flag count does not match the material table")
+        fl = np.frombuffer(take(4 * NM), np.uint32)
+        mats = [dataclasses.replace(m, importance_sampling=not bool(f & 1)) for m, f in zip(mats, fl)]
     return Scene(pos, nrm, uv, idx, tm, sh, lights, mats, cam, env, settings, textures)

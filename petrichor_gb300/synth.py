@@ -498,3 +498,17 @@ def request_stream(seed: int, rate: float, count: int, n_scenes: int = 8,
         depth = depth_lo + int(rng.one() * (depth_hi - depth_lo + 1))
         out.append((t, sc, w, h, spp, min(depth, depth_hi)))
     return out
+
+
+def uniform_lambert(scene: Scene, stride: int = 2) -> Scene:
+    """The scene with importance sampling switched off (MaterialBase::
+    EnableImportanceSampling(false): uniform hemisphere sampling) on every ``stride``-th
+    Lambert material, counted in material order."""
+    mats, k = [], 0
+    for m in scene.materials:
+        if m.kind == MAT_LAMBERT:
+            if k % stride == 0:
+                m = dataclasses.replace(m, importance_sampling=False)
+            k += 1
+        mats.append(m)
+    return dataclasses.replace(scene, materials=mats)

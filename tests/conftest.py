@@ -27,7 +27,8 @@ def golden_scene(golden, name):
 
 
 GOLDEN_CASES = ["cornell_simple", "cornell_mixed_simple", "cornell_mixed_pt", "cornell_lambert_pt",
-                "spheres_pt", "textured_pt", "textured_simple"]
+                "spheres_pt", "textured_pt", "textured_simple", "uniform_lambert_simple",
+                "uniform_lambert_pt"]
 AOV_CASES = ["aov_spheres", "aov_cornell_mixed", "aov_textured"]  # UV, denoising albedo, normal
 
 

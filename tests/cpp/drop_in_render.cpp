@@ -160,6 +160,11 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
                 throw std::runtime_error("cannot load " + path);
         }
     }
+    std::vector<uint32_t> flags(M, 0u);  // bit 0: importance sampling off
+    if (!r.AtEnd()) {
+        if (r.Get<uint32_t>() != M) throw std::runtime_error("material flag count");
+        r.Take(flags.data(), flags.size() * 4);
+    }
     // texture reference byte j of a material's int row: texture index + 1, 0 = none
     auto map = [&](int32_t refs, int j) -> const Texture2D* {
         const int r8 = (int)(((uint32_t)refs >> (8 * j)) & 0xffu);
@@ -175,6 +180,7 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
         case 0: {
             auto l = std::make_unique<Lambert>(V(f));
             if (map(refs, 0)) l->SetTexAlbedo(map(refs, 0));
+            if (flags[k] & 1u) l->EnableImportanceSampling(false);
             m = std::move(l);
             break;
         }

@@ -39,6 +39,10 @@ def cases():
                                           max_bounces=8, env_width=64, env_height=32),
         "textured_pt": synth.textured_spheres(integrator=1),
         "textured_simple": synth.textured_spheres(seed=6, integrator=0, spp=3),
+        "uniform_lambert_simple": synth.uniform_lambert(
+            synth.cornell(width=40, height=32, spp=8, mixed=True, env_texture=True)),
+        "uniform_lambert_pt": synth.uniform_lambert(
+            synth.cornell(width=40, height=40, spp=8, integrator=1, max_bounces=5), stride=1),
     }
 
 

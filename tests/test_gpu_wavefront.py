@@ -88,6 +88,11 @@ def _cases():
         # normal maps; the replay films cover them bit for bit.
         "textured_pt": _without_normal_maps(synth.textured_spheres(width=32, height=18, spp=1)),
         "textured_simple": synth.textured_spheres(width=32, height=18, spp=1, integrator=0),
+        # Lambert with importance sampling off (uniform hemisphere sampling)
+        "uniform_lambert_pt": synth.uniform_lambert(
+            synth.cornell(width=24, height=24, spp=1, integrator=1, max_bounces=5), stride=1),
+        "uniform_lambert_simple": synth.uniform_lambert(
+            synth.cornell(width=24, height=16, spp=1, mixed=True, env_texture=True)),
     }
 
 
