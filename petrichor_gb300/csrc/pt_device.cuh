@@ -676,28 +676,20 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         onb.template Build<M>(n);
         float r0, r1;
         s2.Next(r0, r1);
-        if (m.uniform) {
-            // importance sampling off (Lambert.cpp:85-107): cos theta = r0, weight f cos / pdf
-            const float ct = r0;
-            const float st = sqrtf(1.0f - ct * ct);
-            const float phi = 2.0f * kPi * r1;
-            const float cu = M::MulCos(st, phi);
-            const float cv = M::MulSin(st, phi);
-            out.o = si.pos + kEps * n;
-            out.d = cu * onb.u + cv * onb.v + ct * onb.w;
-            const V3 f = BxDF<M>(m, in.d, out.d, n);
-            out.T = in.T * ((f * ct) / (0.5f * kInvPi));
-            out.bounce = in.bounce + 1;
-            return out;
-        }
+        // importance sampling on: sin theta = sqrt(r0), cos theta = sqrt(1 - sin^2);
+        // off (Lambert.cpp:85-107): cos theta = r0, sin theta = sqrt(1 - r0^2), weight
+        // f cos / pdf. One body with selects keeps the shade step's code small.
+        const bool uni = m.uniform != 0;
         const float phi = 2.0f * kPi * r1;
-        const float st = sqrtf(r0);
+        const float st = sqrtf(uni ? 1.0f - r0 * r0 : r0);
         const float cu = M::MulCos(st, phi);
         const float cv = M::MulSin(st, phi);
-        const float cw = sqrtf(SMax(0.0f, 1.0f - st * st));  // >= 0 already with IEEE sqrt
+        const float cw = uni ? r0 : sqrtf(SMax(0.0f, 1.0f - st * st));  // >= 0 already with IEEE sqrt
         out.o = si.pos + kEps * n;
         out.d = cu * onb.u + cv * onb.v + cw * onb.w;
-        out.T = in.T * V3(m.ar, m.ag, m.ab);
+        V3 w(m.ar, m.ag, m.ab);
+        if (uni) w = (BxDF<M>(m, in.d, out.d, n) * cw) / (0.5f * kInvPi);
+        out.T = in.T * w;
         out.bounce = in.bounce + 1;
         return out;
     }

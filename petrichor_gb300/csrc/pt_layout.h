@@ -51,7 +51,7 @@ enum MaterialKind : int32_t {
     kMix = 4,
 };
 
-struct DevMaterial {  // 76 B
+struct __align__(16) DevMaterial {  // 80 B: whole-struct copies take 16-byte loads
     int32_t kind;
     float cr, cg, cb;  // Lambert kd / GGX reflectance strength / Glass color / Emission radiance
     float alpha;       // GGX roughness^2 (GGX.cpp:16-20)
@@ -63,6 +63,7 @@ struct DevMaterial {  // 76 B
     int32_t texAlbedo, texF0, texRough, texNormal;  // texture index or -1
     float roughStrength, normalStrength;             // GGX map strengths (normal clamped to [0, 1])
     int32_t uniform;   // Lambert: importance sampling off (uniform hemisphere, Lambert.cpp:85-107)
+    int32_t pad;
 };
 
 struct DevCamera {  // derived Camera state (Core/Camera.h:121-130)

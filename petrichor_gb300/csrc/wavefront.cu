@@ -669,6 +669,8 @@ __device__ __forceinline__ void ShadowRay(const DevScene& S, float4 e0, float4 e
     r.tmax = env ? kFltMax : e0.w + 0.05f;
 }
 
+__device__ __noinline__ void ApplyAreaLight(const DevScene& S, const float4* e, V3 o, V3 d, int best,
+                                            float tBest, int path, float4* pathL);
 // Adds a traced next-event entry's contribution to its path's radiance; e holds the
 // entry's four float4 (read only as needed: an occluded environment entry reads one).
 __device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, const LaneRay& r,
@@ -688,15 +690,21 @@ __device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, 
     }
     // area light: the closest hit must be an emitter at the sampled point
     if (r.best < 0) return;
+    ApplyAreaLight(S, e, r.o, r.d, r.best, r.tBest, path, pathL);
+}
+// The area-light part of ApplyShadow, out of line: it runs once per traced entry, and
+// inlined its registers crowd the traversal loop of the shadow kernel.
+__device__ __noinline__ void ApplyAreaLight(const DevScene& S, const float4* e, V3 o, V3 d, int best,
+                                            float tBest, int path, float4* pathL) {
     const float4 e0 = e[0], e2 = e[2], e3 = e[3];
-    const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, r.best), e3.w);
+    const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, best), e3.w);
     if (S.mats[m].kind != kEmission) return;
-    const Shading sl = Interpolate<FastMath>(S, r.best, r.o, r.d, r.tBest);
-    const V3 pl = r.o + r.d * e0.w;
+    const Shading sl = Interpolate<FastMath>(S, best, o, d, tBest);
+    const V3 pl = o + d * e0.w;
     if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
     const V3 sipos(e3.x, e3.y, e3.z);
     const float l2 = SqLen(sl.pos - sipos);
-    const float cosP = fabsf(Dot(r.d, sl.n));
+    const float cosP = fabsf(Dot(d, sl.n));
     const float pdfArea = S.lightPdfArea;
     float mis = 0.0f;
     if (l2 > 0.0f) {
