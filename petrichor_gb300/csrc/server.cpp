@@ -298,6 +298,7 @@ private:
     // One planned and enqueued wave: what it did, to retire once its event fires.
     struct InFlight {
         cudaEvent_t done = nullptr;
+        int64_t paths = 0;  // paths the wave traces (for the throughput estimate)
         std::vector<std::pair<Request*, int>> scheduled;  // request, samples in this wave
         std::vector<Request*> finishing;
         cudaError_t error = cudaSuccess;
@@ -354,20 +355,39 @@ private:
 
     // mu_ held. Packs the next sample blocks into a wave, least remaining work
     // first (short requests finish in the next wave; long ones take what is left).
+    // Under sustained load that order would keep postponing the longest requests: a
+    // request is overdue once it has waited kOverdueWaves waves plus kOverdueFactor
+    // times its own rendering time (its samples at the measured path rate), and the
+    // overdue ones, oldest first, are guaranteed kOverdueShare of every wave. Short
+    // requests finish long before that, so they keep the least-work order. Each request
+    // gets at most one sample block per wave.
     void Plan(std::vector<WaveUnit>* units, InFlight* w, int* paths, int* pixels) {
-        std::vector<Request*> order;
+        const double now = Now();
+        const double slack = kOverdueWaves * cfg_.wave_paths / pathRate_;
+        std::vector<Request*> fresh, overdue;
+        int64_t overdueWork = 0;
         for (uint64_t id : active_) {
             Request& r = *reqs_[id];
-            if (!r.cancel && r.scheduled < r.spp) order.push_back(&r);
+            if (r.cancel || r.scheduled >= r.spp) continue;
+            const double own = (double)r.spp * r.pixels / pathRate_;
+            if (now - r.submit > slack + kOverdueFactor * own) {
+                overdue.push_back(&r);
+                overdueWork += (int64_t)(r.spp - r.scheduled) * r.pixels;
+            } else {
+                fresh.push_back(&r);
+            }
         }
-        std::stable_sort(order.begin(), order.end(), [](const Request* a, const Request* b) {
-            return (int64_t)(a->spp - a->scheduled) * a->pixels <
-                   (int64_t)(b->spp - b->scheduled) * b->pixels;
+        std::stable_sort(fresh.begin(), fresh.end(), [](const Request* a, const Request* b) {
+            return (int64_t)(a->spp - a->scheduled) * a->pixels < (int64_t)(b->spp - b->scheduled) * b->pixels;
         });
+        std::stable_sort(overdue.begin(), overdue.end(),
+                         [](const Request* a, const Request* b) { return a->submit < b->submit; });
         const int cap = cfg_.wave_paths;
-        for (Request* r : order) {
-            const int room = (cap - *paths) / r->pixels;
-            if (room < 1 || (int)units->size() >= kMaxUnitsPerWave) continue;
+        const int reserve = (int)std::min<int64_t>((int64_t)(kOverdueShare * cap), overdueWork);
+        std::vector<char> placed(fresh.size(), 0);
+        auto place = [&](Request* r, int limit) {
+            const int room = (limit - *paths) / r->pixels;
+            if (room < 1 || (int)units->size() >= kMaxUnitsPerWave) return false;
             const int sw = std::min(r->spp - r->scheduled, room);
             WaveUnit u{};
             u.job = r->slot;
@@ -377,12 +397,18 @@ private:
             u.pixelBase = *pixels;
             units->push_back(u);
             *paths += r->pixels * sw;
+            w->paths += (int64_t)r->pixels * sw;
             *pixels += r->pixels;
             r->scheduled += sw;
             r->inFlight++;
             w->scheduled.push_back({r, sw});
             if (r->scheduled == r->spp) w->finishing.push_back(r);
-        }
+            return true;
+        };
+        for (size_t k = 0; k < fresh.size(); k++) placed[k] = place(fresh[k], cap - reserve);
+        for (Request* r : overdue) place(r, cap);
+        for (size_t k = 0; k < fresh.size(); k++)
+            if (!placed[k]) place(fresh[k], cap);
     }
 
     // ctx->mu held. Enqueues the admitted requests' job entries, the wave and the
@@ -446,6 +472,12 @@ private:
         if (e == cudaSuccess) e = cudaEventSynchronize(w.done);
         cudaEventDestroy(w.done);
         std::lock_guard<std::mutex> g(mu_);
+        // path rate from back-to-back retirements (the next wave is queued behind each
+        // one, so the gap is the GPU time of a wave), smoothed over a few waves
+        const double now = Now();
+        if (e == cudaSuccess && lastRetire_ > 0.0 && now > lastRetire_ && w.paths > (int64_t)1 << 20)
+            pathRate_ = 0.75 * pathRate_ + 0.25 * ((double)w.paths / (now - lastRetire_));
+        lastRetire_ = flight.empty() ? 0.0 : now;
         for (auto& [r, sw] : w.scheduled) {
             r->finished += sw;
             r->inFlight--;
@@ -518,6 +550,11 @@ private:
     std::vector<DevJob> slotJobs_;
     cudaStream_t stream_ = nullptr;
     Clock::time_point t0_;
+    static constexpr double kOverdueFactor = 1.0;
+    static constexpr double kOverdueWaves = 6.0;
+    static constexpr double kOverdueShare = 1.0;
+    double pathRate_ = 1.5e9;  // paths per second (measured, smoothed)
+    double lastRetire_ = 0.0;  // when the previous wave retired while another was queued
 };
 
 }  // namespace ptg

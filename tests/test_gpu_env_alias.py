@@ -136,3 +136,26 @@ def test_alias_sampling_rejects_bad_settings(gpu_ctx):
                                                               env_sampling=capi.ENV_SAMPLING_ALIAS))
     finally:
         gpu_ctx.release(sid)
+
+
+def test_alias_served_request_equals_render(lit):
+    _, sc, _, _, _, _, _, _ = lit
+    ctx = capi.Context()
+    try:
+        sid = ctx.upload(sc)
+        cam = capi.camera_from_scene(sc)
+        st = capi.settings_from_scene(sc, capi.MODE_WAVEFRONT, seed=9, spp=4,
+                                      env_sampling=capi.ENV_SAMPLING_ALIAS)
+        ref = ctx.render(sid, cam, st)
+        # small waves: the request spans several of them
+        ctx.serve_start(wave_paths=12000, max_active=4, state_budget=1 << 24)
+        try:
+            host = np.full((st.height, st.width, 3), np.nan, np.float32)
+            rid = ctx.serve_submit(sid, cam, st, film_host=host)
+            assert ctx.serve_wait(rid, 60).state == capi.REQ_DONE
+            assert np.array_equal(host.view(np.uint32), ref.view(np.uint32))
+        finally:
+            ctx.serve_stop()
+        ctx.release(sid)
+    finally:
+        ctx.close()
