@@ -472,23 +472,28 @@ __device__ __forceinline__ float EnvPdf(const DevScene& S, V3 d) {
 
 // Optional environment importance sampling from an alias table over the map's texels
 // (weights: the largest luminance of the texel's bilinear footprint times sin theta at
-// its centre, built at the first render that asks for it). A texel is drawn from
-// (r0, r1) and a point inside it from (j0, j1), uniform in (u, v): the density over
-// (u, v) is the texel's table pdf, which the reference's MIS formulas take as pdfuv
-// (PathTracing.cpp:282-327 convert it to solid angle with 2 pi^2 sin theta). Directions
-// map to (u, v) exactly as EnvColor reads the map. Out of line: a render without it
-// never runs this code.
+// its centre, built at the first render that asks for it). The table column is drawn
+// as a row from r0 and a column from j0 (a float holds 24 bits, too few to index the
+// 2^25 cells of an 8192x4096 map at once), kept or replaced by its alias by r1, and the
+// point inside the chosen cell is uniform in (u, v): the fraction of j0 W across, j1
+// down. The density over (u, v) is the cell's table pdf, which the reference's MIS
+// formulas take as pdfuv (PathTracing.cpp:282-327 convert it to solid angle with
+// 2 pi^2 sin theta). Directions map to (u, v) exactly as EnvColor reads the map. Out of
+// line: a render without it never runs this code.
 template <class M>
 __device__ __noinline__ V3 EnvSampleAlias(const DevScene& S, float r0, float r1, float j0, float j1,
                                           float& pdfuv) {
-    const int W = S.envW, H = S.envH, N = W * H;
-    int i = (int)(r0 * (float)N);
-    i = min(max(i, 0), N - 1);
+    const int W = S.envW, H = S.envH;
+    const int row = min(max((int)(r0 * (float)H), 0), H - 1);
+    const float x = j0 * (float)W;
+    const int column = min(max((int)x, 0), W - 1);
+    const float fx = fminf(fmaxf(x - (float)column, 0.0f), 1.0f);
+    const int i = row * W + column;
     const float4 col = __ldg(S.envAlias + i);
     const int t = r1 < col.x ? i : __float_as_int(col.y);
     pdfuv = t == i ? col.z : __ldg(S.envAlias + t).z;
     const int ix = t % W, iy = t / W;
-    const float u0 = ((float)ix + j0) / (float)W, v0 = ((float)iy + j1) / (float)H;
+    const float u0 = ((float)ix + fx) / (float)W, v0 = ((float)iy + j1) / (float)H;
     const float theta = v0 * kPi;
     const float phi = 2.0f * kPi * (1.0f - u0) + S.envRot;
     const float cx = M::SinCos(theta, phi), cy = M::SinSin(theta, phi), cz = M::Cos(theta);
