@@ -159,3 +159,17 @@ def test_alias_served_request_equals_render(lit):
         ctx.release(sid)
     finally:
         ctx.close()
+
+
+def test_alias_black_map_falls_back_to_area_weights(gpu_ctx):
+    # no positive luminance anywhere: the table weighs cells by their area (sin theta)
+    sc = _scene()
+    sc = dataclasses.replace(sc, env=dataclasses.replace(sc.env, texture=np.zeros_like(sc.env.texture)))
+    sid = gpu_ctx.upload(sc)
+    try:
+        a = _render(gpu_ctx, sid, sc, 3, 2, env_sampling=capi.ENV_SAMPLING_ALIAS)
+        r = _render(gpu_ctx, sid, sc, 3, 2)
+        assert np.isfinite(a).all()
+        assert float(a.max()) == 0.0 and float(r.max()) == 0.0  # a black sky lights nothing
+    finally:
+        gpu_ctx.release(sid)
