@@ -520,17 +520,19 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
             float mis = 1.0f;
             if (k == 0) {
                 flags |= kFlagNoSignCheck;
-            } else if (S.envAlias) {
+            } else {
                 // alias sampler: densities in solid angle with the map's own sin theta; a
-                // bounce off glass (pdf 0) had no environment sample to share the weight
-                const float se = sqrtf(SMax(0.0f, 1.0f - d.z * d.z));
-                if (lastPdf > 0.0f && se > 0.0f) {
-                    const float pE = EnvPdfAlias<FastMath>(S, d) / (2.0f * kPi * kPi * se);
+                // bounce off glass (pdf 0) had no environment sample to share the weight.
+                // One body for both samplers keeps the shade step's code small.
+                const bool alias = S.envAlias != nullptr;
+                const float sinT = alias ? sqrtf(SMax(0.0f, 1.0f - d.z * d.z)) : lastSin;
+                const bool weigh = alias ? (lastPdf > 0.0f && sinT > 0.0f)
+                                         : (S.envValid && d.x != 0 && d.y != 0 && lastSin > 0);
+                if (weigh) {
+                    const float pdfuv = alias ? EnvPdfAlias<FastMath>(S, d) : EnvPdf<FastMath>(S, d);
+                    const float pE = pdfuv / (2.0f * kPi * kPi * sinT);
                     mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
                 }
-            } else if (S.envValid && d.x != 0 && d.y != 0 && lastSin > 0) {
-                const float pE = EnvPdf<FastMath>(S, d) / (2.0f * kPi * kPi * lastSin);
-                mis = lastPdf * lastPdf / (pE * pE + lastPdf * lastPdf);
             }
             L = L + mis * in.T * EnvColor<FastMath>(S, d);
         } else {
@@ -563,18 +565,19 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                         rng.Next(e0, e1);
                         float pdfuv = 0.0f;
                         V3 sd;
-                        float sn;  // sin theta of the (u, v) -> solid angle Jacobian
-                        if (S.envAlias) {
+                        const bool alias = S.envAlias != nullptr;
+                        if (alias) {
                             float j0, j1;
                             rng.Next(j0, j1);
                             sd = EnvSampleAlias<FastMath>(S, e0, e1, j0, j1, pdfuv);
-                            sn = sqrtf(SMax(0.0f, 1.0f - sd.z * sd.z));
                         } else {
                             sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
                         }
                         const float c = fabsf(Dot(sd, si.n));
-                        // the reference measures theta from the shading normal
-                        if (!S.envAlias) sn = sqrtf(SMax(0.0f, 1.0f - c * c));
+                        // sin theta of the (u, v) -> solid angle Jacobian: the map's polar
+                        // angle (alias sampler), or the angle to the normal (the reference)
+                        const float zc = alias ? sd.z : c;
+                        const float sn = sqrtf(SMax(0.0f, 1.0f - zc * zc));
                         const float pB = 2.0f * kPi * kPi * sn * BsdfPdf<FastMath>(M, d, sd, nb);
                         const float mis = pdfuv * pdfuv / (pdfuv * pdfuv + pB * pB);
                         const V3 li = EnvColor<FastMath>(S, sd);
