@@ -8,7 +8,7 @@
  *
  * Reference interfaces replaced (paths relative to the Petrichor project):
  *   pt_render            Petrichor::Core::Petrichor::Render(const Scene&)
- *                        (LibPetrichor/Core/Petrichor.h:30-31, Petrichor.cpp:103-333)
+ *                        (LibPetrichor/Core/Petrichor.h:30-31, Petrichor.cpp:35-264)
  *   pt_scene_upload      what Render reads from Scene: GetGeometries/GetLights/
  *                        GetEnvironment/GetMaterial (LibPetrichor/Core/Scene.h:95-173)
  *                        plus BinnedSAHBVH::Build (Core/Accel/BinnedSAHBVH.cpp:15-225)
@@ -20,11 +20,11 @@
  *   pt_get_progress      Petrichor::GetNumRenderedTiles / GetNumTiles
  *                        (LibPetrichor/Core/Petrichor.h:41-51)
  *   pt_batch_render      repeated Petrichor::Render calls, one per scene and image
- *                        (LibPetrichor/Core/Petrichor.cpp:103-171): many images in shared waves
+ *                        (LibPetrichor/Core/Petrichor.cpp:35-102): many images in shared waves
  *   pt_serve_*           no reference counterpart: a resident render service (scenes
  *                        stay in HBM; requests are batched continuously)
  *   pt_render_profile    SCOPE_LOGGER timers around the render passes
- *                        (LibPetrichor/Core/Logger.h:63-94, used at Petrichor.cpp:106,124)
+ *                        (LibPetrichor/Core/Logger.h:63-94, used at Petrichor.cpp:37,58)
  *   pt_bvh_build         BinnedSAHBVH::Build alone, on the host, returning the tree
  *                        (LibPetrichor/Core/Accel/BinnedSAHBVH.cpp:15-225)
  *   pt_bvh_build_device  the same build on the GPU (the same tree, node for node)
@@ -381,6 +381,9 @@ int pt_get_tuning(pt_context* ctx, pt_tuning* out);
  * PT_ERR_INVALID_ARG. The first call on a device looks up the array's address;
  * make it before any stream capture. All calls share the array, so calls that
  * overlap on the GPU race. Enqueued on `stream` (NULL = the context's stream).
+ * pt_get_stats after this call waits for the render and reports its status word
+ * in last_device_status (0 = clean; kernel error bits otherwise) and its device
+ * time in last_render_ms; pt_get_progress reports all of its tiles once it has run.
  * No counterpart in the reference. */
 int pt_render_replay_noalloc(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
                              const pt_settings* settings, float* film_rgb_device, void* stream);

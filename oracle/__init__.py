@@ -34,9 +34,21 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(ref_root: str = "/root/reference", jobs: int = 8) -> Optional[str]:
+def reference_root() -> Optional[str]:
+    """Where the reference checkout lives: $PETRICHOR_REF, else a ``reference``
+    directory beside this repository; None when neither holds LibPetrichor."""
+    env = os.environ.get("PETRICHOR_REF")
+    cands = [env] if env else [os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "LibPetrichor")):
+            return c
+    return None
+
+
+def build_reference(ref_root: Optional[str] = None, jobs: int = 8) -> Optional[str]:
     """Compile the reference renderer's own sources + harness into oracle/_ref (if present)."""
-    if not os.path.isdir(os.path.join(ref_root, "LibPetrichor")):
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "LibPetrichor")):
         return None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}",
                            f"-j{jobs}"])

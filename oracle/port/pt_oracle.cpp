@@ -1185,7 +1185,7 @@ int oracle_bvh_dump(void* sp, float* bounds, int32_t* ints, int32_t* ids) {
 }
 
 // Render tiles [tileBegin, tileEnd) (tileEnd < 0: all) into film (W*H*3 floats) with
-// `threads` workers (0: hardware concurrency). Seeds as in Petrichor.cpp:141-146.
+// `threads` workers (0: hardware concurrency). Seeds as in Petrichor.cpp:72-77.
 // Returns render seconds (BVH built first if needed, not included), or -1 on error.
 double oracle_render(void* sp, float* film, int threads, int tileBegin, int tileEnd) {
     Scene& s = *(Scene*)sp;

@@ -4,9 +4,9 @@
 // (Scene::AppendGeometry/AppendLight/RegisterMaterial/SetMainCamera/
 // SetEnvironment/SetTargetTexture/LoadRenderSetting, Core/Scene.h:60-218) and
 // runs the reference code unchanged:
-//   film  : Petrichor::Render (SimplePathTracing, Core/Petrichor.cpp:103-171), or
+//   film  : Petrichor::Render (SimplePathTracing, Core/Petrichor.cpp:35-102), or
 //           for the MIS integrator the same tile loop with PathTracing
-//           (Core/Integrator/PathTracing.cpp:20-200), seeds as Petrichor.cpp:141-146
+//           (Core/Integrator/PathTracing.cpp:20-200), seeds as Petrichor.cpp:72-77
 //   hits  : Camera::GenerateRay + BinnedSAHBVH::Intersect for one ray per pixel,
 //           with the triangle index, distance and number of triangle tests
 //   bvh   : BinnedSAHBVH::Build, dumping its nodes and primitive order
@@ -289,7 +289,7 @@ static double Now() {
       .count();
 }
 
-// Rendered pass with PathTracing: the tile loop of Petrichor.cpp:129-165 with its seeds.
+// Rendered pass with PathTracing: the tile loop of Petrichor.cpp:62-95 with its seeds.
 static void RenderPathTracing(const Scene& scene, const AccelBase& accel, Texture2D* target) {
     PathTracing pt;
     const TileManager tm(target->GetWidth(), target->GetHeight(),
@@ -328,7 +328,7 @@ int main(int argc, char** argv) {
             if (L.integrator == 0) {
                 Core::Petrichor renderer;
                 t2 = Now();
-                renderer.Render(scene);  // rebuilds the BVH itself (Petrichor.cpp:110-114)
+                renderer.Render(scene);  // rebuilds the BVH itself (Petrichor.cpp:41-45)
                 t3 = Now();
             } else {
                 t2 = Now();

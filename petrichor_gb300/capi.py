@@ -3,7 +3,7 @@
 This is the host-side mirror of the reference's render call for Python users:
 ``Context.upload(scene)`` plays the part of filling a ``Petrichor::Core::Scene``
 and ``Context.render(...)`` the part of ``Petrichor::Render(scene)``
-(``LibPetrichor/Core/Petrichor.cpp:103-333``), writing a film with the layout of
+(``LibPetrichor/Core/Petrichor.cpp:35-264``), writing a film with the layout of
 ``Texture2D::GetRawDataPtr`` (row-major RGB float32).
 
 The library is built in-tree (``petrichor_gb300/_lib``); there is no fallback:

@@ -418,6 +418,7 @@ int RenderOnStream(pt_context* ctx, SceneGpu& sg, const pt_camera* cam, const pt
 }
 
 int FinishStats(pt_context* ctx, cudaStream_t stream) {
+    ctx->noallocPending = false;
     cudaError_t e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return CudaFail(ctx, e, "render");
     float ms = 0.0f;
@@ -1048,10 +1049,19 @@ int pt_render_replay_noalloc(pt_context* ctx, pt_scene_id scene, const pt_camera
     cudaError_t e = NoAllocScratch(&status, &stacks);
     if (e != cudaSuccess) return CudaFail(ctx, e, "no-allocation scratch lookup");
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    e = cudaMemsetAsync(status, 0, sizeof(int), s);  // status word starts at zero
+    ctx->noallocPending = false;
+    e = cudaEventRecord(ctx->ev0, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(int), s);  // status starts at zero
     if (e != cudaSuccess) return CudaFail(ctx, e, "status clear");
+    ctx->tilesTotal = (uint32_t)tiles;
+    ctx->tilesDone = 0;
     e = LaunchReplay(sg->dev, ToDev(cam), S, dFilm, stacks, status, 0, tiles, s);
     if (e != cudaSuccess) return CudaFail(ctx, e, "replay launch");
+    // pt_get_stats waits for this event, then reads the status word and the time
+    e = cudaEventRecord(ctx->ev1, s);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "cudaEventRecord");
+    ctx->noallocStatus = status;
+    ctx->noallocPending = true;
     ctx->stats.kernel_launches++;
     ctx->stats.renders++;
     return PT_OK;
@@ -1212,6 +1222,22 @@ int pt_set_bvh_builder(pt_context* ctx, int32_t builder) {
 int pt_get_stats(pt_context* ctx, pt_stats* out) {
     if (!ctx || !out) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> g(ctx->mu);
+    if (ctx->noallocPending) {
+        // the last render was a no-allocation one: wait for it, then read its status
+        // word from the fixed array (a 4-byte copy into host memory; nothing allocated)
+        int rc = SetDevice(ctx);
+        if (rc != PT_OK) return rc;
+        cudaError_t e = cudaEventSynchronize(ctx->ev1);
+        int status = 0;
+        if (e == cudaSuccess)
+            e = cudaMemcpy(&status, ctx->noallocStatus, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return CudaFail(ctx, e, "no-allocation render status");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) ctx->stats.last_render_ms = ms;
+        ctx->stats.last_device_status = status;
+        ctx->tilesDone = ctx->tilesTotal;
+        ctx->noallocPending = false;
+    }
     ctx->stats.device_bytes_in_use = ctx->used;
     *out = ctx->stats;
     return PT_OK;
@@ -1219,6 +1245,11 @@ int pt_get_stats(pt_context* ctx, pt_stats* out) {
 
 int pt_get_progress(pt_context* ctx, uint32_t* done, uint32_t* total) {
     if (!ctx || !done || !total) return PT_ERR_INVALID_ARG;
+    // a no-allocation render is one launch: all of its tiles are done once it has run
+    if (ctx->noallocPending && cudaEventQuery(ctx->ev1) == cudaSuccess) {
+        *done = *total = ctx->tilesTotal;
+        return PT_OK;
+    }
     *done = ctx->tilesDone;
     *total = ctx->tilesTotal;
     return PT_OK;

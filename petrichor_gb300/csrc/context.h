@@ -71,6 +71,10 @@ struct pt_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_stats stats{};
     uint32_t tilesDone = 0, tilesTotal = 0;
+    // status word of the last no-allocation replay render (inside the fixed device
+    // array), read back by pt_get_stats once ev1 has completed
+    int* noallocStatus = nullptr;
+    std::atomic<bool> noallocPending{false};
     std::unique_ptr<ptg::Server> server;
     // defined where ptg::Server is complete (server.cpp)
     pt_context();

@@ -475,8 +475,8 @@ __device__ __forceinline__ float EnvPdf(const DevScene& S, V3 d) {
 // its centre, built at the first render that asks for it). The table column is drawn
 // as a row from r0 and a column from j0 (a float holds 24 bits, too few to index the
 // 2^25 cells of an 8192x4096 map at once), kept or replaced by its alias by r1, and the
-// point inside the chosen cell is uniform in (u, v): the fraction of j0 W across, j1
-// down. The density over (u, v) is the cell's table pdf, which the reference's MIS
+// point inside the chosen cell is uniform in (u, v): r1 rescaled within its keep/alias
+// branch across, j1 down. The density over (u, v) is the cell's table pdf, which the reference's MIS
 // formulas take as pdfuv (PathTracing.cpp:282-327 convert it to solid angle with
 // 2 pi^2 sin theta). Directions map to (u, v) exactly as EnvColor reads the map. Out of
 // line: a render without it never runs this code.
@@ -485,12 +485,15 @@ __device__ __noinline__ V3 EnvSampleAlias(const DevScene& S, float r0, float r1,
                                           float& pdfuv) {
     const int W = S.envW, H = S.envH;
     const int row = min(max((int)(r0 * (float)H), 0), H - 1);
-    const float x = j0 * (float)W;
-    const int column = min(max((int)x, 0), W - 1);
-    const float fx = fminf(fmaxf(x - (float)column, 0.0f), 1.0f);
+    const int column = min(max((int)(j0 * (float)W), 0), W - 1);
     const int i = row * W + column;
     const float4 col = __ldg(S.envAlias + i);
-    const int t = r1 < col.x ? i : __float_as_int(col.y);
+    const bool keep = r1 < col.x;
+    const int t = keep ? i : __float_as_int(col.y);
+    // the offset across the cell: r1 rescaled to [0, 1) within the branch it took, which
+    // is uniform and independent of the cell chosen (j0's fraction after the column
+    // would keep only log2(W) fewer bits than a float's 24)
+    const float fx = fminf(fmaxf(keep ? r1 / col.x : (r1 - col.x) / (1.0f - col.x), 0.0f), 0.99999994f);
     pdfuv = t == i ? col.z : __ldg(S.envAlias + t).z;
     const int ix = t % W, iy = t / W;
     const float u0 = ((float)ix + fx) / (float)W, v0 = ((float)iy + j1) / (float)H;

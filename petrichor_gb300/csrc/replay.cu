@@ -1,7 +1,7 @@
 // Replay kernel: reproduces the reference renderer's film bit for bit.
 //
 // The reference draws its random numbers from one XorShift stream per 16x16
-// tile, visiting the tile's pixels row-major (Core/Petrichor.cpp:129-165), so a
+// tile, visiting the tile's pixels row-major (Core/Petrichor.cpp:79-91), so a
 // pixel's samples depend on every earlier pixel of its tile. This kernel runs
 // one thread per tile with that stream, the reference's BVH traversal order and
 // the reference's arithmetic (ExactMath, built with -fmad=false). It is the

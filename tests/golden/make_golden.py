@@ -1,13 +1,13 @@
 """Generates tests/golden/golden.npz from the reference renderer itself.
 
-Run in a checkout where the reference sources are available (default
-/root/reference): the reference's LibPetrichor is compiled unchanged by
+Run in a checkout where the reference sources are available ($PETRICHOR_REF, or
+a ``reference`` directory beside this repository): the reference's LibPetrichor is compiled unchanged by
 oracle/ref/Makefile (with the project's stand-ins for its absent third-party
 libraries) and driven by oracle/ref/harness.cpp through its public C++ API.
 Each case stores the scene bytes it was rendered from, so the fixtures do not
 depend on regenerating identical scenes elsewhere.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference checkout>]
 """
 from __future__ import annotations
 
@@ -60,8 +60,10 @@ def aov_cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="reference checkout (default: $PETRICHOR_REF, else ../reference)")
     args = ap.parse_args()
+    args.ref = args.ref or oracle.reference_root() or "(not found)"
     if oracle.build_reference(args.ref) is None:
         raise SystemExit(f"reference sources not found under {args.ref}")
     work = os.path.join(ROOT, "oracle", "_ref", "work")
