@@ -74,6 +74,8 @@ def lib():
         L.oracle_num_tiles.argtypes = [vp]
         L.oracle_render_decorrelated.restype = ctypes.c_double
         L.oracle_render_decorrelated.argtypes = [vp, f32p, i32, ctypes.c_uint32]
+        L.oracle_render_tiles_decorrelated.restype = ctypes.c_double
+        L.oracle_render_tiles_decorrelated.argtypes = [vp, f32p, i32, i32p, i32, ctypes.c_uint32]
         L.oracle_render_tiles.restype = ctypes.c_double
         L.oracle_render_tiles.argtypes = [vp, f32p, i32, i32p, i32]
         L.oracle_hits.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, f32p, i32p]
@@ -160,6 +162,26 @@ class OracleScene:
             h = s.tile_height if j != ny else s.height - ny * s.tile_height
             px += w * h
         return film, secs, px
+
+    def render_tiles_decorrelated(self, tiles, seed: int, threads: int = 0):
+        """The listed tiles with independent per-tile random streams (seeded as in
+        render_decorrelated); returns (film, seconds)."""
+        s = self.scene.settings
+        film = np.zeros((s.height, s.width, 3), np.float32)
+        t = np.ascontiguousarray(tiles, np.int32)
+        secs = lib().oracle_render_tiles_decorrelated(self._h, _fp(film), threads, _ip(t), t.size,
+                                                      seed)
+        return film, secs
+
+    def tile_mask(self, tiles) -> np.ndarray:
+        """Boolean (H, W) mask of the pixels of the listed tiles."""
+        s = self.scene.settings
+        m = np.zeros((s.height, s.width), bool)
+        nx = s.width // s.tile_width
+        for k in np.asarray(tiles).ravel():
+            i, j = int(k) % (nx + 1), int(k) // (nx + 1)
+            m[j * s.tile_height:(j + 1) * s.tile_height, i * s.tile_width:(i + 1) * s.tile_width] = True
+        return m
 
     def hits(self, seed_a: int = 7, seed_b: int = 11):
         s = self.scene.settings

@@ -1335,6 +1335,47 @@ double oracle_render_decorrelated(void* sp, float* film, int threads, uint32_t s
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// The listed tiles only, with the decorrelated generators of
+// oracle_render_decorrelated (tile t seeded as there), so replicates over a sample
+// of tiles are independent of each other and of the pixels outside the sample.
+double oracle_render_tiles_decorrelated(void* sp, float* film, int threads, const int32_t* list,
+                                        int n, uint32_t seed) {
+    Scene& s = *(Scene*)sp;
+    if (!s.built) BuildBVH(s);
+    const int nx = s.W / s.tileW, ny = s.H / s.tileH;
+    const int remW = s.W - nx * s.tileW, remH = s.H - ny * s.tileH;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next(0);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= n) break;
+            const int t = list[k], i = t % (nx + 1), j = t / (nx + 1);
+            if (j > ny) continue;
+            const int x0 = i * s.tileW, y0 = j * s.tileH;
+            const int w = i != nx ? s.tileW : remW, h = j != ny ? s.tileH : remH;
+            Sampler1D s1(HashU32(HashU32(seed) ^ (uint32_t)(3 * t)));
+            Sampler2D s2(HashU32(HashU32(seed) ^ (uint32_t)(3 * t + 1)),
+                         HashU32(HashU32(seed) ^ (uint32_t)(3 * t + 2)));
+            for (int m = 0; m < 64; m++) {
+                s1.Next();
+                float a, b;
+                s2.Next(&a, &b);
+            }
+            for (int y = y0; y < y0 + h; y++)
+                for (int x = x0; x < x0 + w; x++) {
+                    if (s.integrator == 0) RenderSimple(s, x, y, film, s1, s2);
+                    else RenderPT(s, x, y, film, s1, s2);
+                }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 0; i < threads; i++) pool.emplace_back(work);
+    for (auto& th : pool) th.join();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 // Number of tiles of the film (TileManager.cpp:8-43).
 int oracle_num_tiles(void* sp) {
     Scene& s = *(Scene*)sp;

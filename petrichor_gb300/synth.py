@@ -465,18 +465,70 @@ def batch_instances(seed: int = 3, n: int = 64, tri_lo: float = 1e4, tri_hi: flo
     return out
 
 
+def _map_texture(seed: int, size: int) -> np.ndarray:
+    """A procedural RGB material map in [0.05, 0.95]: a product of sinusoids times a
+    bilinear value-noise field on a 64x64 lattice (seeded), (size, size, 3) float32."""
+    rng = Rng(seed)
+    f = rng.uniform(4, 2.0, 9.0)
+    x = (np.arange(size, dtype=np.float32) + 0.5) / size
+    wave = 0.5 + 0.5 * np.sin(np.float32(f[0] * 2 * math.pi) * x)[None, :] * \
+        np.cos(np.float32(f[1] * 2 * math.pi) * x)[:, None]
+    lat = rng.uniform(65 * 65).astype(np.float32).reshape(65, 65)
+    g = x * 64.0
+    i0 = np.minimum(g.astype(np.int32), 63)
+    w1 = (g - i0).astype(np.float32)
+    rows = lat[i0] * (1 - w1)[:, None] + lat[i0 + 1] * w1[:, None]          # (size, 65)
+    noise = rows[:, i0] * (1 - w1)[None, :] + rows[:, i0 + 1] * w1[None, :]  # (size, size)
+    v = (0.05 + 0.6 * wave + 0.3 * noise).astype(np.float32)
+    tint = np.array([1.0, 0.8, 0.6], np.float32)
+    return np.clip(v[..., None] * tint, 0.05, 0.95).astype(np.float32)
+
+
 def serving_scenes(seed: int = 4, n: int = 8, tri_lo: float = 1e5, tri_hi: float = 4e6,
-                   env_width: int = 8192, env_height: int = 4096):
+                   env_width: int = 8192, env_height: int = 4096, map_size: int = 4096,
+                   maps_per_scene: int = 3):
     """``n`` resident scenes for the serving workload, triangle counts spread
-    log-uniformly over [tri_lo, tri_hi] (first and last at the ends)."""
-    # one procedural sky, uploaded as each scene's own texture
+    log-uniformly over [tri_lo, tri_hi] (first and last at the ends). Each scene has
+    its own sky (the procedural sky turned about +Z by a per-scene azimuth, so the sun
+    stands elsewhere) and ``maps_per_scene`` material maps of ``map_size``^2 texels
+    (Lambert albedo maps; GGX reflectance and roughness maps), each its own variant of
+    one procedural map (shifted and tinted). At the defaults that is about 12 GB of
+    BVH, triangles, skies and maps resident on the device."""
     sky = sky_env(Rng(seed), env_width, env_height)
+    base_map = _map_texture(seed + 77, map_size) if maps_per_scene > 0 else None
     out = []
     for k in range(n):
         f = k / max(1, n - 1)
         tris = int(math.exp(math.log(tri_lo) + f * (math.log(tri_hi) - math.log(tri_lo))))
-        out.append(spheres_grids(seed=2000 + k + seed, tri_budget=tris, width=64, height=64,
-                                 spp=1, env_texture=sky))
+        rng = Rng(3000 + k + seed)
+        env_k = np.roll(sky, (k * env_width) // n, axis=1)
+        sc = spheres_grids(seed=2000 + k + seed, tri_budget=tris, width=64, height=64, spp=1,
+                           env_texture=env_k)
+        if maps_per_scene <= 0:
+            out.append(sc)
+            continue
+        textures = []
+        for m in range(maps_per_scene):
+            sh = (int(rng.one() * map_size), int(rng.one() * map_size))
+            tint = rng.uniform(3, 0.6, 1.0).astype(np.float32)
+            textures.append(np.roll(base_map, sh, axis=(0, 1)) * tint)
+        mats = []
+        for mat in sc.materials:
+            mat = dataclasses.replace(mat)
+            if mat.kind == MAT_LAMBERT:
+                mat.albedo_tex = int(rng.one() * maps_per_scene) % maps_per_scene
+            elif mat.kind == MAT_GLOSSY:
+                if rng.one() < 0.5:
+                    mat.f0_tex = int(rng.one() * maps_per_scene) % maps_per_scene
+                if rng.one() < 0.5:
+                    mat.roughness_tex = int(rng.one() * maps_per_scene) % maps_per_scene
+                    mat.roughness_map_strength = rng.one(0.5, 1.2)
+            mats.append(mat)
+        uv = sc.uvs.copy()
+        flat = ~np.any(uv != 0.0, axis=1)  # grids: planar uvs
+        uv[flat, 0] = 0.37 * sc.positions[flat, 0]
+        uv[flat, 1] = 0.29 * sc.positions[flat, 1]
+        out.append(sc.copy_with(materials=mats, uvs=uv.astype(np.float32), textures=textures))
     return out
 
 

@@ -10,7 +10,12 @@
 // raw float32 RGB rows.
 //
 //   drop_in_render <scene.ptscene> <film.bin> [wavefront | aov <denoising spp>]
+//   drop_in_render <scene.ptscene> <film.bin> wavefront --repeat K
 //
+// With --repeat the scene is built once and Petrichor::Render is called 1 + K times
+// (the first call is a warm-up); the output line lists the wall seconds of the K
+// timed calls. Each call does what an application's call does: flatten the scene,
+// upload it, build its BVH, render, copy the film back and release the scene.
 // Without "wavefront" the renderer keeps its defaults (replay mode with
 // SimplePathTracing: the reference's own Render output). With "aov" the UV,
 // DenoisingAlbedo and DenoisingNormal targets are set too, and the file holds the
@@ -19,6 +24,7 @@
 #include <petrichor_gb300/Petrichor.hpp>
 #include <petrichor_gb300.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -235,7 +241,7 @@ void BuildScene(const std::string& path, const std::string& scratch, App& app) {
 
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront | wavefront-alias | aov <spp>]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <scene.ptscene> <film.bin> [wavefront | wavefront-alias | aov <spp>] [--repeat K]\n", argv[0]);
         return 2;
     }
     try {
@@ -258,10 +264,22 @@ int main(int argc, char** argv) {
         renderer.SetIntegrator(app.integrator);
         float seconds = -1.0f;
         renderer.SetRenderCallback([&](const RenderingResult& r) { seconds = r.totalSec; });
-        renderer.Render(app.scene);
-        std::printf("{\"status\": %d, \"tiles\": [%u, %u], \"seconds\": %.6f}\n",
+        int repeat = 0;
+        for (int a = 3; a + 1 < argc; a++)
+            if (std::string(argv[a]) == "--repeat") repeat = std::stoi(argv[a + 1]);
+        std::vector<double> calls;
+        for (int k = 0; k <= repeat; k++) {
+            const auto t0 = std::chrono::steady_clock::now();
+            renderer.Render(app.scene);
+            const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (k > 0) calls.push_back(dt);
+            if (renderer.GetLastStatus() != PT_OK) break;
+        }
+        std::printf("{\"status\": %d, \"tiles\": [%u, %u], \"seconds\": %.6f, \"call_seconds\": [",
                     renderer.GetLastStatus(), renderer.GetNumRenderedTiles(),
                     renderer.GetNumTiles(), seconds);
+        for (size_t k = 0; k < calls.size(); k++) std::printf("%s%.6f", k ? ", " : "", calls[k]);
+        std::printf("]}\n");
         if (renderer.GetLastStatus() != PT_OK) {
             std::fprintf(stderr, "render failed: %s\n", renderer.GetLastError().c_str());
             return 3;
