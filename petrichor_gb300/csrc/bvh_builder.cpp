@@ -229,6 +229,11 @@ struct WideCollapser {
     std::vector<float>& out;  // WideNodeFloats(K) floats per wide node
     const int K;
     bool ok = true;
+    // Child boxes are widened by eps on every side (eps = 2^-18 of the scene's largest
+    // coordinate magnitude). The slab test's rounding (a few ulps of the plane distance)
+    // then can never cut off a ray that meets a triangle inside: the traversal reports
+    // every triangle the triangle test accepts, as a test of all triangles would.
+    float eps = 0.0f;
 
     static float Area(const BvhNodeOut& n) {
         const float dx = n.hi[0] - n.lo[0], dy = n.hi[1] - n.lo[1], dz = n.hi[2] - n.lo[2];
@@ -245,8 +250,8 @@ struct WideCollapser {
     void SetChild(int w, int i, const float* lo, const float* hi, int32_t code) {
         float* f = &out[(size_t)w * WideNodeFloats(K)];
         for (int a = 0; a < 3; a++) {
-            f[K * a + i] = lo[a];
-            f[K * (3 + a) + i] = hi[a];
+            f[K * a + i] = lo[a] - eps;
+            f[K * (3 + a) + i] = hi[a] + eps;
         }
         std::memcpy(&f[6 * K + i], &code, 4);
     }
@@ -311,6 +316,9 @@ bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width) {
     if (width < 2 || width > 8) return false;
     WideCollapser c{bvh, *wide, width};
     const BvhNodeOut& root = bvh.nodes[0];
+    float m = 0.0f;
+    for (int a = 0; a < 3; a++) m = std::max(m, std::max(std::fabs(root.lo[a]), std::fabs(root.hi[a])));
+    c.eps = std::ldexp(std::max(m, 1e-30f), -18);
     if (root.leaf) {  // the root itself is a leaf: a wide root with that one leaf child
         const int w = c.NewNode();
         c.SetChild(w, 0, root.lo, root.hi, c.Leaf(root));

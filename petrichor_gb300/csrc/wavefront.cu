@@ -85,7 +85,7 @@ constexpr int kRefillLanes = PT_REFILL_LANES;
 struct LaneRay {
     V3 o, d, inv;
     float tmin, tmax, tBest;
-    int best;
+    int best;  // slot of the closest hit; -1 none; -2 - slot when another hit tied it
     bool anyHit;
     const float4* nodes;  // the lane's 4-wide tree (rays of different jobs share a warp)
     const float4* tris;
@@ -171,10 +171,14 @@ __device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur, 
         V3 v0, e1, e2;
         LoadTri(r.tris, k, v0, e1, e2);
         float t;
-        if (TriIntersect(v0, e1, e2, r.o, r.d, t) && t >= r.tmin && t <= r.tmax && t < r.tBest) {
-            r.tBest = t;
-            r.best = k;
-            if (r.anyHit) return true;
+        if (TriIntersect(v0, e1, e2, r.o, r.d, t) && t >= r.tmin && t <= r.tmax) {
+            if (t < r.tBest) {
+                r.tBest = t;
+                r.best = k;
+                if (r.anyHit) return true;
+            } else if (t == r.tBest && r.best >= 0) {
+                r.best = -2 - r.best;  // an exact tie: settled by the reference's order
+            }
         }
     }
     cur = stk.Pop(r.tBest);
@@ -254,6 +258,28 @@ __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur,
     for (int i = K - 1; i >= 1; i--)
         if (t[i] != inf) stk.Push(c[i], t[i]);
     cur = c[0];
+}
+
+// Exact distance ties. Which of two triangles at the same distance a closest-hit query
+// reports depends on the order they are tested in, and the wide traversal tests them
+// in another order than the reference's binary traversal. When a ray's closest
+// distance was reached by more than one triangle, the reference's own traversal
+// (BinnedSAHBVH::Intersect order) is run for it and its answer taken, so closest hits
+// are the reference's, ties included. Out of line where it can be: ties are rare.
+__device__ __forceinline__ void ResolveTieInline(const DevScene* S, V3 o, V3 d, float tmin,
+                                                 float tmax, int* best, float* tBest) {
+    int stack[kWaveStackDepth];
+    int status = 0;
+    float bd;
+    const int b = TraverseReference<false>(*S, o, d, tmin, tmax, bd, stack, &status);
+    if (b >= 0 && status == 0) {
+        *best = b;
+        *tBest = bd;
+    }
+}
+__device__ __noinline__ void ResolveTie(const DevScene* S, V3 o, V3 d, float tmin, float tmax,
+                                        int* best, float* tBest) {
+    ResolveTieInline(S, o, d, tmin, tmax, best, tBest);
 }
 
 // Q provides: void Load(int i, LaneRay&) (ray, range, and the scene: nodes = nullptr
@@ -396,6 +422,8 @@ struct ExtendQueue {
         r.numTris = J.S.numTris;
 #endif
     }
+    // a tied hit is stored as -2 - slot; the shade kernel settles it (SettleTie), which
+    // keeps the reference traversal out of this kernel's registers
     __device__ void Finish(int i, const LaneRay& r) const {
         hit[i] = make_float2(r.tBest, __int_as_float(r.best));
     }
@@ -630,6 +658,17 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
     sink.Done(cont, out, lastPdf, lastSin, flags, L);
 }
 
+// A closest hit the extend stage stored as tied (-2 - slot): the reference's answer
+// for that ray (ResolveTie), with the extend query's range.
+__device__ __noinline__ float2 SettleTie(const DevJob& J, V3 o, V3 d, float2 h) {
+    int best = -2 - __float_as_int(h.y);
+    float tb = h.x;
+    // SimplePathTracing intersects with distMin = kEps, PathTracing with 0 (as ExtendQueue)
+    ResolveTie(&J.S, o, d, J.st.integrator == kSimplePathTracing ? kEps : 0.0f, kFltMax, &best,
+               &tb);
+    return make_float2(tb, __int_as_float(best));
+}
+
 template <int kInteg>
 __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                    int cur) {
@@ -639,9 +678,10 @@ __global__ void __launch_bounds__(128, PT_SHADE_MIN_BLOCKS) ShadeKernel(const De
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[4] = 0;  // the next extend fetches from zero
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 ra = wb.ray[cur][2 * i], rb = wb.ray[cur][2 * i + 1];
-        const float2 h = wb.hit[i];
+        float2 h = wb.hit[i];
         const int path = __float_as_int(ra.w);
         const DevJob& J = jobs[JobOf(wb.pathJob, sole, path)];
+        if (__float_as_int(h.y) < -1) h = SettleTie(J, V3(ra.x, ra.y, ra.z), V3(rb.x, rb.y, rb.z), h);
 #if PT_CHECK
         if (__float_as_int(h.y) >= J.S.numTris || (unsigned)path >= (unsigned)wb.capacity) {
             atomicOr(wb.counts + 3, kErrBounds);
@@ -682,7 +722,7 @@ __device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, 
     const int tag = __float_as_int(e1.w);
     const int path = tag & 0x7FFFFFFF;
     if (tag >= 0) {  // environment: adds when unoccluded
-        if (r.best >= 0) return;
+        if (r.best != -1) return;
         const float4 e2 = e[2];
         float4 l = pathL[path];
         l.x += e2.x;
@@ -692,7 +732,7 @@ __device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, 
         return;
     }
     // area light: the closest hit must be an emitter at the sampled point
-    if (r.best < 0) return;
+    if (r.best == -1) return;
     ApplyAreaLight(S, e, r.o, r.d, r.best, r.tBest, path, pathL);
 }
 // The area-light part of ApplyShadow, out of line: it runs once per traced entry, and
@@ -700,6 +740,10 @@ __device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, 
 __device__ __noinline__ void ApplyAreaLight(const DevScene& S, const float4* e, V3 o, V3 d, int best,
                                             float tBest, int path, float4* pathL) {
     const float4 e0 = e[0], e2 = e[2], e3 = e[3];
+    if (best < -1) {  // a tied closest hit: the reference's answer (range as ShadowRay's)
+        best = -2 - best;
+        ResolveTieInline(&S, o, d, 0.0f, e0.w + 0.05f, &best, &tBest);
+    }
     const int m = ResolveMaterial(S.mats, SlotMaterial(S.shade, best), e3.w);
     if (S.mats[m].kind != kEmission) return;
     const Shading sl = Interpolate<FastMath>(S, best, o, d, tBest);
@@ -828,6 +872,10 @@ __global__ void __launch_bounds__(128) TailKernel(const DevJob* __restrict__ job
             r.numTris = S.numTris;
 #endif
             TraceOne(r, stk, err);
+            if (r.best < -1) {
+                r.best = -2 - r.best;
+                ResolveTie(&S, r.o, r.d, r.tmin, r.tmax, &r.best, &r.tBest);
+            }
             TailSink sink{wb.pathL, path};
             ShadeOne<kInteg>(J, path, o, d, s0, s2, ior, make_float2(r.tBest, __int_as_float(r.best)), rng,
                              sink);
@@ -913,6 +961,7 @@ __global__ void FinalizeKernel(const DevJob* __restrict__ jobs, const int* __res
 }
 
 struct RayBatchQueue {
+    const DevScene* S;
     const float4* nodes;
     const float4* tris;
     int numWide, numTris;
@@ -935,16 +984,22 @@ struct RayBatchQueue {
 #endif
     }
     __device__ void Finish(int i, const LaneRay& r) const {
-        triOut[i] = r.best >= 0 ? TriId(tris, r.best) : -1;
-        distOut[i] = r.best >= 0 ? r.tBest : -1.0f;
+        int best = r.best;
+        float tb = r.tBest;
+        if (best < -1) {
+            best = -2 - best;
+            ResolveTie(S, r.o, r.d, r.tmin, r.tmax, &best, &tb);
+        }
+        triOut[i] = best >= 0 ? TriId(tris, best) : -1;
+        distOut[i] = best >= 0 ? tb : -1.0f;
     }
 };
 
 __global__ void __launch_bounds__(128) TraceKernel(DevScene S, int n, const float* __restrict__ rays,
                                                    float tmin, float tmax, int* __restrict__ triOut,
                                                    float* __restrict__ distOut, int* fetch) {
-    RayBatchQueue q{S.numWide > 0 ? S.wide : nullptr, S.tris, S.numWide, S.numTris, rays, tmin, tmax,
-                    triOut, distOut};
+    RayBatchQueue q{&S, S.numWide > 0 ? S.wide : nullptr, S.tris, S.numWide, S.numTris, rays, tmin,
+                    tmax, triOut, distOut};
     int err = 0;
     TraceQueue(q, n, fetch, err);
 }
