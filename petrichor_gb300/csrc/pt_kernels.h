@@ -45,7 +45,8 @@ struct DevJob {
 };
 
 // One job's samples [s0, s0 + sw) over all its pixels: paths
-// [pathBase, pathBase + W*H*sw) of the wave; pixelBase indexes the accumulate pass.
+// [pathBase, pathBase + W*H*sw) of the wave, pixel-major (pixel q of the band order owns
+// paths pathBase + q*sw .. + sw - 1); pixelBase indexes the accumulate pass.
 struct WaveUnit {
     int32_t job, s0, sw, pathBase;
     int32_t pixelBase, pad[3];

@@ -369,9 +369,10 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WaveUnit u = units[FindUnit(units, nUnits, i, false)];
         const DevJob& J = jobs[u.job];
-        const int W = J.st.width, H = J.st.height, P = W * H;
+        const int W = J.st.width, H = J.st.height;
+        // pixel-major path order: a pixel's samples of the unit are consecutive paths
         const int local = i - u.pathBase;
-        const int q = local % P, s = u.s0 + local / P;
+        const int q = local / u.sw, s = u.s0 + local % u.sw;
         int x, y;
         PixelOfIndex(q, W, H, wd.band, x, y);
         PathRng rng(PathKey(J.st.seed, (uint32_t)(y * W + x), (uint32_t)s));
@@ -924,14 +925,14 @@ __global__ void AccumulateKernel(const DevJob* __restrict__ jobs, const WaveUnit
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WaveUnit u = units[FindUnit(units, nUnits, i, true)];
         const DevJob& J = jobs[u.job];
-        const int W = J.st.width, H = J.st.height, P = W * H;
+        const int W = J.st.width, H = J.st.height;
         const int q = i - u.pixelBase;
         int x, y;
         PixelOfIndex(q, W, H, wd.band, x, y);
         const size_t pixel = (size_t)y * W + x;
         float4 acc = J.accum[pixel];
         for (int s = 0; s < u.sw; s++) {
-            const int p = u.pathBase + s * P + q;
+            const int p = u.pathBase + q * u.sw + s;
             const float4 l = wb.pathL[p];
             const int flags = __float_as_int(l.w);
             // PathTracing.cpp:191-195 drops a sample whose smallest channel is
