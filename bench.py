@@ -72,6 +72,11 @@ def parse():
                     help="only the serving loop at 20/100/500 requests/s vs the plain path")
     ap.add_argument("--plain-only", action="store_true",
                     help="the plain line alone (no image error, drop-in, serve or batch objects)")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU-baseline leg (profiling and A/B runs only)")
+    ap.add_argument("--trace-primary", action="store_true",
+                    help="trace the first bounce through the BVH instead of rasterising it "
+                         "(A/B runs; the films are the same)")
     ap.add_argument("--requests", type=int, default=100, help="requests per arrival rate (serve)")
     ap.add_argument("--serve-rates", default="",
                     help="comma-separated arrival rates of the serve object (default 500; "
@@ -434,10 +439,13 @@ def batch_summary(args, steps: int, warmup: int):
 
         def run_batched_ungraphed():
             t = ctx.get_tuning()
-            ctx.set_tuning(t.wave_paths, t.blocks_per_sm, t.band_rows, 0)
+            keep = dict(wave_paths=t.wave_paths, blocks_per_sm=t.blocks_per_sm, band_rows=t.band_rows,
+                        sort_rays=t.sort_rays, tail_bounce=t.tail_bounce,
+                        primary_traversal=t.primary_traversal)
+            ctx.set_tuning(use_graphs=0, **keep)
             run_batched()
             torch.cuda.synchronize()
-            ctx.set_tuning(t.wave_paths, t.blocks_per_sm, t.band_rows, t.use_graphs)
+            ctx.set_tuning(use_graphs=t.use_graphs, **keep)
 
         for _ in range(max(1, warmup)):
             run_plain()
@@ -711,6 +719,8 @@ def main():
     gen_s = time.perf_counter() - t0
     st = scene.settings
     ctx = capi.Context(local)
+    if args.trace_primary:
+        ctx.set_tuning(primary_traversal=1)
     t0 = time.perf_counter()
     sid = ctx.upload(scene)
     upload_s = time.perf_counter() - t0
@@ -826,7 +836,7 @@ def main():
                                     (sum(stages.values()) / 1e3) / 1e6},
         "image_mean": img_mean,
     }
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base, o, cpu_film, cpu_tiles, per_tile_s, order = cpu_baseline(scene, args.cpu_seconds)
         line["cpu_baseline"] = base
         if not args.plain_only:

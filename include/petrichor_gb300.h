@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PT_ABI_VERSION 3
+#define PT_ABI_VERSION 4
 
 /* status codes */
 #define PT_OK 0
@@ -360,6 +360,9 @@ typedef struct pt_tuning {
   int32_t use_graphs;    /* 1: replay each wave's stage sequence from a captured CUDA graph */
   int32_t sort_rays;     /* 1: reorder each bounce's rays by direction and origin cell */
   int32_t tail_bounce;   /* > 0: from this bounce on, one launch finishes every path (0: off) */
+  int32_t primary_traversal; /* 1: trace first-bounce rays through the BVH; 0: rasterise them
+                                when the wave allows (one pinhole job, enough rays per triangle) */
+  int32_t reserved;
   double probe_ms;       /* pt_autotune: probe render time of the chosen configuration */
 } pt_tuning;
 /* Times candidate grids, pixel bands and graph replay on probe renders of one job

@@ -124,6 +124,7 @@ class PtTuning(ctypes.Structure):
     _fields_ = [("wave_paths", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("band_rows", ctypes.c_int32), ("use_graphs", ctypes.c_int32),
                 ("sort_rays", ctypes.c_int32), ("tail_bounce", ctypes.c_int32),
+                ("primary_traversal", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("probe_ms", ctypes.c_double)]
 
     def as_dict(self):
@@ -499,8 +500,10 @@ class Context:
         return b[:n.value], q[:n.value], ids, h.value, st
 
     def set_tuning(self, wave_paths: int = 0, blocks_per_sm: int = 0, band_rows: int = 0,
-                   use_graphs: int = 1, sort_rays: int = 0, tail_bounce: int = 0):
-        t = PtTuning(wave_paths, blocks_per_sm, band_rows, use_graphs, sort_rays, tail_bounce, 0.0)
+                   use_graphs: int = 1, sort_rays: int = 0, tail_bounce: int = 0,
+                   primary_traversal: int = 0):
+        t = PtTuning(wave_paths, blocks_per_sm, band_rows, use_graphs, sort_rays, tail_bounce,
+                     primary_traversal, 0, 0.0)
         self._check(self.L.pt_set_tuning(self.h, ctypes.byref(t)), "pt_set_tuning")
 
     def get_tuning(self) -> PtTuning:

@@ -834,7 +834,8 @@ int pt_set_tuning(pt_context* ctx, const pt_tuning* t) {
     std::lock_guard<std::mutex> g(ctx->mu);
     if (t->wave_paths < 0 || t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->band_rows < 0 ||
         t->band_rows > 4096 || (t->use_graphs != 0 && t->use_graphs != 1) ||
-        (t->sort_rays != 0 && t->sort_rays != 1) || t->tail_bounce < 0 || t->tail_bounce > 64)
+        (t->sort_rays != 0 && t->sort_rays != 1) || t->tail_bounce < 0 || t->tail_bounce > 64 ||
+        (t->primary_traversal != 0 && t->primary_traversal != 1))
         return Fail(ctx, PT_ERR_INVALID_ARG, "bad tuning");
     ctx->tunedWavePaths = t->wave_paths;
     ctx->tuning.blocksPerSm = t->blocks_per_sm;
@@ -842,6 +843,7 @@ int pt_set_tuning(pt_context* ctx, const pt_tuning* t) {
     ctx->tuning.graphs = t->use_graphs;
     ctx->tuning.sortRays = t->sort_rays;
     ctx->tuning.tailBounce = t->tail_bounce;
+    ctx->tuning.primaryTraversal = t->primary_traversal;
     return PT_OK;
 }
 
@@ -854,6 +856,7 @@ int pt_get_tuning(pt_context* ctx, pt_tuning* out) {
     out->use_graphs = ctx->tuning.graphs;
     out->sort_rays = ctx->tuning.sortRays;
     out->tail_bounce = ctx->tuning.tailBounce;
+    out->primary_traversal = ctx->tuning.primaryTraversal;
     out->probe_ms = ctx->tunedProbeMs;
     return PT_OK;
 }
@@ -926,6 +929,7 @@ int pt_autotune(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const 
         out->use_graphs = best.graphs;
         out->sort_rays = best.sortRays;
         out->tail_bounce = best.tailBounce;
+        out->primary_traversal = best.primaryTraversal;
         out->probe_ms = bestMs;
     }
     return PT_OK;

@@ -109,6 +109,10 @@ struct WaveProfile {
 struct WaveShape {
     int nUnits = 0, nPaths = 0, nPixelUnits = 0;
     int iters = 0, integrator = -1, soleJob = -1;
+    // > 0: the first bounce may be rasterised (raster_primary.cuh): the triangle count of
+    // the wave's one unit of one pinhole-camera PathTracing job, with at least two rays per
+    // triangle
+    int raster = 0;
 };
 // Launch configuration (all choices give the same films). 0 = default.
 struct WaveTuning {
@@ -117,6 +121,7 @@ struct WaveTuning {
     int graphs = 1;       // replay each wave's stage sequence from a captured CUDA graph
     int sortRays = 0;     // reorder each bounce's rays by direction and origin cell before tracing
     int tailBounce = 0;   // > 0: from this bounce on, one launch finishes every path (TailKernel)
+    int primaryTraversal = 0;  // 1: trace the first bounce through the BVH even when it could be rasterised
 };
 // Captured stage sequences, keyed by wave shape and buffers (owned by a context or server).
 struct WaveGraphCache;

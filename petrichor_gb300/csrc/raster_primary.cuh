@@ -1,0 +1,281 @@
+// Primary visibility by rasterisation (included by wavefront.cu inside namespace ptg).
+//
+// The first bounce of a wave whose one job looks through a pinhole (every primary ray
+// starts at the camera position) is computed by visiting, for each triangle, the
+// samples whose rays can reach it, instead of tracing each ray through the BVH:
+//   setup  one thread per triangle: the three planes through the camera and the
+//          triangle's edges (the cone a ray must lie in to hit it, widened by a small
+//          angular margin) and the rectangle of pixels it covers (its vertices
+//          projected with the camera's own mapping, one pixel of margin for the sample
+//          offsets; the whole image when it reaches the camera plane); the rectangle is
+//          cut into row segments of at most kRasterSeg pixels, appended to a work list;
+//   visit  one warp per segment: the lanes step through the segment's (pixel, sample)
+//          pairs, test each direction against the cone, and for those inside run the
+//          exact triangle test of the traversal (TriIntersect) and keep the nearest hit
+//          with a 64-bit atomic minimum over {distance bits, slot};
+//   finish one thread per path: the nearest hit into the hit queue, an exact tie with
+//          another triangle marked as the traversal marks it.
+// The cone test only skips pairs whose ray certainly misses, and every remaining pair
+// runs the same triangle test with the same ray, so a sample's closest distance and
+// triangle are the traversal's (which, with its widened boxes, also finds every hit).
+// Scratch: the next queue's ray buffer holds the keys and the tie marks (12 of its 32
+// bytes per path); the shadow queue holds the per-triangle records and the work list.
+// Both are free until the first shade. Paths are in pixel-major order, so a pixel's
+// samples are consecutive queue entries and their directions are read where raygen
+// wrote them.
+#pragma once
+
+constexpr int kRasterSeg = 32;  // pixels per work item (one row segment)
+constexpr unsigned long long kNoKey = ~0ull;
+
+struct RasterScratch {
+    unsigned long long* key;  // per path: {distance bits, slot}, kNoKey = no hit
+    unsigned* tie;            // per path: smallest distance bits at which two triangles tied
+    float4* rec;              // per triangle: 4 float4 (cone planes with margins, pixel rect)
+    uint2* items;             // {triangle slot, row | segment << 16}
+    int* overflow;            // triangles whose items did not fit (visited whole)
+    long long itemCap;
+};
+
+__device__ __forceinline__ RasterScratch CarveRaster(const WaveBuffers& wb, int cur, int numTris) {
+    const size_t C = (size_t)wb.capacity;
+    RasterScratch r;
+    r.key = reinterpret_cast<unsigned long long*>(wb.ray[cur ^ 1]);
+    r.tie = reinterpret_cast<unsigned*>(r.key + C);
+    r.rec = wb.shadow;
+    r.overflow = reinterpret_cast<int*>(wb.shadow + 4 * (size_t)numTris);
+    r.items = reinterpret_cast<uint2*>(r.overflow + ((numTris + 3) & ~3));
+    const long long bytes = (long long)(64 * C) - 64LL * numTris - 4LL * ((numTris + 3) & ~3);
+    r.itemCap = bytes > 0 ? bytes / 8 : 0;
+    return r;
+}
+
+// Pixel coordinate (continuous, origin at the image corner) of a point with camera-basis
+// coordinates (X, Y, Z) (multiples of right, up, forward), Z > 0: the inverse of
+// GenerateRay's sensor mapping.
+__device__ __forceinline__ void ProjectPx(const DevCamera& c, float X, float Y, float Z, int W, int H,
+                                          float& px, float& py) {
+    const float aspect = (float)W / H;
+    px = (X / (Z * c.hPerf * aspect) + 0.5f) * W;
+    py = (-Y / (Z * c.hPerf) + 0.5f) * H;
+    px = fminf(fmaxf(px, -1.0e9f), 1.0e9f);
+    py = fminf(fmaxf(py, -1.0e9f), 1.0e9f);
+}
+
+__global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restrict__ jobs,
+                                                         WaveBuffers wb, int cur) {
+    const WaveDesc wd = *wb.desc;
+    const DevJob& J = jobs[wd.soleJob];
+    const DevScene& S = J.S;
+    const int T = S.numTris, W = J.st.width, H = J.st.height;
+    const RasterScratch rs = CarveRaster(wb, cur, T);
+    const V3 pos = LoadV3(J.C.pos), right = LoadV3(J.C.right), up = LoadV3(J.C.up),
+             fwd = LoadV3(J.C.fwd);
+    const float rr = 1.0f / SqLen(right), uu = 1.0f / SqLen(up);
+    const int lane = threadIdx.x & 31;
+    // whole warps step together (the item appends are warp-aggregated)
+    for (int base = blockIdx.x * blockDim.x; base < T; base += gridDim.x * blockDim.x) {
+        const int k = base + threadIdx.x;
+        int nItems = 0;
+        int x0 = 0, x1 = -1, y0 = 0, y1 = -1;
+        if (k < T) {
+            V3 v0, e1, e2;
+            LoadTri(S.tris, k, v0, e1, e2);
+            const V3 a[3] = {v0 - pos, (v0 + e1) - pos, (v0 + e2) - pos};
+            // the plane through the camera and edge k is a_k x a_k+1 = a_k x (edge k): formed
+            // from the short edge vector it has no cancellation (the cross product of two
+            // long, nearly parallel vectors from a distant camera would lose most digits)
+            V3 n[3] = {Cross(a[0], e1), Cross(a[1], e2 - e1), Cross(a[2], e2 * -1.0f)};
+            const V3 ce = Cross(e1, e2);
+            const float side = Dot(a[0], ce);  // which side of the triangle the camera is on
+            float m[3];
+            if (fabsf(side) > 1.0e-5f * sqrtf(SqLen(a[0]) * SqLen(ce))) {
+                const float sg = side > 0.0f ? 1.0f : -1.0f;
+                for (int e = 0; e < 3; e++) {
+                    n[e] = n[e] * sg;
+                    m[e] = 2.0e-5f * sqrtf(SqLen(n[e]));  // angular margin ~2e-5 rad
+                }
+            } else {  // camera (nearly) in the triangle's plane, or a degenerate triangle: no cone test
+                for (int e = 0; e < 3; e++) {
+                    n[e] = V3(0.f, 0.f, 0.f);
+                    m[e] = 1.0f;
+                }
+            }
+            // coordinates in the camera basis: right and up are orthogonal to forward but not
+            // unit length (Camera::SetViewDir crosses forward with the world up), and
+            // GenerateRay scales them as they are
+            float X[3], Y[3], Z[3], zmax = 0.0f;
+            bool front = true, anyFront = false;
+            for (int v = 0; v < 3; v++) {
+                X[v] = Dot(a[v], right) * rr;
+                Y[v] = Dot(a[v], up) * uu;
+                Z[v] = Dot(a[v], fwd);
+                zmax = fmaxf(zmax, fabsf(Z[v]));
+            }
+            const float zc = 1.0e-6f * zmax + 1.0e-30f;
+            for (int v = 0; v < 3; v++) {
+                front = front && Z[v] > zc;
+                anyFront = anyFront || Z[v] > 0.0f;
+            }
+            // pixel rectangle of the vertices' projections; a triangle reaching the camera
+            // plane gets the whole image (primary rays only meet points in front, so one
+            // wholly behind gets none)
+            if (front) {
+                float lx = 3.0e38f, hx = -3.0e38f, ly = 3.0e38f, hy = -3.0e38f;
+                for (int v = 0; v < 3; v++) {
+                    float px, py;
+                    ProjectPx(J.C, X[v], Y[v], Z[v], W, H, px, py);
+                    lx = fminf(lx, px);
+                    hx = fmaxf(hx, px);
+                    ly = fminf(ly, py);
+                    hy = fmaxf(hy, py);
+                }
+                // a sample of pixel i sits at i + r, r in [0, 1]: pixels floor(px) - 1 .. floor(px)
+                x0 = max(0, (int)floorf(lx - 0.01f) - 1);
+                x1 = min(W - 1, (int)floorf(hx + 0.01f));
+                y0 = max(0, (int)floorf(ly - 0.01f) - 1);
+                y1 = min(H - 1, (int)floorf(hy + 0.01f));
+            } else if (anyFront) {
+                x0 = 0;
+                x1 = W - 1;
+                y0 = 0;
+                y1 = H - 1;
+            }
+            if (x0 <= x1 && y0 <= y1) {
+                nItems = (y1 - y0 + 1) * ((x1 - x0 + kRasterSeg) / kRasterSeg);
+                float4* r = rs.rec + 4 * (size_t)k;
+                r[0] = make_float4(n[0].x, n[0].y, n[0].z, m[0]);
+                r[1] = make_float4(n[1].x, n[1].y, n[1].z, m[1]);
+                r[2] = make_float4(n[2].x, n[2].y, n[2].z, m[2]);
+                r[3] = make_float4(__int_as_float(x0), __int_as_float(x1), __int_as_float(y0),
+                                   __int_as_float(y1));
+            }
+        }
+        // warp-aggregated reservation of the work list (a 64-bit count in counts[8..9])
+        int incl = nItems;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(kFullMask, incl, 31);
+        unsigned long long wbase = 0;
+        if (lane == 31 && total > 0)
+            wbase = atomicAdd(reinterpret_cast<unsigned long long*>(wb.counts + 8), (unsigned long long)total);
+        wbase = __shfl_sync(kFullMask, wbase, 31);
+        if (nItems > 0) {
+            const long long first = (long long)wbase + incl - nItems;
+            if (first + nItems <= rs.itemCap) {
+                const int segs = (x1 - x0 + kRasterSeg) / kRasterSeg;
+                long long it = first;
+                for (int y = y0; y <= y1; y++)
+                    for (int sgi = 0; sgi < segs; sgi++)
+                        rs.items[it++] = make_uint2((unsigned)k, (unsigned)y | ((unsigned)sgi << 16));
+            } else {
+                const int o = atomicAdd(wb.counts + 10, 1);
+                rs.overflow[o] = k;
+            }
+        }
+    }
+}
+
+// Visits one row segment of triangle k: every (pixel, sample) pair of the wave's unit.
+// Pixel (x, y) is pixel q = qrow + x * hb of the band order (PixelOfIndex), and its
+// samples are paths pathBase + q * sw + j, whose directions are in the ray queue.
+__device__ __forceinline__ void RasterSegment(const RasterScratch& rs, const float4* __restrict__ rays,
+                                             const float4* __restrict__ tris, int k, int y, int xa,
+                                             int xb, int W, int H, int band, int pathBase, int sw,
+                                             V3 o, float tmin, int lane) {
+    const float4 r0 = __ldg(rs.rec + 4 * (size_t)k), r1 = __ldg(rs.rec + 4 * (size_t)k + 1),
+                 r2 = __ldg(rs.rec + 4 * (size_t)k + 2);
+    V3 v0, e1, e2;
+    LoadTri(tris, k, v0, e1, e2);
+    const int y0 = (y / band) * band, hb = min(band, H - y0);
+    const size_t qrow = (size_t)y0 * W + (y - y0);
+    const int n = (xb - xa + 1) * sw;
+    // (pixel, sample) of pair f = lane + 32 i, advanced without a division per pair
+    const int dq = 32 / sw, dr = 32 % sw;
+    int x = xa + lane / sw, j = lane % sw;
+    for (int f = lane; f < n; f += 32) {
+        const size_t idx = (size_t)pathBase + (qrow + (size_t)x * hb) * sw + j;
+        const float4 dv = __ldg(rays + 2 * idx + 1);
+        const float c0 = r0.x * dv.x + r0.y * dv.y + r0.z * dv.z + r0.w;
+        const float c1 = r1.x * dv.x + r1.y * dv.y + r1.z * dv.z + r1.w;
+        const float c2 = r2.x * dv.x + r2.y * dv.y + r2.z * dv.z + r2.w;
+        if (c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f) {
+            float t;
+            if (TriIntersect(v0, e1, e2, o, V3(dv.x, dv.y, dv.z), t) && t >= tmin && t < kFltMax) {
+                const unsigned tb = __float_as_uint(t + 0.0f);  // +0 for a zero distance
+                const unsigned long long key = ((unsigned long long)tb << 32) | (unsigned)k;
+                const unsigned long long old = atomicMin(rs.key + idx, key);
+                if ((unsigned)(old >> 32) == tb && (unsigned)old != (unsigned)k) atomicMin(rs.tie + idx, tb);
+            }
+        }
+        j += dr;
+        x += dq;
+        if (j >= sw) {
+            j -= sw;
+            x++;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) RasterVisitKernel(const DevJob* __restrict__ jobs,
+                                                         const WaveUnit* __restrict__ units,
+                                                         WaveBuffers wb, int cur) {
+    const WaveDesc wd = *wb.desc;
+    const DevJob& J = jobs[wd.soleJob];
+    const int T = J.S.numTris, W = J.st.width, H = J.st.height, band = wd.band;
+    const RasterScratch rs = CarveRaster(wb, cur, T);
+    const float4* rays = wb.ray[cur];
+    const WaveUnit u = units[0];
+    const float tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
+    const V3 o = LoadV3(J.C.pos);
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    long long nItems = *reinterpret_cast<const long long*>(wb.counts + 8);
+    if (nItems > rs.itemCap) nItems = rs.itemCap;
+    for (long long w = warp; w < nItems; w += warps) {
+        const uint2 it = rs.items[w];
+        const int k = (int)it.x, y = (int)(it.y & 0xffffu), sg = (int)(it.y >> 16);
+#if PT_CHECK
+        if (k < 0 || k >= T) continue;
+#endif
+        const float4 r3 = __ldg(rs.rec + 4 * (size_t)k + 3);
+        const int xa = __float_as_int(r3.x) + sg * kRasterSeg;
+        const int xb = min(__float_as_int(r3.y), xa + kRasterSeg - 1);
+        RasterSegment(rs, rays, J.S.tris, k, y, xa, xb, W, H, band, u.pathBase, u.sw, o, tmin, lane);
+    }
+    // triangles whose items did not fit in the list: whole, one warp each
+    const int nOver = wb.counts[10];
+    for (long long w = warp; w < nOver; w += warps) {
+        const int k = rs.overflow[w];
+        const float4 r3 = __ldg(rs.rec + 4 * (size_t)k + 3);
+        const int x0 = __float_as_int(r3.x), x1 = __float_as_int(r3.y), y0 = __float_as_int(r3.z),
+                  y1 = __float_as_int(r3.w);
+        for (int y = y0; y <= y1; y++)
+            for (int xa = x0; xa <= x1; xa += kRasterSeg)
+                RasterSegment(rs, rays, J.S.tris, k, y, xa, min(x1, xa + kRasterSeg - 1), W, H, band,
+                              u.pathBase, u.sw, o, tmin, lane);
+    }
+}
+
+// The nearest hit of every path into the hit queue (queue entry i = path i at the first
+// bounce), as ExtendKernel would write it: {distance, slot}, {kFltMax, -1} for a miss,
+// -2 - slot when another triangle tied at that distance.
+__global__ void RasterFinishKernel(const DevJob* __restrict__ jobs, WaveBuffers wb, int cur) {
+    const WaveDesc wd = *wb.desc;
+    const RasterScratch rs = CarveRaster(wb, cur, jobs[wd.soleJob].S.numTris);
+    const int n = wd.nPaths;
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur ^ 1] = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long key = rs.key[i];
+        float2 h = make_float2(kFltMax, __int_as_float(-1));
+        if (key != kNoKey) {
+            const unsigned tb = (unsigned)(key >> 32);
+            const int slot = (int)(unsigned)key;
+            h = make_float2(__uint_as_float(tb), __int_as_float(rs.tie[i] == tb ? -2 - slot : slot));
+        }
+        wb.hit[i] = h;
+    }
+}

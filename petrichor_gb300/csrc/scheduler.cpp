@@ -83,6 +83,12 @@ WaveShape ShapeOf(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& 
     shape.iters = WaveIterations(jobs, units);
     shape.integrator = WaveIntegrator(jobs, units);
     shape.soleJob = WaveSoleJob(units);
+    if (shape.soleJob >= 0 && units.size() == 1 && shape.iters >= 0) {
+        const DevJob& J = jobs[shape.soleJob];
+        shape.raster = J.C.aperture == 0.0f && J.S.numTris > 0 && J.st.height < 65536 &&
+                       J.st.integrator == kPathTracing &&
+                       (int64_t)shape.nPaths >= 2 * (int64_t)J.S.numTris ? J.S.numTris : 0;
+    }
     return shape;
 }
 

@@ -362,10 +362,15 @@ __device__ __forceinline__ int FindUnit(const WaveUnit* __restrict__ units, int 
     return lo;
 }
 
+#include "raster_primary.cuh"
+
+// raster != 0: the first bounce is rasterised (raster_primary.cuh), whose keys and tie
+// marks start empty here.
 __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __restrict__ units,
-                             WaveBuffers wb, int cur) {
+                             WaveBuffers wb, int cur, int raster) {
     const WaveDesc wd = *wb.desc;
     const int n = wd.nPaths, nUnits = wd.nUnits;
+    const RasterScratch rs = CarveRaster(wb, cur, 0);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WaveUnit u = units[FindUnit(units, nUnits, i, false)];
         const DevJob& J = jobs[u.job];
@@ -379,7 +384,12 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         float r0, r1, r2, r3;
         rng.Next(r0, r1);
         rng.Next(r2, r3);
-        const Ray ray = GenerateRay<FastMath>(J.C, x, y, W, H, r0, r1, r2, r3);
+        Ray ray = GenerateRay<FastMath>(J.C, x, y, W, H, r0, r1, r2, r3);
+        if (J.C.aperture == 0.0f) ray.o = LoadV3(J.C.pos);  // a pinhole: exactly the camera position
+        if (raster) {
+            rs.key[i] = kNoKey;
+            rs.tie[i] = 0xffffffffu;
+        }
         wb.ray[cur][2 * i] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float(i));
         wb.ray[cur][2 * i + 1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 1.0f);
         wb.qs0[cur][i] = make_float4(ray.T.x, ray.T.y, ray.T.z, 1.0f);
@@ -391,6 +401,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wb.counts[cur] = n;
         wb.counts[2] = wb.counts[4] = wb.counts[5] = wb.counts[6] = 0;
+        wb.counts[8] = wb.counts[9] = wb.counts[10] = 0;  // raster work list (64-bit) and overflow
     }
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kSortBins; k += gridDim.x * blockDim.x)
         wb.sortBins[k] = 0;  // ray-sort counts start at zero in every wave
@@ -1284,9 +1295,10 @@ struct StageOverlap {
 };
 
 // tailFrom > 0: bounces from it0 + tailFrom on run in one TailKernel launch.
-static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integrator, int grid,
-                          int it0, int count, cudaStream_t stream, WaveProfile* prof, int* nl,
-                          bool sort, StageOverlap* ov, int tailFrom = 0) {
+static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveBuffers& wb,
+                          int integrator, int grid, int it0, int count, cudaStream_t stream,
+                          WaveProfile* prof, int* nl, bool sort, StageOverlap* ov, int tailFrom = 0,
+                          int rasterTris = 0) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     const int block = kTraceBlock;
     const int sgrid = ShadeGrid(grid);
@@ -1310,7 +1322,15 @@ static void LaunchBounces(const DevJob* jobs, const WaveBuffers& wb, int integra
             break;
         }
         if (ev) ev->Begin(1, stream);
-        ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+        if (it == 0 && rasterTris > 0) {  // first bounce rasterised (raster_primary.cuh)
+            const int sgrid = std::max(1, std::min((rasterTris + block - 1) / block, SmCount() * 32));
+            RasterSetupKernel<<<sgrid, block, 0, stream>>>(jobs, wb, cur);
+            RasterVisitKernel<<<SmCount() * 16, block, 0, stream>>>(jobs, units, wb, cur);
+            RasterFinishKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+            *nl += 2;  // one more below
+        } else {
+            ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+        }
         if (ev) {
             ev->End(1, stream);
             if (prof->countReference)
@@ -1364,11 +1384,11 @@ struct WaveGraphKey {
     const void* jobs;
     const void* units;
     const void* buffers;
-    int capacity, iters, integrator, grid, sort, accum, tail;
+    int capacity, iters, integrator, grid, sort, accum, tail, raster;
     bool operator==(const WaveGraphKey& o) const {
         return jobs == o.jobs && units == o.units && buffers == o.buffers && capacity == o.capacity &&
                iters == o.iters && integrator == o.integrator && grid == o.grid && sort == o.sort &&
-               accum == o.accum && tail == o.tail;
+               accum == o.accum && tail == o.tail && raster == o.raster;
     }
 };
 struct WaveGraph {
@@ -1486,13 +1506,16 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     // whose stage timers need one stream)
     StageOverlap* ov =
       (graphs && !prof && graphs->overlap[lane & 1].Ready()) ? &graphs->overlap[lane & 1] : nullptr;
+    // the first bounce rasterised where the wave allows it (raster_primary.cuh)
+    const int rasterTris =
+      (shape.raster > 0 && !tune.primaryTraversal && !sort && shape.iters >= 0) ? shape.raster : 0;
     const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
-                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom};
+                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom, rasterTris};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
-            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort, ov,
-                          tailFrom);
+            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, rasterTris > 0);
+            LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort,
+                          ov, tailFrom, rasterTris);
             if (accumulate) AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             *n += accumulate ? 2 : 1;
         };
@@ -1500,10 +1523,10 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             e = ReplayCaptured(graphs, key, stream, &nl, record);
         } else {
             if (ev) ev->Begin(0, stream);
-            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
+            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, rasterTris > 0);
             if (ev) ev->End(0, stream);
-            LaunchBounces(jobs, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort, ov,
-                          tailFrom);
+            LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort,
+                          ov, tailFrom, rasterTris);
             if (accumulate) {
                 if (ev) ev->Begin(4, stream);
                 AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
@@ -1515,7 +1538,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     } else {
         // SimplePathTracing has no depth cap: run blocks of bounces until the queue drains
         if (ev) ev->Begin(0, stream);
-        RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0);
+        RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, 0);
         if (ev) ev->End(0, stream);
         nl++;
         for (int it = 0;; it += kPollEvery) {
@@ -1528,12 +1551,12 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
                 WaveGraphKey k = key;
                 k.iters = -kPollEvery;
                 e = ReplayCaptured(graphs, k, stream, &nl, [&](int* n) {
-                    LaunchBounces(jobs, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n, sort,
+                    LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n, sort,
                                   ov);
                 });
                 if (e != cudaSuccess) break;
             } else {
-                LaunchBounces(jobs, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort, ov);
+                LaunchBounces(jobs, units, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort, ov);
             }
         }
         if (e == cudaSuccess && accumulate) {

@@ -1,9 +1,10 @@
 """Launch configuration of the wavefront path: captured CUDA graphs, grid sizes,
-pixel bands, wave sizes and the autotuner.
+pixel bands, wave sizes, first-bounce rasterisation and the autotuner.
 
 None of these may change a film: the random stream is keyed by (seed, pixel,
-sample), every ray visits its nodes in its own fixed order, and each pixel sums
-its samples in sample order.
+sample), every ray visits its nodes in its own fixed order, each pixel sums its
+samples in sample order, and a rasterised first bounce finds the same closest hits as
+the traversal (exact ties settled in the reference's order by both).
 """
 import numpy as np
 import pytest
@@ -23,6 +24,8 @@ CONFIGS = [
     dict(sort_rays=1, use_graphs=0, wave_paths=3000),
     dict(tail_bounce=1),                                      # one launch from bounce 1 on
     dict(tail_bounce=3, use_graphs=0, wave_paths=3000),
+    dict(primary_traversal=1),                                # first bounce traced, not rasterised
+    dict(primary_traversal=1, use_graphs=0, wave_paths=3000),
 ]
 
 
@@ -33,7 +36,21 @@ def _scenes():
         "simple": synth.cornell(width=33, height=17, spp=5),  # queue-polled bounce blocks
         "tris": synth.spheres_grids(tri_budget=30000, width=64, height=36, spp=4, max_bounces=8,
                                     env_width=128, env_height=64),
+        # enough rays per triangle for the rasterised first bounce; a tilted camera (the
+        # camera basis is not unit length)
+        "raster": synth.spheres_grids(tri_budget=20000, width=96, height=64, spp=8, max_bounces=6,
+                                      env_width=128, env_height=64),
+        # a camera inside the box: walls reach behind the camera plane (whole-image rectangles)
+        "inside": _inside_box(),
     }
+
+
+def _inside_box():
+    from petrichor_gb300.scene_io import Camera
+    sc = synth.cornell(width=48, height=40, spp=8, mixed=True, integrator=1, max_bounces=5,
+                       env_texture=True)
+    return sc.copy_with(camera=Camera(pos=(0.05, -0.6, 1.1), view_dir=(0.2, 1.0, -0.1),
+                                      fov=1.6, focus_target=None, aperture=0.0))
 
 
 @pytest.fixture(scope="module")
@@ -55,7 +72,7 @@ def _render(ctx, sid, cam, st):
     return film.cpu().numpy()
 
 
-@pytest.mark.parametrize("name", ["pt", "simple", "tris"])
+@pytest.mark.parametrize("name", ["pt", "simple", "tris", "raster", "inside"])
 def test_films_do_not_depend_on_launch_configuration(tuned_ctx, name):
     ctx, jobs = tuned_ctx
     sid, cam, st = jobs[name]
@@ -106,7 +123,7 @@ def test_set_tuning_rejects_bad_values(tuned_ctx):
     ctx, _ = tuned_ctx
     for bad in (dict(blocks_per_sm=-1), dict(blocks_per_sm=65), dict(band_rows=-2),
                 dict(wave_paths=-5), dict(use_graphs=2), dict(sort_rays=3), dict(tail_bounce=-2),
-                dict(tail_bounce=65)):
+                dict(tail_bounce=65), dict(primary_traversal=2)):
         with pytest.raises(capi.PtError):
             ctx.set_tuning(**bad)
     ctx.set_tuning()
