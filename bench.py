@@ -70,6 +70,9 @@ def parse():
                     help="only the batched form: 64 scenes in shared waves vs 64 plain launches")
     ap.add_argument("--serve", action="store_true",
                     help="only the serving loop at 20/100/500 requests/s vs the plain path")
+    ap.add_argument("--stress-forms", action="store_true",
+                    help="the stress scene's frame as 4 requests of a quarter of its spp: served, "
+                         "batched and plain, against one plain render of the whole frame")
     ap.add_argument("--plain-only", action="store_true",
                     help="the plain line alone (no image error, drop-in, serve or batch objects)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
@@ -220,7 +223,7 @@ def run_reference_arm(args):
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no alias-table "
                           "environment sampler (its AliasMethod is never called on the render path)"}))
         return
-    if args.batch or args.serve:
+    if args.batch or args.serve or args.stress_forms:
         print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or "
                           "serving form; its arm times the plain render workload only"}))
         return
@@ -260,28 +263,14 @@ def run_reference_arm(args):
 
 
 # ------------------------------------------------------------------ measurements
-def l2_copy_peak(torch, mib: int = 24, reps: int = 200):
-    """Copy bandwidth of a buffer pair that stays in L2 (2 x `mib` MiB against the
-    129 MB L2): read + write bytes per copy over the CUDA-event time of `reps` copies."""
-    n = mib * 2 ** 20 // 4
-    a = torch.ones(n, dtype=torch.float32, device="cuda")
-    b = torch.empty_like(a)
-    for _ in range(20):
-        b.copy_(a)
-    s = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for _ in range(3):
-        e0.record(s)
-        for _ in range(reps):
-            b.copy_(a)
-        e1.record(s)
-        torch.cuda.synchronize()
-        best = max(best, 2 * a.numel() * 4 * reps / (e0.elapsed_time(e1) / 1e3) / 1e9)
-    del a, b
-    return {"gbs": best, "method": f"torch copy_ of {mib} MiB float32 into a second {mib} MiB "
-            f"buffer (both resident in L2), {reps} copies between CUDA events, best of 3; "
-            f"read + write bytes"}
+def l2_read_peak(ctx):
+    """Measured L2 read bandwidth (pt_probe_bandwidth): the roofline denominator of the
+    traversal kernels, whose algorithmic bytes are served mostly from L2."""
+    mib, passes, reps = 32, 16, 10
+    return {"gbs": ctx.probe_l2_read_gbs(mib << 20, passes, reps),
+            "method": f"pt_probe_bandwidth: a {mib} MiB buffer (L2-resident) read {passes} times "
+                      f"per launch with 16-byte L1-bypassing loads by 4 blocks of 512 threads per "
+                      f"SM, {reps} launches between CUDA events after one warm-up"}
 
 
 def counters_profile(name):
@@ -335,6 +324,12 @@ def image_error(ctx, sid, cam, sets, scene, film_t, stream, o, cpu_film, cpu_til
     ref_mean = float(o_u.mean())
     rel = abs(float(g_u.mean()) - ref_mean) / ref_mean
     ref_t = float(cpu_film[mask_t].mean())
+    # independent-stream spread scaled to T's sample count: one reference replicate plus
+    # the mean of S GPU seeds (the reference's correlated streams spread wider, so the
+    # z below overstates the deviation)
+    var_t = pooled * float(mask_u.sum()) / max(1.0, float(mask_t.sum()))
+    se_t = math.sqrt(var_t * (1.0 + 1.0 / S))
+    g_t_mean = float(np.mean(g_t))
     return {
         "rel": rel, "sigma_rel": se / ref_mean, "z": rel * ref_mean / se if se > 0 else None,
         "pass": bool(rel <= 0.005 or rel <= 4.5 * se / ref_mean),
@@ -343,10 +338,13 @@ def image_error(ctx, sid, cam, sets, scene, film_t, stream, o, cpu_film, cpu_til
         "samples_per_replicate": int(mask_u.sum()) * st.spp, "oracle_seconds": round(o_secs, 2),
         "rule": "rel <= 0.5% or within 4.5 sigma; sigma from pooled replicate variance",
         "reference_stream": {"tiles": int(len(cpu_tiles)), "oracle_mean": ref_t,
-                             "gpu_mean": float(np.mean(g_t)),
-                             "rel": abs(float(np.mean(g_t)) - ref_t) / ref_t,
+                             "gpu_mean": g_t_mean, "rel": abs(g_t_mean - ref_t) / ref_t,
+                             "sigma_rel": se_t / ref_t,
+                             "z": abs(g_t_mean - ref_t) / se_t if se_t > 0 else None,
                              "note": "one replicate of the reference's own streams (the CPU "
-                                     "baseline's film) against the mean of the GPU seeds"},
+                                     "baseline's film) against the mean of the GPU seeds; sigma "
+                                     "from the independent-stream spread, which the reference's "
+                                     "correlated streams exceed"},
     }
 
 
@@ -689,6 +687,81 @@ def serve_object(s, rate):
             "config": s["config"]}
 
 
+# ------------------------------------------------------------------ stress scene, all forms
+def run_stress_forms(args):
+    """The memory-bound stress workload (20M triangles, 3840x2160, 256 spp, 12 bounces,
+    8192x4096 sky) rendered four ways with the same samples: one plain render at 256 spp;
+    four requests of 64 spp (seeds 1-4) through the serving loop, through one batched
+    launch, and as four plain renders. Device time from CUDA events (serve: submission to
+    the last completion, host clock)."""
+    import torch
+    from petrichor_gb300 import capi, synth
+    t0 = time.perf_counter()
+    scene = synth.terrain_rocks()
+    gen_s = time.perf_counter() - t0
+    st = scene.settings
+    ctx = capi.Context(0)
+    res = {}
+    try:
+        sid = ctx.upload(scene)
+        cam = capi.camera_from_scene(scene)
+        npx = st.width * st.height
+        q = 4
+        whole = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=1)
+        parts = [capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=k + 1, spp=st.spp // q)
+                 for k in range(q)]
+        films = [torch.empty(npx * 3, dtype=torch.float32, device="cuda") for _ in range(q)]
+        stream = torch.cuda.Stream()
+        samples = npx * st.spp
+
+        def timed(fn):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            l0 = ctx.stats().kernel_launches
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            secs = e0.elapsed_time(e1) / 1e3
+            return {"seconds": secs, "msamples_per_s": samples / secs / 1e6,
+                    "gpu_launches": int(ctx.stats().kernel_launches - l0)}
+
+        ctx.render_device(sid, cam, parts[0], films[0].data_ptr(), stream.cuda_stream)  # warm
+        res["plain_whole_frame"] = timed(
+            lambda: ctx.render_device(sid, cam, whole, films[0].data_ptr(), stream.cuda_stream))
+        res["plain_4_requests"] = timed(lambda: [
+            ctx.render_device(sid, cam, parts[k], films[k].data_ptr(), stream.cuda_stream)
+            for k in range(q)])
+        res["batched_4_requests"] = timed(lambda: ctx.batch_render(
+            [(sid, cam, parts[k], films[k].data_ptr()) for k in range(q)], stream.cuda_stream))
+        ctx.serve_start(wave_paths=args.wave_paths, max_active=64, state_budget=150 * 2 ** 30)
+        torch.cuda.synchronize()
+        rids = [ctx.serve_submit(sid, cam, parts[k], film_device=films[k].data_ptr())
+                for k in range(q)]
+        sts = [ctx.serve_wait(r, 600) for r in rids]
+        secs = max(x.done_s for x in sts) - min(x.submit_s for x in sts)
+        ctx.serve_stop()
+        res["served_4_requests"] = {"seconds": secs, "msamples_per_s": samples / secs / 1e6,
+                                    "completed": sum(x.state == capi.REQ_DONE for x in sts)}
+        prof = ctx.render_profile(sid, cam, whole, films[0].data_ptr(), count_reference=False).as_dict()
+        ctx.release(sid)
+    finally:
+        ctx.close()
+    base = res["plain_whole_frame"]["msamples_per_s"]
+    for k in ("plain_4_requests", "batched_4_requests", "served_4_requests"):
+        res[k]["vs_plain_whole_frame"] = res[k]["msamples_per_s"] / base
+    print(json.dumps({"metric": "stress_forms_msamples_per_s", "unit": UNIT, "n_gpus": 1,
+                      "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": STRESS_WORKLOAD, "triangles": scene.num_triangles,
+                                 "resolution": [st.width, st.height], "spp": st.spp,
+                                 "max_bounces": st.max_bounces, "requests": q,
+                                 "scene_gen_s": round(gen_s, 1)},
+                      "forms": res,
+                      "stage_ms_whole_frame": {k: prof[k] for k in
+                                               ("raygen_ms", "extend_ms", "shade_ms", "shadow_ms",
+                                                "accumulate_ms")}}))
+
+
 # ------------------------------------------------------------------ plain path (default)
 def main():
     args = parse()
@@ -698,6 +771,8 @@ def main():
         return run_batch(args)
     if args.serve:
         return run_serve(args)
+    if args.stress_forms:
+        return run_stress_forms(args)
     import torch
     from petrichor_gb300 import capi
 
@@ -793,7 +868,7 @@ def main():
     if os.path.exists(peaks_path):
         with open(peaks_path) as fh:
             peak, peak_src = float(json.load(fh)["hbm_gbs"]), "measured"
-    l2 = l2_copy_peak(torch)
+    l2 = l2_read_peak(ctx)
     # small-case ncu counters of ExtendKernel (one kernel, three launches, 640x360 of the
     # same scene): DRAM bytes per ray, SIMT efficiency, issue-slot use
     cnt = counters_profile("extend_kernel_counters_spheres_grids_1M_640x360.json") \

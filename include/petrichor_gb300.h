@@ -391,6 +391,14 @@ int pt_get_tuning(pt_context* ctx, pt_tuning* out);
 int pt_render_replay_noalloc(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
                              const pt_settings* settings, float* film_rgb_device, void* stream);
 
+/* Measured L2 read bandwidth of this device, the roofline denominator of kernels
+ * served from L2: a `bytes` buffer (0: 32 MiB; it must fit in L2) read `passes`
+ * times per launch (0: 16) over `reps` launches (0: 10) with loads that bypass L1,
+ * timed with CUDA events. *gbs = bytes read / time. Allocates and frees its buffer.
+ * Synchronous. No reference counterpart (a measurement helper, like
+ * pt_render_profile). */
+int pt_probe_bandwidth(pt_context* ctx, uint64_t bytes, int32_t passes, int32_t reps, double* gbs);
+
 int pt_get_stats(pt_context* ctx, pt_stats* out);
 /* Tiles finished / total of the last replay render (reference tile grid). */
 int pt_get_progress(pt_context* ctx, uint32_t* rendered_tiles, uint32_t* num_tiles);

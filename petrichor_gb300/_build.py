@@ -22,7 +22,7 @@ LIB = os.path.join(OUT_DIR, "libpetrichor_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
-CU_SOURCES = ["replay.cu", "wavefront.cu", "noalloc.cu", "bvh_gpu.cu", "denoise.cu"]
+CU_SOURCES = ["replay.cu", "wavefront.cu", "noalloc.cu", "bvh_gpu.cu", "denoise.cu", "probe.cu"]
 # The throughput kernels use approximate division and square root (a few ulps), except
 # where the code asks for correctly rounded results (traversal reciprocals, the
 # triangle test); the replay kernel keeps IEEE arithmetic throughout.

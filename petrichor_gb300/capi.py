@@ -137,6 +137,7 @@ EXPORTED = [
     "pt_last_error", "pt_camera_init", "pt_scene_upload", "pt_scene_release",
     "pt_scene_info_get", "pt_render", "pt_render_device", "pt_trace_closest", "pt_get_stats",
     "pt_get_progress", "pt_bvh_build", "pt_render_profile", "pt_render_replay_noalloc", "pt_batch_render",
+    "pt_probe_bandwidth",
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
     "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
     "pt_render_aov", "pt_render_aov_device", "pt_bvh_build_device", "pt_set_bvh_builder",
@@ -200,6 +201,7 @@ def load(build: bool = True):
     L.pt_render_profile.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
                                     vp, i32, ctypes.POINTER(PtProfile)]
     L.pt_get_progress.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.pt_probe_bandwidth.argtypes = [vp, ctypes.c_uint64, i32, i32, ctypes.POINTER(ctypes.c_double)]
     L.pt_autotune.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings), i32,
                               ctypes.POINTER(PtTuning)]
     L.pt_set_tuning.argtypes = [vp, ctypes.POINTER(PtTuning)]
@@ -520,6 +522,13 @@ class Context:
         s = PtStats()
         self._check(self.L.pt_get_stats(self.h, ctypes.byref(s)), "pt_get_stats")
         return s
+
+    def probe_l2_read_gbs(self, bytes_: int = 0, passes: int = 0, reps: int = 0) -> float:
+        """Measured L2 read bandwidth (GB/s) of this context's device (pt_probe_bandwidth)."""
+        v = ctypes.c_double()
+        self._check(self.L.pt_probe_bandwidth(self.h, bytes_, passes, reps, ctypes.byref(v)),
+                    "pt_probe_bandwidth")
+        return v.value
 
     def progress(self):
         d, t = ctypes.c_uint32(), ctypes.c_uint32()

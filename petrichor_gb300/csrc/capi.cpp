@@ -1223,6 +1223,34 @@ int pt_set_bvh_builder(pt_context* ctx, int32_t builder) {
     return PT_OK;
 }
 
+int pt_probe_bandwidth(pt_context* ctx, uint64_t bytes, int32_t passes, int32_t reps, double* gbs) {
+    if (!ctx || !gbs || passes < 0 || reps < 0) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (bytes == 0) bytes = uint64_t(32) << 20;
+    if (passes == 0) passes = 16;
+    if (reps == 0) reps = 10;
+    bytes &= ~uint64_t(15);
+    if (bytes == 0) return Fail(ctx, PT_ERR_INVALID_ARG, "probe buffer under 16 bytes");
+    int rc = SetDevice(ctx);
+    if (rc != PT_OK) return rc;
+    DeviceBuffer buf, sink;
+    if ((rc = Alloc(ctx, buf, bytes)) != PT_OK) return rc;
+    if ((rc = Alloc(ctx, sink, 16)) != PT_OK) {
+        Free(ctx, buf);
+        return rc;
+    }
+    cudaError_t e = cudaMemsetAsync(buf.ptr, 0, bytes, ctx->stream);
+    float ms = 0.0f;
+    if (e == cudaSuccess)
+        e = ProbeL2Read(buf.ptr, bytes, passes, reps, (float*)sink.ptr, ctx->stream, &ms);
+    ctx->stats.kernel_launches += reps + 1;
+    Free(ctx, buf);
+    Free(ctx, sink);
+    if (e != cudaSuccess) return CudaFail(ctx, e, "bandwidth probe");
+    *gbs = (double)bytes * passes * reps / (ms / 1e3) / 1e9;
+    return PT_OK;
+}
+
 int pt_get_stats(pt_context* ctx, pt_stats* out) {
     if (!ctx || !out) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> g(ctx->mu);

@@ -18,6 +18,11 @@ constexpr int kWaveStackDepth = 64;
 
 int NumTiles(const DevSettings& st);
 
+// Reads `bytes` of `buf` (L2-resident sizes) `passes` times per launch, `reps` launches
+// after one warm-up; *ms = CUDA-event time of the reps launches (probe.cu).
+cudaError_t ProbeL2Read(const void* buf, size_t bytes, int passes, int reps, float* sink,
+                        cudaStream_t stream, float* ms);
+
 // Replay: one thread per tile in [tileBegin, tileEnd). stackScratch holds
 // (tileEnd - tileBegin) * S.stackDepth ints. status receives error bits (OR).
 cudaError_t LaunchReplay(const DevScene& S, const DevCamera& C, const DevSettings& st, float* film,
