@@ -51,10 +51,12 @@ struct DevJob {
 
 // One job's samples [s0, s0 + sw) over all its pixels: paths
 // [pathBase, pathBase + W*H*sw) of the wave, pixel-major (pixel q of the band order owns
-// paths pathBase + q*sw .. + sw - 1); pixelBase indexes the accumulate pass.
+// paths pathBase + q*sw .. + sw - 1); pixelBase indexes the accumulate pass. recBase:
+// for a unit whose first bounce is rasterised, its first per-triangle record in the
+// raster scratch (the wave's raster units come last); -1 otherwise.
 struct WaveUnit {
     int32_t job, s0, sw, pathBase;
-    int32_t pixelBase, pad[3];
+    int32_t pixelBase, recBase, pad[2];
 };
 
 // Scalars of the wave being run, read by the kernels from device memory so that
@@ -63,7 +65,9 @@ struct WaveDesc {
     int32_t nUnits, nPaths, nPixelUnits;
     int32_t soleJob;  // the wave's only job, or -1 (then read pathJob)
     int32_t band;     // rows per pixel band of the path order
-    int32_t pad[3];
+    // rasterised first bounce: paths [rasterFrom, nPaths) of units [rasterUnit0, nUnits),
+    // with rasterRecs per-triangle records in all
+    int32_t rasterFrom, rasterUnit0, rasterRecs;
 };
 
 // Path state travels with its ray through the compacted queues (so the shade
@@ -114,10 +118,9 @@ struct WaveProfile {
 struct WaveShape {
     int nUnits = 0, nPaths = 0, nPixelUnits = 0;
     int iters = 0, integrator = -1, soleJob = -1;
-    // > 0: the first bounce may be rasterised (raster_primary.cuh): the triangle count of
-    // the wave's one unit of one pinhole-camera PathTracing job, with at least two rays per
-    // triangle
-    int raster = 0;
+    // > 0: the first bounce of units [rasterUnit0, nUnits) (paths [rasterFrom, nPaths)) may
+    // be rasterised (raster_primary.cuh); raster = their per-triangle records in all
+    int raster = 0, rasterFrom = 0, rasterUnit0 = 0;
 };
 // Launch configuration (all choices give the same films). 0 = default.
 struct WaveTuning {

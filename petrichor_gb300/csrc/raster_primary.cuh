@@ -1,9 +1,11 @@
 // Primary visibility by rasterisation (included by wavefront.cu inside namespace ptg).
 //
-// The first bounce of a wave whose one job looks through a pinhole (every primary ray
+// The first bounce of a wave unit whose job looks through a pinhole (every primary ray
 // starts at the camera position) is computed by visiting, for each triangle, the
-// samples whose rays can reach it, instead of tracing each ray through the BVH:
-//   setup  one thread per triangle: the three planes through the camera and the
+// samples whose rays can reach it, instead of tracing each ray through the BVH. The
+// wave's rasterised units come after its traced ones (PrepareRasterUnits), so the extend
+// kernel traces paths [0, rasterFrom) and these kernels settle [rasterFrom, nPaths):
+//   setup  one thread per (unit, triangle): the three planes through the camera and the
 //          triangle's edges (the cone a ray must lie in to hit it, widened by a small
 //          angular margin) and the rectangle of pixels it covers (its vertices
 //          projected with the camera's own mapping, one pixel of margin for the sample
@@ -32,22 +34,35 @@ struct RasterScratch {
     unsigned long long* key;  // per path: {distance bits, slot}, kNoKey = no hit
     unsigned* tie;            // per path: smallest distance bits at which two triangles tied
     float4* rec;              // per triangle: 4 float4 (cone planes with margins, pixel rect)
-    uint2* items;             // {triangle slot, row | segment << 16}
-    int* overflow;            // triangles whose items did not fit (visited whole)
+    uint4* items;             // {triangle slot, unit, row | segment << 16, 0}
+    int2* overflow;           // {triangle slot, unit} whose items did not fit (visited whole)
     long long itemCap;
 };
 
-__device__ __forceinline__ RasterScratch CarveRaster(const WaveBuffers& wb, int cur, int numTris) {
+// numRecs: the wave's per-triangle records over all its rasterised units.
+__device__ __forceinline__ RasterScratch CarveRaster(const WaveBuffers& wb, int cur, int numRecs) {
     const size_t C = (size_t)wb.capacity;
     RasterScratch r;
     r.key = reinterpret_cast<unsigned long long*>(wb.ray[cur ^ 1]);
     r.tie = reinterpret_cast<unsigned*>(r.key + C);
     r.rec = wb.shadow;
-    r.overflow = reinterpret_cast<int*>(wb.shadow + 4 * (size_t)numTris);
-    r.items = reinterpret_cast<uint2*>(r.overflow + ((numTris + 3) & ~3));
-    const long long bytes = (long long)(64 * C) - 64LL * numTris - 4LL * ((numTris + 3) & ~3);
-    r.itemCap = bytes > 0 ? bytes / 8 : 0;
+    const size_t over = ((size_t)numRecs + 1) & ~(size_t)1;  // int2 entries, 16-byte multiple
+    r.overflow = reinterpret_cast<int2*>(wb.shadow + 4 * (size_t)numRecs);
+    r.items = reinterpret_cast<uint4*>(r.overflow + over);
+    const long long bytes = (long long)(64 * C) - 64LL * numRecs - 8LL * (long long)over;
+    r.itemCap = bytes > 0 ? bytes / 16 : 0;
     return r;
+}
+
+// The rasterised unit that owns record r (units [u0, n) with ascending recBase).
+__device__ __forceinline__ int RasterUnitOf(const WaveUnit* __restrict__ units, int u0, int n, int r) {
+    int lo = u0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (units[mid].recBase <= r) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // Pixel coordinate (continuous, origin at the image corner) of a point with camera-basis
@@ -63,22 +78,26 @@ __device__ __forceinline__ void ProjectPx(const DevCamera& c, float X, float Y, 
 }
 
 __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restrict__ jobs,
+                                                         const WaveUnit* __restrict__ units,
                                                          WaveBuffers wb, int cur) {
     const WaveDesc wd = *wb.desc;
-    const DevJob& J = jobs[wd.soleJob];
-    const DevScene& S = J.S;
-    const int T = S.numTris, W = J.st.width, H = J.st.height;
-    const RasterScratch rs = CarveRaster(wb, cur, T);
-    const V3 pos = LoadV3(J.C.pos), right = LoadV3(J.C.right), up = LoadV3(J.C.up),
-             fwd = LoadV3(J.C.fwd);
-    const float rr = 1.0f / SqLen(right), uu = 1.0f / SqLen(up);
+    const int R = wd.rasterRecs;
+    const RasterScratch rs = CarveRaster(wb, cur, R);
     const int lane = threadIdx.x & 31;
     // whole warps step together (the item appends are warp-aggregated)
-    for (int base = blockIdx.x * blockDim.x; base < T; base += gridDim.x * blockDim.x) {
-        const int k = base + threadIdx.x;
-        int nItems = 0;
+    for (int base = blockIdx.x * blockDim.x; base < R; base += gridDim.x * blockDim.x) {
+        const int rec = base + threadIdx.x;
+        int nItems = 0, unit = 0, k = 0;
         int x0 = 0, x1 = -1, y0 = 0, y1 = -1;
-        if (k < T) {
+        if (rec < R) {
+            unit = RasterUnitOf(units, wd.rasterUnit0, wd.nUnits, rec);
+            k = rec - units[unit].recBase;
+            const DevJob& J = jobs[units[unit].job];
+            const DevScene& S = J.S;
+            const int W = J.st.width, H = J.st.height;
+            const V3 pos = LoadV3(J.C.pos), right = LoadV3(J.C.right), up = LoadV3(J.C.up),
+                     fwd = LoadV3(J.C.fwd);
+            const float rr = 1.0f / SqLen(right), uu = 1.0f / SqLen(up);
             V3 v0, e1, e2;
             LoadTri(S.tris, k, v0, e1, e2);
             const V3 a[3] = {v0 - pos, (v0 + e1) - pos, (v0 + e2) - pos};
@@ -143,7 +162,7 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
             }
             if (x0 <= x1 && y0 <= y1) {
                 nItems = (y1 - y0 + 1) * ((x1 - x0 + kRasterSeg) / kRasterSeg);
-                float4* r = rs.rec + 4 * (size_t)k;
+                float4* r = rs.rec + 4 * (size_t)rec;
                 r[0] = make_float4(n[0].x, n[0].y, n[0].z, m[0]);
                 r[1] = make_float4(n[1].x, n[1].y, n[1].z, m[1]);
                 r[2] = make_float4(n[2].x, n[2].y, n[2].z, m[2]);
@@ -169,10 +188,11 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
                 long long it = first;
                 for (int y = y0; y <= y1; y++)
                     for (int sgi = 0; sgi < segs; sgi++)
-                        rs.items[it++] = make_uint2((unsigned)k, (unsigned)y | ((unsigned)sgi << 16));
+                        rs.items[it++] = make_uint4((unsigned)k, (unsigned)unit,
+                                                    (unsigned)y | ((unsigned)sgi << 16), 0u);
             } else {
                 const int o = atomicAdd(wb.counts + 10, 1);
-                rs.overflow[o] = k;
+                rs.overflow[o] = make_int2(k, unit);
             }
         }
     }
@@ -182,11 +202,11 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
 // Pixel (x, y) is pixel q = qrow + x * hb of the band order (PixelOfIndex), and its
 // samples are paths pathBase + q * sw + j, whose directions are in the ray queue.
 __device__ __forceinline__ void RasterSegment(const RasterScratch& rs, const float4* __restrict__ rays,
-                                             const float4* __restrict__ tris, int k, int y, int xa,
-                                             int xb, int W, int H, int band, int pathBase, int sw,
-                                             V3 o, float tmin, int lane) {
-    const float4 r0 = __ldg(rs.rec + 4 * (size_t)k), r1 = __ldg(rs.rec + 4 * (size_t)k + 1),
-                 r2 = __ldg(rs.rec + 4 * (size_t)k + 2);
+                                             const float4* __restrict__ tris, int k, int rec, int y,
+                                             int xa, int xb, int W, int H, int band, int pathBase,
+                                             int sw, V3 o, float tmin, int lane) {
+    const float4 r0 = __ldg(rs.rec + 4 * (size_t)rec), r1 = __ldg(rs.rec + 4 * (size_t)rec + 1),
+                 r2 = __ldg(rs.rec + 4 * (size_t)rec + 2);
     V3 v0, e1, e2;
     LoadTri(tris, k, v0, e1, e2);
     const int y0 = (y / band) * band, hb = min(band, H - y0);
@@ -219,56 +239,63 @@ __device__ __forceinline__ void RasterSegment(const RasterScratch& rs, const flo
     }
 }
 
+// One work item's (row segment's) unit: its job's scene, camera and image, its paths.
+__device__ __forceinline__ void RasterItem(const DevJob* __restrict__ jobs, const WaveUnit& u,
+                                          const RasterScratch& rs, const float4* __restrict__ rays,
+                                          int band, int k, int y, int xa, int xb, int lane) {
+    const DevJob& J = jobs[u.job];
+    const float tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
+    RasterSegment(rs, rays, J.S.tris, k, u.recBase + k, y, xa, xb, J.st.width, J.st.height, band,
+                  u.pathBase, u.sw, LoadV3(J.C.pos), tmin, lane);
+}
+
 __global__ void __launch_bounds__(128) RasterVisitKernel(const DevJob* __restrict__ jobs,
                                                          const WaveUnit* __restrict__ units,
                                                          WaveBuffers wb, int cur) {
     const WaveDesc wd = *wb.desc;
-    const DevJob& J = jobs[wd.soleJob];
-    const int T = J.S.numTris, W = J.st.width, H = J.st.height, band = wd.band;
-    const RasterScratch rs = CarveRaster(wb, cur, T);
+    const RasterScratch rs = CarveRaster(wb, cur, wd.rasterRecs);
     const float4* rays = wb.ray[cur];
-    const WaveUnit u = units[0];
-    const float tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
-    const V3 o = LoadV3(J.C.pos);
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
     long long nItems = *reinterpret_cast<const long long*>(wb.counts + 8);
     if (nItems > rs.itemCap) nItems = rs.itemCap;
     for (long long w = warp; w < nItems; w += warps) {
-        const uint2 it = rs.items[w];
-        const int k = (int)it.x, y = (int)(it.y & 0xffffu), sg = (int)(it.y >> 16);
+        const uint4 it = rs.items[w];
+        const int k = (int)it.x, y = (int)(it.z & 0xffffu), sg = (int)(it.z >> 16);
+        const WaveUnit u = units[it.y];
 #if PT_CHECK
-        if (k < 0 || k >= T) continue;
+        if (k < 0 || k >= jobs[u.job].S.numTris) continue;
 #endif
-        const float4 r3 = __ldg(rs.rec + 4 * (size_t)k + 3);
+        const float4 r3 = __ldg(rs.rec + 4 * (size_t)(u.recBase + k) + 3);
         const int xa = __float_as_int(r3.x) + sg * kRasterSeg;
         const int xb = min(__float_as_int(r3.y), xa + kRasterSeg - 1);
-        RasterSegment(rs, rays, J.S.tris, k, y, xa, xb, W, H, band, u.pathBase, u.sw, o, tmin, lane);
+        RasterItem(jobs, u, rs, rays, wd.band, k, y, xa, xb, lane);
     }
     // triangles whose items did not fit in the list: whole, one warp each
     const int nOver = wb.counts[10];
     for (long long w = warp; w < nOver; w += warps) {
-        const int k = rs.overflow[w];
-        const float4 r3 = __ldg(rs.rec + 4 * (size_t)k + 3);
+        const int2 ov = rs.overflow[w];
+        const WaveUnit u = units[ov.y];
+        const float4 r3 = __ldg(rs.rec + 4 * (size_t)(u.recBase + ov.x) + 3);
         const int x0 = __float_as_int(r3.x), x1 = __float_as_int(r3.y), y0 = __float_as_int(r3.z),
                   y1 = __float_as_int(r3.w);
         for (int y = y0; y <= y1; y++)
             for (int xa = x0; xa <= x1; xa += kRasterSeg)
-                RasterSegment(rs, rays, J.S.tris, k, y, xa, min(x1, xa + kRasterSeg - 1), W, H, band,
-                              u.pathBase, u.sw, o, tmin, lane);
+                RasterItem(jobs, u, rs, rays, wd.band, ov.x, y, xa, min(x1, xa + kRasterSeg - 1), lane);
     }
 }
 
 // The nearest hit of every path into the hit queue (queue entry i = path i at the first
 // bounce), as ExtendKernel would write it: {distance, slot}, {kFltMax, -1} for a miss,
 // -2 - slot when another triangle tied at that distance.
-__global__ void RasterFinishKernel(const DevJob* __restrict__ jobs, WaveBuffers wb, int cur) {
+__global__ void RasterFinishKernel(WaveBuffers wb, int cur) {
     const WaveDesc wd = *wb.desc;
-    const RasterScratch rs = CarveRaster(wb, cur, jobs[wd.soleJob].S.numTris);
+    const RasterScratch rs = CarveRaster(wb, cur, wd.rasterRecs);
     const int n = wd.nPaths;
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur ^ 1] = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = wd.rasterFrom + blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
         const unsigned long long key = rs.key[i];
         float2 h = make_float2(kFltMax, __int_as_float(-1));
         if (key != kNoKey) {

@@ -64,6 +64,49 @@ int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
     return integ < 0 ? -1 : integ;
 }
 
+void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* units,
+                        WaveShape* shape) {
+    shape->raster = 0;
+    shape->rasterFrom = shape->nPaths;
+    shape->rasterUnit0 = (int)units->size();
+    std::vector<WaveUnit> trace, raster;
+    for (WaveUnit u : *units) {
+        const DevJob& J = jobs[u.job];
+        const int64_t paths = (int64_t)J.st.width * J.st.height * u.sw;
+        const bool ok = shape->iters >= 0 && J.C.aperture == 0.0f && J.S.numTris > 0 &&
+                        J.st.height < 65536 && J.st.integrator == kPathTracing &&
+                        paths >= 2 * (int64_t)J.S.numTris &&
+                        (int64_t)shape->raster + J.S.numTris < (int64_t(1) << 30);
+        u.recBase = -1;
+        if (ok) {
+            u.recBase = shape->raster;
+            shape->raster += J.S.numTris;
+            raster.push_back(u);
+        } else {
+            trace.push_back(u);
+        }
+    }
+    if (raster.empty()) {
+        for (WaveUnit& u : *units) u.recBase = -1;
+        return;
+    }
+    // traced units first, rasterised units last; path and pixel ranges follow the order
+    units->clear();
+    units->insert(units->end(), trace.begin(), trace.end());
+    units->insert(units->end(), raster.begin(), raster.end());
+    int paths = 0, pixels = 0;
+    for (size_t k = 0; k < units->size(); k++) {
+        WaveUnit& u = (*units)[k];
+        const int P = jobs[u.job].st.width * jobs[u.job].st.height;
+        if (k == trace.size()) shape->rasterFrom = paths;
+        u.pathBase = paths;
+        u.pixelBase = pixels;
+        paths += P * u.sw;
+        pixels += P;
+    }
+    shape->rasterUnit0 = (int)trace.size();
+}
+
 int WaveSoleJob(const std::vector<WaveUnit>& units) {
     for (const WaveUnit& u : units)
         if (u.job != units.front().job) return -1;
@@ -72,7 +115,7 @@ int WaveSoleJob(const std::vector<WaveUnit>& units) {
 
 namespace {
 
-WaveShape ShapeOf(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units) {
+WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units) {
     WaveShape shape;
     for (const WaveUnit& u : units) {
         const int P = jobs[u.job].st.width * jobs[u.job].st.height;
@@ -83,12 +126,7 @@ WaveShape ShapeOf(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& 
     shape.iters = WaveIterations(jobs, units);
     shape.integrator = WaveIntegrator(jobs, units);
     shape.soleJob = WaveSoleJob(units);
-    if (shape.soleJob >= 0 && units.size() == 1 && shape.iters >= 0) {
-        const DevJob& J = jobs[shape.soleJob];
-        shape.raster = J.C.aperture == 0.0f && J.S.numTris > 0 && J.st.height < 65536 &&
-                       J.st.integrator == kPathTracing &&
-                       (int64_t)shape.nPaths >= 2 * (int64_t)J.S.numTris ? J.S.numTris : 0;
-    }
+    PrepareRasterUnits(jobs, &units, &shape);
     return shape;
 }
 
@@ -157,13 +195,14 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
     if (!twoLanes) {
         e = cudaMemsetAsync(wb.counts, 0, 16 * sizeof(int), stream);
         for (size_t w = 0; w < waves.size() && e == cudaSuccess; w++) {
-            const std::vector<WaveUnit>& units = waves[w];
+            std::vector<WaveUnit>& units = waves[w];
+            const WaveShape shape = ShapeOf(jobs, units);  // may reorder the units
             // pageable source: the copy is staged before the call returns, so the
             // next wave may reuse the host vector
             e = cudaMemcpyAsync(T.units, units.data(), units.size() * sizeof(WaveUnit),
                                 cudaMemcpyHostToDevice, stream);
             if (e == cudaSuccess)
-                e = RunWave(T.jobs, T.units, ShapeOf(jobs, units), wb, stream, launches, prof, tune, graphs);
+                e = RunWave(T.jobs, T.units, shape, wb, stream, launches, prof, tune, graphs);
             if (e == cudaSuccess) e = FinalizeDone(jobs, T, lastWave, w, stream, launches, prof);
         }
         return e;
@@ -177,12 +216,13 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
     for (size_t w = 0; w < waves.size() && e == cudaSuccess; w++) {
         const int k = (int)(w & 1);
         cudaStream_t s = laneStream[k];
-        const std::vector<WaveUnit>& units = waves[w];
+        std::vector<WaveUnit>& units = waves[w];
+        const WaveShape shape = ShapeOf(jobs, units);  // may reorder the units
         e = cudaMemcpyAsync(unitTable[k], units.data(), units.size() * sizeof(WaveUnit),
                             cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
-            e = RunWave(T.jobs, unitTable[k], ShapeOf(jobs, units), lane[k], s, launches, nullptr, tune,
-                        graphs, k, false);
+            e = RunWave(T.jobs, unitTable[k], shape, lane[k], s, launches, nullptr, tune, graphs, k,
+                        false);
         // accumulate and finalise after the previous wave did
         if (e == cudaSuccess && w > 0) e = cudaStreamWaitEvent(s, done[k ^ 1], 0);
         if (e == cudaSuccess) e = AccumulateWave(T.jobs, unitTable[k], lane[k], tune, s, launches);

@@ -38,5 +38,12 @@ int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
 int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
 // The job of all of a wave's units, or -1 when they belong to several.
 int WaveSoleJob(const std::vector<WaveUnit>& units);
+// Picks the units whose first bounce is rasterised (a pinhole PathTracing job with at
+// least two of the unit's rays per triangle; none in a queue-polled wave), moves them
+// after the traced units, renumbers every unit's path and pixel ranges, gives each its
+// record base, and sets shape's raster, rasterFrom and rasterUnit0 (shape's nPaths and
+// iters already set). A wave's films do not depend on its unit order.
+void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* units,
+                        WaveShape* shape);
 
 }  // namespace ptg

@@ -430,17 +430,19 @@ private:
             if (e == cudaSuccess) e = cudaMemsetAsync(J.accum, 0, r->accumBytes, stream_);
         }
         if (units.empty()) return e;
+        WaveShape shape;
+        shape.nUnits = (int)units.size();
+        shape.nPaths = paths;
+        shape.nPixelUnits = pixels;
+        shape.iters = WaveIterations(slotJobs_, units);
+        shape.integrator = WaveIntegrator(slotJobs_, units);
+        shape.soleJob = WaveSoleJob(units);
+        std::vector<WaveUnit> ordered = units;  // rasterised units last
+        PrepareRasterUnits(slotJobs_, &ordered, &shape);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(units_.ptr, units.data(), units.size() * sizeof(WaveUnit),
+            e = cudaMemcpyAsync(units_.ptr, ordered.data(), ordered.size() * sizeof(WaveUnit),
                                 cudaMemcpyHostToDevice, stream_);
         if (e == cudaSuccess) {
-            WaveShape shape;
-            shape.nUnits = (int)units.size();
-            shape.nPaths = paths;
-            shape.nPixelUnits = pixels;
-            shape.iters = WaveIterations(slotJobs_, units);
-            shape.integrator = WaveIntegrator(slotJobs_, units);
-            shape.soleJob = WaveSoleJob(units);
             e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, shape, wb_, stream_, launches,
                         nullptr, tune_, graphs_);
         }

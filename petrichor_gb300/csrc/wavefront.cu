@@ -386,7 +386,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         rng.Next(r2, r3);
         Ray ray = GenerateRay<FastMath>(J.C, x, y, W, H, r0, r1, r2, r3);
         if (J.C.aperture == 0.0f) ray.o = LoadV3(J.C.pos);  // a pinhole: exactly the camera position
-        if (raster) {
+        if (raster && i >= wd.rasterFrom) {
             rs.key[i] = kNoKey;
             rs.tie[i] = 0xffffffffu;
         }
@@ -443,9 +443,10 @@ struct ExtendQueue {
 
 // counts: [0],[1] ray queues, [2] shadow queue, [3] error bits,
 //         [4] extend fetch counter, [5] shadow fetch counter, [6] shadow blocks finished
+// rasterFirst: the first bounce, whose paths from wb.desc->rasterFrom on are rasterised
 __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
-                                                    int cur) {
-    const int n = wb.counts[cur];
+                                                    int cur, int rasterFirst) {
+    const int n = rasterFirst ? min(wb.counts[cur], wb.desc->rasterFrom) : wb.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur ^ 1] = 0;
     int err = 0;
     ExtendQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.ray[cur], wb.hit};
@@ -1298,7 +1299,7 @@ struct StageOverlap {
 static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveBuffers& wb,
                           int integrator, int grid, int it0, int count, cudaStream_t stream,
                           WaveProfile* prof, int* nl, bool sort, StageOverlap* ov, int tailFrom = 0,
-                          int rasterTris = 0) {
+                          bool raster = false) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     const int block = kTraceBlock;
     const int sgrid = ShadeGrid(grid);
@@ -1322,14 +1323,14 @@ static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveB
             break;
         }
         if (ev) ev->Begin(1, stream);
-        if (it == 0 && rasterTris > 0) {  // first bounce rasterised (raster_primary.cuh)
-            const int sgrid = std::max(1, std::min((rasterTris + block - 1) / block, SmCount() * 32));
-            RasterSetupKernel<<<sgrid, block, 0, stream>>>(jobs, wb, cur);
+        if (it == 0 && raster) {  // the traced units' paths, then the rasterised ones
+            ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, 1);
+            RasterSetupKernel<<<SmCount() * 32, block, 0, stream>>>(jobs, units, wb, cur);
             RasterVisitKernel<<<SmCount() * 16, block, 0, stream>>>(jobs, units, wb, cur);
-            RasterFinishKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
-            *nl += 2;  // one more below
+            RasterFinishKernel<<<grid, block, 0, stream>>>(wb, cur);
+            *nl += 3;  // one more below
         } else {
-            ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+            ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, 0);
         }
         if (ev) {
             ev->End(1, stream);
@@ -1495,6 +1496,12 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     d.nPixelUnits = shape.nPixelUnits;
     d.soleJob = shape.soleJob;
     d.band = tune.band > 0 ? tune.band : 8;
+    // the first bounce rasterised where the wave allows it (raster_primary.cuh)
+    const bool raster = shape.raster > 0 && !tune.primaryTraversal && tune.sortRays == 0 &&
+                        shape.iters >= 0;
+    d.rasterFrom = raster ? shape.rasterFrom : shape.nPaths;
+    d.rasterUnit0 = raster ? shape.rasterUnit0 : shape.nUnits;
+    d.rasterRecs = raster ? shape.raster : 0;
     cudaError_t e = cudaMemcpyAsync(wb.desc, &d, sizeof(d), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     int nl = 0;
@@ -1506,16 +1513,13 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     // whose stage timers need one stream)
     StageOverlap* ov =
       (graphs && !prof && graphs->overlap[lane & 1].Ready()) ? &graphs->overlap[lane & 1] : nullptr;
-    // the first bounce rasterised where the wave allows it (raster_primary.cuh)
-    const int rasterTris =
-      (shape.raster > 0 && !tune.primaryTraversal && !sort && shape.iters >= 0) ? shape.raster : 0;
     const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
-                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom, rasterTris};
+                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom, raster ? 1 : 0};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
-            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, rasterTris > 0);
+            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, raster ? 1 : 0);
             LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort,
-                          ov, tailFrom, rasterTris);
+                          ov, tailFrom, raster);
             if (accumulate) AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             *n += accumulate ? 2 : 1;
         };
@@ -1523,10 +1527,10 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             e = ReplayCaptured(graphs, key, stream, &nl, record);
         } else {
             if (ev) ev->Begin(0, stream);
-            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, rasterTris > 0);
+            RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, raster ? 1 : 0);
             if (ev) ev->End(0, stream);
             LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort,
-                          ov, tailFrom, rasterTris);
+                          ov, tailFrom, raster);
             if (accumulate) {
                 if (ev) ev->Begin(4, stream);
                 AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);

@@ -69,6 +69,22 @@ def test_batch_of_repeated_jobs(served):
         assert np.array_equal(f.cpu().numpy().view(np.uint32), solo[idx].view(np.uint32))
 
 
+def test_batch_first_bounce_traced_or_rasterised_alike(served):
+    """In a batched wave the units whose first bounce can be rasterised (pinhole
+    PathTracing jobs with enough rays per triangle) are, the others traced; with the
+    first bounce traced for every unit the films are the same bits."""
+    ctx, jobs, solo = served
+    seq = [jobs[0], jobs[1], jobs[3], jobs[0]]
+    for traced in (1, 0):
+        ctx.set_tuning(primary_traversal=traced)
+        films = [torch.empty(j[2].width * j[2].height * 3, device="cuda") for j in seq]
+        ctx.batch_render([(sid, cam, st, f.data_ptr()) for (sid, cam, st), f in zip(seq, films)])
+        torch.cuda.synchronize()
+        for f, idx in zip(films, [0, 1, 3, 0]):
+            assert np.array_equal(f.cpu().numpy().view(np.uint32), solo[idx].view(np.uint32)), traced
+    ctx.set_tuning()
+
+
 def test_serve_request_same_alone_and_in_mix(served):
     ctx, jobs, solo = served
     # small waves so every request spans several waves and shares them with others
