@@ -29,6 +29,7 @@
 
 constexpr int kRasterSeg = 32;  // pixels per work item (one row segment)
 constexpr unsigned long long kNoKey = ~0ull;
+constexpr unsigned kNoItem = ~0u;  // an empty work-list slot
 
 struct RasterScratch {
     unsigned long long* key;  // per path: {distance bits, slot}, kNoKey = no hit
@@ -191,6 +192,10 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
                         rs.items[it++] = make_uint4((unsigned)k, (unsigned)unit,
                                                     (unsigned)y | ((unsigned)sgi << 16), 0u);
             } else {
+                // the list is full: the triangle is visited whole; the part of its
+                // reservation that lies inside the list is marked empty, so every slot the
+                // visit kernel reads was written
+                for (long long it = first; it < rs.itemCap; it++) rs.items[it] = make_uint4(kNoItem, 0u, 0u, 0u);
                 const int o = atomicAdd(wb.counts + 10, 1);
                 rs.overflow[o] = make_int2(k, unit);
             }
@@ -262,6 +267,7 @@ __global__ void __launch_bounds__(128) RasterVisitKernel(const DevJob* __restric
     if (nItems > rs.itemCap) nItems = rs.itemCap;
     for (long long w = warp; w < nItems; w += warps) {
         const uint4 it = rs.items[w];
+        if (it.x == kNoItem) continue;
         const int k = (int)it.x, y = (int)(it.z & 0xffffu), sg = (int)(it.z >> 16);
         const WaveUnit u = units[it.y];
 #if PT_CHECK

@@ -42,6 +42,10 @@ def _scenes():
                                       env_width=128, env_height=64),
         # a camera inside the box: walls reach behind the camera plane (whole-image rectangles)
         "inside": _inside_box(),
+        # one ray per two triangles at 1 spp: the raster work list fills up, and the
+        # triangles that do not fit are visited whole
+        "overflow": synth.spheres_grids(tri_budget=60000, width=360, height=340, spp=1,
+                                        max_bounces=4, env_width=128, env_height=64),
     }
 
 
@@ -72,7 +76,7 @@ def _render(ctx, sid, cam, st):
     return film.cpu().numpy()
 
 
-@pytest.mark.parametrize("name", ["pt", "simple", "tris", "raster", "inside"])
+@pytest.mark.parametrize("name", ["pt", "simple", "tris", "raster", "inside", "overflow"])
 def test_films_do_not_depend_on_launch_configuration(tuned_ctx, name):
     ctx, jobs = tuned_ctx
     sid, cam, st = jobs[name]
