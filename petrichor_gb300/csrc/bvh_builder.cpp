@@ -284,11 +284,12 @@ struct WideCollapser {
     int32_t Node(int bi) {
         const BvhNodeOut& n = b.nodes[bi];
         if (n.leaf) return Leaf(n);
-        std::vector<int> cand = {n.child[0], n.child[1]};
-        while ((int)cand.size() < K) {
+        int cand[8] = {n.child[0], n.child[1]};
+        int nc = 2;
+        while (nc < K) {
             int best = -1;
             float bestA = -1.0f;
-            for (int i = 0; i < (int)cand.size(); i++)
+            for (int i = 0; i < nc; i++)
                 if (!b.nodes[cand[i]].leaf && Area(b.nodes[cand[i]]) > bestA) {
                     bestA = Area(b.nodes[cand[i]]);
                     best = i;
@@ -296,10 +297,10 @@ struct WideCollapser {
             if (best < 0) break;
             const int open = cand[best];
             cand[best] = b.nodes[open].child[0];
-            cand.push_back(b.nodes[open].child[1]);
+            cand[nc++] = b.nodes[open].child[1];
         }
         const int w = NewNode();
-        for (int i = 0; i < (int)cand.size(); i++) {
+        for (int i = 0; i < nc; i++) {
             const BvhNodeOut& c = b.nodes[cand[i]];
             const int32_t code = c.leaf ? Leaf(c) : Node(cand[i]);
             SetChild(w, i, c.lo, c.hi, code);
@@ -314,6 +315,7 @@ bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width) {
     wide->clear();
     if (bvh.primIds.empty()) return true;
     if (width < 2 || width > 8) return false;
+    wide->reserve((bvh.nodes.size() / 3 + 16) * (size_t)WideNodeFloats(width));
     WideCollapser c{bvh, *wide, width};
     const BvhNodeOut& root = bvh.nodes[0];
     float m = 0.0f;

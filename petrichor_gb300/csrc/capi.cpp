@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bvh_builder.h"
@@ -42,6 +43,26 @@ int CudaFail(pt_context* ctx, cudaError_t e, const char* what) {
                         e == cudaErrorHardwareStackError;
     return Fail(ctx, sticky ? PT_ERR_DEVICE_FAULT : PT_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// fn(i) for i in [0, n) on the host's cores (serially for small n); fn must be safe to
+// run concurrently for different i.
+template <class F>
+void ParallelFor(size_t n, F&& fn) {
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min<size_t>(hw, n / 65536 + 1);
+    if (nt <= 1) {
+        for (size_t i = 0; i < n; i++) fn(i);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const size_t chunk = (n + nt - 1) / nt;
+    for (size_t t = 0; t < nt; t++)
+        pool.emplace_back([&, t] {
+            const size_t e = std::min(n, (t + 1) * chunk);
+            for (size_t i = t * chunk; i < e; i++) fn(i);
+        });
+    for (std::thread& th : pool) th.join();
 }
 
 int Alloc(pt_context* ctx, DeviceBuffer& b, size_t bytes) {
@@ -571,7 +592,8 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     std::memcpy(wide.data(), wideF.data(), wideF.size() * sizeof(float));
     // triangles in leaf order
     std::vector<float4> tris((size_t)T * 3);
-    for (int k = 0; k < T; k++) {
+    ParallelFor((size_t)T, [&](size_t kk) {
+        const int k = (int)kk;
         const int t = bvh.primIds[k];
         const HV3 v0 = Load(d->positions + 3 * d->indices[3 * t]);
         const HV3 e1 = Sub(Load(d->positions + 3 * d->indices[3 * t + 1]), v0);
@@ -579,11 +601,12 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         tris[3 * (size_t)k] = F4(v0.x, v0.y, v0.z, e1.x);
         tris[3 * (size_t)k + 1] = F4(e1.y, e1.z, e2.x, e2.y);
         tris[3 * (size_t)k + 2] = F4(e2.z, IntBits(t), 0.0f, 0.0f);
-    }
+    });
     // shading records, also in leaf order: a hit's slot addresses both records
     // without a dependent read of the triangle id
     std::vector<float4> shade((size_t)T * 3);
-    for (int k = 0; k < T; k++) {
+    ParallelFor((size_t)T, [&](size_t kk) {
+        const int k = (int)kk;
         const int t = bvh.primIds[k];
         HV3 n[3] = {{0, 0, 1}, {0, 0, 1}, {0, 0, 1}};
         if (d->normals)
@@ -592,7 +615,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         shade[3 * (size_t)k] = F4(n[0].x, n[0].y, n[0].z, IntBits(d->tri_material[t]));
         shade[3 * (size_t)k + 1] = F4(n[1].x, n[1].y, n[1].z, IntBits(smooth));
         shade[3 * (size_t)k + 2] = F4(n[2].x, n[2].y, n[2].z, 0.0f);
-    }
+    });
     // vertex uvs in leaf order, for the UV pass and texture maps (omitted when the
     // scene has neither)
     bool anyTex = false;
@@ -603,24 +626,32 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         for (size_t i = 0; i < (size_t)d->num_vertices * 3 && !anyUV; i++) anyUV = d->uvs[i] != 0.0f;
     if (anyUV || anyTex) {
         uvs.assign((size_t)std::max(T, 1) * 3, F4(0.0f, 0.0f, 0.0f, 0.0f));
-        for (int k = 0; k < T && d->uvs; k++) {
-            const int t = bvh.primIds[k];
-            for (int v = 0; v < 3; v++) {
-                const float* u = d->uvs + 3 * (size_t)d->indices[3 * t + v];
-                uvs[3 * (size_t)k + v] = F4(u[0], u[1], u[2], 0.0f);
-            }
-        }
+        if (d->uvs)
+            ParallelFor((size_t)T, [&](size_t k) {
+                const int t = bvh.primIds[k];
+                for (int v = 0; v < 3; v++) {
+                    const float* u = d->uvs + 3 * (size_t)d->indices[3 * t + v];
+                    uvs[3 * k + v] = F4(u[0], u[1], u[2], 0.0f);
+                }
+            });
     }
     // material texture maps: texels as {r, g, b, 0}, one texture after another
     std::vector<float4> texels(1, F4(0.0f, 0.0f, 0.0f, 0.0f));
     std::vector<int4> texInfo(std::max<uint32_t>(d->num_textures, 1), int4{0, 0, 0, 0});
     if (anyTex) {
-        texels.clear();
+        size_t total = 0;
         for (uint32_t t = 0; t < d->num_textures; t++) {
             const pt_texture& X = d->textures[t];
-            texInfo[t] = int4{(int)texels.size(), X.width, X.height, 0};
-            for (size_t i = 0; i < (size_t)X.width * X.height; i++)
-                texels.push_back(F4(X.rgb[3 * i], X.rgb[3 * i + 1], X.rgb[3 * i + 2], 0.0f));
+            texInfo[t] = int4{(int)total, X.width, X.height, 0};
+            total += (size_t)X.width * X.height;
+        }
+        texels.assign(std::max<size_t>(total, 1), F4(0.0f, 0.0f, 0.0f, 0.0f));
+        for (uint32_t t = 0; t < d->num_textures; t++) {
+            const pt_texture& X = d->textures[t];
+            float4* dst = texels.data() + texInfo[t].x;
+            ParallelFor((size_t)X.width * X.height, [&](size_t i) {
+                dst[i] = F4(X.rgb[3 * i], X.rgb[3 * i + 1], X.rgb[3 * i + 2], 0.0f);
+            });
         }
     }
     // materials
@@ -665,10 +696,10 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     // Environment::PreCalcCumulativeDistTex depend on H alone; the kernels evaluate them)
     const int W = d->env_width, H = d->env_height;
     std::vector<float4> env((size_t)std::max(W * H, 1));
-    if (W > 0) {
-        for (size_t i = 0; i < (size_t)W * H; i++)
+    if (W > 0)
+        ParallelFor((size_t)W * H, [&](size_t i) {
             env[i] = F4(d->env_rgb[3 * i], d->env_rgb[3 * i + 1], d->env_rgb[3 * i + 2], 0.0f);
-    }
+        });
     SceneGpu& s = *sg;
     DevScene& D = s.dev;
     if ((rc = Upload(ctx, s, nodes, &D.nodes)) != PT_OK ||
