@@ -299,9 +299,7 @@ void Petrichor::Render(const Scene& scene) {
         textures.push_back(pt_texture{t->GetWidth(), t->GetHeight(), t->GetRawDataPtr()});
         return texIndex[t] = (int32_t)textures.size();
     };
-    std::unordered_map<const Vertex*, int32_t> vertexIndex;
     std::unordered_map<const MaterialBase*, int32_t> matIndex;
-    std::unordered_map<const GeometryBase*, int32_t> triIndex;
     std::function<int32_t(const MaterialBase*)> addMaterial = [&](const MaterialBase* m) -> int32_t {
         auto it = matIndex.find(m);
         if (it != matIndex.end()) return it->second;
@@ -354,28 +352,53 @@ void Petrichor::Render(const Scene& scene) {
         mats.push_back(pm);
         return matIndex[m] = (int32_t)mats.size() - 1;
     };
-    auto addVertex = [&](const Vertex* v) -> int32_t {
-        auto it = vertexIndex.find(v);
-        if (it != vertexIndex.end()) return it->second;
-        const int32_t k = (int32_t)(pos.size() / 3);
-        for (float f : {v->pos.x, v->pos.y, v->pos.z}) pos.push_back(f);
-        for (float f : {v->normal.x, v->normal.y, v->normal.z}) nrm.push_back(f);
-        for (float f : {v->uv.x, v->uv.y, v->uv.z}) uv.push_back(f);
-        return vertexIndex[v] = k;
-    };
-    for (const GeometryBase* g : scene.GetGeometries()) {
-        const auto* t = dynamic_cast<const Triangle*>(g);
+    // every triangle gets its own three corner vertices (the values of the vertices it
+    // points at; the device keeps per-triangle records, so shared vertices need no
+    // lookup), and consecutive triangles usually share a material
+    const auto& geoms = scene.GetGeometries();
+    const size_t G = geoms.size();
+    pos.resize(9 * G);
+    nrm.resize(9 * G);
+    uv.resize(9 * G);
+    idx.resize(3 * G);
+    triMat.resize(G);
+    shading.resize(G);
+    const MaterialBase* lastMat = nullptr;
+    int32_t lastIdx = -1;
+    for (size_t i = 0; i < G; i++) {
+        const auto* t = dynamic_cast<const Triangle*>(geoms[i]);
         if (!t) return fail(PT_ERR_UNSUPPORTED, "only triangle geometry is supported");
-        if (!t->GetMaterialPointer()) return fail(PT_ERR_INVALID_ARG, "geometry without material");
-        triIndex[g] = (int32_t)triMat.size();
-        for (const Vertex* v : t->GetVertices()) idx.push_back(addVertex(v));
-        triMat.push_back(addMaterial(t->GetMaterialPointer()));
-        shading.push_back(t->GetShadingType() == ShadingTypes::Smooth ? 1 : 0);
+        const MaterialBase* m = t->GetMaterialPointer();
+        if (!m) return fail(PT_ERR_INVALID_ARG, "geometry without material");
+        int c = 0;
+        for (const Vertex* v : t->GetVertices()) {
+            const size_t k = 3 * i + c++;
+            const float p3[9] = {v->pos.x, v->pos.y, v->pos.z, v->normal.x, v->normal.y, v->normal.z,
+                                 v->uv.x, v->uv.y, v->uv.z};
+            std::memcpy(&pos[3 * k], p3, 12);
+            std::memcpy(&nrm[3 * k], p3 + 3, 12);
+            std::memcpy(&uv[3 * k], p3 + 6, 12);
+            idx[k] = (int32_t)k;
+        }
+        if (m != lastMat) {
+            lastMat = m;
+            lastIdx = addMaterial(m);
+        }
+        triMat[i] = lastIdx;
+        shading[i] = t->GetShadingType() == ShadingTypes::Smooth ? 1 : 0;
     }
-    for (const GeometryBase* l : scene.GetLights()) {
-        auto it = triIndex.find(l);
-        if (it == triIndex.end()) return fail(PT_ERR_INVALID_ARG, "light is not a scene geometry");
-        lights.push_back(it->second);
+    if (!scene.GetLights().empty()) {
+        std::unordered_map<const GeometryBase*, int32_t> lightSlot;
+        for (size_t j = 0; j < scene.GetLights().size(); j++) lightSlot[scene.GetLights()[j]] = -1;
+        for (size_t i = 0; i < G; i++) {
+            auto it = lightSlot.find(geoms[i]);
+            if (it != lightSlot.end()) it->second = (int32_t)i;  // the last occurrence, as before
+        }
+        for (const GeometryBase* l : scene.GetLights()) {
+            const int32_t t = lightSlot[l];
+            if (t < 0) return fail(PT_ERR_INVALID_ARG, "light is not a scene geometry");
+            lights.push_back(t);
+        }
     }
     if (mats.empty()) mats.push_back(pt_material{});  // an empty scene still needs one
     if (!texError.empty()) return fail(PT_ERR_INVALID_ARG, texError);
