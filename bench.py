@@ -855,6 +855,15 @@ def main():
     prof2 = ctx.render_profile(sid, cam, sets, film.data_ptr(), count_reference=False).as_dict()
     stages = {k: prof2[k] for k in ("raygen_ms", "extend_ms", "shade_ms", "shadow_ms", "accumulate_ms")}
     dominant = max(stages, key=stages.get)
+    # extension rays of the first four bounces (renders cut after bounce b, differenced):
+    # the units behind one ExtendKernel launch of a profiler capture
+    rays_per_bounce, prev = [], 0
+    for b in range(4):
+        sb = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=replicas.replica_seed(1, rank),
+                                      env_sampling=env, max_bounces=b)
+        n = ctx.render_profile(sid, cam, sb, film.data_ptr(), count_reference=False).as_dict()
+        rays_per_bounce.append(int(n["extend_rays"] - prev))
+        prev = n["extend_rays"]
     # algorithmic bytes of a traced ray (reference traversal order): 32 B per node
     # popped and slab-tested, 48 B per triangle test, 32 B ray in, 16 B hit out
     rays = max(1, prof["ref_rays"])
@@ -907,6 +916,7 @@ def main():
                      "ref_tris_per_ray": prof["ref_tri_tests"] / rays,
                      "dominant_stage": dominant, "stage_ms": stages,
                      "rays_extended": prof2["extend_rays"], "shadow_rays": prof2["shadow_rays"],
+                     "rays_per_bounce_0_3": rays_per_bounce,
                      "mrays_per_s": (prof2["extend_rays"] + prof2["shadow_rays"]) /
                                     (sum(stages.values()) / 1e3) / 1e6},
         "image_mean": img_mean,
