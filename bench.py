@@ -853,23 +853,33 @@ def main():
     # ---- roofline of the dominant kernel (CUDA events around every stage launch)
     prof = ctx.render_profile(sid, cam, sets, film.data_ptr(), count_reference=True).as_dict()
     prof2 = ctx.render_profile(sid, cam, sets, film.data_ptr(), count_reference=False).as_dict()
-    stages = {k: prof2[k] for k in ("raygen_ms", "extend_ms", "shade_ms", "shadow_ms", "accumulate_ms")}
+    stages = {k: prof2[k] for k in ("raygen_ms", "extend_ms", "raster_ms", "shade_ms", "shadow_ms",
+                                     "accumulate_ms")}
     dominant = max(stages, key=stages.get)
     # extension rays of the first four bounces (renders cut after bounce b, differenced):
-    # the units behind one ExtendKernel launch of a profiler capture
-    rays_per_bounce, prev = [], 0
+    # the units behind one ExtendKernel launch of a profiler capture; bounce 0 counted in
+    # the reference's traversal order too (its rays are rasterised, not traced)
+    rays_per_bounce, prev, prof0 = [], 0, None
     for b in range(4):
         sb = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=replicas.replica_seed(1, rank),
                                       env_sampling=env, max_bounces=b)
-        n = ctx.render_profile(sid, cam, sb, film.data_ptr(), count_reference=False).as_dict()
+        n = ctx.render_profile(sid, cam, sb, film.data_ptr(), count_reference=(b == 0)).as_dict()
+        if b == 0:
+            prof0 = n
         rays_per_bounce.append(int(n["extend_rays"] - prev))
         prev = n["extend_rays"]
-    # algorithmic bytes of a traced ray (reference traversal order): 32 B per node
-    # popped and slab-tested, 48 B per triangle test, 32 B ray in, 16 B hit out
-    rays = max(1, prof["ref_rays"])
-    bytes_per_ray = (32.0 * prof["ref_node_tests"] + 48.0 * prof["ref_tri_tests"]) / rays + 48.0
+    # ExtendKernel alone: the rays it traces (every extension ray but the rasterised
+    # first-bounce ones) over its own time (the raster kernels are timed apart).
+    # Algorithmic bytes of a traced ray (reference traversal order): 32 B per node popped
+    # and slab-tested, 48 B per triangle test, 32 B ray in, 16 B hit out
+    share0 = prof2["raster_paths"] / max(1, prof0["ref_rays"])  # of bounce 0 rasterised
+    nodes = prof["ref_node_tests"] - share0 * prof0["ref_node_tests"]
+    tris = prof["ref_tri_tests"] - share0 * prof0["ref_tri_tests"]
+    traced = max(1, prof2["extend_rays"] - prof2["raster_paths"])
+    bytes_per_ray = (32.0 * nodes + 48.0 * tris) / traced + 48.0
     ext_launches = max(1, prof2["extend_launches"])
-    bytes_per_launch = bytes_per_ray * prof2["extend_rays"] / ext_launches
+    busy_launches = ext_launches - (1 if prof2["raster_paths"] >= prof0["ref_rays"] > 0 else 0)
+    bytes_per_launch = bytes_per_ray * traced / ext_launches
     avg_launch_s = prof2["extend_ms"] / 1e3 / ext_launches
     achieved = bytes_per_launch / avg_launch_s / 1e9
     peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
@@ -878,13 +888,19 @@ def main():
         with open(peaks_path) as fh:
             peak, peak_src = float(json.load(fh)["hbm_gbs"]), "measured"
     l2 = l2_read_peak(ctx)
-    # small-case ncu counters of ExtendKernel (one kernel, three launches, 640x360 of the
-    # same scene): DRAM bytes per ray, SIMT efficiency, issue-slot use
-    cnt = counters_profile("extend_kernel_counters_spheres_grids_1M_640x360.json") \
+    # single-kernel ncu counters of ExtendKernel on the same scene at 1920x1080 and 2 / 4
+    # spp: DRAM bytes = fixed part per launch + bytes per ray, SIMT efficiency, issue use
+    cnt = counters_profile("extend_kernel_counters_spheres_grids_1M_1080p_2_4spp.json") \
         if workload_name(args) == WORKLOAD else None
     traffic = None
     if cnt is not None:
-        traffic = cnt["dram_bytes_per_ray"] * prof2["extend_rays"] / ext_launches
+        traffic = (cnt["dram_bytes_per_ray"] * traced +
+                   cnt["dram_bytes_fixed_per_launch"] * busy_launches) / ext_launches
+    raster_stage = None
+    if prof2["raster_paths"] > 0:
+        raster_stage = {"kernels": "RasterSetupKernel, RasterVisitKernel, RasterFinishKernel",
+                        "ms": prof2["raster_ms"], "paths": prof2["raster_paths"],
+                        "mpaths_per_s": prof2["raster_paths"] / (prof2["raster_ms"] / 1e3) / 1e6}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -908,12 +924,16 @@ def main():
                      "simt_eff": cnt.get("simt_eff") if cnt else None,
                      "issue_active": cnt.get("issue_active") if cnt else None,
                      "counters_source": cnt.get("source") if cnt else None,
-                     "note": "achieved = algorithmic bytes (reference traversal order) / kernel "
-                             "time; served mostly from L1/L2, so the limiter is issue rate at "
-                             "the stated SIMT efficiency, not DRAM",
+                     "note": "achieved = algorithmic bytes of the rays ExtendKernel traces "
+                             "(reference traversal order) / ExtendKernel time; served mostly "
+                             "from L1/L2, so the limiter is issue rate at the stated SIMT "
+                             "efficiency, not DRAM; traffic = the counters' DRAM model at this "
+                             "frame's rays per launch",
                      "bytes_per_ray": bytes_per_ray,
-                     "ref_nodes_per_ray": prof["ref_node_tests"] / rays,
-                     "ref_tris_per_ray": prof["ref_tri_tests"] / rays,
+                     "traced_rays": int(traced),
+                     "ref_nodes_per_ray": nodes / traced,
+                     "ref_tris_per_ray": tris / traced,
+                     "raster_stage": raster_stage,
                      "dominant_stage": dominant, "stage_ms": stages,
                      "rays_extended": prof2["extend_rays"], "shadow_rays": prof2["shadow_rays"],
                      "rays_per_bounce_0_3": rays_per_bounce,

@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PT_ABI_VERSION 4
+#define PT_ABI_VERSION 5
 
 /* status codes */
 #define PT_OK 0
@@ -339,11 +339,16 @@ int pt_set_bvh_builder(pt_context* ctx, int32_t builder);
 /* Per-stage device times (CUDA events around every stage launch) and work tallies
  * of one wavefront render. With count_reference != 0 every extended ray is also
  * walked in the reference's traversal order to count its node and triangle
- * tests (the algorithmic work per ray). Synchronous. */
+ * tests (the algorithmic work per ray). Synchronous. extend_rays counts every
+ * path's closest-hit query, including the first-bounce ones that the raster
+ * kernels settle (raster_paths of them, in raster_ms; extend_ms is the traversal
+ * kernel alone). */
 typedef struct pt_profile {
   double raygen_ms, extend_ms, shade_ms, shadow_ms, accumulate_ms;
   uint64_t extend_rays, shadow_rays, extend_launches, shadow_launches;
   uint64_t ref_node_tests, ref_tri_tests, ref_rays;
+  double raster_ms;
+  uint64_t raster_paths;
 } pt_profile;
 int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* camera,
                       const pt_settings* settings, float* film_rgb_device, int32_t count_reference,

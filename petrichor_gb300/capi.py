@@ -114,7 +114,8 @@ class PtProfile(ctypes.Structure):
                 ("accumulate_ms", ctypes.c_double), ("extend_rays", ctypes.c_uint64),
                 ("shadow_rays", ctypes.c_uint64), ("extend_launches", ctypes.c_uint64),
                 ("shadow_launches", ctypes.c_uint64), ("ref_node_tests", ctypes.c_uint64),
-                ("ref_tri_tests", ctypes.c_uint64), ("ref_rays", ctypes.c_uint64)]
+                ("ref_tri_tests", ctypes.c_uint64), ("ref_rays", ctypes.c_uint64),
+                ("raster_ms", ctypes.c_double), ("raster_paths", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

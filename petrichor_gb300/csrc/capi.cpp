@@ -1012,6 +1012,8 @@ int pt_render_profile(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
     out->ref_node_tests = prof.refNodeTests;
     out->ref_tri_tests = prof.refTriTests;
     out->ref_rays = prof.refRays;
+    out->raster_ms = prof.ms[5];
+    out->raster_paths = prof.rasterPaths;
     return PT_OK;
 }
 

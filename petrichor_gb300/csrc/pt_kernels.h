@@ -104,8 +104,9 @@ size_t WaveBuffersBytesTwoLanes(int capacity);
 // Optional per-stage profile (CUDA events around every stage launch; ray tallies;
 // reference-order traversal work over the extended rays).
 struct WaveProfile {
-    double ms[5] = {0, 0, 0, 0, 0};  // raygen, extend, shade, shadow, accumulate+finalize
+    double ms[6] = {0, 0, 0, 0, 0, 0};  // raygen, extend, shade, shadow, accumulate+finalize, raster
     unsigned long long extendRays = 0, shadowRays = 0, extendLaunches = 0, shadowLaunches = 0;
+    unsigned long long rasterPaths = 0;  // first-bounce paths settled by the raster kernels
     unsigned long long refNodeTests = 0, refTriTests = 0, refRays = 0;
     bool countReference = false;
     unsigned long long* devCounters = nullptr;  // 8 device words, zeroed by the caller

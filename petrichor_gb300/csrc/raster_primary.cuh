@@ -16,26 +16,29 @@
 //          exact triangle test of the traversal (TriIntersect) and keep the nearest hit
 //          with a 64-bit atomic minimum over {distance bits, slot};
 //   finish one thread per path: the nearest hit into the hit queue, an exact tie with
-//          another triangle marked as the traversal marks it.
+//          another triangle marked as the traversal marks it (a second minimum over
+//          {distance bits, ~slot} holds the largest slot at the nearest distance: a tie
+//          when it differs from the smallest).
 // The cone test only skips pairs whose ray certainly misses, and every remaining pair
 // runs the same triangle test with the same ray, so a sample's closest distance and
 // triangle are the traversal's (which, with its widened boxes, also finds every hit).
-// Scratch: the next queue's ray buffer holds the keys and the tie marks (12 of its 32
-// bytes per path); the shadow queue holds the per-triangle records and the work list.
+// Scratch: the next queue's ray buffer holds the two keys (16 of its 32 bytes per path);
+// the shadow queue holds the per-triangle records and the work list.
 // Both are free until the first shade. Paths are in pixel-major order, so a pixel's
 // samples are consecutive queue entries and their directions are read where raygen
 // wrote them.
 #pragma once
 
-constexpr int kRasterSeg = 32;  // pixels per work item (one row segment)
+constexpr int kRasterSeg = 32;   // pixels per work item (one row segment)
+constexpr int kRasterBatch = 4;  // (pixel, sample) pairs a lane loads before testing them
 constexpr unsigned long long kNoKey = ~0ull;
 constexpr unsigned kNoItem = ~0u;  // an empty work-list slot
 
 struct RasterScratch {
-    unsigned long long* key;  // per path: {distance bits, slot}, kNoKey = no hit
-    unsigned* tie;            // per path: smallest distance bits at which two triangles tied
-    float4* rec;              // per triangle: 4 float4 (cone planes with margins, pixel rect)
-    uint4* items;             // {triangle slot, unit, row | segment << 16, 0}
+    unsigned long long* key;   // per path: min {distance bits, slot}, kNoKey = no hit
+    unsigned long long* key2;  // per path: min {distance bits, ~slot}
+    float4* rec;               // per triangle: 4 float4 (cone planes with margins, pixel rect)
+    uint4* items;              // {triangle slot, unit, row | segment << 16, xa | xb << 16}
     int2* overflow;           // {triangle slot, unit} whose items did not fit (visited whole)
     long long itemCap;
 };
@@ -45,7 +48,7 @@ __device__ __forceinline__ RasterScratch CarveRaster(const WaveBuffers& wb, int 
     const size_t C = (size_t)wb.capacity;
     RasterScratch r;
     r.key = reinterpret_cast<unsigned long long*>(wb.ray[cur ^ 1]);
-    r.tie = reinterpret_cast<unsigned*>(r.key + C);
+    r.key2 = r.key + C;
     r.rec = wb.shadow;
     const size_t over = ((size_t)numRecs + 1) & ~(size_t)1;  // int2 entries, 16-byte multiple
     r.overflow = reinterpret_cast<int2*>(wb.shadow + 4 * (size_t)numRecs);
@@ -188,9 +191,12 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
                 const int segs = (x1 - x0 + kRasterSeg) / kRasterSeg;
                 long long it = first;
                 for (int y = y0; y <= y1; y++)
-                    for (int sgi = 0; sgi < segs; sgi++)
+                    for (int sgi = 0; sgi < segs; sgi++) {
+                        const int xa = x0 + sgi * kRasterSeg, xb = min(x1, xa + kRasterSeg - 1);
                         rs.items[it++] = make_uint4((unsigned)k, (unsigned)unit,
-                                                    (unsigned)y | ((unsigned)sgi << 16), 0u);
+                                                    (unsigned)y | ((unsigned)sgi << 16),
+                                                    (unsigned)xa | ((unsigned)xb << 16));
+                    }
             } else {
                 // the list is full: the triangle is visited whole; the part of its
                 // reservation that lies inside the list is marked empty, so every slot the
@@ -220,26 +226,38 @@ __device__ __forceinline__ void RasterSegment(const RasterScratch& rs, const flo
     // (pixel, sample) of pair f = lane + 32 i, advanced without a division per pair
     const int dq = 32 / sw, dr = 32 % sw;
     int x = xa + lane / sw, j = lane % sw;
-    for (int f = lane; f < n; f += 32) {
-        const size_t idx = (size_t)pathBase + (qrow + (size_t)x * hb) * sw + j;
-        const float4 dv = __ldg(rays + 2 * idx + 1);
-        const float c0 = r0.x * dv.x + r0.y * dv.y + r0.z * dv.z + r0.w;
-        const float c1 = r1.x * dv.x + r1.y * dv.y + r1.z * dv.z + r1.w;
-        const float c2 = r2.x * dv.x + r2.y * dv.y + r2.z * dv.z + r2.w;
-        if (c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f) {
-            float t;
-            if (TriIntersect(v0, e1, e2, o, V3(dv.x, dv.y, dv.z), t) && t >= tmin && t < kFltMax) {
-                const unsigned tb = __float_as_uint(t + 0.0f);  // +0 for a zero distance
-                const unsigned long long key = ((unsigned long long)tb << 32) | (unsigned)k;
-                const unsigned long long old = atomicMin(rs.key + idx, key);
-                if ((unsigned)(old >> 32) == tb && (unsigned)old != (unsigned)k) atomicMin(rs.tie + idx, tb);
+    // kRasterBatch pairs per lane at a time: their directions are loaded before any is
+    // tested, so the loads' latencies overlap; the minima are fire-and-forget reductions
+    for (int f0 = lane; f0 < n; f0 += 32 * kRasterBatch) {
+        float4 dv[kRasterBatch];
+        size_t idx[kRasterBatch];
+#pragma unroll
+        for (int b = 0; b < kRasterBatch; b++) {
+            idx[b] = (size_t)pathBase + (qrow + (size_t)x * hb) * sw + j;
+            if (f0 + 32 * b < n) dv[b] = __ldg(rays + 2 * idx[b] + 1);
+            j += dr;
+            x += dq;
+            if (j >= sw) {
+                j -= sw;
+                x++;
             }
         }
-        j += dr;
-        x += dq;
-        if (j >= sw) {
-            j -= sw;
-            x++;
+#pragma unroll
+        for (int b = 0; b < kRasterBatch; b++) {
+            if (f0 + 32 * b >= n) break;
+            const float c0 = r0.x * dv[b].x + r0.y * dv[b].y + r0.z * dv[b].z + r0.w;
+            const float c1 = r1.x * dv[b].x + r1.y * dv[b].y + r1.z * dv[b].z + r1.w;
+            const float c2 = r2.x * dv[b].x + r2.y * dv[b].y + r2.z * dv[b].z + r2.w;
+            if (c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f) {
+                float t;
+                if (TriIntersect(v0, e1, e2, o, V3(dv[b].x, dv[b].y, dv[b].z), t) && t >= tmin &&
+                    t < kFltMax) {
+                    // t + 0: a zero distance as +0, so that distance bits order as floats
+                    const unsigned long long tb = (unsigned long long)__float_as_uint(t + 0.0f) << 32;
+                    atomicMin(rs.key + idx[b], tb | (unsigned)k);
+                    atomicMin(rs.key2 + idx[b], tb | ~(unsigned)k);
+                }
+            }
         }
     }
 }
@@ -265,18 +283,18 @@ __global__ void __launch_bounds__(128) RasterVisitKernel(const DevJob* __restric
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
     long long nItems = *reinterpret_cast<const long long*>(wb.counts + 8);
     if (nItems > rs.itemCap) nItems = rs.itemCap;
+    // the next item is loaded while the current one is visited
+    uint4 next = warp < nItems ? rs.items[warp] : make_uint4(kNoItem, 0u, 0u, 0u);
     for (long long w = warp; w < nItems; w += warps) {
-        const uint4 it = rs.items[w];
+        const uint4 it = next;
+        if (w + warps < nItems) next = rs.items[w + warps];
         if (it.x == kNoItem) continue;
-        const int k = (int)it.x, y = (int)(it.z & 0xffffu), sg = (int)(it.z >> 16);
+        const int k = (int)it.x, y = (int)(it.z & 0xffffu);
         const WaveUnit u = units[it.y];
 #if PT_CHECK
         if (k < 0 || k >= jobs[u.job].S.numTris) continue;
 #endif
-        const float4 r3 = __ldg(rs.rec + 4 * (size_t)(u.recBase + k) + 3);
-        const int xa = __float_as_int(r3.x) + sg * kRasterSeg;
-        const int xb = min(__float_as_int(r3.y), xa + kRasterSeg - 1);
-        RasterItem(jobs, u, rs, rays, wd.band, k, y, xa, xb, lane);
+        RasterItem(jobs, u, rs, rays, wd.band, k, y, (int)(it.w & 0xffffu), (int)(it.w >> 16), lane);
     }
     // triangles whose items did not fit in the list: whole, one warp each
     const int nOver = wb.counts[10];
@@ -307,7 +325,8 @@ __global__ void RasterFinishKernel(WaveBuffers wb, int cur) {
         if (key != kNoKey) {
             const unsigned tb = (unsigned)(key >> 32);
             const int slot = (int)(unsigned)key;
-            h = make_float2(__uint_as_float(tb), __int_as_float(rs.tie[i] == tb ? -2 - slot : slot));
+            const bool tie = (unsigned)key != ~(unsigned)rs.key2[i];
+            h = make_float2(__uint_as_float(tb), __int_as_float(tie ? -2 - slot : slot));
         }
         wb.hit[i] = h;
     }

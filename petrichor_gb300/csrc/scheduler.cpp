@@ -74,7 +74,8 @@ void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* 
         const DevJob& J = jobs[u.job];
         const int64_t paths = (int64_t)J.st.width * J.st.height * u.sw;
         const bool ok = shape->iters >= 0 && J.C.aperture == 0.0f && J.S.numTris > 0 &&
-                        J.st.height < 65536 && J.st.integrator == kPathTracing &&
+                        J.st.width < 65536 && J.st.height < 65536 &&
+                        J.st.integrator == kPathTracing &&
                         paths >= 2 * (int64_t)J.S.numTris &&
                         (int64_t)shape->raster + J.S.numTris < (int64_t(1) << 30);
         u.recBase = -1;

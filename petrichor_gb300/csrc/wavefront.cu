@@ -388,7 +388,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         if (J.C.aperture == 0.0f) ray.o = LoadV3(J.C.pos);  // a pinhole: exactly the camera position
         if (raster && i >= wd.rasterFrom) {
             rs.key[i] = kNoKey;
-            rs.tie[i] = 0xffffffffu;
+            rs.key2[i] = kNoKey;
         }
         wb.ray[cur][2 * i] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float(i));
         wb.ray[cur][2 * i + 1] = make_float4(ray.d.x, ray.d.y, ray.d.z, 1.0f);
@@ -1053,7 +1053,7 @@ __global__ void __launch_bounds__(128) RefCountKernel(const DevJob* __restrict__
 
 namespace {
 struct StageEvents {
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[5];
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[6];
     void Begin(int k, cudaStream_t s) {
         cudaEvent_t a, b;
         cudaEventCreate(&a);
@@ -1063,7 +1063,7 @@ struct StageEvents {
     }
     void End(int k, cudaStream_t s) { cudaEventRecord(ev[k].back().second, s); }
     void Collect(double* ms) {
-        for (int k = 0; k < 5; k++) {
+        for (int k = 0; k < 6; k++) {
             for (auto& p : ev[k]) {
                 float t = 0.0f;
                 cudaEventElapsedTime(&t, p.first, p.second);
@@ -1325,9 +1325,17 @@ static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveB
         if (ev) ev->Begin(1, stream);
         if (it == 0 && raster) {  // the traced units' paths, then the rasterised ones
             ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, 1);
+            if (ev) {  // the raster kernels have a timer of their own
+                ev->End(1, stream);
+                ev->Begin(5, stream);
+            }
             RasterSetupKernel<<<SmCount() * 32, block, 0, stream>>>(jobs, units, wb, cur);
             RasterVisitKernel<<<SmCount() * 16, block, 0, stream>>>(jobs, units, wb, cur);
             RasterFinishKernel<<<grid, block, 0, stream>>>(wb, cur);
+            if (ev) {
+                ev->End(5, stream);
+                ev->Begin(1, stream);  // an empty interval closed below
+            }
             *nl += 3;  // one more below
         } else {
             ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, 0);
@@ -1502,6 +1510,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     d.rasterFrom = raster ? shape.rasterFrom : shape.nPaths;
     d.rasterUnit0 = raster ? shape.rasterUnit0 : shape.nUnits;
     d.rasterRecs = raster ? shape.raster : 0;
+    if (prof && raster) prof->rasterPaths += (unsigned long long)(shape.nPaths - shape.rasterFrom);
     cudaError_t e = cudaMemcpyAsync(wb.desc, &d, sizeof(d), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     int nl = 0;

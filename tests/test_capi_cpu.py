@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_status_strings():
     lib = capi.load()
-    assert lib.pt_abi_version() == 4
+    assert lib.pt_abi_version() == 5
     assert lib.pt_status_string(0) == b"ok"
     assert b"budget" in lib.pt_status_string(-3)
 
