@@ -365,8 +365,10 @@ typedef struct pt_tuning {
   int32_t use_graphs;    /* 1: replay each wave's stage sequence from a captured CUDA graph */
   int32_t sort_rays;     /* 1: reorder each bounce's rays by direction and origin cell */
   int32_t tail_bounce;   /* > 0: from this bounce on, one launch finishes every path (0: off) */
-  int32_t primary_traversal; /* 1: trace first-bounce rays through the BVH; 0: rasterise them
-                                when the wave allows (one pinhole job, enough rays per triangle) */
+  int32_t primary_traversal; /* first-bounce rays of a pinhole PathTracing job: 0 rasterised
+                                when the unit has at least 16 rays per triangle, else traced;
+                                1 always traced through the BVH; 2 rasterised whenever the
+                                unit has at least 2 rays per triangle */
   int32_t reserved;
   double probe_ms;       /* pt_autotune: probe render time of the chosen configuration */
 } pt_tuning;

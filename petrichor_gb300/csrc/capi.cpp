@@ -866,7 +866,7 @@ int pt_set_tuning(pt_context* ctx, const pt_tuning* t) {
     if (t->wave_paths < 0 || t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->band_rows < 0 ||
         t->band_rows > 4096 || (t->use_graphs != 0 && t->use_graphs != 1) ||
         (t->sort_rays != 0 && t->sort_rays != 1) || t->tail_bounce < 0 || t->tail_bounce > 64 ||
-        (t->primary_traversal != 0 && t->primary_traversal != 1))
+        t->primary_traversal < 0 || t->primary_traversal > 2)
         return Fail(ctx, PT_ERR_INVALID_ARG, "bad tuning");
     ctx->tunedWavePaths = t->wave_paths;
     ctx->tuning.blocksPerSm = t->blocks_per_sm;

@@ -130,7 +130,9 @@ struct WaveTuning {
     int graphs = 1;       // replay each wave's stage sequence from a captured CUDA graph
     int sortRays = 0;     // reorder each bounce's rays by direction and origin cell before tracing
     int tailBounce = 0;   // > 0: from this bounce on, one launch finishes every path (TailKernel)
-    int primaryTraversal = 0;  // 1: trace the first bounce through the BVH even when it could be rasterised
+    // first bounce: 0 rasterised for units with enough rays per triangle, else traced;
+    // 1 always traced through the BVH; 2 rasterised wherever the camera allows it
+    int primaryTraversal = 0;
 };
 // Captured stage sequences, keyed by wave shape and buffers (owned by a context or server).
 struct WaveGraphCache;

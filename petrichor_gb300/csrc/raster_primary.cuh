@@ -30,7 +30,7 @@
 #pragma once
 
 constexpr int kRasterSeg = 32;   // pixels per work item (one row segment)
-constexpr int kRasterBatch = 4;  // (pixel, sample) pairs a lane loads before testing them
+constexpr int kRasterBatch = 2;  // (pixel, sample) pairs a lane loads before testing them
 constexpr unsigned long long kNoKey = ~0ull;
 constexpr unsigned kNoItem = ~0u;  // an empty work-list slot
 

@@ -65,10 +65,18 @@ int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
 }
 
 void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* units,
-                        WaveShape* shape) {
+                        WaveShape* shape, int primaryTraversal) {
     shape->raster = 0;
     shape->rasterFrom = shape->nPaths;
     shape->rasterUnit0 = (int)units->size();
+    if (primaryTraversal == 1) {  // every first bounce traced
+        for (WaveUnit& u : *units) u.recBase = -1;
+        return;
+    }
+    // rays per triangle: at least kRasterMinPathsPerTri to pick rasterisation by itself;
+    // at least 2 in any case, which keeps the per-triangle records (64 B each) within half
+    // of the shadow queue (64 B per path) the raster kernels carve them from
+    const int64_t perTri = primaryTraversal == 2 ? 2 : kRasterMinPathsPerTri;
     std::vector<WaveUnit> trace, raster;
     for (WaveUnit u : *units) {
         const DevJob& J = jobs[u.job];
@@ -76,7 +84,7 @@ void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* 
         const bool ok = shape->iters >= 0 && J.C.aperture == 0.0f && J.S.numTris > 0 &&
                         J.st.width < 65536 && J.st.height < 65536 &&
                         J.st.integrator == kPathTracing &&
-                        paths >= 2 * (int64_t)J.S.numTris &&
+                        paths >= perTri * (int64_t)J.S.numTris &&
                         (int64_t)shape->raster + J.S.numTris < (int64_t(1) << 30);
         u.recBase = -1;
         if (ok) {
@@ -116,7 +124,8 @@ int WaveSoleJob(const std::vector<WaveUnit>& units) {
 
 namespace {
 
-WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units) {
+WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units,
+                  int primaryTraversal) {
     WaveShape shape;
     for (const WaveUnit& u : units) {
         const int P = jobs[u.job].st.width * jobs[u.job].st.height;
@@ -127,7 +136,7 @@ WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units)
     shape.iters = WaveIterations(jobs, units);
     shape.integrator = WaveIntegrator(jobs, units);
     shape.soleJob = WaveSoleJob(units);
-    PrepareRasterUnits(jobs, &units, &shape);
+    PrepareRasterUnits(jobs, &units, &shape, primaryTraversal);
     return shape;
 }
 
@@ -197,7 +206,7 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
         e = cudaMemsetAsync(wb.counts, 0, 16 * sizeof(int), stream);
         for (size_t w = 0; w < waves.size() && e == cudaSuccess; w++) {
             std::vector<WaveUnit>& units = waves[w];
-            const WaveShape shape = ShapeOf(jobs, units);  // may reorder the units
+            const WaveShape shape = ShapeOf(jobs, units, tune.primaryTraversal);  // may reorder the units
             // pageable source: the copy is staged before the call returns, so the
             // next wave may reuse the host vector
             e = cudaMemcpyAsync(T.units, units.data(), units.size() * sizeof(WaveUnit),
@@ -218,7 +227,7 @@ cudaError_t RenderJobs(const std::vector<DevJob>& jobs, const WaveTables& T, con
         const int k = (int)(w & 1);
         cudaStream_t s = laneStream[k];
         std::vector<WaveUnit>& units = waves[w];
-        const WaveShape shape = ShapeOf(jobs, units);  // may reorder the units
+        const WaveShape shape = ShapeOf(jobs, units, tune.primaryTraversal);  // may reorder the units
         e = cudaMemcpyAsync(unitTable[k], units.data(), units.size() * sizeof(WaveUnit),
                             cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)

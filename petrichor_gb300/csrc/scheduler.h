@@ -38,12 +38,19 @@ int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
 int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
 // The job of all of a wave's units, or -1 when they belong to several.
 int WaveSoleJob(const std::vector<WaveUnit>& units);
+// Rays per triangle from which a unit's first bounce is rasterised by default. Measured
+// on GB300 with films alike: at 133 (1.0M triangles, 1920x1080, 64 spp) the raster pass
+// takes 5.5 ms against about 10 ms of first-bounce traversal; at 3.3 (20.0M triangles,
+// 3840x2160, waves of 8 spp) it takes 21 ms per wave against 13 ms, its per-triangle work
+// (one warp visit per row segment) outweighing the rays it saves.
+constexpr int64_t kRasterMinPathsPerTri = 16;
 // Picks the units whose first bounce is rasterised (a pinhole PathTracing job with at
-// least two of the unit's rays per triangle; none in a queue-polled wave), moves them
-// after the traced units, renumbers every unit's path and pixel ranges, gives each its
-// record base, and sets shape's raster, rasterFrom and rasterUnit0 (shape's nPaths and
-// iters already set). A wave's films do not depend on its unit order.
+// least kRasterMinPathsPerTri of the unit's rays per triangle, or 2 with
+// primaryTraversal 2; none with primaryTraversal 1 or in a queue-polled wave), moves
+// them after the traced units, renumbers every unit's path and pixel ranges, gives each
+// its record base, and sets shape's raster, rasterFrom and rasterUnit0 (shape's nPaths
+// and iters already set). A wave's films do not depend on its unit order.
 void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* units,
-                        WaveShape* shape);
+                        WaveShape* shape, int primaryTraversal);
 
 }  // namespace ptg

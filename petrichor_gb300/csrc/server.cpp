@@ -438,7 +438,7 @@ private:
         shape.integrator = WaveIntegrator(slotJobs_, units);
         shape.soleJob = WaveSoleJob(units);
         std::vector<WaveUnit> ordered = units;  // rasterised units last
-        PrepareRasterUnits(slotJobs_, &ordered, &shape);
+        PrepareRasterUnits(slotJobs_, &ordered, &shape, tune_.primaryTraversal);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(units_.ptr, ordered.data(), ordered.size() * sizeof(WaveUnit),
                                 cudaMemcpyHostToDevice, stream_);

@@ -1505,7 +1505,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     d.soleJob = shape.soleJob;
     d.band = tune.band > 0 ? tune.band : 8;
     // the first bounce rasterised where the wave allows it (raster_primary.cuh)
-    const bool raster = shape.raster > 0 && !tune.primaryTraversal && tune.sortRays == 0 &&
+    const bool raster = shape.raster > 0 && tune.primaryTraversal != 1 && tune.sortRays == 0 &&
                         shape.iters >= 0;
     d.rasterFrom = raster ? shape.rasterFrom : shape.nPaths;
     d.rasterUnit0 = raster ? shape.rasterUnit0 : shape.nUnits;

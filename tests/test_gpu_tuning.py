@@ -26,6 +26,8 @@ CONFIGS = [
     dict(tail_bounce=3, use_graphs=0, wave_paths=3000),
     dict(primary_traversal=1),                                # first bounce traced, not rasterised
     dict(primary_traversal=1, use_graphs=0, wave_paths=3000),
+    dict(primary_traversal=2),                                # rasterised at 2+ rays per triangle
+    dict(primary_traversal=2, use_graphs=0, wave_paths=3000),
 ]
 
 
@@ -36,14 +38,14 @@ def _scenes():
         "simple": synth.cornell(width=33, height=17, spp=5),  # queue-polled bounce blocks
         "tris": synth.spheres_grids(tri_budget=30000, width=64, height=36, spp=4, max_bounces=8,
                                     env_width=128, env_height=64),
-        # enough rays per triangle for the rasterised first bounce; a tilted camera (the
-        # camera basis is not unit length)
-        "raster": synth.spheres_grids(tri_budget=20000, width=96, height=64, spp=8, max_bounces=6,
+        # enough rays per triangle (over 16) for the rasterised first bounce by default; a
+        # tilted camera (the camera basis is not unit length)
+        "raster": synth.spheres_grids(tri_budget=20000, width=96, height=64, spp=64, max_bounces=6,
                                       env_width=128, env_height=64),
         # a camera inside the box: walls reach behind the camera plane (whole-image rectangles)
         "inside": _inside_box(),
-        # one ray per two triangles at 1 spp: the raster work list fills up, and the
-        # triangles that do not fit are visited whole
+        # two rays per triangle at 1 spp (rasterised with primary_traversal=2): the raster
+        # work list fills up, and the triangles that do not fit are visited whole
         "overflow": synth.spheres_grids(tri_budget=60000, width=360, height=340, spp=1,
                                         max_bounces=4, env_width=128, env_height=64),
     }
@@ -127,7 +129,8 @@ def test_set_tuning_rejects_bad_values(tuned_ctx):
     ctx, _ = tuned_ctx
     for bad in (dict(blocks_per_sm=-1), dict(blocks_per_sm=65), dict(band_rows=-2),
                 dict(wave_paths=-5), dict(use_graphs=2), dict(sort_rays=3), dict(tail_bounce=-2),
-                dict(tail_bounce=65), dict(primary_traversal=2)):
+                dict(tail_bounce=65), dict(primary_traversal=3),
+                dict(primary_traversal=-1)):
         with pytest.raises(capi.PtError):
             ctx.set_tuning(**bad)
     ctx.set_tuning()
