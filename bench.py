@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--trace-primary", action="store_true",
                     help="trace the first bounce through the BVH instead of rasterising it "
                          "(A/B runs; the films are the same)")
+    ap.add_argument("--tuning", default="",
+                    help="pt_tuning fields of the plain line, k=v,... (A/B runs; films are the same)")
     ap.add_argument("--requests", type=int, default=100, help="requests per arrival rate (serve)")
     ap.add_argument("--serve-rates", default="",
                     help="comma-separated arrival rates of the serve object (default 500; "
@@ -794,8 +796,11 @@ def main():
     gen_s = time.perf_counter() - t0
     st = scene.settings
     ctx = capi.Context(local)
+    tuning = {k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(",") if kv)}
     if args.trace_primary:
-        ctx.set_tuning(primary_traversal=1)
+        tuning["primary_traversal"] = 1
+    if tuning:
+        ctx.set_tuning(**tuning)
     t0 = time.perf_counter()
     sid = ctx.upload(scene)
     upload_s = time.perf_counter() - t0
@@ -910,7 +915,7 @@ def main():
         "setup": {"bvh_nodes": info.num_nodes, "mode": "wavefront",
                   "resident_bytes": int(info.device_bytes),
                   "scene_gen_s": round(gen_s, 2), "scene_upload_s": round(upload_s, 2),
-                  "bvh_build_s": round(info.build_seconds, 2)},
+                  "bvh_build_s": round(info.build_seconds, 2), "tuning": tuning or "default"},
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": 64 + 48, "d2h_bytes_per_step": npx * 12,
                 "path": "pt_render (C ABI) with the scene resident, film into pinned host memory"},
