@@ -498,20 +498,21 @@ def run_batch(args):
 # ------------------------------------------------------------------ serving form
 def full_rate_probe(ctx, sid, cam, scene, depth, film_ptr, stream, torch, cache):
     """Msamples/s of the plain path on one whole-GPU wave of this scene at this depth
-    (2048x2048 at 8 spp = 33.5M paths): the rate a request's samples could reach if
+    (2048x2048 at 32 spp = 2^27 paths, the largest wave, whose first bounce is
+    rasterised on every serving scene): the rate a request's samples could reach if
     the GPU were always full. Cached per (scene, depth)."""
     from petrichor_gb300 import capi
     key = (sid, depth)
     if key not in cache:
         st = capi.settings_from_scene(scene, capi.MODE_WAVEFRONT, seed=77, width=2048,
-                                      height=2048, spp=8, max_bounces=depth)
+                                      height=2048, spp=32, max_bounces=depth)
         ctx.render_device(sid, cam, st, film_ptr, stream.cuda_stream)  # warm
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         ctx.render_device(sid, cam, st, film_ptr, stream.cuda_stream)
         e1.record(stream)
         torch.cuda.synchronize()
-        cache[key] = 2048 * 2048 * 8 / (e0.elapsed_time(e1) / 1e3) / 1e6
+        cache[key] = 2048 * 2048 * 32 / (e0.elapsed_time(e1) / 1e3) / 1e6
     return cache[key]
 
 
@@ -625,8 +626,8 @@ def serve_summary(args, rates, count: int, oracle_checks: int = 3):
                 "msamples_per_s_bound": samples / best_makespan / 1e6,
                 "speedup_bound": samples / best_makespan / 1e6 / plain_msps,
                 "method": "each request's samples at the plain path's rate on a whole-GPU wave "
-                          "(2048x2048 x 8 spp) of its scene and depth; makespan >= max(sum of "
-                          "those times, arrival span + the last request's time)"}
+                          "(2048x2048 x 32 spp, 2^27 paths) of its scene and depth; makespan >= "
+                          "max(sum of those times, arrival span + the last request's time)"}
             out["rates"][str(int(rate))] = res
             del films
         # ---- per-request error against the oracle (the reference's estimator) on the

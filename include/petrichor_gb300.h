@@ -292,6 +292,20 @@ int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float*
                      float dist_min, float dist_max, int32_t* tri_device, float* dist_device,
                      void* stream);
 
+/* The first bounce of a wavefront render, for checking it: every camera ray of the
+ * render (width * height * spp of them, which must fit in one wave) and its closest
+ * hit, computed as a render computes them (rasterised or traced through the BVH, as
+ * pt_tuning.primary_traversal and the scene allow; exact ties settled in the
+ * reference's traversal order). Written per (pixel, sample), index
+ * (y * width + x) * spp + s, to device buffers: rays_device 6 floats (o.xyz, dir.xyz),
+ * tri_device the original triangle index (or -1), dist_device the distance (or -1).
+ * Wavefront mode only. Enqueued on `stream`.
+ * No counterpart in the reference: its closest hits are what pt_trace_closest
+ * returns for the same rays (AccelBase::Intersect). */
+int pt_primary_hits(pt_context* ctx, pt_scene_id scene, const pt_camera* cam,
+                    const pt_settings* settings, float* rays_device, int32_t* tri_device,
+                    float* dist_device, void* stream);
+
 /* Host-only binned-SAH build of the triangles (no device needed). Call with
  * NULL outputs to get *num_nodes; then with bounds (num_nodes*6 floats: lo.xyz,
  * hi.xyz), node_ints (num_nodes*5: child0, child1, begin, end, is_leaf) and

@@ -2,9 +2,13 @@
 
 nvcc compiles the kernels for ``-gencode arch=compute_103a,code=sm_103a``; the
 host C++ is compiled by g++ with ``-ffp-contract=off`` (the reference's x86-64
-rounding for the few host-derived floats). The kernels are compiled with
-``-fmad=false`` so that the replay kernel reproduces the reference's
-unfused float arithmetic and the throughput kernels share its triangle test.
+rounding for the few host-derived floats). The kernels are compiled
+with ``-fmad=false``: the replay kernel reproduces the reference's unfused float
+arithmetic, and no code path's results depend on where the compiler would have
+chosen to fuse. A throughput-path result computed by two kernels (the staged
+shade kernel and the tail kernel, a single-job and a mixed wave) is then the same
+bits in both; the fused multiply-adds the throughput path does use are written
+out (``fmaf``), so they are the same in every kernel too.
 """
 from __future__ import annotations
 

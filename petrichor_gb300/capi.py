@@ -142,7 +142,7 @@ EXPORTED = [
     "pt_serve_start", "pt_serve_submit", "pt_serve_poll", "pt_serve_wait", "pt_serve_cancel",
     "pt_serve_release", "pt_serve_stop", "pt_autotune", "pt_set_tuning", "pt_get_tuning",
     "pt_render_aov", "pt_render_aov_device", "pt_bvh_build_device", "pt_set_bvh_builder",
-    "pt_denoise", "pt_denoise_device", "pt_serve_set_deadline",
+    "pt_denoise", "pt_denoise_device", "pt_serve_set_deadline", "pt_primary_hits",
 ]
 
 BVH_BUILDER_HOST, BVH_BUILDER_DEVICE = 0, 1
@@ -187,6 +187,8 @@ def load(build: bool = True):
     L.pt_render_device.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
                                    vp, vp]
     L.pt_trace_closest.argtypes = [vp, i32, i32, vp, ctypes.c_float, ctypes.c_float, vp, vp, vp]
+    L.pt_primary_hits.argtypes = [vp, i32, ctypes.POINTER(PtCamera), ctypes.POINTER(PtSettings),
+                                  vp, vp, vp, vp]
     L.pt_get_stats.argtypes = [vp, ctypes.POINTER(PtStats)]
     L.pt_batch_render.argtypes = [vp, i32, ctypes.POINTER(PtJob), vp]
     u64 = ctypes.c_uint64
@@ -518,6 +520,14 @@ class Context:
                       tri_ptr: int, dist_ptr: int, stream_ptr: int = 0):
         self._check(self.L.pt_trace_closest(self.h, sid, n, rays_ptr, dist_min, dist_max, tri_ptr,
                                             dist_ptr, stream_ptr or None), "pt_trace_closest")
+
+    def primary_hits(self, sid: int, camera: PtCamera, settings: PtSettings, rays_ptr: int,
+                     tri_ptr: int, dist_ptr: int, stream_ptr: int = 0):
+        """The render's camera rays and their first closest hits (pt_primary_hits), per
+        (pixel row-major, sample), into device buffers."""
+        self._check(self.L.pt_primary_hits(self.h, sid, ctypes.byref(camera), ctypes.byref(settings),
+                                           rays_ptr, tri_ptr, dist_ptr, stream_ptr or None),
+                    "pt_primary_hits")
 
     def stats(self) -> PtStats:
         s = PtStats()

@@ -1122,6 +1122,43 @@ int pt_trace_closest(pt_context* ctx, pt_scene_id scene, int32_t n, const float*
     return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "trace");
 }
 
+int pt_primary_hits(pt_context* ctx, pt_scene_id scene, const pt_camera* cam, const pt_settings* st,
+                    float* rays, int32_t* tri, float* dist, void* stream) {
+    if (!ctx) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    SceneGpu* sg = nullptr;
+    int rc = CheckArgs(ctx, scene, cam, st, &sg);
+    if (rc != PT_OK) return rc;
+    if (!rays || !tri || !dist) return Fail(ctx, PT_ERR_INVALID_ARG, "output buffer is NULL");
+    if (st->mode != PT_MODE_WAVEFRONT)
+        return Fail(ctx, PT_ERR_UNSUPPORTED, "primary hits are those of the wavefront mode");
+    const int cap = WaveCapacity(ctx, st);
+    if ((int64_t)st->width * st->height * st->spp > cap)
+        return Fail(ctx, PT_ERR_INVALID_ARG, "the camera rays do not fit in one wave");
+    if ((rc = SetDevice(ctx)) != PT_OK) return rc;
+    if ((rc = EnsureWaveBuffers(ctx, cap)) != PT_OK) return rc;
+    if ((rc = EnsureTables(ctx, 1, (size_t)st->width * st->height)) != PT_OK) return rc;
+    std::vector<DevJob> jobs(1);
+    jobs[0].S = JobScene(*sg, st);
+    jobs[0].C = ToDev(cam);
+    jobs[0].st = ToDev(st);
+    jobs[0].accum = (float4*)ctx->accum.ptr;
+    std::vector<WaveUnit> units(1);
+    units[0] = WaveUnit{0, 0, st->spp, 0, 0, -1, {0, 0}};
+    const WaveShape shape = ShapeOf(jobs, units, ctx->tuning.primaryTraversal);
+    const WaveTables T = Tables(ctx);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    int launches = 0;
+    cudaError_t e = cudaMemcpyAsync(T.jobs, jobs.data(), sizeof(DevJob), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(T.units, units.data(), sizeof(WaveUnit), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = RunPrimaryHits(T.jobs, T.units, shape, ctx->wb, ctx->tuning, st->spp, rays, tri, dist, s,
+                           &launches);
+    ctx->stats.kernel_launches += launches;
+    return e == cudaSuccess ? PT_OK : CudaFail(ctx, e, "primary hits");
+}
+
 int pt_bvh_build(const float* positions, uint32_t numVertices, const int32_t* indices,
                  uint32_t numTriangles, int32_t threads, uint32_t* numNodes, uint32_t* height,
                  float* bounds, int32_t* nodeInts, int32_t* primIds) {

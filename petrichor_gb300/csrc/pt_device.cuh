@@ -45,6 +45,24 @@ __device__ __forceinline__ V3 Cross(V3 a, V3 b) {
     return V3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 __device__ __forceinline__ float SqLen(V3 a) { return Dot(a, a); }
+// Unfused forms: every product and sum rounded on its own, as g++ evaluates the
+// reference's float expressions. __fmul_rn/__fadd_rn are never contracted into fused
+// multiply-adds, so these give the reference's bits in a file built with -fmad=true
+// (the throughput kernels) as in one built with -fmad=false (the replay kernels).
+__device__ __forceinline__ float DotRn(V3 a, V3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ V3 CrossRn(V3 a, V3 b) {
+    return V3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)),
+              __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float SqLenRn(V3 a) { return DotRn(a, a); }
+// (lo + hi) * 0.5f, the product kept apart from the subtraction that follows it
+__device__ __forceinline__ V3 CentreRn(V3 lo, V3 hi) {
+    const V3 s = lo + hi;
+    return V3(__fmul_rn(s.x, 0.5f), __fmul_rn(s.y, 0.5f), __fmul_rn(s.z, 0.5f));
+}
 __device__ __forceinline__ float Length(V3 a) { return sqrtf(Dot(a, a)); }  // = (float)sqrt(double)
 __device__ __forceinline__ V3 Normalized(V3 a) { return a / Length(a); }
 // 1 / d per component, correctly rounded whatever the file's division flags: the
@@ -205,17 +223,18 @@ __device__ __forceinline__ int SlotMaterial(const float4* __restrict__ shade, in
     return __float_as_int(__ldg(&shade[3 * k].w));
 }
 
-// Triangle::Intersect (Core/Geometry/Triangle.cpp:51-88)
+// Triangle::Intersect (Core/Geometry/Triangle.cpp:51-88), unfused and correctly
+// rounded in every build: closest-hit IDs and distances are the reference's.
 __device__ __forceinline__ bool TriIntersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& dist) {
-    const V3 ce = Cross(e1, e2);
-    const float invDet = __fdiv_rn(1.0f, Dot(-d, ce));  // correctly rounded in every build
+    const V3 ce = CrossRn(e1, e2);
+    const float invDet = __fdiv_rn(1.0f, DotRn(-d, ce));
     const V3 vec = o - v0;
-    const float w1 = Dot(vec, Cross(d, e2)) * invDet;
-    const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+    const float w1 = __fmul_rn(DotRn(vec, CrossRn(d, e2)), invDet);
+    const float w2 = __fmul_rn(DotRn(vec, CrossRn(e1, d)), invDet);
     if (w1 < 0.0f || w1 >= 1.0f) return false;
     if (w2 < 0.0f || w2 >= 1.0f) return false;
-    if (w1 + w2 >= 1.0f) return false;
-    const float t = Dot(vec, ce) * invDet;
+    if (__fadd_rn(w1, w2) >= 1.0f) return false;
+    const float t = __fmul_rn(DotRn(vec, ce), invDet);
     if (t < 0.0f) return false;
     dist = t;
     return true;
@@ -794,15 +813,15 @@ __device__ int TraverseReference(const DevScene& S, V3 o, V3 d, float distMin, f
         const float4 na = __ldg(S.nodes + 2 * ni), nb = __ldg(S.nodes + 2 * ni + 1);
         const V3 lo(na.x, na.y, na.z), hi(na.w, nb.x, nb.y);
         const V3 b0 = s0 ? hi : lo, b1 = s0 ? lo : hi;  // aabb[sign], aabb[1 - sign] for x
-        float tMin = (b0.x - o.x) * inv.x;
-        float tMax = (b1.x - o.x) * inv.x;
-        const float tyMin = ((s1 ? hi : lo).y - o.y) * inv.y;
-        const float tyMax = ((s1 ? lo : hi).y - o.y) * inv.y;
+        float tMin = __fmul_rn(b0.x - o.x, inv.x);
+        float tMax = __fmul_rn(b1.x - o.x, inv.x);
+        const float tyMin = __fmul_rn((s1 ? hi : lo).y - o.y, inv.y);
+        const float tyMax = __fmul_rn((s1 ? lo : hi).y - o.y, inv.y);
         if (tyMax < tMin || tMax < tyMin) continue;
         if (tMin < tyMin) tMin = tyMin;
         if (tyMax < tMax) tMax = tyMax;
-        const float tzMin = ((s2 ? hi : lo).z - o.z) * inv.z;
-        const float tzMax = ((s2 ? lo : hi).z - o.z) * inv.z;
+        const float tzMin = __fmul_rn((s2 ? hi : lo).z - o.z, inv.z);
+        const float tzMax = __fmul_rn((s2 ? lo : hi).z - o.z, inv.z);
         if (tzMax < tMin || tMax < tzMin) continue;
         if (tMin < tzMin) tMin = tzMin;
         if (tzMax < tMax) tMax = tzMax;
@@ -840,8 +859,8 @@ __device__ int TraverseReference(const DevScene& S, V3 o, V3 d, float distMin, f
         } else {
             const float4 la = __ldg(S.nodes + 2 * a), lb = __ldg(S.nodes + 2 * a + 1);
             const float4 ra = __ldg(S.nodes + 2 * a + 2), rb = __ldg(S.nodes + 2 * a + 3);
-            const float dl = SqLen((V3(la.x, la.y, la.z) + V3(la.w, lb.x, lb.y)) * 0.5f - o);
-            const float dr = SqLen((V3(ra.x, ra.y, ra.z) + V3(ra.w, rb.x, rb.y)) * 0.5f - o);
+            const float dl = SqLenRn(CentreRn(V3(la.x, la.y, la.z), V3(la.w, lb.x, lb.y)) - o);
+            const float dr = SqLenRn(CentreRn(V3(ra.x, ra.y, ra.z), V3(ra.w, rb.x, rb.y)) - o);
             if (sp + 2 > S.stackDepth) {
                 *status |= kErrStackOverflow;
                 return best;

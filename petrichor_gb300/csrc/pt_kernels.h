@@ -119,6 +119,7 @@ struct WaveProfile {
 struct WaveShape {
     int nUnits = 0, nPaths = 0, nPixelUnits = 0;
     int iters = 0, integrator = -1, soleJob = -1;
+    int areaLights = 1;  // 0: no job of the wave has area lights (next-event rays are any-hit)
     // > 0: the first bounce of units [rasterUnit0, nUnits) (paths [rasterFrom, nPaths)) may
     // be rasterised (raster_primary.cuh); raster = their per-triangle records in all
     int raster = 0, rasterFrom = 0, rasterUnit0 = 0;
@@ -164,6 +165,14 @@ cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream);
 
 int DefaultStageGrid();
 int StageGrid(const WaveTuning& tune);
+
+// The first bounce of a one-job, one-wave render (units: its one unit; shape as RunWave
+// takes it): raygen, then the closest hit of every camera ray (rasterised or traced as a
+// render would), written out per (pixel row-major, sample): the ray (6 floats), the
+// original triangle index (or -1) and the distance (or -1).
+cudaError_t RunPrimaryHits(const DevJob* jobs, const WaveUnit* units, const WaveShape& shape,
+                           const WaveBuffers& wb, const WaveTuning& tune, int spp, float* raysOut,
+                           int* triOut, float* distOut, cudaStream_t stream, int* launches);
 
 // Closest-hit traversal of the throughput path for caller rays (o.xyz, d.xyz per ray).
 // fetchCounter: one device int of scratch for the persistent fetch.

@@ -101,22 +101,22 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
             const int W = J.st.width, H = J.st.height;
             const V3 pos = LoadV3(J.C.pos), right = LoadV3(J.C.right), up = LoadV3(J.C.up),
                      fwd = LoadV3(J.C.fwd);
-            const float rr = 1.0f / SqLen(right), uu = 1.0f / SqLen(up);
+            const float rr = 1.0f / SqLenRn(right), uu = 1.0f / SqLenRn(up);
             V3 v0, e1, e2;
             LoadTri(S.tris, k, v0, e1, e2);
             const V3 a[3] = {v0 - pos, (v0 + e1) - pos, (v0 + e2) - pos};
             // the plane through the camera and edge k is a_k x a_k+1 = a_k x (edge k): formed
             // from the short edge vector it has no cancellation (the cross product of two
             // long, nearly parallel vectors from a distant camera would lose most digits)
-            V3 n[3] = {Cross(a[0], e1), Cross(a[1], e2 - e1), Cross(a[2], e2 * -1.0f)};
-            const V3 ce = Cross(e1, e2);
-            const float side = Dot(a[0], ce);  // which side of the triangle the camera is on
+            V3 n[3] = {CrossRn(a[0], e1), CrossRn(a[1], e2 - e1), CrossRn(a[2], e2 * -1.0f)};
+            const V3 ce = CrossRn(e1, e2);
+            const float side = DotRn(a[0], ce);  // which side of the triangle the camera is on
             float m[3];
-            if (fabsf(side) > 1.0e-5f * sqrtf(SqLen(a[0]) * SqLen(ce))) {
+            if (fabsf(side) > 1.0e-5f * sqrtf(__fmul_rn(SqLenRn(a[0]), SqLenRn(ce)))) {
                 const float sg = side > 0.0f ? 1.0f : -1.0f;
                 for (int e = 0; e < 3; e++) {
                     n[e] = n[e] * sg;
-                    m[e] = 2.0e-5f * sqrtf(SqLen(n[e]));  // angular margin ~2e-5 rad
+                    m[e] = 2.0e-5f * sqrtf(SqLenRn(n[e]));  // angular margin ~2e-5 rad
                 }
             } else {  // camera (nearly) in the triangle's plane, or a degenerate triangle: no cone test
                 for (int e = 0; e < 3; e++) {
@@ -130,9 +130,9 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
             float X[3], Y[3], Z[3], zmax = 0.0f;
             bool front = true, anyFront = false;
             for (int v = 0; v < 3; v++) {
-                X[v] = Dot(a[v], right) * rr;
-                Y[v] = Dot(a[v], up) * uu;
-                Z[v] = Dot(a[v], fwd);
+                X[v] = __fmul_rn(DotRn(a[v], right), rr);
+                Y[v] = __fmul_rn(DotRn(a[v], up), uu);
+                Z[v] = DotRn(a[v], fwd);
                 zmax = fmaxf(zmax, fabsf(Z[v]));
             }
             const float zc = 1.0e-6f * zmax + 1.0e-30f;

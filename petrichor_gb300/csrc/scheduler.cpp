@@ -116,13 +116,17 @@ void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* 
     shape->rasterUnit0 = (int)trace.size();
 }
 
+int WaveAreaLights(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units) {
+    for (const WaveUnit& u : units)
+        if (jobs[u.job].S.numLights > 0) return 1;
+    return 0;
+}
+
 int WaveSoleJob(const std::vector<WaveUnit>& units) {
     for (const WaveUnit& u : units)
         if (u.job != units.front().job) return -1;
     return units.empty() ? -1 : units.front().job;
 }
-
-namespace {
 
 WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units,
                   int primaryTraversal) {
@@ -136,9 +140,12 @@ WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units,
     shape.iters = WaveIterations(jobs, units);
     shape.integrator = WaveIntegrator(jobs, units);
     shape.soleJob = WaveSoleJob(units);
+    shape.areaLights = WaveAreaLights(jobs, units);
     PrepareRasterUnits(jobs, &units, &shape, primaryTraversal);
     return shape;
 }
+
+namespace {
 
 // Finalises the jobs whose last wave is w (film = sums / spp), on `stream`.
 cudaError_t FinalizeDone(const std::vector<DevJob>& jobs, const WaveTables& T,

@@ -38,6 +38,12 @@ int WaveIterations(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>&
 int WaveIntegrator(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
 // The job of all of a wave's units, or -1 when they belong to several.
 int WaveSoleJob(const std::vector<WaveUnit>& units);
+// 1 when a job of the wave has area lights (its next-event rays include closest-hit ones).
+int WaveAreaLights(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units);
+// The shape of a wave of these units (path and pixel counts, iterations, integrator,
+// sole job, area lights, rasterised units, which it moves last and renumbers).
+WaveShape ShapeOf(const std::vector<DevJob>& jobs, std::vector<WaveUnit>& units,
+                  int primaryTraversal);
 // Rays per triangle from which a unit's first bounce is rasterised by default. Measured
 // on GB300 with films alike: at 133 (1.0M triangles, 1920x1080, 64 spp) the raster pass
 // takes 5.5 ms against about 10 ms of first-bounce traversal; at 3.3 (20.0M triangles,

@@ -437,6 +437,7 @@ private:
         shape.iters = WaveIterations(slotJobs_, units);
         shape.integrator = WaveIntegrator(slotJobs_, units);
         shape.soleJob = WaveSoleJob(units);
+        shape.areaLights = WaveAreaLights(slotJobs_, units);
         std::vector<WaveUnit> ordered = units;  // rasterised units last
         PrepareRasterUnits(slotJobs_, &ordered, &shape, tune_.primaryTraversal);
         if (e == cudaSuccess)

@@ -48,14 +48,30 @@ __device__ __forceinline__ void PixelOfIndex(int q, int W, int H, int rows, int&
     y = y0 + r % hb;
 }
 
-// Box test against [tmin, tmax]; returns the entry distance.
-__device__ __forceinline__ bool SlabFast(float4 a, float4 b, V3 o, V3 inv, float tmin, float tmax,
+// Three-input maximum and minimum (max.f32 / min.f32 with three sources, sm_100 and
+// later); a NaN operand is ignored, as by fmaxf / fminf.
+__device__ __forceinline__ float Max3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float Min3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Box test against [tmin, tmax]; returns the entry distance. Each plane distance is
+// one fused multiply-add, plane * inv - oi with oi = o * inv. Its rounding
+// (a few units in the last place of the origin's and the distance's coordinates) is
+// far inside the 2^-18 widening of the child boxes, so no hit box is missed.
+__device__ __forceinline__ bool SlabFast(float4 a, float4 b, V3 oi, V3 inv, float tmin, float tmax,
                                          float& tEnter) {
-    const float tx0 = (a.x - o.x) * inv.x, tx1 = (a.w - o.x) * inv.x;
-    const float ty0 = (a.y - o.y) * inv.y, ty1 = (b.x - o.y) * inv.y;
-    const float tz0 = (a.z - o.z) * inv.z, tz1 = (b.y - o.z) * inv.z;
-    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    const float tx0 = fmaf(a.x, inv.x, -oi.x), tx1 = fmaf(a.w, inv.x, -oi.x);
+    const float ty0 = fmaf(a.y, inv.y, -oi.y), ty1 = fmaf(b.x, inv.y, -oi.y);
+    const float tz0 = fmaf(a.z, inv.z, -oi.z), tz1 = fmaf(b.y, inv.z, -oi.z);
+    const float tn = Max3(fminf(tx0, tx1), fminf(ty0, ty1), fmaxf(fminf(tz0, tz1), tmin));
+    const float tf = Min3(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fminf(fmaxf(tz0, tz1), tmax));
     tEnter = tn;
     return tn <= tf;
 }
@@ -135,6 +151,18 @@ struct TravStack {
         }
         sp++;
     }
+    // Any-hit rays: entries without distances (nothing is culled before the first hit,
+    // which ends the ray).
+    __device__ __forceinline__ void PushCode(int c) {
+        if (sp < kSmemStack) code[sp * kTraceBlock + threadIdx.x] = c;
+        else deep[sp - kSmemStack].x = c;
+        sp++;
+    }
+    __device__ __forceinline__ int PopCode() {
+        if (sp == 0) return kDone;
+        --sp;
+        return sp < kSmemStack ? code[sp * kTraceBlock + threadIdx.x] : deep[sp - kSmemStack].x;
+    }
     // Next entry whose box starts no farther than tBest, or kDone.
     __device__ __forceinline__ int Pop(float tBest) {
         while (sp > 0) {
@@ -157,6 +185,8 @@ struct TravStack {
 
 // Tests the triangles of leaf `cur`; returns true when an any-hit ray is done.
 // Otherwise `cur` becomes the next item from the stack (or kDone).
+// kAnyHit: every ray of the queue is an any-hit ray (known at compile time).
+template <bool kAnyHit>
 __device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur, int& err) {
     const int v = -cur - 1;
     const int first = v >> 6, cnt = v & 63;
@@ -175,18 +205,22 @@ __device__ __forceinline__ bool VisitLeaf(LaneRay& r, TravStack& stk, int& cur, 
             if (t < r.tBest) {
                 r.tBest = t;
                 r.best = k;
-                if (r.anyHit) return true;
+                if (kAnyHit || r.anyHit) return true;
             } else if (t == r.tBest && r.best >= 0) {
                 r.best = -2 - r.best;  // an exact tie: settled by the reference's order
             }
         }
     }
-    cur = stk.Pop(r.tBest);
+    cur = kAnyHit ? stk.PopCode() : stk.Pop(r.tBest);
     return false;
 }
 
 // Tests the children of wide node `cur`; `cur` becomes the nearest hit child and
 // the other hit children are pushed farthest first (or the next stack item).
+// kAnyHit: only the nearest child is picked out; the others are pushed in slot order
+// (an any-hit ray ends at its first hit, and whether it hits does not depend on the
+// order its boxes are visited in).
+template <bool kAnyHit>
 __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur, int& err) {
     constexpr int K = kWide, Q = kWide / 4;
 #if PT_CHECK
@@ -218,15 +252,39 @@ __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur,
         c[4 * j + 3] = v.w;
     }
     const float inf = __int_as_float(0x7f800000);
+    const V3 oi = r.o * r.inv;
     float t[K];
 #pragma unroll
     for (int i = 0; i < K; i++) {
         float te;
         t[i] = (c[i] != INT_MIN && SlabFast(make_float4(b[0][i], b[1][i], b[2][i], b[3][i]),
-                                            make_float4(b[4][i], b[5][i], 0.f, 0.f), r.o, r.inv,
+                                            make_float4(b[4][i], b[5][i], 0.f, 0.f), oi, r.inv,
                                             0.0f, r.tBest, te))
                  ? te
                  : inf;
+    }
+    if (kAnyHit && K == 4) {
+        // the nearest into slot 0
+        SortPair(t[0], c[0], t[1], c[1]);
+        SortPair(t[2], c[2], t[3], c[3]);
+        SortPair(t[0], c[0], t[2], c[2]);
+        if (t[0] == inf) {
+            cur = stk.PopCode();
+            return;
+        }
+        int pushes = 0;
+#pragma unroll
+        for (int i = 1; i < K; i++) pushes += t[i] != inf;
+        if (stk.sp + pushes > kWaveStackDepth) {
+            err |= kErrStackOverflow;
+            cur = kDone;
+            return;
+        }
+#pragma unroll
+        for (int i = K - 1; i >= 1; i--)
+            if (t[i] != inf) stk.PushCode(c[i]);
+        cur = c[0];
+        return;
     }
     // sorting network, nearest first
     if (K == 4) {
@@ -285,7 +343,8 @@ __device__ __noinline__ void ResolveTie(const DevScene* S, V3 o, V3 d, float tmi
 // Q provides: void Load(int i, LaneRay&) (ray, range, and the scene: nodes = nullptr
 // for an empty scene) and void Finish(int i, const LaneRay&).
 // Must be called by every lane of the warp, in blocks of kTraceBlock threads.
-template <class Q>
+// kAnyHit: every ray Q loads is an any-hit ray.
+template <bool kAnyHit, class Q>
 __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
     __shared__ int sCode[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
     __shared__ float sDist[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
@@ -336,12 +395,12 @@ __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
         if (active) {
             bool done = false;
 #if PT_WHILE_WHILE
-            while (cur >= 0) VisitInner(r, stk, cur, err);
+            while (cur >= 0) VisitInner<kAnyHit>(r, stk, cur, err);
             __syncwarp(busy);  // the lanes' leaves are intersected together
-            if (cur != kDone) done = VisitLeaf(r, stk, cur, err);
+            if (cur != kDone) done = VisitLeaf<kAnyHit>(r, stk, cur, err);
 #else
-            if (cur >= 0) VisitInner(r, stk, cur, err);
-            else if (cur != kDone) done = VisitLeaf(r, stk, cur, err);
+            if (cur >= 0) VisitInner<kAnyHit>(r, stk, cur, err);
+            else if (cur != kDone) done = VisitLeaf<kAnyHit>(r, stk, cur, err);
 #endif
             if (done || cur == kDone) {
                 q.Finish(idx, r);
@@ -450,7 +509,7 @@ __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const D
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur ^ 1] = 0;
     int err = 0;
     ExtendQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.ray[cur], wb.hit};
-    TraceQueue(q, n, wb.counts + 4, err);
+    TraceQueue<false>(q, n, wb.counts + 4, err);
     if (err) atomicOr(wb.counts + 3, err);
 }
 
@@ -729,12 +788,14 @@ __device__ __noinline__ void ApplyAreaLight(const DevScene& S, const float4* e, 
                                             float tBest, int path, float4* pathL);
 // Adds a traced next-event entry's contribution to its path's radiance; e holds the
 // entry's four float4 (read only as needed: an occluded environment entry reads one).
+// kEnvOnly: the entry is an environment entry (no area light in the wave).
+template <bool kEnvOnly = false>
 __device__ __forceinline__ void ApplyShadow(const DevScene& S, const float4* e, const LaneRay& r,
                                             float4* pathL) {
     const float4 e1 = e[1];
     const int tag = __float_as_int(e1.w);
     const int path = tag & 0x7FFFFFFF;
-    if (tag >= 0) {  // environment: adds when unoccluded
+    if (kEnvOnly || tag >= 0) {  // environment: adds when unoccluded
         if (r.best != -1) return;
         const float4 e2 = e[2];
         float4 l = pathL[path];
@@ -780,6 +841,7 @@ __device__ __noinline__ void ApplyAreaLight(const DevScene& S, const float4* e, 
     pathL[path] = l;
 }
 
+template <bool kEnvOnly>
 struct ShadowQueue {
     const DevJob* jobs;
     const int* pathJob;
@@ -792,7 +854,7 @@ struct ShadowQueue {
     }
     __device__ void Finish(int j, const LaneRay& r) const {
         const int path = __float_as_int(entries[4 * j + 1].w) & 0x7FFFFFFF;
-        ApplyShadow(jobs[JobOf(pathJob, soleJob, path)].S, entries + 4 * j, r, pathL);
+        ApplyShadow<kEnvOnly>(jobs[JobOf(pathJob, soleJob, path)].S, entries + 4 * j, r, pathL);
     }
 };
 
@@ -806,8 +868,8 @@ __device__ __forceinline__ void TraceOne(LaneRay& r, TravStack& stk, int& err) {
     if (!r.nodes) return;
     int cur = 0;  // wide root
     while (cur != kDone) {
-        if (cur >= 0) VisitInner(r, stk, cur, err);
-        else if (VisitLeaf(r, stk, cur, err)) break;
+        if (cur >= 0) VisitInner<false>(r, stk, cur, err);
+        else if (VisitLeaf<false>(r, stk, cur, err)) break;
     }
 }
 
@@ -913,11 +975,14 @@ __global__ void __launch_bounds__(128) TailKernel(const DevJob* __restrict__ job
 // It may run beside the next bounce's extend kernel (which touches neither the
 // shadow queue nor its counters); its last block to finish clears the shadow queue
 // size and fetch counter for the next shade.
+// kEnvOnly: no job of the wave has area lights, so every entry is an environment
+// entry, an any-hit ray (the traversal specialised for it).
+template <bool kEnvOnly>
 __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ShadowKernel(const DevJob* __restrict__ jobs, WaveBuffers wb) {
     const int n = wb.counts[2];
     int err = 0;
-    ShadowQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.shadow, wb.pathL};
-    TraceQueue(q, n, wb.counts + 5, err);
+    ShadowQueue<kEnvOnly> q{jobs, wb.pathJob, wb.desc->soleJob, wb.shadow, wb.pathL};
+    TraceQueue<kEnvOnly>(q, n, wb.counts + 5, err);
     if (err) atomicOr(wb.counts + 3, err);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1014,7 +1079,7 @@ __global__ void __launch_bounds__(128) TraceKernel(DevScene S, int n, const floa
     RayBatchQueue q{&S, S.numWide > 0 ? S.wide : nullptr, S.tris, S.numWide, S.numTris, rays, tmin,
                     tmax, triOut, distOut};
     int err = 0;
-    TraceQueue(q, n, fetch, err);
+    TraceQueue<false>(q, n, fetch, err);
 }
 
 // Profiling helpers: ray tallies and the reference traversal's work per ray.
@@ -1296,10 +1361,11 @@ struct StageOverlap {
 };
 
 // tailFrom > 0: bounces from it0 + tailFrom on run in one TailKernel launch.
+// envOnly: no job of the wave has area lights (the any-hit shadow kernel).
 static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveBuffers& wb,
                           int integrator, int grid, int it0, int count, cudaStream_t stream,
-                          WaveProfile* prof, int* nl, bool sort, StageOverlap* ov, int tailFrom = 0,
-                          bool raster = false) {
+                          WaveProfile* prof, int* nl, bool sort, StageOverlap* ov, bool envOnly,
+                          int tailFrom = 0, bool raster = false) {
     StageEvents* ev = prof ? (StageEvents*)prof->events : nullptr;
     const int block = kTraceBlock;
     const int sgrid = ShadeGrid(grid);
@@ -1364,11 +1430,14 @@ static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveB
         if (ov) {
             cudaEventRecord(ov->fork, stream);
             cudaStreamWaitEvent(ov->side, ov->fork, 0);
-            ShadowKernel<<<grid, block, 0, ov->side>>>(jobs, wb);
+            if (envOnly) ShadowKernel<true><<<grid, block, 0, ov->side>>>(jobs, wb);
+            else ShadowKernel<false><<<grid, block, 0, ov->side>>>(jobs, wb);
             cudaEventRecord(ov->join, ov->side);
             pendingShadow = true;
+        } else if (envOnly) {
+            ShadowKernel<true><<<grid, block, 0, stream>>>(jobs, wb);
         } else {
-            ShadowKernel<<<grid, block, 0, stream>>>(jobs, wb);
+            ShadowKernel<false><<<grid, block, 0, stream>>>(jobs, wb);
         }
         if (ev) ev->End(3, stream);
         *nl += 3;
@@ -1393,11 +1462,11 @@ struct WaveGraphKey {
     const void* jobs;
     const void* units;
     const void* buffers;
-    int capacity, iters, integrator, grid, sort, accum, tail, raster;
+    int capacity, iters, integrator, grid, sort, accum, tail, raster, envOnly;
     bool operator==(const WaveGraphKey& o) const {
         return jobs == o.jobs && units == o.units && buffers == o.buffers && capacity == o.capacity &&
                iters == o.iters && integrator == o.integrator && grid == o.grid && sort == o.sort &&
-               accum == o.accum && tail == o.tail && raster == o.raster;
+               accum == o.accum && tail == o.tail && raster == o.raster && envOnly == o.envOnly;
     }
 };
 struct WaveGraph {
@@ -1522,13 +1591,14 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
     // whose stage timers need one stream)
     StageOverlap* ov =
       (graphs && !prof && graphs->overlap[lane & 1].Ready()) ? &graphs->overlap[lane & 1] : nullptr;
+    const bool envOnly = !shape.areaLights;
     const WaveGraphKey key{jobs, units, wb.ray[0], wb.capacity, shape.iters, shape.integrator, grid,
-                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom, raster ? 1 : 0};
+                           sort ? 1 : 0, accumulate ? 1 : 0, tailFrom, raster ? 1 : 0, envOnly ? 1 : 0};
     if (shape.iters >= 0) {
         auto record = [&](int* n) {
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, raster ? 1 : 0);
             LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, shape.iters, stream, prof, n, sort,
-                          ov, tailFrom, raster);
+                          ov, envOnly, tailFrom, raster);
             if (accumulate) AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
             *n += accumulate ? 2 : 1;
         };
@@ -1539,7 +1609,7 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
             RaygenKernel<<<grid, block, 0, stream>>>(jobs, units, wb, 0, raster ? 1 : 0);
             if (ev) ev->End(0, stream);
             LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, shape.iters, stream, prof, &nl, sort,
-                          ov, tailFrom, raster);
+                          ov, envOnly, tailFrom, raster);
             if (accumulate) {
                 if (ev) ev->Begin(4, stream);
                 AccumulateKernel<<<grid, block, 0, stream>>>(jobs, units, wb);
@@ -1565,11 +1635,12 @@ cudaError_t RunWave(const DevJob* jobs, const WaveUnit* units, const WaveShape& 
                 k.iters = -kPollEvery;
                 e = ReplayCaptured(graphs, k, stream, &nl, [&](int* n) {
                     LaunchBounces(jobs, units, wb, shape.integrator, grid, 0, kPollEvery, stream, nullptr, n, sort,
-                                  ov);
+                                  ov, envOnly);
                 });
                 if (e != cudaSuccess) break;
             } else {
-                LaunchBounces(jobs, units, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort, ov);
+                LaunchBounces(jobs, units, wb, shape.integrator, grid, it, kPollEvery, stream, prof, &nl, sort, ov,
+                              envOnly);
             }
         }
         if (e == cudaSuccess && accumulate) {
@@ -1617,6 +1688,69 @@ cudaError_t CollectProfile(WaveProfile* prof, cudaStream_t stream) {
 }
 
 void* NewStageEvents() { return new StageEvents(); }
+
+// Each path's camera ray and first closest hit, in (pixel row-major, sample) order:
+// index (y * W + x) * spp + s. Ties are settled in the reference's order, as the shade
+// stage settles them.
+__global__ void PrimaryOutKernel(const DevJob* __restrict__ jobs, WaveBuffers wb, int spp,
+                                 float* __restrict__ raysOut, int* __restrict__ triOut,
+                                 float* __restrict__ distOut) {
+    const WaveDesc wd = *wb.desc;
+    const DevJob& J = jobs[0];
+    const int W = J.st.width, H = J.st.height;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < wd.nPaths; i += gridDim.x * blockDim.x) {
+        const float4 a = wb.ray[0][2 * i], b = wb.ray[0][2 * i + 1];
+        float2 h = wb.hit[i];
+        if (__float_as_int(h.y) < -1) h = SettleTie(J, V3(a.x, a.y, a.z), V3(b.x, b.y, b.z), h);
+        const int best = __float_as_int(h.y);
+        int x, y;
+        PixelOfIndex(i / spp, W, H, wd.band, x, y);
+        const size_t o = ((size_t)y * W + x) * spp + i % spp;
+        float* r = raysOut + 6 * o;
+        r[0] = a.x;
+        r[1] = a.y;
+        r[2] = a.z;
+        r[3] = b.x;
+        r[4] = b.y;
+        r[5] = b.z;
+        triOut[o] = best >= 0 ? TriId(J.S.tris, best) : -1;
+        distOut[o] = best >= 0 ? h.x : -1.0f;
+    }
+}
+
+cudaError_t RunPrimaryHits(const DevJob* jobs, const WaveUnit* units, const WaveShape& shape,
+                           const WaveBuffers& wb, const WaveTuning& tune, int spp, float* raysOut,
+                           int* triOut, float* distOut, cudaStream_t stream, int* launches) {
+    if (shape.nUnits != 1 || shape.nPaths <= 0 || shape.nPaths > wb.capacity)
+        return cudaErrorInvalidValue;
+    const int grid = StageGrid(tune);
+    const bool raster = shape.raster > 0 && tune.primaryTraversal != 1 && tune.sortRays == 0 &&
+                        shape.iters >= 0;
+    WaveDesc d{};
+    d.nUnits = shape.nUnits;
+    d.nPaths = shape.nPaths;
+    d.nPixelUnits = shape.nPixelUnits;
+    d.soleJob = 0;
+    d.band = tune.band > 0 ? tune.band : 8;
+    d.rasterFrom = raster ? shape.rasterFrom : shape.nPaths;
+    d.rasterUnit0 = raster ? shape.rasterUnit0 : shape.nUnits;
+    d.rasterRecs = raster ? shape.raster : 0;
+    cudaError_t e = cudaMemcpyAsync(wb.desc, &d, sizeof(d), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(wb.counts, 0, 16 * sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    RaygenKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, units, wb, 0, raster ? 1 : 0);
+    ExtendKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, wb, 0, raster ? 1 : 0);
+    int nl = 3;
+    if (raster) {
+        RasterSetupKernel<<<SmCount() * 32, kTraceBlock, 0, stream>>>(jobs, units, wb, 0);
+        RasterVisitKernel<<<SmCount() * 16, kTraceBlock, 0, stream>>>(jobs, units, wb, 0);
+        RasterFinishKernel<<<grid, kTraceBlock, 0, stream>>>(wb, 0);
+        nl += 3;
+    }
+    PrimaryOutKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, wb, spp, raysOut, triOut, distOut);
+    if (launches) *launches += nl;
+    return cudaGetLastError();
+}
 
 cudaError_t LaunchTraceClosest(const DevScene& S, int n, const float* rays, float distMin,
                                float distMax, int* triOut, float* distOut, int* fetchCounter,

@@ -445,24 +445,39 @@ def bvh_ties(seed: int = 6, n_lattice: int = 2400, n_zero: int = 500, n_free: in
     return Scene(pos, nrm, uv, idx, tm, sh, np.zeros(0, np.int32), mats, cam, env, st)
 
 
-def batch_instances(seed: int = 3, n: int = 64, tri_lo: float = 1e4, tri_hi: float = 2e6,
-                    px_lo: float = 256 ** 2, px_hi: float = 1024 ** 2, spps=(4, 16, 64, 256),
-                    env_width: int = 1024, env_height: int = 512, max_bounces: int = 16):
-    """``n`` independent spheres-and-grids scenes of uneven size: triangle counts and
-    pixel counts log-uniform, aspect uniform in [0.5, 2], spp drawn from ``spps``."""
+def batch_instance_params(seed: int = 3, n: int = 64, tri_lo: float = 1e4, tri_hi: float = 2e6,
+                          px_lo: float = 256 ** 2, px_hi: float = 1024 ** 2, spps=(4, 16, 64, 256)):
+    """(triangle budget, width, height, spp) of each of ``batch_instances``' scenes."""
     rng = Rng(seed)
     out = []
-    for k in range(n):
+    for _ in range(n):
         tris = int(math.exp(rng.one(math.log(tri_lo), math.log(tri_hi))))
         px = math.exp(rng.one(math.log(px_lo), math.log(px_hi)))
         aspect = rng.one(0.5, 2.0)
         w = max(8, int(round(math.sqrt(px * aspect))))
         h = max(8, int(round(px / w)))
         spp = spps[int(rng.one() * len(spps)) % len(spps)]
-        out.append(spheres_grids(seed=1000 + k, tri_budget=tris, width=w, height=h, spp=spp,
-                                 max_bounces=max_bounces, env_width=env_width,
-                                 env_height=env_height))
+        out.append((tris, w, h, spp))
     return out
+
+
+def batch_instance(k: int, seed: int = 3, env_width: int = 1024, env_height: int = 512,
+                   max_bounces: int = 16, **ranges):
+    """Scene k of ``batch_instances`` alone."""
+    tris, w, h, spp = batch_instance_params(seed, k + 1, **ranges)[k]
+    return spheres_grids(seed=1000 + k, tri_budget=tris, width=w, height=h, spp=spp,
+                         max_bounces=max_bounces, env_width=env_width, env_height=env_height)
+
+
+def batch_instances(seed: int = 3, n: int = 64, tri_lo: float = 1e4, tri_hi: float = 2e6,
+                    px_lo: float = 256 ** 2, px_hi: float = 1024 ** 2, spps=(4, 16, 64, 256),
+                    env_width: int = 1024, env_height: int = 512, max_bounces: int = 16):
+    """``n`` independent spheres-and-grids scenes of uneven size: triangle counts and
+    pixel counts log-uniform, aspect uniform in [0.5, 2], spp drawn from ``spps``."""
+    return [spheres_grids(seed=1000 + k, tri_budget=tris, width=w, height=h, spp=spp,
+                          max_bounces=max_bounces, env_width=env_width, env_height=env_height)
+            for k, (tris, w, h, spp) in enumerate(batch_instance_params(
+                seed, n, tri_lo, tri_hi, px_lo, px_hi, spps))]
 
 
 def _map_texture(seed: int, size: int) -> np.ndarray:

@@ -69,6 +69,23 @@ def test_batch_of_repeated_jobs(served):
         assert np.array_equal(f.cpu().numpy().view(np.uint32), solo[idx].view(np.uint32))
 
 
+def test_batch_with_tail_kernel_equals_staged_solo_films(served):
+    """Late bounces finished in one launch (the tail kernel) inside batched waves, on a
+    launch grid other than the default: each film is still its solo, fully staged film.
+    The tail kernel and the staged shade kernel run the same shading code, compiled into
+    two kernels; their results agree bit for bit because no float operation is left to
+    the compiler to fuse."""
+    ctx, jobs, solo = served
+    for tune in (dict(tail_bounce=2), dict(tail_bounce=3, blocks_per_sm=12, band_rows=4)):
+        ctx.set_tuning(**tune)
+        films = [torch.empty(j[2].width * j[2].height * 3, device="cuda") for j in jobs]
+        ctx.batch_render([(sid, cam, st, f.data_ptr()) for (sid, cam, st), f in zip(jobs, films)])
+        torch.cuda.synchronize()
+        for f, ref in zip(films, solo):
+            assert np.array_equal(f.cpu().numpy().view(np.uint32), ref.view(np.uint32)), tune
+    ctx.set_tuning()
+
+
 def test_batch_first_bounce_traced_or_rasterised_alike(served):
     """In a batched wave the units whose first bounce can be rasterised (pinhole
     PathTracing jobs with enough rays per triangle) are, the others traced; with the
