@@ -311,7 +311,7 @@ struct WideCollapser {
 
 }  // namespace
 
-bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width) {
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width, float* epsOut) {
     wide->clear();
     if (bvh.primIds.empty()) return true;
     if (width < 2 || width > 8) return false;
@@ -321,6 +321,7 @@ bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width) {
     float m = 0.0f;
     for (int a = 0; a < 3; a++) m = std::max(m, std::max(std::fabs(root.lo[a]), std::fabs(root.hi[a])));
     c.eps = std::ldexp(std::max(m, 1e-30f), -18);
+    if (epsOut) *epsOut = c.eps;
     if (root.leaf) {  // the root itself is a leaf: a wide root with that one leaf child
         const int w = c.NewNode();
         c.SetChild(w, 0, root.lo, root.hi, c.Leaf(root));

@@ -32,7 +32,9 @@ struct BvhResult {
 // children and repeatedly opens the largest-area inner child until it has `width`.
 // Leaves of more than 63 primitives become chains of leaf chunks. Returns false if
 // a leaf starts beyond the 2^25 slots the child code can hold.
-bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width = 4);
+// epsOut: the widening of every child box (each side moves out by it).
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width = 4,
+                  float* epsOut = nullptr);
 constexpr int kWideLeafMax = 63;
 // Floats per wide node of the given width (6 bounds + 1 code per child, padded to
 // whole 128-byte lines).

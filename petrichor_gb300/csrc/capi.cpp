@@ -586,10 +586,19 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     }
     // wide collapse for the throughput traversal
     std::vector<float> wideF;
-    if (!CollapseWide(bvh, &wideF, kWide))
+    float wideEps = 0.0f;
+    if (!CollapseWide(bvh, &wideF, kWide, &wideEps))
         return Fail(ctx, PT_ERR_UNSUPPORTED, "too many triangles for the wide BVH leaf encoding");
     std::vector<float4> wide(wideF.size() / 4);
     std::memcpy(wide.data(), wideF.data(), wideF.size() * sizeof(float));
+    // the binary leaf node of every primitive slot, as an offset in float4 from the wide
+    // tree (stored after the binary nodes): its widened box bounds where the throughput
+    // traversal counts a hit (a hit before the ray enters that box is not one)
+    std::vector<int32_t> boxOf((size_t)T, 0);
+    for (size_t i = 0; i < bvh.nodes.size(); i++)
+        if (bvh.nodes[i].leaf)
+            for (int k = bvh.nodes[i].begin; k < bvh.nodes[i].end; k++)
+                boxOf[(size_t)k] = (int32_t)(2 * i) - (int32_t)nodes.size();
     // triangles in leaf order
     std::vector<float4> tris((size_t)T * 3);
     ParallelFor((size_t)T, [&](size_t kk) {
@@ -600,7 +609,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         const HV3 e2 = Sub(Load(d->positions + 3 * d->indices[3 * t + 2]), v0);
         tris[3 * (size_t)k] = F4(v0.x, v0.y, v0.z, e1.x);
         tris[3 * (size_t)k + 1] = F4(e1.y, e1.z, e2.x, e2.y);
-        tris[3 * (size_t)k + 2] = F4(e2.z, IntBits(t), 0.0f, 0.0f);
+        tris[3 * (size_t)k + 2] = F4(e2.z, IntBits(t), IntBits(boxOf[(size_t)k]), wideEps);
     });
     // shading records, also in leaf order: a hit's slot addresses both records
     // without a dependent read of the triangle id
@@ -702,8 +711,12 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         });
     SceneGpu& s = *sg;
     DevScene& D = s.dev;
-    if ((rc = Upload(ctx, s, nodes, &D.nodes)) != PT_OK ||
-        (rc = Upload(ctx, s, wide, &D.wide)) != PT_OK ||
+    // binary nodes and wide tree in one allocation, the wide tree right after the nodes
+    std::vector<float4> tree;
+    tree.reserve(nodes.size() + wide.size());
+    tree.insert(tree.end(), nodes.begin(), nodes.end());
+    tree.insert(tree.end(), wide.begin(), wide.end());
+    if ((rc = Upload(ctx, s, tree, &D.nodes)) != PT_OK ||
         (rc = Upload(ctx, s, tris, &D.tris)) != PT_OK ||
         (rc = Upload(ctx, s, shade, &D.shade)) != PT_OK ||
         (rc = Upload(ctx, s, mats, &D.mats)) != PT_OK ||
@@ -715,6 +728,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
         for (auto& b : s.buffers) Free(ctx, b);
         return rc;
     }
+    D.wide = D.nodes + nodes.size();
     D.numNodes = T > 0 ? (int)bvh.nodes.size() : 0;
     D.numWide = (int)(wide.size() / (kWideFloats / 4));
     D.numTris = T;
@@ -725,6 +739,7 @@ int pt_scene_upload(pt_context* ctx, const pt_scene_desc* d, pt_scene_id* out) {
     D.envH = H;
     D.envValid = W > 0 ? 1 : 0;
     D.stackDepth = bvh.height + 2;
+    D.wideEps = wideEps;
     for (int a = 0; a < 3; a++) D.envBase[a] = d->env_base_color[a];
     D.envRot = d->env_z_rotation;
     D.lightPdfArea = 1.0f / sumArea;

@@ -47,8 +47,7 @@ __device__ __forceinline__ V3 Cross(V3 a, V3 b) {
 __device__ __forceinline__ float SqLen(V3 a) { return Dot(a, a); }
 // Unfused forms: every product and sum rounded on its own, as g++ evaluates the
 // reference's float expressions. __fmul_rn/__fadd_rn are never contracted into fused
-// multiply-adds, so these give the reference's bits in a file built with -fmad=true
-// (the throughput kernels) as in one built with -fmad=false (the replay kernels).
+// multiply-adds, so these give the reference's bits whatever the file's -fmad flag.
 __device__ __forceinline__ float DotRn(V3 a, V3 b) {
     return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
 }
@@ -105,6 +104,11 @@ struct ExactMath {
     static __device__ __forceinline__ float SinSin(float t, float p) {
         return (float)(sin((double)t) * sin((double)p));
     }
+    // Vector3f::Dot / Cross / Length: each product and sum rounded on its own
+    static __device__ __forceinline__ float Dot(V3 a, V3 b) { return ::ptg::Dot(a, b); }
+    static __device__ __forceinline__ V3 Cross(V3 a, V3 b) { return ::ptg::Cross(a, b); }
+    static __device__ __forceinline__ float SqLen(V3 a) { return ::ptg::SqLen(a); }
+    static __device__ __forceinline__ float Length(V3 a) { return ::ptg::Length(a); }
     // Vector3f::Normalized: each component divided by the length
     static __device__ __forceinline__ V3 Norm(V3 a) { return Normalized(a); }
     // -0.5f + 0.5f * sqrt(x) evaluated in double (GGX.cpp:148)
@@ -133,6 +137,16 @@ struct FastMath {
     }
     static __device__ __forceinline__ float SinCos(float t, float p) { return Sin(t) * Cos(p); }
     static __device__ __forceinline__ float SinSin(float t, float p) { return Sin(t) * Sin(p); }
+    // dot and cross products as explicit fused multiply-adds (the same in every kernel
+    // that inlines them, unlike compiler-chosen contraction)
+    static __device__ __forceinline__ float Dot(V3 a, V3 b) {
+        return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x));
+    }
+    static __device__ __forceinline__ V3 Cross(V3 a, V3 b) {
+        return V3(fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x)));
+    }
+    static __device__ __forceinline__ float SqLen(V3 a) { return Dot(a, a); }
+    static __device__ __forceinline__ float Length(V3 a) { return sqrtf(Dot(a, a)); }
     // one division and three products instead of three divisions
     static __device__ __forceinline__ V3 Norm(V3 a) { return a * (1.0f / Length(a)); }
     static __device__ __forceinline__ float SmithLambda(float x) { return -0.5f + 0.5f * sqrtf(x); }
@@ -258,15 +272,15 @@ __device__ __forceinline__ Shading Interpolate(const DevScene& S, int k, V3 o, V
     LoadTri(S.tris, k, v0, e1, e2);
     const float4 s0 = __ldg(S.shade + 3 * k);
     const float4 s1 = __ldg(S.shade + 3 * k + 1);
-    const V3 ce = Cross(e1, e2);
+    const V3 ce = M::Cross(e1, e2);
     if (__float_as_int(s1.w) == 0) {
         si.n = M::Norm(ce);
     } else {
         const float4 s2 = __ldg(S.shade + 3 * k + 2);
-        const float invDet = 1.0f / Dot(-d, ce);
+        const float invDet = 1.0f / M::Dot(-d, ce);
         const V3 vec = o - v0;
-        const float w1 = Dot(vec, Cross(d, e2)) * invDet;
-        const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+        const float w1 = M::Dot(vec, M::Cross(d, e2)) * invDet;
+        const float w2 = M::Dot(vec, M::Cross(e1, d)) * invDet;
         const V3 n0(s0.x, s0.y, s0.z), n1(s1.x, s1.y, s1.z), n2(s2.x, s2.y, s2.z);
         si.n = M::Norm(w1 * (n1 - n0) + w2 * (n2 - n0) + n0);
     }
@@ -318,9 +332,10 @@ struct ONB {  // Math/OrthonormalBasis.cpp:10-62
     __device__ __forceinline__ void Build(V3 ww, V3 uu) {
         w = M::Norm(ww);
         u = M::Norm(uu);
-        v = Cross(w, u);
+        v = M::Cross(w, u);
     }
-    __device__ __forceinline__ V3 WorldToLocal(V3 a) const { return V3(Dot(a, u), Dot(a, v), Dot(a, w)); }
+    template <class M>
+    __device__ __forceinline__ V3 WorldToLocal(V3 a) const { return V3(M::Dot(a, u), M::Dot(a, v), M::Dot(a, w)); }
     __device__ __forceinline__ V3 LocalToWorld(V3 a) const { return u * a.x + v * a.y + w * a.z; }
 };
 
@@ -342,8 +357,8 @@ __device__ __forceinline__ Ray GenerateRay(const DevCamera& c, int i, int j, int
     Ray ray;
     ray.o = onLens;
     ray.d = M::Norm(onSensor - onLens);
-    const float dd = Dot(ray.d, fwd);
-    ray.T = V3(1.f, 1.f, 1.f) * dd * dd * c.focusDist * c.focusDist / SqLen(onSensor - onLens);
+    const float dd = M::Dot(ray.d, fwd);
+    ray.T = V3(1.f, 1.f, 1.f) * dd * dd * c.focusDist * c.focusDist / M::SqLen(onSensor - onLens);
     return ray;
 }
 
@@ -581,11 +596,11 @@ __device__ __noinline__ PointTextures TexturedPoint(const DevScene& S, int mat, 
     const bool smooth = __float_as_int(__ldg(&S.shade[3 * k + 1].w)) != 0;
     V3 v0, e1, e2;
     LoadTri(S.tris, k, v0, e1, e2);
-    const V3 ce = Cross(e1, e2);
-    const float invDet = __fdiv_rn(1.0f, Dot(-d, ce));
+    const V3 ce = M::Cross(e1, e2);
+    const float invDet = __fdiv_rn(1.0f, M::Dot(-d, ce));
     const V3 vec = o - v0;
-    const float w1 = Dot(vec, Cross(d, e2)) * invDet;
-    const float w2 = Dot(vec, Cross(e1, d)) * invDet;
+    const float w1 = M::Dot(vec, M::Cross(d, e2)) * invDet;
+    const float w2 = M::Dot(vec, M::Cross(e1, d)) * invDet;
     const float4 a = __ldg(S.uvs + 3 * k), b = __ldg(S.uvs + 3 * k + 1), c = __ldg(S.uvs + 3 * k + 2);
     const V3 uv0(a.x, a.y, a.z), uv1(b.x, b.y, b.z), uv2(c.x, c.y, c.z);
     const V3 duv1 = uv1 - uv0, duv2 = uv2 - uv0;
@@ -599,9 +614,9 @@ __device__ __noinline__ PointTextures TexturedPoint(const DevScene& S, int mat, 
     }
     if (m.texNormal < 0) return r;
     V3 tangent = duv2.y * e1 - duv1.y * e2;
-    if (smooth) tangent = tangent - Dot(n, tangent) * n;
-    if (SqLen(tangent) == 0.0f) tangent = V3(1.f, 0.f, 0.f);
-    const V3 bw = M::Norm(n), bu = M::Norm(tangent), bv = Cross(bw, bu);
+    if (smooth) tangent = tangent - M::Dot(n, tangent) * n;
+    if (M::SqLen(tangent) == 0.0f) tangent = V3(1.f, 0.f, 0.f);
+    const V3 bw = M::Norm(n), bu = M::Norm(tangent), bv = M::Cross(bw, bu);
     const V3 nm = TexByUV(S, m.texNormal, uv.x, uv.y);
     const V3 ln = M::Norm(2.0f * nm - V3(1.f, 1.f, 1.f));
     const float s = 1.0f - m.normalStrength;
@@ -630,7 +645,7 @@ __device__ __forceinline__ V3 GgxF0(const DevMaterial& m) {
 template <class M>
 __device__ __forceinline__ float GgxLambda(V3 dir, V3 h, float alpha) {  // GGX.cpp:140-152
     const float a2 = alpha * alpha;
-    const float c = fabsf(Dot(dir, h));
+    const float c = fabsf(M::Dot(dir, h));
     const float tan2 = c > 0 ? 1.0f / (c * c) - 1.0f : kInfinity;
     return M::SmithLambda(1.0f + a2 * tan2);
 }
@@ -641,15 +656,15 @@ __device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) 
     if (m.kind == kLambert) return MatColor(m) * V3(m.ar, m.ag, m.ab) * kInvPi;
     if (m.kind == kGlossy) {
         const V3 h = M::Norm(-din + dout);
-        const float hn = fabsf(Dot(h, n));
+        const float hn = fabsf(M::Dot(h, n));
         const float a = m.alpha, a2 = a * a, hn2 = hn * hn;
         const float k = (a2 - 1.0f) * hn2 + 1.0f;
         const float D = a2 / (kPi * k * k);
         const float li = GgxLambda<M>(dout, h, a), lo = GgxLambda<M>(-din, h, a);
         const float G = 1.0f / (1.0f + li + lo);
-        const float hl = fabsf(Dot(h, dout));
+        const float hl = fabsf(M::Dot(h, dout));
         const V3 F = GgxF0(m) + (V3(1.f, 1.f, 1.f) - GgxF0(m)) * Pow5(1.0f - hl);
-        const float ln = fabsf(Dot(dout, n)), vn = fabsf(Dot(-din, n));
+        const float ln = fabsf(M::Dot(dout, n)), vn = fabsf(M::Dot(-din, n));
         return D * G * F / (4.0f * ln * vn);
     }
     return V3(0.f, 0.f, 0.f);
@@ -657,10 +672,10 @@ __device__ __forceinline__ V3 BxDF(const DevMaterial& m, V3 din, V3 dout, V3 n) 
 // MaterialBase::PDF (Lambert.cpp:33-47, GGX.cpp:59-76, Glass.cpp:20-27)
 template <class M>
 __device__ __forceinline__ float BsdfPdf(const DevMaterial& m, V3 din, V3 dout, V3 n) {
-    if (m.kind == kLambert) return m.uniform ? 0.5f * kInvPi : fabsf(Dot(dout, n)) * kInvPi;
+    if (m.kind == kLambert) return m.uniform ? 0.5f * kInvPi : fabsf(M::Dot(dout, n)) * kInvPi;
     if (m.kind == kGlossy) {
         const V3 h = M::Norm(-din + dout);
-        const float hn = fabsf(Dot(h, n));
+        const float hn = fabsf(M::Dot(h, n));
         const float a2 = m.alpha * m.alpha, hn2 = hn * hn;
         const float tmp = 1.0f - (1.0f - a2) * hn2;
         return tmp > 0 ? kInvPi * a2 / (tmp * tmp) : kInfinity;
@@ -670,16 +685,16 @@ __device__ __forceinline__ float BsdfPdf(const DevMaterial& m, V3 din, V3 dout, 
 // GGX::SampleGGXVNDF (GGX.cpp:154-208)
 template <class M>
 __device__ __forceinline__ V3 SampleVNDF(const DevMaterial& m, V3 view, V3 n0, float u0, float u1) {
-    const V3 n = n0 * copysignf(1.0f, Dot(view, n0));
+    const V3 n = n0 * copysignf(1.0f, M::Dot(view, n0));
     ONB surf;
-    const V3 t = (fabsf(n.z) < 0.9999f) ? Cross(n, V3(0.f, 0.f, 1.f)) : V3(1.f, 0.f, 0.f);
+    const V3 t = (fabsf(n.z) < 0.9999f) ? M::Cross(n, V3(0.f, 0.f, 1.f)) : V3(1.f, 0.f, 0.f);
     surf.template Build<M>(n, t);
-    V3 v = surf.WorldToLocal(view);
+    V3 v = surf.template WorldToLocal<M>(view);
     const float alpha = m.alpha;
     v = v * V3(alpha, alpha, 1.0f);
-    v = v / Length(v);
-    const V3 t1 = (v.z < 0.9999f) ? M::Norm(Cross(v, V3(0.f, 0.f, 1.f))) : V3(1.f, 0.f, 0.f);
-    const V3 t2 = Cross(t1, v);
+    v = v / M::Length(v);
+    const V3 t1 = (v.z < 0.9999f) ? M::Norm(M::Cross(v, V3(0.f, 0.f, 1.f))) : V3(1.f, 0.f, 0.f);
+    const V3 t2 = M::Cross(t1, v);
     const float a = 1.0f / (1.0f + v.z);
     const float r = sqrtf(u0);
     const float phi = (u1 < a) ? u1 / a * kPi : kPi + (u1 - a) / (1.0f - a) * kPi;
@@ -689,7 +704,7 @@ __device__ __forceinline__ V3 SampleVNDF(const DevMaterial& m, V3 view, V3 n0, f
     V3 h = p1 * t1 + p2 * t2 + w * v;
     h = V3(alpha * h.x, alpha * h.y, SMax(0.0f, h.z));
     h = surf.LocalToWorld(h);
-    return h / Length(h);
+    return h / M::Length(h);
 }
 // MaterialBase::CreateNextRay for Lambert (Lambert.cpp:49-98), GGX (GGX.cpp:78-138)
 // and Glass (Glass.cpp:29-95). The sampler is drawn exactly where the reference
@@ -698,7 +713,7 @@ template <class M, class S2>
 __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, const Shading& si, S2& s2) {
     Ray out;
     if (m.kind == kLambert) {
-        const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
+        const V3 n = si.n * copysignf(1.0f, -M::Dot(in.d, si.n));
         ONB onb;
         onb.template Build<M>(n);
         float r0, r1;
@@ -721,12 +736,12 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         return out;
     }
     if (m.kind == kGlossy) {
-        const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
+        const V3 n = si.n * copysignf(1.0f, -M::Dot(in.d, si.n));
         float u0, u1;
         s2.Next(u0, u1);
         const V3 h = SampleVNDF<M>(m, -in.d, si.n, u0, u1);
         const V3 od = Reflected(in.d, h);
-        const float hl = fabsf(Dot(h, od));
+        const float hl = fabsf(M::Dot(h, od));
         const V3 f0 = GgxF0(m);
         const V3 F = f0 + (V3(1.f, 1.f, 1.f) - f0) * Pow5(1.0f - hl);
         const float li = GgxLambda<M>(od, h, m.alpha), lo = GgxLambda<M>(-in.d, h, m.alpha);
@@ -740,9 +755,9 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         return out;
     }
     if (m.kind == kGlass) {
-        const V3 n = si.n * copysignf(1.0f, -Dot(in.d, si.n));
+        const V3 n = si.n * copysignf(1.0f, -M::Dot(in.d, si.n));
         const float eta = m.ior / in.ior;
-        const float dn = Dot(in.d, si.n);
+        const float dn = M::Dot(in.d, si.n);
         const float disc = dn * dn - 1 + eta * eta;
         if (disc < 0) {  // total internal reflection
             out.o = si.pos + kEps * n;
@@ -755,7 +770,7 @@ __device__ __forceinline__ Ray NextRay(const DevMaterial& m, const Ray& in, cons
         }
         const V3 rd = (1.0f / eta) * (in.d - si.n * M::RefractScale(-dn, disc));
         out.d = M::Norm(rd);
-        const float nd = Dot(si.n, out.d);
+        const float nd = M::Dot(si.n, out.d);
         const float q = (1.0f - eta) / (1.0f + eta);
         const float f0 = q * q;
         const float refl = f0 + (1.0f - f0) * Pow5(1.0f - fabsf(nd));

@@ -14,7 +14,11 @@
 //                then the child codes: >= 0 wide node; < 0 leaf, -(first*64+count)-1;
 //                INT_MIN empty slot; padding to whole 128-byte lines
 //   tris       3 x float4 per primitive slot (48 B), in leaf order:
-//                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) 0 0
+//                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) box(bits) eps
+//              box: where the slot's binary leaf node is, in float4 from `wide` (the
+//              binary nodes are stored right before the wide tree, in one allocation);
+//              eps: the widening of the wide tree's child boxes (a leaf's child box is
+//              that node's box moved out by eps on every side)
 //              e1 = v1 - v0, e2 = v2 - v0 exactly as Triangle::Intersect forms
 //              them (Core/Geometry/Triangle.cpp:53-54).
 //   shade      3 x float4 per primitive slot (48 B), in leaf order like tris:
@@ -92,7 +96,9 @@ struct DevScene {
     float lightPdfArea;  // 1 / sum(1/pdfArea_i), PathTracing.cpp:363-383 (summed in light order)
     int32_t numWide;
     int32_t numTextures;
-    int32_t pad;
+    // the widening of the wide tree's child boxes (2^-18 of the largest coordinate): a
+    // leaf's child box is its binary node's box moved out by this on every side
+    float wideEps;
 };
 
 // Integrators

@@ -31,13 +31,17 @@
 
 constexpr int kRasterSeg = 32;   // pixels per work item (one row segment)
 constexpr int kRasterBatch = 2;  // (pixel, sample) pairs a lane loads before testing them
+constexpr int kRasterRecF4 = 4;    // float4 per per-triangle record
 constexpr unsigned long long kNoKey = ~0ull;
+constexpr unsigned kUncertain = 0x80000000u;  // key bit: the hit may lie outside its leaf box
 constexpr unsigned kNoItem = ~0u;  // an empty work-list slot
 
 struct RasterScratch {
     unsigned long long* key;   // per path: min {distance bits, slot}, kNoKey = no hit
     unsigned long long* key2;  // per path: min {distance bits, ~slot}
-    float4* rec;               // per triangle: 4 float4 (cone planes with margins, pixel rect)
+    int* retrace;              // paths whose nearest hit is uncertain (RetraceKernel)
+    float4* rec;               // per triangle: kRasterRecF4 float4 (cone planes with margins,
+                               // pixel rect)
     uint4* items;              // {triangle slot, unit, row | segment << 16, xa | xb << 16}
     int2* overflow;           // {triangle slot, unit} whose items did not fit (visited whole)
     long long itemCap;
@@ -49,11 +53,12 @@ __device__ __forceinline__ RasterScratch CarveRaster(const WaveBuffers& wb, int 
     RasterScratch r;
     r.key = reinterpret_cast<unsigned long long*>(wb.ray[cur ^ 1]);
     r.key2 = r.key + C;
+    r.retrace = reinterpret_cast<int*>(r.key2 + C);  // the ray buffer's second half
     r.rec = wb.shadow;
     const size_t over = ((size_t)numRecs + 1) & ~(size_t)1;  // int2 entries, 16-byte multiple
-    r.overflow = reinterpret_cast<int2*>(wb.shadow + 4 * (size_t)numRecs);
+    r.overflow = reinterpret_cast<int2*>(wb.shadow + kRasterRecF4 * (size_t)numRecs);
     r.items = reinterpret_cast<uint4*>(r.overflow + over);
-    const long long bytes = (long long)(64 * C) - 64LL * numRecs - 8LL * (long long)over;
+    const long long bytes = (long long)(64 * C) - 16LL * kRasterRecF4 * numRecs - 8LL * (long long)over;
     r.itemCap = bytes > 0 ? bytes / 16 : 0;
     return r;
 }
@@ -114,9 +119,17 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
             float m[3];
             if (fabsf(side) > 1.0e-5f * sqrtf(__fmul_rn(SqLenRn(a[0]), SqLenRn(ce)))) {
                 const float sg = side > 0.0f ? 1.0f : -1.0f;
+                // The triangle test's rounding reaches outside the triangle: for a point
+                // of the plane, n_e . d equals its barycentric coordinate opposite edge e
+                // times |side| / t, and the test's barycentric error is at most a few ulps
+                // of (|v0 - camera| + |edge|) |edge| t / |side|, so an absolute margin of
+                // 2^-19 max|edge| (|v0 - camera| + max|edge|) (32 ulps of that) covers it
+                // whatever the triangle's shape (a sliver's short edge has a small n_e).
+                const float emax = sqrtf(fmaxf(fmaxf(SqLenRn(e1), SqLenRn(e2)), SqLenRn(e2 - e1)));
+                const float mt = ldexpf(emax * (sqrtf(SqLenRn(a[0])) + emax), -19);
                 for (int e = 0; e < 3; e++) {
                     n[e] = n[e] * sg;
-                    m[e] = 2.0e-5f * sqrtf(SqLenRn(n[e]));  // angular margin ~2e-5 rad
+                    m[e] = 2.0e-5f * sqrtf(SqLenRn(n[e])) + mt;  // angular margin ~2e-5 rad
                 }
             } else {  // camera (nearly) in the triangle's plane, or a degenerate triangle: no cone test
                 for (int e = 0; e < 3; e++) {
@@ -166,7 +179,7 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
             }
             if (x0 <= x1 && y0 <= y1) {
                 nItems = (y1 - y0 + 1) * ((x1 - x0 + kRasterSeg) / kRasterSeg);
-                float4* r = rs.rec + 4 * (size_t)rec;
+                float4* r = rs.rec + kRasterRecF4 * (size_t)rec;
                 r[0] = make_float4(n[0].x, n[0].y, n[0].z, m[0]);
                 r[1] = make_float4(n[1].x, n[1].y, n[1].z, m[1]);
                 r[2] = make_float4(n[2].x, n[2].y, n[2].z, m[2]);
@@ -209,17 +222,54 @@ __global__ void __launch_bounds__(128) RasterSetupKernel(const DevJob* __restric
     }
 }
 
+// Whether the hit point at distance t is certainly inside the triangle's leaf box, the box
+// whose entry distance the traversal tests before it tests the triangle: the point lies
+// within the triangle's own bounds widened by g, the leaf box's widening (the record's
+// eps) less 2^-20 (|o| + |coordinates|), which exceeds the rounding of the point, of
+// v0 + e1 and of the traversal's slab distances (a few ulps each). A hit the triangle test
+// accepts elsewhere (its rounding can reach far outside a triangle met at a grazing angle)
+// is found by the traversal or not depending on the order it visits boxes in; such a
+// path is traced instead (RetraceKernel), which gives the traversal's own answer.
+// The bounds are formed once per triangle (TriangleNearBox); lo > hi when g <= 0.
+struct NearBox {
+    V3 lo, hi;
+};
+__device__ __forceinline__ NearBox TriangleNearBox(V3 v0, V3 e1, V3 e2, V3 o, float wideEps) {
+    const V3 v1 = v0 + e1, v2 = v0 + e2;
+    NearBox b;
+    b.lo = V3(Min3(v0.x, v1.x, v2.x), Min3(v0.y, v1.y, v2.y), Min3(v0.z, v1.z, v2.z));
+    b.hi = V3(Max3(v0.x, v1.x, v2.x), Max3(v0.y, v1.y, v2.y), Max3(v0.z, v1.z, v2.z));
+    const float m = Max3(fabsf(o.x), fabsf(o.y), fabsf(o.z)) +
+                    fmaxf(Max3(fabsf(b.lo.x), fabsf(b.lo.y), fabsf(b.lo.z)),
+                          Max3(fabsf(b.hi.x), fabsf(b.hi.y), fabsf(b.hi.z)));
+    const float g = wideEps - ldexpf(m, -20);
+    if (g > 0.0f) {
+        b.lo = b.lo - V3(g, g, g);
+        b.hi = b.hi + V3(g, g, g);
+    } else {
+        b.lo = V3(1.f, 1.f, 1.f);
+        b.hi = V3(-1.f, -1.f, -1.f);
+    }
+    return b;
+}
+__device__ __forceinline__ bool HitNearTriangle(const NearBox& b, V3 o, V3 d, float t) {
+    const V3 p = o + d * t;
+    return p.x >= b.lo.x && p.x <= b.hi.x && p.y >= b.lo.y && p.y <= b.hi.y && p.z >= b.lo.z &&
+           p.z <= b.hi.z;
+}
+
 // Visits one row segment of triangle k: every (pixel, sample) pair of the wave's unit.
 // Pixel (x, y) is pixel q = qrow + x * hb of the band order (PixelOfIndex), and its
 // samples are paths pathBase + q * sw + j, whose directions are in the ray queue.
 __device__ __forceinline__ void RasterSegment(const RasterScratch& rs, const float4* __restrict__ rays,
-                                             const float4* __restrict__ tris, int k, int rec, int y,
+                                             const DevScene& S, int k, int rec, int y,
                                              int xa, int xb, int W, int H, int band, int pathBase,
                                              int sw, V3 o, float tmin, int lane) {
-    const float4 r0 = __ldg(rs.rec + 4 * (size_t)rec), r1 = __ldg(rs.rec + 4 * (size_t)rec + 1),
-                 r2 = __ldg(rs.rec + 4 * (size_t)rec + 2);
+    const float4* rp = rs.rec + kRasterRecF4 * (size_t)rec;
+    const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
     V3 v0, e1, e2;
-    LoadTri(tris, k, v0, e1, e2);
+    LoadTri(S.tris, k, v0, e1, e2);
+    const NearBox nb = TriangleNearBox(v0, e1, e2, o, S.wideEps);
     const int y0 = (y / band) * band, hb = min(band, H - y0);
     const size_t qrow = (size_t)y0 * W + (y - y0);
     const int n = (xb - xa + 1) * sw;
@@ -250,12 +300,15 @@ __device__ __forceinline__ void RasterSegment(const RasterScratch& rs, const flo
             const float c2 = r2.x * dv[b].x + r2.y * dv[b].y + r2.z * dv[b].z + r2.w;
             if (c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f) {
                 float t;
-                if (TriIntersect(v0, e1, e2, o, V3(dv[b].x, dv[b].y, dv[b].z), t) && t >= tmin &&
-                    t < kFltMax) {
+                const V3 d(dv[b].x, dv[b].y, dv[b].z);
+                if (TriIntersect(v0, e1, e2, o, d, t) && t >= tmin && t < kFltMax) {
+                    // a hit point not certainly inside the triangle's leaf box is marked
+                    // (kUncertain); the path is traced if such a hit is its nearest
+                    const unsigned w = (unsigned)k | (HitNearTriangle(nb, o, d, t) ? 0u : kUncertain);
                     // t + 0: a zero distance as +0, so that distance bits order as floats
                     const unsigned long long tb = (unsigned long long)__float_as_uint(t + 0.0f) << 32;
-                    atomicMin(rs.key + idx[b], tb | (unsigned)k);
-                    atomicMin(rs.key2 + idx[b], tb | ~(unsigned)k);
+                    atomicMin(rs.key + idx[b], tb | w);
+                    atomicMin(rs.key2 + idx[b], tb | ~w);
                 }
             }
         }
@@ -268,7 +321,7 @@ __device__ __forceinline__ void RasterItem(const DevJob* __restrict__ jobs, cons
                                           int band, int k, int y, int xa, int xb, int lane) {
     const DevJob& J = jobs[u.job];
     const float tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
-    RasterSegment(rs, rays, J.S.tris, k, u.recBase + k, y, xa, xb, J.st.width, J.st.height, band,
+    RasterSegment(rs, rays, J.S, k, u.recBase + k, y, xa, xb, J.st.width, J.st.height, band,
                   u.pathBase, u.sw, LoadV3(J.C.pos), tmin, lane);
 }
 
@@ -301,7 +354,7 @@ __global__ void __launch_bounds__(128) RasterVisitKernel(const DevJob* __restric
     for (long long w = warp; w < nOver; w += warps) {
         const int2 ov = rs.overflow[w];
         const WaveUnit u = units[ov.y];
-        const float4 r3 = __ldg(rs.rec + 4 * (size_t)(u.recBase + ov.x) + 3);
+        const float4 r3 = __ldg(rs.rec + kRasterRecF4 * (size_t)(u.recBase + ov.x) + 3);
         const int x0 = __float_as_int(r3.x), x1 = __float_as_int(r3.y), y0 = __float_as_int(r3.z),
                   y1 = __float_as_int(r3.w);
         for (int y = y0; y <= y1; y++)
@@ -312,22 +365,31 @@ __global__ void __launch_bounds__(128) RasterVisitKernel(const DevJob* __restric
 
 // The nearest hit of every path into the hit queue (queue entry i = path i at the first
 // bounce), as ExtendKernel would write it: {distance, slot}, {kFltMax, -1} for a miss,
-// -2 - slot when another triangle tied at that distance.
+// -2 - slot when another triangle tied at that distance. A path whose hits at the nearest
+// distance include an uncertain one goes to the retrace list instead.
+// Whole warps step together (the list appends are warp-aggregated).
 __global__ void RasterFinishKernel(WaveBuffers wb, int cur) {
     const WaveDesc wd = *wb.desc;
     const RasterScratch rs = CarveRaster(wb, cur, wd.rasterRecs);
     const int n = wd.nPaths;
     if (blockIdx.x == 0 && threadIdx.x == 0) wb.counts[cur ^ 1] = 0;
-    for (int i = wd.rasterFrom + blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x) {
-        const unsigned long long key = rs.key[i];
-        float2 h = make_float2(kFltMax, __int_as_float(-1));
-        if (key != kNoKey) {
-            const unsigned tb = (unsigned)(key >> 32);
-            const int slot = (int)(unsigned)key;
-            const bool tie = (unsigned)key != ~(unsigned)rs.key2[i];
-            h = make_float2(__uint_as_float(tb), __int_as_float(tie ? -2 - slot : slot));
+    for (int b = wd.rasterFrom + blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const int i = b + threadIdx.x;
+        bool retrace = false;
+        if (i < n) {
+            const unsigned long long key = rs.key[i];
+            float2 h = make_float2(kFltMax, __int_as_float(-1));
+            if (key != kNoKey) {
+                const unsigned tb = (unsigned)(key >> 32);
+                const unsigned w1 = (unsigned)key, w2 = ~(unsigned)rs.key2[i];  // min and max word
+                const int slot = (int)(w1 & ~kUncertain);
+                retrace = ((w1 | w2) & kUncertain) != 0;
+                h = make_float2(__uint_as_float(tb), __int_as_float(w1 != w2 ? -2 - slot : slot));
+            }
+            wb.hit[i] = h;
         }
-        wb.hit[i] = h;
+        const int at = WarpAppend(wb.counts + 11, retrace);
+        if (retrace) rs.retrace[at] = i;
     }
 }
+

@@ -2,6 +2,7 @@
 #include "scheduler.h"
 
 #include <algorithm>
+#include <cmath>
 
 namespace ptg {
 
@@ -81,7 +82,13 @@ void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* 
     for (WaveUnit u : *units) {
         const DevJob& J = jobs[u.job];
         const int64_t paths = (int64_t)J.st.width * J.st.height * u.sw;
-        const bool ok = shape->iters >= 0 && J.C.aperture == 0.0f && J.S.numTris > 0 &&
+        // a camera within twice the scene's largest coordinate of the origin: then a hit
+        // point inside its triangle's bounds is certainly inside its leaf box by a margin
+        // (raster_primary.cuh HitNearTriangle) of at least a quarter of the box widening
+        const float camMax = std::max(std::fabs(J.C.pos[0]), std::max(std::fabs(J.C.pos[1]),
+                                                                      std::fabs(J.C.pos[2])));
+        const bool near = camMax <= 2.0f * std::ldexp(J.S.wideEps, 18);
+        const bool ok = shape->iters >= 0 && J.C.aperture == 0.0f && J.S.numTris > 0 && near &&
                         J.st.width < 65536 && J.st.height < 65536 &&
                         J.st.integrator == kPathTracing &&
                         paths >= perTri * (int64_t)J.S.numTris &&

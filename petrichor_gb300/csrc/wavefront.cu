@@ -461,6 +461,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         wb.counts[cur] = n;
         wb.counts[2] = wb.counts[4] = wb.counts[5] = wb.counts[6] = 0;
         wb.counts[8] = wb.counts[9] = wb.counts[10] = 0;  // raster work list (64-bit) and overflow
+        wb.counts[11] = wb.counts[12] = 0;                 // raster retrace list and its fetch
     }
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kSortBins; k += gridDim.x * blockDim.x)
         wb.sortBins[k] = 0;  // ray-sort counts start at zero in every wave
@@ -500,8 +501,37 @@ struct ExtendQueue {
     }
 };
 
+// The paths of the retrace list through the traversal (ExtendKernel's closest-hit query,
+// the same ray): their hit queue entries are the traversal's own answers.
+struct RetraceQueue {
+    const DevJob* jobs;
+    const int* pathJob;
+    int soleJob;
+    const float4* rays;
+    const int* list;
+    float2* hit;
+    __device__ void Load(int j, LaneRay& r) const {
+        const int i = list[j];
+        ExtendQueue{jobs, pathJob, soleJob, rays, hit}.Load(i, r);
+    }
+    __device__ void Finish(int j, const LaneRay& r) const {
+        hit[list[j]] = make_float2(r.tBest, __int_as_float(r.best));
+    }
+};
+__global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) RetraceKernel(const DevJob* __restrict__ jobs,
+                                                                          WaveBuffers wb, int cur) {
+    const RasterScratch rs = CarveRaster(wb, cur, 0);
+    const int n = wb.counts[11];
+    int err = 0;
+    RetraceQueue q{jobs, wb.pathJob, wb.desc->soleJob, wb.ray[cur], rs.retrace, wb.hit};
+    TraceQueue<false>(q, n, wb.counts + 12, err);
+    if (err) atomicOr(wb.counts + 3, err);
+}
+
 // counts: [0],[1] ray queues, [2] shadow queue, [3] error bits,
-//         [4] extend fetch counter, [5] shadow fetch counter, [6] shadow blocks finished
+//         [4] extend fetch counter, [5] shadow fetch counter, [6] shadow blocks finished,
+//         [8..9] raster work list (64-bit), [10] raster overflow, [11] retrace list,
+//         [12] retrace fetch counter
 // rasterFirst: the first bounce, whose paths from wb.desc->rasterFrom on are rasterised
 __global__ void __launch_bounds__(128, PT_TRACE_MIN_BLOCKS) ExtendKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                     int cur, int rasterFirst) {
@@ -643,8 +673,8 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                     L = L + in.T * MatColor(M);
                     flags |= kFlagNoSignCheck;
                 } else {
-                    const float l2 = SqLen(si.pos - o);
-                    const float cosP = fabsf(Dot(d, si.n));
+                    const float l2 = FastMath::SqLen(si.pos - o);
+                    const float cosP = fabsf(FastMath::Dot(d, si.n));
                     const float pL = l2 / cosP * S.lightPdfArea;
                     const float mis = lastPdf * lastPdf / (pL * pL + lastPdf * lastPdf);
                     L = L + mis * in.T * MatColor(M);
@@ -654,7 +684,7 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                 DevMaterial M;
                 const V3 nb = PointMaterial<FastMath>(S, si.mat, slot, o, d, si.n, M);
                 // ---- next-event estimation (PathTracing.cpp:202-327)
-                const float dt = -Dot(d, si.n);
+                const float dt = -FastMath::Dot(d, si.n);
                 const V3 p = si.pos + kEps * copysignf(1.0f, dt) * si.n;
                 const int nl = S.numLights;
                 int index = (int)(rng.Next() * (float)(nl + 1));
@@ -673,7 +703,7 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                         } else {
                             sd = EnvSample<FastMath>(S, e0, e1, pdfuv);
                         }
-                        const float c = fabsf(Dot(sd, si.n));
+                        const float c = fabsf(FastMath::Dot(sd, si.n));
                         // sin theta of the (u, v) -> solid angle Jacobian: the map's polar
                         // angle (alias sampler), or the angle to the normal (the reference)
                         const float zc = alias ? sd.z : c;
@@ -696,13 +726,13 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                     rng.Next(u0, u1);
                     const V3 pl = SampleLightPoint<FastMath>(S, index, u0, u1);
                     const V3 dl = pl - p;
-                    const float dist = Length(dl);
+                    const float dist = FastMath::Length(dl);
                     const V3 ld = dl / dist;
                     const V3 f = BxDF<FastMath>(M, d, ld, nb);
                     // emitter material pick for the visibility test (GetMaterial with a draw)
                     const float pick = rng.Next();
                     if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
-                        const V3 Tfc = in.T * f * fabsf(Dot(ld, si.n));
+                        const V3 Tfc = in.T * f * fabsf(FastMath::Dot(ld, si.n));
                         shadow = true;
                         sh0 = make_float4(p.x, p.y, p.z, dist);
                         sh1 = make_float4(ld.x, ld.y, ld.z, __int_as_float(path | (1 << 31)));
@@ -717,10 +747,10 @@ __device__ __forceinline__ void ShadeOne(const DevJob& J, int path, V3 o, V3 d, 
                 Shading sb = si;
                 sb.n = nb;
                 out = NextRay<FastMath>(M, in, sb, rng);
-                if (!(fabsf(SqLen(out.T) - 0.0f) < kEps)) {
+                if (!(fabsf(FastMath::SqLen(out.T) - 0.0f) < kEps)) {
                     cont = true;
                     lastPdf = BsdfPdf<FastMath>(M, d, out.d, nb);
-                    const float c = fabsf(Dot(si.n, out.d));
+                    const float c = fabsf(FastMath::Dot(si.n, out.d));
                     lastSin = sqrtf(SMax(0.0f, 1.0f - c * c));
                     out.bounce = k + 1;
                 }
@@ -822,10 +852,10 @@ __device__ __noinline__ void ApplyAreaLight(const DevScene& S, const float4* e, 
     if (S.mats[m].kind != kEmission) return;
     const Shading sl = Interpolate<FastMath>(S, best, o, d, tBest);
     const V3 pl = o + d * e0.w;
-    if (!(fabsf(SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
+    if (!(fabsf(FastMath::SqLen(pl - sl.pos) - 0.0f) < kEps)) return;
     const V3 sipos(e3.x, e3.y, e3.z);
-    const float l2 = SqLen(sl.pos - sipos);
-    const float cosP = fabsf(Dot(d, sl.n));
+    const float l2 = FastMath::SqLen(sl.pos - sipos);
+    const float cosP = fabsf(FastMath::Dot(d, sl.n));
     const float pdfArea = S.lightPdfArea;
     float mis = 0.0f;
     if (l2 > 0.0f) {
@@ -1398,11 +1428,12 @@ static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveB
             RasterSetupKernel<<<SmCount() * 32, block, 0, stream>>>(jobs, units, wb, cur);
             RasterVisitKernel<<<SmCount() * 16, block, 0, stream>>>(jobs, units, wb, cur);
             RasterFinishKernel<<<grid, block, 0, stream>>>(wb, cur);
+            RetraceKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
             if (ev) {
                 ev->End(5, stream);
                 ev->Begin(1, stream);  // an empty interval closed below
             }
-            *nl += 3;  // one more below
+            *nl += 4;  // one more below
         } else {
             ExtendKernel<<<grid, block, 0, stream>>>(jobs, wb, cur, 0);
         }
@@ -1745,7 +1776,8 @@ cudaError_t RunPrimaryHits(const DevJob* jobs, const WaveUnit* units, const Wave
         RasterSetupKernel<<<SmCount() * 32, kTraceBlock, 0, stream>>>(jobs, units, wb, 0);
         RasterVisitKernel<<<SmCount() * 16, kTraceBlock, 0, stream>>>(jobs, units, wb, 0);
         RasterFinishKernel<<<grid, kTraceBlock, 0, stream>>>(wb, 0);
-        nl += 3;
+        RetraceKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, wb, 0);
+        nl += 4;
     }
     PrimaryOutKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, wb, spp, raysOut, triOut, distOut);
     if (launches) *launches += nl;

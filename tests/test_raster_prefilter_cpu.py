@@ -59,10 +59,13 @@ def _setup(cam, W, H, v0, e1, e2):
     side = _dot(a[0], ce)
     ok = np.abs(side) > f32(1e-5) * np.sqrt(_dot(a[0], a[0]) * _dot(ce, ce))
     sg = np.where(side > 0, f32(1), f32(-1))
+    # the absolute part of the margin: 2^-19 max|edge| (|v0 - camera| + max|edge|)
+    emax = np.sqrt(np.maximum(np.maximum(_dot(e1, e1), _dot(e2, e2)), _dot(e2 - e1, e2 - e1)))
+    mt = np.ldexp(emax * (np.sqrt(_dot(a[0], a[0])) + emax), -19).astype(f32)
     m = []
     for k in range(3):
         n[k] = np.where(ok[:, None], n[k] * sg[:, None], f32(0))
-        m.append(np.where(ok, f32(2e-5) * np.sqrt(_dot(n[k], n[k])), f32(1)))
+        m.append(np.where(ok, f32(2e-5) * np.sqrt(_dot(n[k], n[k])) + mt, f32(1)))
     rr, uu = f32(1) / _dot(right, right), f32(1) / _dot(up, up)
     X = np.stack([_dot(av, right) * rr for av in a], 1)
     Y = np.stack([_dot(av, up) * uu for av in a], 1)
@@ -155,6 +158,33 @@ def test_benchmark_scene_filters_keep_every_hit():
     for win, seed in (((900, 940, 520, 548), 1), ((300, 330, 800, 824), 2), ((1500, 1530, 200, 220), 3)):
         hits += _check(sc, cam, W, H, win, spp=4, seed=seed)
     assert hits > 3000
+
+
+def test_sliver_triangles_filters_keep_every_hit():
+    """Long thin triangles (edge ratios up to 2000:1), many seen nearly edge-on: relative
+    to a short edge, the triangle test's rounding reaches farthest outside such
+    triangles; the cone margin's absolute part bounds it whatever the shape."""
+    from types import SimpleNamespace
+    rng = np.random.default_rng(11)
+    n = 4000
+    c = rng.uniform(-2.0, 2.0, (n, 3)).astype(f32) * f32([1, 1, 0.5]) + f32([0, 4, 1])
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    w = np.cross(u, rng.normal(size=(n, 3)))
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    length = rng.uniform(0.05, 1.0, n)
+    width = length / np.exp(rng.uniform(np.log(5), np.log(2000), n))
+    v0 = c
+    v1 = (c + u * length[:, None]).astype(f32)
+    v2 = (c + u * (0.5 * length)[:, None] + w * width[:, None]).astype(f32)
+    pos = np.stack([v0, v1, v2], 1).reshape(-1, 3)
+    sc = SimpleNamespace(positions=pos, indices=np.arange(3 * n, dtype=np.int32).reshape(n, 3))
+    cam = Camera(pos=(0.0, -3.0, 1.2), view_dir=(0.0, 1.0, -0.05), fov=0.9, focus_target=None,
+                 aperture=0.0)
+    W, H = 160, 120
+    hits = _check(sc, capi.camera_from_scene(SimpleNamespace(camera=cam)), W, H, (0, W, 0, H),
+                  spp=4, cand_margin=1e9)
+    assert hits > 1000
 
 
 def test_camera_inside_the_box_filters_keep_every_hit():
