@@ -455,7 +455,7 @@ __global__ void RaygenKernel(const DevJob* __restrict__ jobs, const WaveUnit* __
         wb.qs1[cur][i] = make_float4(0.f, 0.f, __int_as_float(0), __int_as_float(0));
         wb.qrng[cur][i] = rng.s;
         wb.pathL[i] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
-        wb.pathJob[i] = u.job;
+        if (wd.soleJob < 0) wb.pathJob[i] = u.job;  // read only where a wave mixes jobs (JobOf)
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wb.counts[cur] = n;
@@ -1126,7 +1126,7 @@ __global__ void __launch_bounds__(128) RefCountKernel(const DevJob* __restrict__
     int status = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = wb.ray[cur][2 * i], b = wb.ray[cur][2 * i + 1];
-        const DevJob& J = jobs[wb.pathJob[__float_as_int(a.w)]];
+        const DevJob& J = jobs[JobOf(wb.pathJob, wb.desc->soleJob, __float_as_int(a.w))];
         const float tmin = J.st.integrator == kSimplePathTracing ? kEps : 0.0f;
         unsigned nn = 0, nt = 0;
         float d;
