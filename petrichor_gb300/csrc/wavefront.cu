@@ -1428,7 +1428,8 @@ static void LaunchBounces(const DevJob* jobs, const WaveUnit* units, const WaveB
             RasterSetupKernel<<<SmCount() * 32, block, 0, stream>>>(jobs, units, wb, cur);
             RasterVisitKernel<<<SmCount() * 16, block, 0, stream>>>(jobs, units, wb, cur);
             RasterFinishKernel<<<grid, block, 0, stream>>>(wb, cur);
-            RetraceKernel<<<grid, block, 0, stream>>>(jobs, wb, cur);
+            // few paths, if any: a small grid (an empty launch of the full one took 0.12 ms)
+            RetraceKernel<<<2 * SmCount(), block, 0, stream>>>(jobs, wb, cur);
             if (ev) {
                 ev->End(5, stream);
                 ev->Begin(1, stream);  // an empty interval closed below
@@ -1776,7 +1777,7 @@ cudaError_t RunPrimaryHits(const DevJob* jobs, const WaveUnit* units, const Wave
         RasterSetupKernel<<<SmCount() * 32, kTraceBlock, 0, stream>>>(jobs, units, wb, 0);
         RasterVisitKernel<<<SmCount() * 16, kTraceBlock, 0, stream>>>(jobs, units, wb, 0);
         RasterFinishKernel<<<grid, kTraceBlock, 0, stream>>>(wb, 0);
-        RetraceKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, wb, 0);
+        RetraceKernel<<<2 * SmCount(), kTraceBlock, 0, stream>>>(jobs, wb, 0);
         nl += 4;
     }
     PrimaryOutKernel<<<grid, kTraceBlock, 0, stream>>>(jobs, wb, spp, raysOut, triOut, distOut);
