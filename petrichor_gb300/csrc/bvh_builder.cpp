@@ -239,10 +239,14 @@ struct WideCollapser {
         const float dx = n.hi[0] - n.lo[0], dy = n.hi[1] - n.lo[1], dz = n.hi[2] - n.lo[2];
         return 2.0f * (dx * dy + dy * dz + dz * dx);
     }
+    // Empty child slots: code INT32_MIN and a box at +infinity on every plane, which no
+    // slab test hits (the traversal tests every slot's box without reading its code).
     int NewNode() {
         const size_t nf = (size_t)WideNodeFloats(K);
         const int w = (int)(out.size() / nf);
         out.resize(out.size() + nf, 0.0f);
+        float* f = &out[(size_t)w * nf];
+        for (int i = 0; i < 6 * K; i++) f[i] = std::numeric_limits<float>::infinity();
         int32_t* codes = reinterpret_cast<int32_t*>(&out[(size_t)w * nf + 6 * K]);
         for (int i = 0; i < K; i++) codes[i] = INT32_MIN;
         return w;

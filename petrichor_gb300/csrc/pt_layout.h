@@ -12,7 +12,8 @@
 //              traversal, kWideFloats floats each (4-wide: 128 B, one L2 line):
 //                lo.x lo.y lo.z hi.x hi.y hi.z of the children (kWide floats each, SoA),
 //                then the child codes: >= 0 wide node; < 0 leaf, -(first*64+count)-1;
-//                INT_MIN empty slot; padding to whole 128-byte lines
+//                INT_MIN empty slot (whose box lies at +infinity on every plane, so the
+//                slab test never hits it); padding to whole 128-byte lines
 //   tris       3 x float4 per primitive slot (48 B), in leaf order:
 //                [0] v0.xyz e1.x  [1] e1.yz e2.xy  [2] e2.z  triId(bits) box(bits) eps
 //              box: where the slot's binary leaf node is, in float4 from `wide` (the

@@ -257,9 +257,9 @@ __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur,
 #pragma unroll
     for (int i = 0; i < K; i++) {
         float te;
-        t[i] = (c[i] != INT_MIN && SlabFast(make_float4(b[0][i], b[1][i], b[2][i], b[3][i]),
-                                            make_float4(b[4][i], b[5][i], 0.f, 0.f), oi, r.inv,
-                                            0.0f, r.tBest, te))
+        // an empty slot's box lies at +infinity on every plane and is never hit
+        t[i] = SlabFast(make_float4(b[0][i], b[1][i], b[2][i], b[3][i]),
+                        make_float4(b[4][i], b[5][i], 0.f, 0.f), oi, r.inv, 0.0f, r.tBest, te)
                  ? te
                  : inf;
     }
