@@ -138,17 +138,14 @@ constexpr int kSmemStack = PT_SMEM_STACK;
 constexpr int kDone = INT_MIN;  // no further item (never a child code of a visited slot)
 
 struct TravStack {
-    int* code;   // shared, kSmemStack x kTraceBlock
-    float* dist;
+    int2* ent;   // shared, kSmemStack x kTraceBlock {code, entry distance bits}: closest hit
+    int* code;   // shared, kSmemStack x kTraceBlock codes: any-hit (no distances)
     int2 deep[kWaveStackDepth - kSmemStack > 0 ? kWaveStackDepth - kSmemStack : 1];
     int sp;
     __device__ __forceinline__ void Push(int c, float t) {
-        if (sp < kSmemStack) {
-            code[sp * kTraceBlock + threadIdx.x] = c;
-            dist[sp * kTraceBlock + threadIdx.x] = t;
-        } else {
-            deep[sp - kSmemStack] = make_int2(c, __float_as_int(t));
-        }
+        const int2 e = make_int2(c, __float_as_int(t));  // one 8-byte store
+        if (sp < kSmemStack) ent[sp * kTraceBlock + threadIdx.x] = e;
+        else deep[sp - kSmemStack] = e;
         sp++;
     }
     // Any-hit rays: entries without distances (nothing is culled before the first hit,
@@ -167,17 +164,8 @@ struct TravStack {
     __device__ __forceinline__ int Pop(float tBest) {
         while (sp > 0) {
             --sp;
-            int c;
-            float t;
-            if (sp < kSmemStack) {
-                c = code[sp * kTraceBlock + threadIdx.x];
-                t = dist[sp * kTraceBlock + threadIdx.x];
-            } else {
-                const int2 e = deep[sp - kSmemStack];
-                c = e.x;
-                t = __int_as_float(e.y);
-            }
-            if (t <= tBest) return c;
+            const int2 e = sp < kSmemStack ? ent[sp * kTraceBlock + threadIdx.x] : deep[sp - kSmemStack];
+            if (__int_as_float(e.y) <= tBest) return e.x;
         }
         return kDone;
     }
@@ -346,16 +334,16 @@ __device__ __noinline__ void ResolveTie(const DevScene* S, V3 o, V3 d, float tmi
 // kAnyHit: every ray Q loads is an any-hit ray.
 template <bool kAnyHit, class Q>
 __device__ void TraceQueue(Q& q, int n, int* fetch, int& err) {
-    __shared__ int sCode[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
-    __shared__ float sDist[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
+    __shared__ int2 sEnt[!kAnyHit && kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
+    __shared__ int sCode[kAnyHit && kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
     const int lane = threadIdx.x & 31;
     const unsigned lowerLanes = (1u << lane) - 1u;
     LaneRay r;
     int idx = -1;
     bool active = false;
     TravStack stk;
+    stk.ent = sEnt;
     stk.code = sCode;
-    stk.dist = sDist;
     stk.sp = 0;
     int cur = kDone;
     bool exhausted = false;  // warp-uniform
@@ -943,11 +931,10 @@ struct TailSink {
 template <int kInteg>
 __global__ void __launch_bounds__(128) TailKernel(const DevJob* __restrict__ jobs, WaveBuffers wb,
                                                   int cur, int iters) {
-    __shared__ int sCode[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
-    __shared__ float sDist[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
+    __shared__ int2 sEnt[kSmemStack > 0 ? kSmemStack * kTraceBlock : 1];
     TravStack stk;
-    stk.code = sCode;
-    stk.dist = sDist;
+    stk.ent = sEnt;
+    stk.code = nullptr;  // closest-hit and runtime any-hit visits only (Push / Pop)
     stk.sp = 0;
     const int n = wb.counts[cur];
     const int sole = wb.desc->soleJob;
