@@ -260,10 +260,7 @@ __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur,
             cur = stk.PopCode();
             return;
         }
-        int pushes = 0;
-#pragma unroll
-        for (int i = 1; i < K; i++) pushes += t[i] != inf;
-        if (stk.sp + pushes > kWaveStackDepth) {
+        if (stk.sp > kWaveStackDepth - (K - 1)) {  // room for K - 1 pushes
             err |= kErrStackOverflow;
             cur = kDone;
             return;
@@ -292,10 +289,7 @@ __device__ __forceinline__ void VisitInner(LaneRay& r, TravStack& stk, int& cur,
         cur = stk.Pop(r.tBest);
         return;
     }
-    int pushes = 0;
-#pragma unroll
-    for (int i = 1; i < K; i++) pushes += t[i] != inf;
-    if (stk.sp + pushes > kWaveStackDepth) {
+    if (stk.sp > kWaveStackDepth - (K - 1)) {  // room for K - 1 pushes
         err |= kErrStackOverflow;
         cur = kDone;
         return;
