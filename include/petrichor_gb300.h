@@ -252,7 +252,7 @@ int pt_batch_render(pt_context* ctx, int32_t n, const pt_job* jobs, void* stream
 #define PT_REQ_FAILED 4
 
 typedef struct pt_serve_config {
-  int32_t wave_paths;     /* paths per wave (0: 64M) */
+  int32_t wave_paths;     /* paths per wave (0: 64M); the server holds two waves' state */
   int32_t max_active;     /* requests admitted at once (0: 256) */
   uint64_t state_budget;  /* device bytes for per-request state: sums + film staging (0: 4 GiB) */
 } pt_serve_config;

@@ -1,18 +1,20 @@
 // Serving loop: continuous batching of render requests over resident scenes.
 //
-// A server thread owns a stream, its own wave buffers, a device job table with
-// one slot per admitted request and an arena for per-request state (per-pixel
-// sums, and film staging for host films). Each iteration it
+// A server thread owns two wave lanes (a stream and wave buffers each), a device
+// job table with one slot per admitted request and an arena for per-request state
+// (per-pixel sums, and film staging for host films). Each iteration it
 //   1. admits queued requests while slots and arena space are free,
 //   2. packs the next sample blocks of the admitted requests into one wave,
 //      least remaining work first (a short request that arrives behind a long
 //      one finishes in the next wave; the long one takes what is left),
-//   3. enqueues the wave and the finalization of the requests it completes,
-//      then retires the previous wave (two waves in flight keep the GPU busy
-//      while the host plans).
-// Requests that arrive while a wave runs join the next one. A request's film
-// does not depend on the mix: paths draw from a stream keyed by (seed, pixel,
-// sample) and each pixel sums its samples in sample order.
+//   3. enqueues the wave and the finalization of the requests it completes on
+//      the lane the wave before last used, then retires the previous wave.
+// Consecutive waves run on the two lanes, so a wave starts while the one before
+// it finishes its last, sparse bounces; each wave accumulates only after the one
+// before it has accumulated and finalised (an event chain). Requests that arrive
+// while a wave runs join the next one. A request's film does not depend on the
+// mix or the lanes: paths draw from a stream keyed by (seed, pixel, sample) and
+// each pixel sums its samples in sample order.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -90,8 +92,8 @@ struct Request {
 class Server {
 public:
     Server(pt_context* ctx, const pt_serve_config& cfg) : ctx_(ctx), cfg_(cfg) {
-        // 2^26 paths (15.8 GB of wave state): at saturation the waves are full enough
-        // to beat one-request-at-a-time rendering; under light load they stay small
+        // 2^26 paths (15.8 GB of wave state per lane): at saturation the waves are full
+        // enough to beat one-request-at-a-time rendering; under light load they stay small
         if (cfg_.wave_paths <= 0) cfg_.wave_paths = 1 << 26;
         if (cfg_.max_active <= 0) cfg_.max_active = 256;
         cfg_.max_active = std::min(cfg_.max_active, kMaxJobsPerCall);
@@ -100,15 +102,23 @@ public:
     ~Server() { Stop(); }
 
     int Start() {  // ctx->mu held by the caller
-        cudaError_t e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
-        if (e != cudaSuccess) return CudaFail(ctx_, e, "server stream");
+        for (cudaStream_t& s : stream_) {
+            const cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+            if (e != cudaSuccess) {
+                DestroyStreams();
+                return CudaFail(ctx_, e, "server stream");
+            }
+        }
         int rc;
         if ((rc = Alloc(ctx_, arena_, cfg_.state_budget)) != PT_OK ||
             (rc = Alloc(ctx_, jobTable_, sizeof(DevJob) * cfg_.max_active)) != PT_OK ||
-            (rc = Alloc(ctx_, units_, sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK ||
-            (rc = Alloc(ctx_, jobList_, sizeof(int) * cfg_.max_active)) != PT_OK ||
+            (rc = Alloc(ctx_, units_[0], sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK ||
+            (rc = Alloc(ctx_, units_[1], sizeof(WaveUnit) * kMaxUnitsPerWave)) != PT_OK ||
+            (rc = Alloc(ctx_, jobList_[0], sizeof(int) * cfg_.max_active)) != PT_OK ||
+            (rc = Alloc(ctx_, jobList_[1], sizeof(int) * cfg_.max_active)) != PT_OK ||
             (rc = AllocWave()) != PT_OK) {
             FreeAll();
+            DestroyStreams();
             return rc;
         }
         alloc_.Reset(cfg_.state_budget);
@@ -223,11 +233,9 @@ public:
             if (r.state == PT_REQ_QUEUED || r.state == PT_REQ_RUNNING) Finish(r, PT_REQ_CANCELLED, PT_OK);
         }
         doneCv_.notify_all();
-        if (stream_) {
+        if (stream_[0]) {
             std::lock_guard<std::mutex> cg(ctx_->mu);
-            cudaStreamSynchronize(stream_);
-            cudaStreamDestroy(stream_);
-            stream_ = nullptr;
+            DestroyStreams();
             FreeAll();
         }
     }
@@ -272,14 +280,31 @@ private:
         }
     }
 
-    int AllocWave() {
-        wbBufs_.assign(1, DeviceBuffer{});
-        const int rc = Alloc(ctx_, wbBufs_[0], WaveBuffersBytes(cfg_.wave_paths));
-        if (rc != PT_OK) return rc;
-        wb_ = CarveWaveBuffers(wbBufs_[0].ptr, cfg_.wave_paths);
-        cudaMemset(wb_.counts, 0, 16 * sizeof(int));
-        const cudaError_t e = cudaMallocHost(&wb_.hostCount, sizeof(int) * 4);
-        return e == cudaSuccess ? PT_OK : CudaFail(ctx_, e, "cudaMallocHost");
+    // Waits for and destroys the lanes' streams (ctx->mu held, or before the thread runs).
+    void DestroyStreams() {
+        for (cudaStream_t& s : stream_) {
+            if (!s) continue;
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+            s = nullptr;
+        }
+    }
+
+    int AllocWave() {  // one wave of wave_paths paths per lane (streams created)
+        wbBufs_.assign(2, DeviceBuffer{});
+        int* host = nullptr;
+        const cudaError_t e = cudaMallocHost(&host, sizeof(int) * 4);
+        if (e != cudaSuccess) return CudaFail(ctx_, e, "cudaMallocHost");
+        hostCount_ = host;
+        for (int k = 0; k < 2; k++) {
+            const int rc = Alloc(ctx_, wbBufs_[k], WaveBuffersBytes(cfg_.wave_paths));
+            if (rc != PT_OK) return rc;
+            wb_[k] = CarveWaveBuffers(wbBufs_[k].ptr, cfg_.wave_paths);
+            wb_[k].hostCount = host + k;
+            const cudaError_t z = cudaMemsetAsync(wb_[k].counts, 0, 16 * sizeof(int), stream_[k]);
+            if (z != cudaSuccess) return CudaFail(ctx_, z, "wave counters");
+        }
+        return PT_OK;
     }
 
     void FreeAll() {  // ctx->mu held
@@ -287,17 +312,21 @@ private:
         graphs_ = nullptr;
         for (auto& b : wbBufs_) Free(ctx_, b);
         wbBufs_.clear();
-        if (wb_.hostCount) cudaFreeHost(wb_.hostCount);
-        wb_.hostCount = nullptr;
+        if (hostCount_) cudaFreeHost(hostCount_);
+        hostCount_ = nullptr;
+        for (WaveBuffers& w : wb_) w.hostCount = nullptr;
         Free(ctx_, arena_);
         Free(ctx_, jobTable_);
-        Free(ctx_, units_);
-        Free(ctx_, jobList_);
+        for (int k = 0; k < 2; k++) {
+            Free(ctx_, units_[k]);
+            Free(ctx_, jobList_[k]);
+        }
     }
 
     // One planned and enqueued wave: what it did, to retire once its event fires.
     struct InFlight {
-        cudaEvent_t done = nullptr;
+        cudaEvent_t setup = nullptr;  // its job entries and sums are in place
+        cudaEvent_t done = nullptr;   // accumulated, finalised, films copied
         int64_t paths = 0;  // paths the wave traces (for the throughput estimate)
         std::vector<std::pair<Request*, int>> scheduled;  // request, samples in this wave
         std::vector<Request*> finishing;
@@ -411,11 +440,16 @@ private:
             if (!placed[k]) place(fresh[k], cap);
     }
 
-    // ctx->mu held. Enqueues the admitted requests' job entries, the wave and the
-    // finalization of the requests whose last samples it holds.
+    // ctx->mu held. Enqueues, on the next lane, the admitted requests' job entries, the
+    // wave, its accumulation (after the previous wave's) and the finalization of the
+    // requests whose last samples it holds, and records the wave's events.
     cudaError_t Enqueue(const std::vector<Request*>& admitted, const std::vector<WaveUnit>& units,
                         int paths, int pixels, InFlight* w, int* launches) {
+        const int lane = (int)(seq_++ & 1);
+        cudaStream_t s = stream_[lane];
         cudaError_t e = cudaSuccess;
+        // the other lane's latest job entries before this wave reads the table
+        if (lastSetup_) e = cudaStreamWaitEvent(s, lastSetup_, 0);
         for (Request* r : admitted) {
             DevJob& J = slotJobs_[r->slot];
             J = DevJob{};
@@ -426,27 +460,33 @@ private:
             J.film = r->filmHost ? (float*)((char*)arena_.ptr + r->filmOff) : r->job.film_device;
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync((DevJob*)jobTable_.ptr + r->slot, &J, sizeof(DevJob),
-                                    cudaMemcpyHostToDevice, stream_);
-            if (e == cudaSuccess) e = cudaMemsetAsync(J.accum, 0, r->accumBytes, stream_);
+                                    cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(J.accum, 0, r->accumBytes, s);
         }
-        if (units.empty()) return e;
-        WaveShape shape;
-        shape.nUnits = (int)units.size();
-        shape.nPaths = paths;
-        shape.nPixelUnits = pixels;
-        shape.iters = WaveIterations(slotJobs_, units);
-        shape.integrator = WaveIntegrator(slotJobs_, units);
-        shape.soleJob = WaveSoleJob(units);
-        shape.areaLights = WaveAreaLights(slotJobs_, units);
-        std::vector<WaveUnit> ordered = units;  // rasterised units last
-        PrepareRasterUnits(slotJobs_, &ordered, &shape, tune_.primaryTraversal);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(units_.ptr, ordered.data(), ordered.size() * sizeof(WaveUnit),
-                                cudaMemcpyHostToDevice, stream_);
-        if (e == cudaSuccess) {
-            e = RunWave((DevJob*)jobTable_.ptr, (WaveUnit*)units_.ptr, shape, wb_, stream_, launches,
-                        nullptr, tune_, graphs_);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->setup, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(w->setup, s);
+        WaveUnit* table = (WaveUnit*)units_[lane].ptr;
+        if (e == cudaSuccess && !units.empty()) {
+            WaveShape shape;
+            shape.nUnits = (int)units.size();
+            shape.nPaths = paths;
+            shape.nPixelUnits = pixels;
+            shape.iters = WaveIterations(slotJobs_, units);
+            shape.integrator = WaveIntegrator(slotJobs_, units);
+            shape.soleJob = WaveSoleJob(units);
+            shape.areaLights = WaveAreaLights(slotJobs_, units);
+            std::vector<WaveUnit> ordered = units;  // rasterised units last
+            PrepareRasterUnits(slotJobs_, &ordered, &shape, tune_.primaryTraversal);
+            e = cudaMemcpyAsync(table, ordered.data(), ordered.size() * sizeof(WaveUnit),
+                                cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess)
+                e = RunWave((DevJob*)jobTable_.ptr, table, shape, wb_[lane], s, launches, nullptr, tune_,
+                            graphs_, lane, false);
         }
+        // sums in wave order: this wave accumulates after the previous one has
+        if (e == cudaSuccess && lastDone_) e = cudaStreamWaitEvent(s, lastDone_, 0);
+        if (e == cudaSuccess && !units.empty())
+            e = AccumulateWave((DevJob*)jobTable_.ptr, table, wb_[lane], tune_, s, launches);
         if (e == cudaSuccess && !w->finishing.empty()) {
             std::vector<int> slots;
             int maxPx = 0;
@@ -454,15 +494,21 @@ private:
                 slots.push_back(r->slot);
                 maxPx = std::max(maxPx, r->pixels);
             }
-            e = cudaMemcpyAsync(jobList_.ptr, slots.data(), slots.size() * sizeof(int),
-                                cudaMemcpyHostToDevice, stream_);
+            e = cudaMemcpyAsync(jobList_[lane].ptr, slots.data(), slots.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, s);
             if (e == cudaSuccess)
-                e = FinalizeJobs((DevJob*)jobTable_.ptr, (int*)jobList_.ptr, (int)slots.size(), maxPx,
-                                 stream_, launches, nullptr);
+                e = FinalizeJobs((DevJob*)jobTable_.ptr, (int*)jobList_[lane].ptr, (int)slots.size(),
+                                 maxPx, s, launches, nullptr);
             for (Request* r : w->finishing)
                 if (e == cudaSuccess && r->filmHost)
                     e = cudaMemcpyAsync(r->filmHost, (char*)arena_.ptr + r->filmOff, r->filmBytes,
-                                        cudaMemcpyDeviceToHost, stream_);
+                                        cudaMemcpyDeviceToHost, s);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(w->done, s);
+        if (e == cudaSuccess) {
+            lastSetup_ = w->setup;
+            lastDone_ = w->done;
         }
         return e;
     }
@@ -473,13 +519,27 @@ private:
         flight.pop_front();
         cudaError_t e = w.error;
         if (e == cudaSuccess) e = cudaEventSynchronize(w.done);
-        cudaEventDestroy(w.done);
+        // a retired wave's events have fired: later waves need not wait for them
+        if (lastSetup_ == w.setup) lastSetup_ = nullptr;
+        if (lastDone_ == w.done) lastDone_ = nullptr;
+        if (w.setup) cudaEventDestroy(w.setup);
+        if (w.done) cudaEventDestroy(w.done);
         std::lock_guard<std::mutex> g(mu_);
-        // path rate from back-to-back retirements (the next wave is queued behind each
-        // one, so the gap is the GPU time of a wave), smoothed over a few waves
+        // path rate from the retirements of a busy period (another wave in flight at each):
+        // the paths retired over the span of the last kRateWindow gaps. Two waves run at
+        // once on the two lanes, so consecutive retirements can fall close together; single
+        // gaps would overstate the rate and make every request look overdue.
         const double now = Now();
-        if (e == cudaSuccess && lastRetire_ > 0.0 && now > lastRetire_ && w.paths > (int64_t)1 << 20)
-            pathRate_ = 0.75 * pathRate_ + 0.25 * ((double)w.paths / (now - lastRetire_));
+        if (e == cudaSuccess) {
+            if (lastRetire_ <= 0.0) recent_.clear();  // the GPU may have idled since
+            recent_.push_back({now, w.paths});
+            if ((int)recent_.size() > kRateWindow + 1) recent_.pop_front();
+            int64_t paths = 0;
+            for (size_t i = 1; i < recent_.size(); i++) paths += recent_[i].second;
+            const double span = recent_.back().first - recent_.front().first;
+            if ((int)recent_.size() == kRateWindow + 1 && span > 0.0 && paths > (int64_t)1 << 20)
+                pathRate_ = 0.75 * pathRate_ + 0.25 * ((double)paths / span);
+        }
         lastRetire_ = flight.empty() ? 0.0 : now;
         for (auto& [r, sw] : w.scheduled) {
             r->finished += sw;
@@ -497,8 +557,9 @@ private:
         doneCv_.notify_all();
     }
 
-    // Two waves in flight: while the GPU runs one, the next is planned and enqueued
-    // behind it on the same stream, so the GPU does not wait for the host.
+    // Two waves in flight, one per lane: once the older retires, the next is planned
+    // and enqueued on its lane while the GPU runs the younger, so the GPU does not
+    // wait for the host.
     void Loop() {
         cudaSetDevice(ctx_->device);
         std::deque<InFlight> flight;
@@ -524,8 +585,6 @@ private:
                     w.error = Enqueue(admitted, units, paths, pixels, &w, &launches);
                     ctx_->stats.kernel_launches += launches;
                 }
-                if (w.error == cudaSuccess) w.error = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
-                if (w.error == cudaSuccess) w.error = cudaEventRecord(w.done, stream_);
                 flight.push_back(std::move(w));
             }
             if (flight.size() >= 2 || (units.empty() && !flight.empty())) Retire(flight);
@@ -545,19 +604,25 @@ private:
     std::vector<int> freeSlots_;
     uint64_t nextId_ = 1;
     ArenaAllocator alloc_;
-    DeviceBuffer arena_, jobTable_, units_, jobList_;
+    DeviceBuffer arena_, jobTable_, units_[2], jobList_[2];  // unit tables and job lists per lane
     std::vector<DeviceBuffer> wbBufs_;
-    WaveBuffers wb_{};
+    WaveBuffers wb_[2] = {};
+    int* hostCount_ = nullptr;  // pinned queue-count words of the two lanes
     WaveTuning tune_{};
     WaveGraphCache* graphs_ = nullptr;
     std::vector<DevJob> slotJobs_;
-    cudaStream_t stream_ = nullptr;
+    cudaStream_t stream_[2] = {nullptr, nullptr};  // the lanes' streams
+    uint64_t seq_ = 0;                              // waves enqueued (lane = seq & 1)
+    // events of the latest enqueued wave while it is in flight (null once retired)
+    cudaEvent_t lastSetup_ = nullptr, lastDone_ = nullptr;
     Clock::time_point t0_;
     static constexpr double kOverdueFactor = 1.0;
     static constexpr double kOverdueWaves = 6.0;
     static constexpr double kOverdueShare = 1.0;
     double pathRate_ = 1.5e9;  // paths per second (measured, smoothed)
-    double lastRetire_ = 0.0;  // when the previous wave retired while another was queued
+    double lastRetire_ = 0.0;  // when the previous wave retired while another was in flight
+    static constexpr int kRateWindow = 4;
+    std::deque<std::pair<double, int64_t>> recent_;  // (time, paths) of the latest retirements
 };
 
 }  // namespace ptg
