@@ -65,9 +65,11 @@ __device__ __forceinline__ V3 CentreRn(V3 lo, V3 hi) {
 __device__ __forceinline__ float Length(V3 a) { return sqrtf(Dot(a, a)); }  // = (float)sqrt(double)
 __device__ __forceinline__ V3 Normalized(V3 a) { return a / Length(a); }
 // 1 / d per component, correctly rounded whatever the file's division flags: the
-// traversal's slab tests and the triangle test keep the reference's arithmetic.
+// traversal's slab tests and the triangle test keep the reference's arithmetic. A
+// correctly rounded reciprocal (rcp.rn.f32) is the same number as the correctly
+// rounded quotient 1 / d (div.rn.f32), with fewer instructions.
 __device__ __forceinline__ V3 ExactRecip(V3 d) {
-    return V3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
+    return V3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
 }
 // std::min / std::max argument semantics (NaN handling included)
 __device__ __forceinline__ float SMin(float a, float b) { return (b < a) ? b : a; }
@@ -241,7 +243,7 @@ __device__ __forceinline__ int SlotMaterial(const float4* __restrict__ shade, in
 // rounded in every build: closest-hit IDs and distances are the reference's.
 __device__ __forceinline__ bool TriIntersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& dist) {
     const V3 ce = CrossRn(e1, e2);
-    const float invDet = __fdiv_rn(1.0f, DotRn(-d, ce));
+    const float invDet = __frcp_rn(DotRn(-d, ce));  // = 1 / det, correctly rounded
     const V3 vec = o - v0;
     const float w1 = __fmul_rn(DotRn(vec, CrossRn(d, e2)), invDet);
     const float w2 = __fmul_rn(DotRn(vec, CrossRn(e1, d)), invDet);
@@ -597,7 +599,7 @@ __device__ __noinline__ PointTextures TexturedPoint(const DevScene& S, int mat, 
     V3 v0, e1, e2;
     LoadTri(S.tris, k, v0, e1, e2);
     const V3 ce = M::Cross(e1, e2);
-    const float invDet = __fdiv_rn(1.0f, M::Dot(-d, ce));
+    const float invDet = __frcp_rn(M::Dot(-d, ce));
     const V3 vec = o - v0;
     const float w1 = M::Dot(vec, M::Cross(d, e2)) * invDet;
     const float w2 = M::Dot(vec, M::Cross(e1, d)) * invDet;
