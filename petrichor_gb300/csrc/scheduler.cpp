@@ -123,6 +123,46 @@ void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* 
     shape->rasterUnit0 = (int)trace.size();
 }
 
+std::vector<ServePick> PlanServeWave(const std::vector<ServeRequestView>& reqs,
+                                     const ServePlanLimits& lim) {
+    const double slack = lim.overdueWaves * lim.cap / lim.pathRate;
+    std::vector<int> fresh, overdue;
+    int64_t overdueWork = 0;
+    for (int i = 0; i < (int)reqs.size(); i++) {
+        const ServeRequestView& r = reqs[i];
+        if (r.scheduled >= r.spp) continue;
+        const double own = (double)r.spp * r.pixels / lim.pathRate;
+        if (lim.now - r.submit > slack + lim.overdueFactor * own) {
+            overdue.push_back(i);
+            overdueWork += (int64_t)(r.spp - r.scheduled) * r.pixels;
+        } else {
+            fresh.push_back(i);
+        }
+    }
+    auto remaining = [&](int i) { return (int64_t)(reqs[i].spp - reqs[i].scheduled) * reqs[i].pixels; };
+    std::stable_sort(fresh.begin(), fresh.end(), [&](int a, int b) { return remaining(a) < remaining(b); });
+    std::stable_sort(overdue.begin(), overdue.end(),
+                     [&](int a, int b) { return reqs[a].submit < reqs[b].submit; });
+    const int reserve = (int)std::min<int64_t>((int64_t)(lim.overdueShare * lim.cap), overdueWork);
+    std::vector<ServePick> picks;
+    int paths = 0;
+    auto place = [&](int i, int limit) {
+        const ServeRequestView& r = reqs[i];
+        const int room = (limit - paths) / r.pixels;
+        if (room < 1 || (int)picks.size() >= lim.maxUnits) return false;
+        const int sw = std::min(r.spp - r.scheduled, room);
+        picks.push_back({i, sw});
+        paths += r.pixels * sw;
+        return true;
+    };
+    std::vector<char> placed(fresh.size(), 0);
+    for (size_t k = 0; k < fresh.size(); k++) placed[k] = place(fresh[k], lim.cap - reserve);
+    for (int i : overdue) place(i, lim.cap);
+    for (size_t k = 0; k < fresh.size(); k++)
+        if (!placed[k]) place(fresh[k], lim.cap);
+    return picks;
+}
+
 int WaveAreaLights(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units) {
     for (const WaveUnit& u : units)
         if (jobs[u.job].S.numLights > 0) return 1;

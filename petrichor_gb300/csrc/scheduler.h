@@ -59,4 +59,35 @@ constexpr int64_t kRasterMinPathsPerTri = 16;
 void PrepareRasterUnits(const std::vector<DevJob>& jobs, std::vector<WaveUnit>* units,
                         WaveShape* shape, int primaryTraversal);
 
+// ---- the serving loop's wave plan (server.cpp)
+// A request that still has samples to plan: its pixels, samples, samples already planned
+// and submission time (seconds).
+struct ServeRequestView {
+    int pixels, spp, scheduled;
+    double submit;
+};
+struct ServePlanLimits {
+    int cap;                   // paths per wave
+    int maxUnits;              // sample blocks per wave
+    double now;                // seconds, on the submission clock
+    double pathRate;           // paths per second (measured)
+    double overdueWaves;       // a request is overdue after this many waves' time ...
+    double overdueFactor;      // ... plus this many times its own rendering time
+    double overdueShare;       // share of every wave guaranteed to overdue requests
+};
+// One sample block of the next wave: the request (index into the views) and its samples;
+// blocks are listed in the wave's path order.
+struct ServePick {
+    int request, sw;
+};
+// Packs the next wave, least remaining work first (a short request finishes in the next
+// wave; long ones take what is left). Under sustained load that order would keep
+// postponing the longest requests, so a request is overdue once it has waited
+// overdueWaves waves (cap / pathRate each) plus overdueFactor times its own rendering
+// time (spp * pixels / pathRate), and the overdue ones, oldest first, are guaranteed
+// overdueShare of the wave (as much of it as they can use). Each request gets at most
+// one block per wave.
+std::vector<ServePick> PlanServeWave(const std::vector<ServeRequestView>& reqs,
+                                     const ServePlanLimits& lim);
+
 }  // namespace ptg

@@ -382,62 +382,36 @@ private:
         return admitted;
     }
 
-    // mu_ held. Packs the next sample blocks into a wave, least remaining work
-    // first (short requests finish in the next wave; long ones take what is left).
-    // Under sustained load that order would keep postponing the longest requests: a
-    // request is overdue once it has waited kOverdueWaves waves plus kOverdueFactor
-    // times its own rendering time (its samples at the measured path rate), and the
-    // overdue ones, oldest first, are guaranteed kOverdueShare of every wave. Short
-    // requests finish long before that, so they keep the least-work order. Each request
-    // gets at most one sample block per wave.
+    // mu_ held. Packs the next sample blocks into a wave (PlanServeWave: least remaining
+    // work first, overdue requests guaranteed their share) and records them.
     void Plan(std::vector<WaveUnit>* units, InFlight* w, int* paths, int* pixels) {
-        const double now = Now();
-        const double slack = kOverdueWaves * cfg_.wave_paths / pathRate_;
-        std::vector<Request*> fresh, overdue;
-        int64_t overdueWork = 0;
+        std::vector<Request*> cand;
+        std::vector<ServeRequestView> views;
         for (uint64_t id : active_) {
             Request& r = *reqs_[id];
             if (r.cancel || r.scheduled >= r.spp) continue;
-            const double own = (double)r.spp * r.pixels / pathRate_;
-            if (now - r.submit > slack + kOverdueFactor * own) {
-                overdue.push_back(&r);
-                overdueWork += (int64_t)(r.spp - r.scheduled) * r.pixels;
-            } else {
-                fresh.push_back(&r);
-            }
+            cand.push_back(&r);
+            views.push_back({r.pixels, r.spp, r.scheduled, r.submit});
         }
-        std::stable_sort(fresh.begin(), fresh.end(), [](const Request* a, const Request* b) {
-            return (int64_t)(a->spp - a->scheduled) * a->pixels < (int64_t)(b->spp - b->scheduled) * b->pixels;
-        });
-        std::stable_sort(overdue.begin(), overdue.end(),
-                         [](const Request* a, const Request* b) { return a->submit < b->submit; });
-        const int cap = cfg_.wave_paths;
-        const int reserve = (int)std::min<int64_t>((int64_t)(kOverdueShare * cap), overdueWork);
-        std::vector<char> placed(fresh.size(), 0);
-        auto place = [&](Request* r, int limit) {
-            const int room = (limit - *paths) / r->pixels;
-            if (room < 1 || (int)units->size() >= kMaxUnitsPerWave) return false;
-            const int sw = std::min(r->spp - r->scheduled, room);
+        const ServePlanLimits lim{cfg_.wave_paths, kMaxUnitsPerWave, Now(), pathRate_,
+                                  kOverdueWaves, kOverdueFactor, kOverdueShare};
+        for (const ServePick& p : PlanServeWave(views, lim)) {
+            Request* r = cand[p.request];
             WaveUnit u{};
             u.job = r->slot;
             u.s0 = r->scheduled;
-            u.sw = sw;
+            u.sw = p.sw;
             u.pathBase = *paths;
             u.pixelBase = *pixels;
             units->push_back(u);
-            *paths += r->pixels * sw;
-            w->paths += (int64_t)r->pixels * sw;
+            *paths += r->pixels * p.sw;
+            w->paths += (int64_t)r->pixels * p.sw;
             *pixels += r->pixels;
-            r->scheduled += sw;
+            r->scheduled += p.sw;
             r->inFlight++;
-            w->scheduled.push_back({r, sw});
+            w->scheduled.push_back({r, p.sw});
             if (r->scheduled == r->spp) w->finishing.push_back(r);
-            return true;
-        };
-        for (size_t k = 0; k < fresh.size(); k++) placed[k] = place(fresh[k], cap - reserve);
-        for (Request* r : overdue) place(r, cap);
-        for (size_t k = 0; k < fresh.size(); k++)
-            if (!placed[k]) place(fresh[k], cap);
+        }
     }
 
     // ctx->mu held. Enqueues, on the next lane, the admitted requests' job entries, the
