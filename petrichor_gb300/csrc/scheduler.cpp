@@ -163,6 +163,20 @@ std::vector<ServePick> PlanServeWave(const std::vector<ServeRequestView>& reqs,
     return picks;
 }
 
+void PathRateMeter::Retired(double now, int64_t paths, bool ok, bool busyAfter) {
+    if (ok) {
+        if (!busy_) recent_.clear();
+        recent_.push_back({now, paths});
+        if ((int)recent_.size() > kWindow + 1) recent_.erase(recent_.begin());
+        int64_t sum = 0;
+        for (size_t i = 1; i < recent_.size(); i++) sum += recent_[i].second;
+        const double span = recent_.back().first - recent_.front().first;
+        if ((int)recent_.size() == kWindow + 1 && span > 0.0 && sum > (int64_t)1 << 20)
+            rate_ = 0.75 * rate_ + 0.25 * ((double)sum / span);
+    }
+    busy_ = busyAfter;
+}
+
 int WaveAreaLights(const std::vector<DevJob>& jobs, const std::vector<WaveUnit>& units) {
     for (const WaveUnit& u : units)
         if (jobs[u.job].S.numLights > 0) return 1;

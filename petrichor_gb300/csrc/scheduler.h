@@ -4,6 +4,7 @@
 // its last wave. A job's sample blocks are visited in increasing sample order, so
 // its per-pixel sums (and its film) are the same in any packing.
 #pragma once
+#include <utility>
 #include <vector>
 
 #include "pt_kernels.h"
@@ -89,5 +90,26 @@ struct ServePick {
 // one block per wave.
 std::vector<ServePick> PlanServeWave(const std::vector<ServeRequestView>& reqs,
                                      const ServePlanLimits& lim);
+
+// The GPU's path rate, from wave retirements: the paths retired over the span of the last
+// kWindow gaps between retirements of one busy period (another wave in flight at each),
+// smoothed. Two waves run at once on the serving loop's two lanes, so consecutive
+// retirements can fall close together; single gaps would overstate the rate and make every
+// request look overdue. A retirement after which no wave is in flight ends the busy period:
+// the GPU may idle before the next wave, so the next retirement starts a new window.
+class PathRateMeter {
+public:
+    static constexpr int kWindow = 4;
+    explicit PathRateMeter(double initial) : rate_(initial) {}
+    // A wave of `paths` retired at `now` (seconds); ok: it ran without error; busyAfter:
+    // another wave is still in flight.
+    void Retired(double now, int64_t paths, bool ok, bool busyAfter);
+    double Rate() const { return rate_; }
+
+private:
+    double rate_;
+    bool busy_ = false;                              // the previous retirement left a wave in flight
+    std::vector<std::pair<double, int64_t>> recent_;  // (time, paths), oldest first
+};
 
 }  // namespace ptg

@@ -393,7 +393,7 @@ private:
             cand.push_back(&r);
             views.push_back({r.pixels, r.spp, r.scheduled, r.submit});
         }
-        const ServePlanLimits lim{cfg_.wave_paths, kMaxUnitsPerWave, Now(), pathRate_,
+        const ServePlanLimits lim{cfg_.wave_paths, kMaxUnitsPerWave, Now(), rate_.Rate(),
                                   kOverdueWaves, kOverdueFactor, kOverdueShare};
         for (const ServePick& p : PlanServeWave(views, lim)) {
             Request* r = cand[p.request];
@@ -499,22 +499,7 @@ private:
         if (w.setup) cudaEventDestroy(w.setup);
         if (w.done) cudaEventDestroy(w.done);
         std::lock_guard<std::mutex> g(mu_);
-        // path rate from the retirements of a busy period (another wave in flight at each):
-        // the paths retired over the span of the last kRateWindow gaps. Two waves run at
-        // once on the two lanes, so consecutive retirements can fall close together; single
-        // gaps would overstate the rate and make every request look overdue.
-        const double now = Now();
-        if (e == cudaSuccess) {
-            if (lastRetire_ <= 0.0) recent_.clear();  // the GPU may have idled since
-            recent_.push_back({now, w.paths});
-            if ((int)recent_.size() > kRateWindow + 1) recent_.pop_front();
-            int64_t paths = 0;
-            for (size_t i = 1; i < recent_.size(); i++) paths += recent_[i].second;
-            const double span = recent_.back().first - recent_.front().first;
-            if ((int)recent_.size() == kRateWindow + 1 && span > 0.0 && paths > (int64_t)1 << 20)
-                pathRate_ = 0.75 * pathRate_ + 0.25 * ((double)paths / span);
-        }
-        lastRetire_ = flight.empty() ? 0.0 : now;
+        rate_.Retired(Now(), w.paths, e == cudaSuccess, !flight.empty());
         for (auto& [r, sw] : w.scheduled) {
             r->finished += sw;
             r->inFlight--;
@@ -593,10 +578,7 @@ private:
     static constexpr double kOverdueFactor = 1.0;
     static constexpr double kOverdueWaves = 6.0;
     static constexpr double kOverdueShare = 1.0;
-    double pathRate_ = 1.5e9;  // paths per second (measured, smoothed)
-    double lastRetire_ = 0.0;  // when the previous wave retired while another was in flight
-    static constexpr int kRateWindow = 4;
-    std::deque<std::pair<double, int64_t>> recent_;  // (time, paths) of the latest retirements
+    PathRateMeter rate_{1.5e9};  // paths per second, from the waves' retirements
 };
 
 }  // namespace ptg
