@@ -4,6 +4,10 @@
 // its last wave. A job's sample blocks are visited in increasing sample order, so
 // its per-pixel sums (and its film) are the same in any packing.
 #pragma once
+#include <stddef.h>
+
+#include <iterator>
+#include <map>
 #include <utility>
 #include <vector>
 
@@ -90,6 +94,52 @@ struct ServePick {
 // one block per wave.
 std::vector<ServePick> PlanServeWave(const std::vector<ServeRequestView>& reqs,
                                      const ServePlanLimits& lim);
+
+// First-fit allocator over the offsets of one device buffer, in 256-byte granules: the
+// serving loop's per-request state (sums, film staging) within its state budget. Released
+// ranges merge with free neighbours.
+class ArenaAllocator {
+public:
+    void Reset(size_t bytes) {
+        free_.clear();
+        if (bytes) free_[0] = bytes;
+    }
+    // The lowest free offset with room for `bytes` (rounded up to 256); false if none.
+    bool Alloc(size_t bytes, size_t* off) {
+        bytes = (bytes + 255) & ~size_t(255);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                *off = it->first;
+                const size_t rest = it->second - bytes, start = it->first + bytes;
+                free_.erase(it);
+                if (rest) free_[start] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    // Returns a range Alloc gave (the same `bytes`).
+    void Release(size_t off, size_t bytes) {
+        bytes = (bytes + 255) & ~size_t(255);
+        auto it = free_.emplace(off, bytes).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    const std::map<size_t, size_t>& FreeRanges() const { return free_; }  // offset -> bytes
+
+private:
+    std::map<size_t, size_t> free_;
+};
 
 // The GPU's path rate, from wave retirements: the paths retired over the span of the last
 // kWindow gaps between retirements of one busy period (another wave in flight at each),

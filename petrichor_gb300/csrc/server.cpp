@@ -29,47 +29,6 @@ namespace ptg {
 namespace {
 using Clock = std::chrono::steady_clock;
 
-// First-fit allocator over offsets of one device buffer (256-byte granules).
-class ArenaAllocator {
-public:
-    void Reset(size_t bytes) {
-        free_.clear();
-        if (bytes) free_[0] = bytes;
-    }
-    bool Alloc(size_t bytes, size_t* off) {
-        bytes = (bytes + 255) & ~size_t(255);
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second >= bytes) {
-                *off = it->first;
-                const size_t rest = it->second - bytes, start = it->first + bytes;
-                free_.erase(it);
-                if (rest) free_[start] = rest;
-                return true;
-            }
-        }
-        return false;
-    }
-    void Release(size_t off, size_t bytes) {
-        bytes = (bytes + 255) & ~size_t(255);
-        auto it = free_.emplace(off, bytes).first;
-        auto next = std::next(it);
-        if (next != free_.end() && it->first + it->second == next->first) {
-            it->second += next->second;
-            free_.erase(next);
-        }
-        if (it != free_.begin()) {
-            auto prev = std::prev(it);
-            if (prev->first + prev->second == it->first) {
-                prev->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-
-private:
-    std::map<size_t, size_t> free_;
-};
-
 struct Request {
     uint64_t id = 0;
     pt_job job{};
