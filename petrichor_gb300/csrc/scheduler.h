@@ -2,7 +2,9 @@
 // sample blocks (work units over all of its pixels), packs units into waves of at
 // most `waveCapacity` paths, runs the waves in order and finalizes each job after
 // its last wave. A job's sample blocks are visited in increasing sample order, so
-// its per-pixel sums (and its film) are the same in any packing.
+// its per-pixel sums (and its film) are the same in any packing. Also the serving
+// loop's host parts that need no device: its wave plan, its state allocator and its
+// path-rate meter.
 #pragma once
 #include <stddef.h>
 
