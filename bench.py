@@ -961,10 +961,20 @@ def main():
     if rank == 0 and world == 1 and not args.plain_only:
         line["e2e_dropin"] = e2e_dropin(scene, args.steps)
         if not args.small and not args.stress:
+            # the plain line stands on its own: a failure of a form is recorded in its
+            # object and on stderr, not allowed to swallow the line
             rate = float((args.serve_rates or "500").split(",")[-1])
-            line["serve"] = serve_object(serve_summary(args, [rate], args.requests), rate)
+            try:
+                line["serve"] = serve_object(serve_summary(args, [rate], args.requests), rate)
+            except Exception as e:  # noqa: BLE001
+                line["serve"] = {"error": f"{type(e).__name__}: {e}"}
+                print(f"serve form failed: {line['serve']['error']}", file=sys.stderr)
             torch.cuda.empty_cache()
-            line["batch"] = batch_summary(args, steps=1, warmup=1)
+            try:
+                line["batch"] = batch_summary(args, steps=1, warmup=1)
+            except Exception as e:  # noqa: BLE001
+                line["batch"] = {"error": f"{type(e).__name__}: {e}"}
+                print(f"batch form failed: {line['batch']['error']}", file=sys.stderr)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
