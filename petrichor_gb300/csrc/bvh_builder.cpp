@@ -285,10 +285,12 @@ struct WideCollapser {
         }
         return w;
     }
-    int32_t Node(int bi) {
+    // The children of the wide node made from inner binary node bi: its two children,
+    // then, while there is room, the largest-area inner child replaced by its two.
+    int Pick(int bi, int* cand) const {
         const BvhNodeOut& n = b.nodes[bi];
-        if (n.leaf) return Leaf(n);
-        int cand[8] = {n.child[0], n.child[1]};
+        cand[0] = n.child[0];
+        cand[1] = n.child[1];
         int nc = 2;
         while (nc < K) {
             int best = -1;
@@ -303,29 +305,188 @@ struct WideCollapser {
             cand[best] = b.nodes[open].child[0];
             cand[nc++] = b.nodes[open].child[1];
         }
+        return nc;
+    }
+    // The child code of binary node bi, its wide nodes appended in depth-first preorder.
+    int32_t Code(int bi) { return b.nodes[bi].leaf ? Leaf(b.nodes[bi]) : Node(bi); }
+    int32_t Node(int bi) {
+        int cand[8];
+        const int nc = Pick(bi, cand);
         const int w = NewNode();
         for (int i = 0; i < nc; i++) {
             const BvhNodeOut& c = b.nodes[cand[i]];
-            const int32_t code = c.leaf ? Leaf(c) : Node(cand[i]);
-            SetChild(w, i, c.lo, c.hi, code);
+            SetChild(w, i, c.lo, c.hi, Code(cand[i]));
         }
         return w;
     }
 };
 
+// Below this many primitives the collapse runs on one thread.
+constexpr int kCollapseParallelMin = 1 << 16;
+
+// The same wide tree as one WideCollapser run from the root, built on several threads:
+// the top wide nodes are laid out on one thread, the subtrees below them (tasks) are
+// collapsed in parallel into their own arrays with local node numbers, and every array is
+// then placed at its offset in the depth-first preorder, its node codes moved by that
+// offset. Node for node and bit for bit the serial result.
+bool CollapseParallel(const BvhResult& bvh, std::vector<float>* wide, int K, float eps, int threads) {
+    const size_t nf = (size_t)WideNodeFloats(K);
+    auto prims = [&](int bi) { return bvh.nodes[bi].end - bvh.nodes[bi].begin; };
+    // top nodes: the root, then the largest inner tasks, until there are enough tasks
+    std::vector<char> top(bvh.nodes.size(), 0);
+    top[0] = 1;
+    WideCollapser picker{bvh, *wide, K};
+    const size_t target = (size_t)threads * 8;
+    std::vector<int> open{0};
+    for (;;) {
+        // the tasks of the current top tree, largest inner one first
+        std::vector<int> tasks;
+        for (int t : open) {
+            int cand[8];
+            const int nc = picker.Pick(t, cand);
+            for (int i = 0; i < nc; i++)
+                if (!top[cand[i]]) tasks.push_back(cand[i]);
+        }
+        if (tasks.size() >= target) break;
+        int best = -1;
+        for (int t : tasks)
+            if (!bvh.nodes[t].leaf && prims(t) >= 4096 && (best < 0 || prims(t) > prims(best))) best = t;
+        if (best < 0) break;
+        top[best] = 1;
+        open.push_back(best);
+    }
+    // preorder: top nodes and tasks, as the serial collapse reaches them (a top child's
+    // whole subtree before the next slot)
+    struct Item {
+        int bi;
+        bool isTop;
+    };
+    std::vector<Item> order;
+    struct Emitter {
+        const std::vector<char>& top;
+        const WideCollapser& picker;
+        std::vector<Item>& order;
+        void Emit(int bi) {
+            order.push_back({bi, true});
+            int cand[8];
+            const int nc = picker.Pick(bi, cand);
+            for (int i = 0; i < nc; i++) {
+                if (top[cand[i]]) Emit(cand[i]);
+                else order.push_back({cand[i], false});
+            }
+        }
+    } emitter{top, picker, order};
+    emitter.Emit(0);
+    // the tasks, in parallel
+    std::vector<int> taskOf(order.size(), -1);  // item -> task
+    std::vector<int> taskNodes, taskItem;        // task -> binary node, item
+    for (size_t k = 0; k < order.size(); k++)
+        if (!order[k].isTop) {
+            taskOf[k] = (int)taskNodes.size();
+            taskNodes.push_back(order[k].bi);
+            taskItem.push_back((int)k);
+        }
+    std::vector<std::vector<float>> local(taskNodes.size());
+    std::vector<int32_t> rootCode(taskNodes.size(), 0);
+    std::vector<char> okTask(taskNodes.size(), 1);
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        for (size_t t; (t = next.fetch_add(1)) < taskNodes.size();) {
+            // about one wide node per three binary inner nodes (two per primitive at most)
+            local[t].reserve(((size_t)prims(taskNodes[t]) * 2 / 3 + 16) * nf);
+            WideCollapser c{bvh, local[t], K};
+            c.eps = eps;
+            rootCode[t] = c.Code(taskNodes[t]);
+            okTask[t] = c.ok ? 1 : 0;
+        }
+    };
+    {
+        std::vector<std::thread> pool;
+        for (int i = 1; i < threads; i++) pool.emplace_back(work);
+        work();
+        for (std::thread& th : pool) th.join();
+    }
+    for (char ok : okTask)
+        if (!ok) return false;
+    // offsets in preorder
+    std::vector<int> index(order.size(), 0);
+    size_t total = 0;
+    for (size_t k = 0; k < order.size(); k++) {
+        index[k] = (int)total;
+        total += order[k].isTop ? 1 : local[taskOf[k]].size() / nf;
+    }
+    wide->assign(total * nf, 0.0f);
+    // the top nodes, their children's codes resolved
+    std::vector<int> topIndex(bvh.nodes.size(), -1), taskAt(bvh.nodes.size(), -1);
+    for (size_t k = 0; k < order.size(); k++) {
+        if (order[k].isTop) topIndex[order[k].bi] = index[k];
+        else taskAt[order[k].bi] = (int)k;
+    }
+    WideCollapser writer{bvh, *wide, K};
+    writer.eps = eps;
+    for (size_t k = 0; k < order.size(); k++) {
+        if (!order[k].isTop) continue;
+        const int w = index[k];
+        float* f = &(*wide)[(size_t)w * nf];
+        for (int i = 0; i < 6 * K; i++) f[i] = std::numeric_limits<float>::infinity();
+        int32_t* codes = reinterpret_cast<int32_t*>(f + 6 * K);
+        for (int i = 0; i < K; i++) codes[i] = INT32_MIN;
+        int cand[8];
+        const int nc = picker.Pick(order[k].bi, cand);
+        for (int i = 0; i < nc; i++) {
+            const BvhNodeOut& c = bvh.nodes[cand[i]];
+            int32_t code;
+            if (topIndex[cand[i]] >= 0) {
+                code = topIndex[cand[i]];
+            } else {
+                const int at = taskAt[cand[i]];
+                const int32_t rc = rootCode[taskOf[at]];
+                code = rc >= 0 ? rc + index[at] : rc;
+            }
+            writer.SetChild(w, i, c.lo, c.hi, code);
+        }
+    }
+    // the task arrays at their offsets, node codes moved
+    next = 0;
+    auto place = [&]() {
+        for (size_t t; (t = next.fetch_add(1)) < taskNodes.size();) {
+            const int base = index[taskItem[t]];
+            const std::vector<float>& src = local[t];
+            float* dst = &(*wide)[(size_t)base * nf];
+            std::memcpy(dst, src.data(), src.size() * sizeof(float));
+            for (size_t w = 0; w < src.size() / nf; w++) {
+                int32_t* codes = reinterpret_cast<int32_t*>(dst + w * nf + 6 * K);
+                for (int i = 0; i < K; i++)
+                    if (codes[i] >= 0) codes[i] += base;
+            }
+        }
+    };
+    {
+        std::vector<std::thread> pool;
+        for (int i = 1; i < threads; i++) pool.emplace_back(place);
+        place();
+        for (std::thread& th : pool) th.join();
+    }
+    return true;
+}
+
 }  // namespace
 
-bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width, float* epsOut) {
+bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width, float* epsOut,
+                  int threads) {
     wide->clear();
     if (bvh.primIds.empty()) return true;
     if (width < 2 || width > 8) return false;
-    wide->reserve((bvh.nodes.size() / 3 + 16) * (size_t)WideNodeFloats(width));
     WideCollapser c{bvh, *wide, width};
     const BvhNodeOut& root = bvh.nodes[0];
     float m = 0.0f;
     for (int a = 0; a < 3; a++) m = std::max(m, std::max(std::fabs(root.lo[a]), std::fabs(root.hi[a])));
     c.eps = std::ldexp(std::max(m, 1e-30f), -18);
     if (epsOut) *epsOut = c.eps;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (threads > 1 && !root.leaf && (int)bvh.primIds.size() >= kCollapseParallelMin)
+        return CollapseParallel(bvh, wide, width, c.eps, threads);
+    wide->reserve((bvh.nodes.size() / 3 + 16) * (size_t)WideNodeFloats(width));
     if (root.leaf) {  // the root itself is a leaf: a wide root with that one leaf child
         const int w = c.NewNode();
         c.SetChild(w, 0, root.lo, root.hi, c.Leaf(root));

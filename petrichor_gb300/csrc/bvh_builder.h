@@ -32,9 +32,11 @@ struct BvhResult {
 // children and repeatedly opens the largest-area inner child until it has `width`.
 // Leaves of more than 63 primitives become chains of leaf chunks. Returns false if
 // a leaf starts beyond the 2^25 slots the child code can hold.
-// epsOut: the widening of every child box (each side moves out by it).
+// epsOut: the widening of every child box (each side moves out by it). threads <= 0:
+// hardware concurrency; the result does not depend on the thread count (node for node
+// and bit for bit), nor does it on whether the collapse runs on one thread (small trees).
 bool CollapseWide(const BvhResult& bvh, std::vector<float>* wide, int width = 4,
-                  float* epsOut = nullptr);
+                  float* epsOut = nullptr, int threads = 0);
 constexpr int kWideLeafMax = 63;
 // Floats per wide node of the given width (6 bounds + 1 code per child, padded to
 // whole 128-byte lines).

@@ -12,7 +12,8 @@
 // - a leaf slot (code -((first << 6) | count) - 1) holds 1..63 primitives, and its box
 //   holds their vertices;
 // - every primitive slot is in exactly one leaf;
-// - the widening is 2^-18 of the root's largest coordinate.
+// - the widening is 2^-18 of the root's largest coordinate;
+// - the collapse on 2, 3, 8 and 16 threads gives the same array, bit for bit.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -44,7 +45,16 @@ int main(int argc, char** argv) {
     const ptg::BvhResult b = ptg::BuildBinnedSah(pos.data(), idx.data(), T, 0);
     std::vector<float> wide;
     float eps = 0.0f;
-    if (!ptg::CollapseWide(b, &wide, K, &eps)) return Fail("collapse refused", T, K);
+    if (!ptg::CollapseWide(b, &wide, K, &eps, 1)) return Fail("collapse refused", T, K);
+    // the collapse on several threads gives the same array, bit for bit
+    for (int threads : {2, 3, 8, 16}) {
+        std::vector<float> par;
+        float e2 = 0.0f;
+        if (!ptg::CollapseWide(b, &par, K, &e2, threads)) return Fail("parallel collapse refused", T, threads);
+        if (par.size() != wide.size()) return Fail("parallel collapse size", (long)par.size(), (long)wide.size());
+        if (e2 != eps || std::memcmp(par.data(), wide.data(), wide.size() * sizeof(float)) != 0)
+            return Fail("parallel collapse differs", threads, 0);
+    }
     const int nf = ptg::WideNodeFloats(K);
     const long numWide = (long)(wide.size() / nf);
     if (numWide < 1) return Fail("no wide nodes", T, 0);

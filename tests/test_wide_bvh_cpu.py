@@ -4,8 +4,9 @@ The wide tree is collapsed from the reference's binary tree (CollapseWide,
 csrc/bvh_builder.cpp). The traversal tests every slot's box without reading its code
 first, so empty slots must carry boxes at +infinity; every triangle must sit in exactly
 one leaf whose (widened) box holds its vertices; inner boxes must hold their children's;
-leaves of more than 63 triangles become chains of chunks. A C++ client
-(tests/cpp/wide_bvh.cpp) builds the trees of several soups and walks them.
+leaves of more than 63 triangles become chains of chunks; the collapse of a large tree
+runs on several threads and must give the single-threaded array bit for bit. A C++
+client (tests/cpp/wide_bvh.cpp) builds the trees of several soups and walks them.
 """
 import os
 import subprocess
@@ -61,15 +62,28 @@ def _grid(nx, ny, z=lambda x, y: 0.1 * np.sin(x) * np.cos(y)):
 @pytest.mark.parametrize("width", [4, 8])
 def test_random_soups(checker, tmp_path, width):
     rng = np.random.default_rng(width)
-    for n, scale in [(1, 1.0), (2, 1.0), (5, 3.0), (777, 10.0), (20000, 10.0), (3000, 2.5e4)]:
+    for n, scale in [(1, 1.0), (2, 1.0), (5, 3.0), (777, 10.0), (20000, 10.0), (3000, 2.5e4),
+                     (150_000, 10.0)]:  # from 65536 triangles the collapse runs on threads
         info = _check(checker, tmp_path, *_soup(rng, n, scale), width)
         assert int(info["leaves"]) >= 1
 
 
 @pytest.mark.parametrize("width", [4, 8])
 def test_height_field_grid(checker, tmp_path, width):
-    info = _check(checker, tmp_path, *_grid(120, 90), width)
+    info = _check(checker, tmp_path, *_grid(200, 180), width)
     assert int(info["maxleaf"]) <= 4           # the binned-SAH leaf rule
+
+
+def test_many_identical_triangles_on_threads(checker, tmp_path):
+    """70,000 copies of one triangle beside a soup: a leaf that no split divides becomes a
+    long chain of chunks, collapsed on threads like the rest."""
+    rng = np.random.default_rng(11)
+    same = np.tile(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), (70_000, 1))
+    soup, _ = _soup(rng, 5000, 10.0)
+    pos = np.concatenate([same, soup + np.array([40.0, 0.0, 0.0])])
+    n = len(pos) // 3
+    info = _check(checker, tmp_path, pos, np.arange(3 * n).reshape(n, 3), 4)
+    assert int(info["maxleaf"]) == 63 and int(info["leaves"]) > 70_000 // 63
 
 
 def test_identical_triangles_become_a_chain_of_leaf_chunks(checker, tmp_path):
